@@ -1,0 +1,380 @@
+"""CPU restatement of the Fast-Higashi fit hot path (TEST INFRASTRUCTURE: the checker).
+
+This module is the oracle.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline legs of ``bench.py`` import it; the product (``fh_gb300``) never does.
+It restates, in NumPy, the reference algorithm step by step with the same loop
+structure and operation order, in a selectable precision (float64 by default,
+float32 to time the reference's arithmetic on host cores).
+
+Parity pin: ``tests/golden/make_golden.py`` runs the reference itself in this
+container on seeded inputs and stores its outputs; ``tests/test_oracle_golden.py``
+checks this restatement against them.
+
+Reference files (paths within ma-compbio/Fast-Higashi):
+  fasthigashi/sparse_for_schic.py      tiling (Chrom_Dataset) and densify
+  fasthigashi/partial_rwr.py           partial random walk with restart
+  fasthigashi/project2orthogonal.py    polar factor U Vh (thin SVD)
+  fasthigashi/parafac_integrative.py   CP-ALS inner solver
+  fasthigashi/parafac2_intergrative.py the PARAFAC2-like ALS driver
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+
+# ----------------------------------------------------------------------------------------
+# Tiling: restates Chrom_Dataset.__init__ (sparse_for_schic.py:357-510), compact=True.
+# ----------------------------------------------------------------------------------------
+@dataclass
+class BinBatch:
+    start: int          # first global row bin
+    rows: int           # b
+    local: slice        # columns of the compact tile that hold the same bins as the rows
+    col: slice          # global column bins of the compact tile
+    width: int          # n
+    shift: int          # local col = global col - shift
+
+
+def tile_layout(num_bin: int, bs_bin: int, flank: int):
+    """Bin batches of a chromosome in the compact layout (sparse_for_schic.py:401-492)."""
+    out = []
+    for i in range(0, num_bin, bs_bin):
+        b = min(bs_bin, num_bin - i)
+        right = flank if num_bin - i - b - flank > 0 else num_bin - i - b
+        if i > flank:
+            local = slice(flank, flank + b)
+            col = slice(i - flank, i + b + right)
+            shift = i - flank
+            width = b + flank + right
+        else:
+            local = slice(i, i + b)
+            col = slice(0, i + b + right)
+            shift = 0
+            width = i + b + right
+        out.append(BinBatch(i, b, local, col, width, shift))
+    return out
+
+
+def cell_batches(num_cell: int, bs_cell: int):
+    return [slice(c, min(c + bs_cell, num_cell)) for c in range(0, num_cell, bs_cell)]
+
+
+def tile_coo(indices, values, bb: BinBatch, cells: slice):
+    """Entries of one (bin batch, cell batch) tile, in tile-local coordinates."""
+    r, c, k = indices
+    m = (r >= bb.start) & (r < bb.start + bb.rows) & (k >= cells.start) & (k < cells.stop)
+    return r[m] - bb.start, c[m] - bb.shift, k[m] - cells.start, values[m]
+
+
+def densify(rows, cols, cells, vals, b, n, ncell, dtype=np.float64):
+    """densify_jit with transpose=True, do_conv=False (sparse_for_schic.py:279-320):
+    scatter into a (cells, b+2, n+2) tile at +1 offsets, crop the padding, floor at 1e-8.
+    Entries that land in the padding ring are dropped, as the crop drops them."""
+    d = np.zeros((ncell, b + 2, n + 2), dtype=dtype)
+    d[cells, rows + 1, cols + 1] = vals
+    return np.maximum(d[:, 1:-1, 1:-1], dtype(1e-8)).astype(dtype)
+
+
+# ----------------------------------------------------------------------------------------
+# Partial RWR: restates partial_rwr.py:75-175 (do_conv=False).
+# ----------------------------------------------------------------------------------------
+def rwr_transition(A, s0, s1):
+    """P of partial_rwr.py:84-111 for a (C, b, n) tile."""
+    dt = A.dtype.type
+    b = A.shape[1]
+    ar = np.arange(b)
+    S2 = np.matmul(A, A.transpose(0, 2, 1))                       # :85
+    S2[:, ar, ar] = 0                                             # :86-87
+    S1 = A[:, :, s0:s1].copy()                                    # :88
+    S2 = (S2 / (S2.sum(1, keepdims=True) + dt(1e-15))) * dt(0.25)  # :90
+    S1 = (S1 / (S1.sum(1, keepdims=True) + dt(1e-15))) * dt(0.75)  # :91
+    L = S1 + S2                                                   # :93
+    L[:, ar, ar] += (L.sum(1) == 0)                               # :96-97
+    return L / (L.sum(1, keepdims=True) + dt(1e-15))              # :111
+
+
+def partial_rwr(x, slice_start, slice_end, do_rwr=True, do_col=False, bin_cov=None,
+                force_rwr_epochs=-1, final_transpose=True, return_rwr_iter=False):
+    """x: (C, b, n).  Returns ((b, n, C) if final_transpose else (C, b, n), n_iter)."""
+    n_iter = 0
+    if do_rwr:
+        dt = x.dtype.type
+        A = x
+        P = rwr_transition(A, slice_start, slice_end)
+        b = P.shape[1]
+        eye = np.eye(b, dtype=x.dtype)
+        Q = np.broadcast_to(eye, P.shape).copy()
+        auto = force_rwr_epochs < 0
+        epochs = 60 if auto else force_rwr_epochs
+        count = 0
+        for _ in range(epochs):                                   # :115-126
+            Qn = dt(0.5) * np.matmul(Q, P)
+            Qn[:, np.arange(b), np.arange(b)] += dt(0.5)
+            if auto:
+                delta = np.sqrt(((Q - Qn) ** 2).sum(axis=(1, 2)))
+                Q = Qn
+                if np.max(delta) < 0.01:
+                    break
+            else:
+                Q = Qn
+            count += 1
+        n_iter = count
+        if do_col:                                                # :131-135
+            Q = (Q + Q.transpose(0, 2, 1)) * dt(0.5)
+            Q = np.maximum(Q, 0)
+            Q = Q / (Q.sum(2, keepdims=True) + dt(1e-15))
+            A = A / bin_cov[:, None, :]
+        x = np.matmul(Q, A)                                       # :138
+    if final_transpose:
+        x = x.transpose(1, 2, 0)
+    return (x, n_iter) if return_rwr_iter else (x, 0)
+
+
+# ----------------------------------------------------------------------------------------
+# Polar factor: project2orthogonal.py:6-34 (thin SVD, U[:, :rank] Vh[:rank]).
+# ----------------------------------------------------------------------------------------
+def project2orthogonal(matrix, rank=None):
+    U, S, Vh = np.linalg.svd(matrix, full_matrices=False)
+    if rank is None:
+        rank = min(matrix.shape[-2:])
+    return U[..., :rank] @ Vh[..., :rank, :], S[..., :rank]
+
+
+# ----------------------------------------------------------------------------------------
+# CP-ALS: parafac_integrative.py:12-112.
+# ----------------------------------------------------------------------------------------
+def balance_norm(factors):
+    """parafac_integrative.py:19-27: unit columns, the product of norms folded into the last."""
+    norm = 1
+    for f in factors:
+        norm = norm * np.linalg.norm(f, axis=0)
+    even = norm + 1e-15
+    for i in range(len(factors)):
+        factors[i] = factors[i] / (np.linalg.norm(factors[i], axis=0) + 1e-15)
+    factors[-1] = factors[-1] * even
+
+
+def parafac(X, rank, n_iter_max=100, init=None, dtype=np.float64):
+    """Returns (factors, loss_norm, loss_x) as parafac_integrative.py:28-112."""
+    X = np.asarray(X, dtype=dtype)
+    factors = [np.array(f, dtype=dtype) for f in init]
+    subs = "ijk"
+    balance_norm(factors)
+    history = []
+    for _ in range(n_iter_max):
+        for i in range(3):
+            A = np.ones((rank, rank), dtype=dtype)
+            for j, f in enumerate(factors):
+                if j != i:
+                    A = A * (f.T @ f)                             # calc_A :43-48
+            others = [j for j in range(3) if j != i]
+            spec = "ijk," + ",".join(subs[j] + "r" for j in others) + "->" + subs[i] + "r"
+            B = np.einsum(spec, X, *[factors[j] for j in others], optimize=True)   # calc_B :55-62
+            A = A + np.eye(rank, dtype=dtype) * dtype(1e-10)      # update_factor :12-15
+            factors[i] = np.linalg.solve(A, B.T).T
+        Xhat = np.einsum("ir,jr,kr->ijk", *factors, optimize=True)
+        loss_recon = float(np.sum((X - Xhat) ** 2))
+        loss_norm = float(np.sum(Xhat ** 2))
+        loss_x = float(np.sum(Xhat * X))
+        history.append((loss_recon, loss_norm, loss_x))
+        wdiff = np.nan if len(history) < 2 else (history[-2][0] - history[-1][0]) / history[-2][0]
+        if wdiff < 1e-5:
+            break
+        balance_norm(factors)
+    return factors, history[-1][1], history[-1][2]
+
+
+# ----------------------------------------------------------------------------------------
+# The ALS driver: parafac2_intergrative.py:304-740 with an injected initialisation.
+# ----------------------------------------------------------------------------------------
+@dataclass
+class ChromData:
+    name: str
+    indices: np.ndarray       # int32[3, nnz] (row, col, cell)
+    values: np.ndarray        # float32[nnz]
+    num_bin: int
+    num_cell: int
+    bs_bin: int
+    bs_cell: int
+    flank: int
+
+    def layout(self):
+        return tile_layout(self.num_bin, self.bs_bin, self.flank)
+
+    def cells(self):
+        return cell_batches(self.num_cell, self.bs_cell)
+
+    def tile(self, bb, cs, dtype):
+        r, c, k, v = tile_coo(self.indices, self.values, bb, cs)
+        return densify(r, c, k, v.astype(dtype), bb.rows, bb.width, cs.stop - cs.start, dtype)
+
+
+def chrom2size(datas, rank, size_ratio, resolution):
+    """parafac2_intergrative.py:558-567."""
+    out = {}
+    for d in datas:
+        s = min(int(d.num_bin * size_ratio * resolution / 1000000), rank)
+        out[d.name] = min(out.get(d.name, s), s)
+    return out
+
+
+class ALSOracle:
+    """Holds the factor state (A per chromosome dataset, B and D per chromosome, E) and runs
+    ALS iterations exactly as Fast_Higashi_core.fit does after init_params."""
+
+    def __init__(self, datas, rank, A_list, B_dict, D_dict, E, n_i, dtype=np.float64, cache_rwr=True):
+        self.datas = datas
+        self.rank = rank
+        self.dt = dtype
+        self.A_list = [np.array(a, dtype=dtype) for a in A_list]
+        self.B = {k: np.array(v, dtype=dtype) for k, v in B_dict.items()}
+        self.D = {k: np.array(v, dtype=dtype) for k, v in D_dict.items()}
+        self.E = np.array(E, dtype=dtype)
+        self.n_i = [int(v) for v in n_i]
+        self.size = {d.name: self.B[d.name].shape[0] for d in datas}
+        self._cache = {} if cache_rwr else None
+        self.rec_errors, self.rec_errors_total = [], []
+        self.norm_tensor = None
+        self.core_norm = self._core_norm()
+
+    def rwr_tile(self, ci, bi, cj):
+        """X of one tile after partial RWR with force_rwr_epochs = n_i, as (b, n, C)."""
+        key = (ci, bi, cj)
+        if self._cache is not None and key in self._cache:
+            return self._cache[key]
+        d = self.datas[ci]
+        bb = d.layout()[bi]
+        cs = d.cells()[cj]
+        x = d.tile(bb, cs, self.dt)
+        out, _ = partial_rwr(x, bb.local.start, bb.local.stop, do_rwr=True,
+                             force_rwr_epochs=self.n_i[ci], final_transpose=True)
+        out = np.ascontiguousarray(out)
+        if self._cache is not None:
+            self._cache[key] = out
+        return out
+
+    def _core_norm(self):
+        """parafac2_intergrative.py:621-632 (per dataset, over bin batches)."""
+        out = np.zeros(len(self.datas))
+        for ci, d in enumerate(self.datas):
+            B, D, A = self.B[d.name], self.D[d.name], self.A_list[ci]
+            for i in range(0, d.num_bin, d.bs_bin):
+                c = np.einsum("ir,jr,kr->kij", A[i:i + d.bs_bin], B, D, optimize=True)
+                out[ci] += float(np.sum(c.astype(np.float64) ** 2)) if self.dt == np.float64 else float(np.sum(c ** 2))
+        return out
+
+    def update(self, first_iter=False):
+        """update_meta_embedding_interactions (parafac2_intergrative.py:304-540).
+        Returns (U per (dataset, bin batch), Y per chromosome, err_x_U, err_x_V, tensor_norm)."""
+        dt = self.dt
+        E = self.E
+        SVD_term = np.zeros((E.shape[1], E.shape[0]), dtype=dt)
+        err_x_U = np.zeros(len(self.datas))
+        tnorm = np.zeros(len(self.datas))
+        U_all = []
+        for ci, d in enumerate(self.datas):
+            A, B, D = self.A_list[ci], self.B[d.name], self.D[d.name]
+            C = E @ D                                                    # :336
+            U_list = []
+            for bi, bb in enumerate(d.layout()):
+                rs = slice(bb.start, bb.start + bb.rows)
+                temp = None
+                for cj, cs in enumerate(d.cells()):
+                    X = self.rwr_tile(ci, bi, cj)
+                    if first_iter:
+                        tnorm[ci] += float(np.sum(X.astype(np.float64) ** 2))   # :369
+                    lhs = np.einsum("ir,jr,kr->ikj", A[rs], B, C[cs], optimize=True)   # :374
+                    t = np.matmul(X, lhs)                                # :380-383
+                    temp = t if temp is None else temp + t
+                U, S = project2orthogonal(temp, temp.shape[-1])           # :396
+                U = U.astype(dt)
+                U_list.append(U)
+                err_x_U[ci] += float(np.sum(S))                          # :417
+                lhs2 = np.einsum("ir,jr,kr->kij", A[rs], B, D, optimize=True).reshape(D.shape[0], -1)  # :422-423
+                for cj, cs in enumerate(d.cells()):                       # :429-477
+                    X = self.rwr_tile(ci, bi, cj)
+                    proj = np.matmul(U.transpose(0, 2, 1), X)
+                    SVD_term[:, cs] += lhs2 @ proj.reshape(-1, proj.shape[-1])
+            U_all.append(U_list)
+        E_new, _ = project2orthogonal(SVD_term.T, self.rank)              # :483
+        E_new = E_new.astype(dt)
+        err_x_V = float(np.sum(E_new * SVD_term.T))                       # :486
+        Y = {}
+        for ci, d in enumerate(self.datas):                               # :488-529
+            Yc = np.zeros((d.num_bin, self.size[d.name], self.rank), dtype=dt)
+            for bi, bb in enumerate(d.layout()):
+                g = 0
+                for cj, cs in enumerate(d.cells()):
+                    X = self.rwr_tile(ci, bi, cj)
+                    g = g + np.einsum("ijk,km,ijl->ilm", X, E_new[cs], U_all[ci][bi], optimize=True)
+                Yc[bb.start:bb.start + bb.rows] = g
+            Y[ci] = Yc
+        self.E = E_new
+        return U_all, Y, err_x_U, err_x_V, tnorm
+
+    def iterate(self, iteration, n_iter_parafac=1):
+        """One iteration of the fit loop (parafac2_intergrative.py:635-737).  Datasets are one
+        per chromosome (single resolution), so the per-chromosome Y is the dataset's Y."""
+        first = self.norm_tensor is None
+        U_all, Y, err_x_U, err_x_V, tnorm = self.update(first_iter=first)
+        if first:
+            self.tensor_norm = tnorm
+            self.norm_tensor = np.sqrt(tnorm)
+            self.norm_tensor_all = float(np.linalg.norm(self.norm_tensor))
+        by_block = self.tensor_norm + self.core_norm - 2 * err_x_U
+        rec_V = self.tensor_norm.sum() + self.core_norm.sum() - 2 * err_x_V
+        for ci, d in enumerate(self.datas):                              # :674-695
+            r = self.size[d.name]
+            f, _, _ = parafac(Y[ci], rank=r, n_iter_max=n_iter_parafac,
+                              init=[self.A_list[ci], self.B[d.name], self.D[d.name]], dtype=self.dt)
+            self.A_list[ci], self.B[d.name], self.D[d.name] = f
+        self.core_norm = self._core_norm()                                # :697-706
+        rec = math.sqrt(rec_V) / self.norm_tensor_all                     # :710
+        self.rec_errors_total.append(rec)
+        self.rec_errors.append(np.sqrt(by_block) / self.norm_tensor)
+        return dict(U=U_all, Y=Y, err_x_U=err_x_U, err_x_V=err_x_V, rec_error=rec)
+
+    def fit(self, n_iter_max, n_iter_parafac=1, tol=0.0):
+        for it in range(n_iter_max):
+            if it % 10 == 0 and it > 0 and n_iter_parafac < 10:          # :636-637
+                n_iter_parafac += 1
+            self.iterate(it, n_iter_parafac)
+            if it >= 1:
+                t = self.rec_errors_total
+                diff = (self.rec_errors[-2] ** 2 - self.rec_errors[-1] ** 2) / self.rec_errors[-2] ** 2
+                tdiff = (t[-2] ** 2 - t[-1] ** 2) / t[-2] ** 2
+                if it >= 3 and tol > 0 and (tdiff < tol or diff.max() < tol * 2):
+                    break
+        return self
+
+    def transform(self, U_all):
+        """transform (parafac2_intergrative.py:742-834), good-QC cells only: final SVD_term with
+        the stored projections and the current factors, then its polar factor."""
+        dt = self.dt
+        SVD_term = np.zeros((self.E.shape[1], self.E.shape[0]), dtype=dt)
+        for ci, d in enumerate(self.datas):
+            A, B, D = self.A_list[ci], self.B[d.name], self.D[d.name]
+            for bi, bb in enumerate(d.layout()):
+                rs = slice(bb.start, bb.start + bb.rows)
+                lhs = np.einsum("ir,jr,kr->kij", A[rs], B, D, optimize=True).reshape(D.shape[0], -1)
+                for cj, cs in enumerate(d.cells()):
+                    X = self.rwr_tile(ci, bi, cj)
+                    proj = np.matmul(U_all[ci][bi].transpose(0, 2, 1), X)
+                    SVD_term[:, cs] += lhs @ proj.reshape(-1, proj.shape[-1])
+        E, _ = project2orthogonal(SVD_term.T, self.rank)
+        return E
+
+
+def procrustes_align(X, Y):
+    """Rotation Q minimising ||X Q - Y||_F (orthogonal Procrustes); returns X Q."""
+    U, _, Vh = np.linalg.svd(X.T @ Y)
+    return X @ (U @ Vh)
+
+
+def rel_err(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))

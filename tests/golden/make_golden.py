@@ -1,0 +1,197 @@
+"""Generates the golden fixtures by running the reference Fast-Higashi in this container.
+
+    python tests/golden/make_golden.py          (needs the reference tree; CPU only)
+
+Every output is produced by the reference's own functions on seeded synthetic inputs
+(``fh_gb300.synth``), in float32 on the CPU, with the two import shims described in
+``ref_import.py``.  Fixtures:
+
+  rwr_tiles.npz    every (bin batch, cell batch) tile of the ``tiny`` workload with
+                   bs_bin=12, bs_cell=10, flank=4: the densified input from
+                   ``Chrom_Dataset.fetch`` and ``partial_rwr`` outputs with
+                   force_rwr_epochs=3 and with the auto-stop rule (plus its epoch count).
+  parafac.npz      ``parafac`` on a random 3-way tensor for n_iter_max 1 and 3.
+  als_small.npz    the ``small`` workload with bs_bin=25, bs_cell=40: the state after
+                   ``init_params``, one ``update_meta_embedding_interactions`` call from it,
+                   and a 4-iteration ``fit`` from the same state (loss trajectory,
+                   factors, ``transform`` embedding).
+  c1_fit.npz       the 200-cell, 3-chromosome, R=16, band 10 workload with the reference's
+                   GPU batching: the input, the initial state, the 10-iteration loss
+                   trajectory and the final factors and embedding.
+"""
+import copy
+import os
+import sys
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(HERE, "..", "..", "fast-higashi_gb300"))
+
+from ref_import import import_reference, build_chrom_datasets  # noqa: E402
+from fh_gb300 import synth  # noqa: E402
+
+torch.set_num_threads(4)
+ref = import_reference()
+core = ref["core"]
+CPU = torch.device("cpu")
+
+
+def coo_arrays(prefix, coo):
+    out = {}
+    for k, (idx, vals, shape) in enumerate(coo):
+        # rows, columns and cells of these workloads fit int16; the loaders widen them
+        out["%s_idx%d" % (prefix, k)] = idx.astype(np.int16)
+        out["%s_val%d" % (prefix, k)] = vals.astype(np.float32)
+        out["%s_shape%d" % (prefix, k)] = np.asarray(shape, dtype=np.int64)
+    return out
+
+
+def make_rwr_tiles():
+    w = synth.workload("tiny")
+    coo, _ = synth.generate(w, seed=11)
+    ds = build_chrom_datasets(ref, coo, w.chrom_names, [12] * 2, [10] * 2, w.band, w.resolution)
+    out = coo_arrays("in", coo)
+    out.update(bs_bin=12, bs_cell=10, flank=w.band, n_chrom=len(coo))
+    k = 0
+    for ci, d in enumerate(ds):
+        for bi in range(d.num_bin_batch):
+            loc = d.local_bin_slice_list[bi]
+            for cj in range(d.num_cell_batch):
+                (x, _), kind = d.fetch(bi, cj, save_context=dict(device=CPU), transpose=True)
+                y3, _ = ref["rwr"].partial_rwr(x.clone(), loc.start, loc.stop, False, True, False,
+                                               force_rwr_epochs=3, return_rwr_iter=True)
+                ya, na = ref["rwr"].partial_rwr(x.clone(), loc.start, loc.stop, False, True, False,
+                                                force_rwr_epochs=-1, return_rwr_iter=True,
+                                                final_transpose=False)
+                out["t%d_meta" % k] = np.array([ci, bi, cj, loc.start, loc.stop, na], dtype=np.int64)
+                out["t%d_x" % k] = x.numpy()
+                out["t%d_y3" % k] = y3.contiguous().numpy()
+                out["t%d_yauto" % k] = ya.contiguous().numpy()
+                k += 1
+    out["n_tiles"] = k
+    np.savez_compressed(os.path.join(HERE, "rwr_tiles.npz"), **out)
+    print("rwr_tiles", k, "tiles")
+
+
+def make_parafac():
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((40, 6, 9)).astype(np.float32)
+    init = [1 + 0.01 * rng.standard_normal((40, 6)), np.eye(6) + 0.01 * rng.standard_normal((6, 6)),
+            rng.standard_normal((9, 6))]
+    init = [a.astype(np.float32) for a in init]
+    out = dict(X=X, A0=init[0], B0=init[1], D0=init[2])
+    for n in (1, 3):
+        f, ln, lx = ref["parafac"].parafac(torch.from_numpy(X), rank=6, n_iter_max=n,
+                                           init=[torch.from_numpy(a.copy()) for a in init])
+        out["A%d" % n], out["B%d" % n], out["D%d" % n] = [t.numpy() for t in f]
+        out["ln%d" % n], out["lx%d" % n] = ln, lx
+    np.savez_compressed(os.path.join(HERE, "parafac.npz"), **out)
+    print("parafac")
+
+
+class FitLocals:
+    """Captures the local loss lists of Fast_Higashi_core.fit when it returns."""
+
+    def __init__(self):
+        self.locals = None
+
+    def __enter__(self):
+        def prof(frame, event, arg):
+            if event == "return" and frame.f_code is core.Fast_Higashi_core.fit.__code__:
+                self.locals = dict(frame.f_locals)
+        sys.setprofile(prof)
+        return self
+
+    def __exit__(self, *a):
+        sys.setprofile(None)
+
+
+def snapshot(model):
+    return dict(A=[a.clone() for a in model.A_list],
+                B={k: v.clone() for k, v in model.B_dict.items()},
+                D={k: v.clone() for k, v in model.D_dict.items()},
+                E=model.meta_embedding.clone(), n_i=np.array(model.n_i).copy(),
+                bin_cov=[b.clone() for b in model.bin_cov_list],
+                bad_bin_cov=copy.deepcopy(model.bad_bin_cov_list))
+
+
+def inject(model, st):
+    model.A_list = [a.clone() for a in st["A"]]
+    model.B_dict = {k: v.clone() for k, v in st["B"].items()}
+    model.D_dict = {k: v.clone() for k, v in st["D"].items()}
+    model.meta_embedding = st["E"].clone()
+    model.n_i = st["n_i"].copy()
+    model.bin_cov_list = [b.clone() for b in st["bin_cov"]]
+    model.bad_bin_cov_list = copy.deepcopy(st["bad_bin_cov"])
+
+
+def state_arrays(prefix, st, names):
+    out = {"%s_E" % prefix: st["E"].numpy(), "%s_n_i" % prefix: np.asarray(st["n_i"])}
+    for k, a in enumerate(st["A"]):
+        out["%s_A%d" % (prefix, k)] = a.numpy()
+    for k, n in enumerate(names):
+        out["%s_B%d" % (prefix, k)] = st["B"][n].numpy()
+        out["%s_D%d" % (prefix, k)] = st["D"][n].numpy()
+    return out
+
+
+def run_fit(w, ds, n_iter, init_state, dim1):
+    m = core.Fast_Higashi_core(rank=w.rank, off_diag=w.band, res_list=[w.resolution]).to(CPU)
+    inject(m, init_state)
+    with FitLocals() as fl:
+        m.fit(ds, size_ratio=dim1, n_iter_max=n_iter, n_iter_parafac=1, do_conv=False,
+              do_rwr=True, do_col=False, tol=0, run_init=False)
+    res = m.transform(ds, False, True, False)
+    return m, fl.locals, res
+
+
+def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U=True):
+    w = synth.workload(wname)
+    coo, _ = synth.generate(w, seed=seed)
+    bsb = [bs_bin or synth.recommend_batches(w, nb, w.n_cells)[0] for nb in w.chrom_bins]
+    bsc = [bs_cell or w.n_cells for _ in w.chrom_bins]
+    ds = build_chrom_datasets(ref, coo, w.chrom_names, bsb, bsc, w.band, w.resolution)
+    np.random.seed(seed)
+    torch.manual_seed(seed)
+    m = core.Fast_Higashi_core(rank=w.rank, off_diag=w.band, res_list=[w.resolution]).to(CPU)
+    m.fit(ds, size_ratio=w.dim1, n_iter_max=0, n_iter_parafac=1, do_conv=False, do_rwr=True,
+          do_col=False, tol=0, run_init=True)
+    st0 = snapshot(m)
+    out = coo_arrays("in", coo) if save_input else {}
+    out.update(state_arrays("init", st0, w.chrom_names))
+    out.update(bs_bin=np.asarray(bsb), bs_cell=np.asarray(bsc), flank=w.band, rank=w.rank,
+               resolution=w.resolution, dim1=w.dim1, n_iter=n_iter, seed=seed,
+               n_chrom=len(coo), sizes=np.asarray([m.chrom2size[n] for n in w.chrom_names]))
+    # one update_meta_embedding_interactions call from the initial state
+    proj_list = [[torch.empty(0)] * d.num_bin_batch for d in ds]
+    ptl = {d.chrom: torch.empty([d.num_bin, m.chrom2size[d.chrom], w.rank]) for d in ds}
+    r = m.update_meta_embedding_interactions(ds, proj_list, ptl, do_conv=False, do_rwr=True,
+                                             do_col=False, first_iter=True)
+    pl, ptl, exU, exV, tn = r
+    for ci, d in enumerate(ds):
+        for bi in range(d.num_bin_batch if save_U else 0):
+            out["it1_U%d_%d" % (ci, bi)] = pl[ci][bi].numpy()
+        out["it1_Y%d" % ci] = ptl[d.chrom].numpy()
+    out.update(it1_exU=np.asarray(exU).ravel(), it1_exV=float(exV), it1_tnorm=np.asarray(tn).ravel(),
+               it1_E=m.meta_embedding.numpy())
+    # the fit loop from the same state
+    m2, loc, res = run_fit(w, ds, n_iter, st0, w.dim1)
+    out["fit_rec_total"] = np.asarray(loc["rec_errors_total"], dtype=np.float64)
+    out["fit_rec_block"] = np.stack([np.asarray(x).ravel() for x in loc["rec_errors"]])
+    out.update(state_arrays("fit", snapshot(m2), w.chrom_names))
+    out["fit_E_transform"] = res[1][3].numpy()
+    m3, loc1, _ = run_fit(w, ds, 1, st0, w.dim1)
+    out.update(state_arrays("one", snapshot(m3), w.chrom_names))
+    out["one_rec_total"] = np.asarray(loc1["rec_errors_total"], dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, name), **out)
+    print(name, "rec trajectory", out["fit_rec_total"])
+
+
+if __name__ == "__main__":
+    make_rwr_tiles()
+    make_parafac()
+    make_als("als_small.npz", "small", 25, 40, 4, seed=3)
+    make_als("c1_fit.npz", "c1", None, None, 10, seed=1, save_U=False)

@@ -1,0 +1,84 @@
+"""Pins the oracle (CPU restatement) against the reference's own outputs (tests/golden)."""
+import numpy as np
+import pytest
+
+from oracle import fh_oracle as O
+import golden_io as G
+
+
+def test_tile_layout_and_densify_match_reference_fetch():
+    z = G.load("rwr_tiles.npz")
+    datas = G.chrom_datas(z, O)
+    for k in range(int(z["n_tiles"])):
+        ci, bi, cj, s0, s1, _ = z["t%d_meta" % k]
+        d = datas[ci]
+        bb = d.layout()[bi]
+        assert (bb.local.start, bb.local.stop) == (s0, s1)
+        x = d.tile(bb, d.cells()[cj], np.float32)
+        np.testing.assert_array_equal(x, z["t%d_x" % k])
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.float32, 2e-6), (np.float64, 1e-5)])
+def test_partial_rwr_matches_reference(dtype, tol):
+    z = G.load("rwr_tiles.npz")
+    for k in range(int(z["n_tiles"])):
+        _, _, _, s0, s1, n_auto = z["t%d_meta" % k]
+        x = z["t%d_x" % k].astype(dtype)
+        y3, _ = O.partial_rwr(x.copy(), s0, s1, force_rwr_epochs=3)
+        assert O.rel_err(y3, z["t%d_y3" % k]) < tol
+        ya, na = O.partial_rwr(x.copy(), s0, s1, force_rwr_epochs=-1, final_transpose=False,
+                               return_rwr_iter=True)
+        assert na == n_auto
+        assert O.rel_err(ya, z["t%d_yauto" % k]) < tol
+
+
+@pytest.mark.parametrize("n", [1, 3])
+def test_parafac_matches_reference(n):
+    z = G.load("parafac.npz")
+    f, ln, lx = O.parafac(z["X"], 6, n_iter_max=n, init=[z["A0"], z["B0"], z["D0"]])
+    for a, name in zip(f, "ABD"):
+        assert O.rel_err(a, z["%s%d" % (name, n)]) < 1e-4
+    assert abs(ln - float(z["ln%d" % n])) / abs(float(z["ln%d" % n])) < 1e-5
+    assert abs(lx - float(z["lx%d" % n])) / abs(float(z["lx%d" % n])) < 1e-5
+
+
+def _oracle_from(z, prefix="init", dtype=np.float64):
+    datas = G.chrom_datas(z, O)
+    A, B, D, E, n_i = G.state(z, prefix, len(datas))
+    return O.ALSOracle(datas, int(z["rank"]), A, B, D, E, n_i, dtype=dtype)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_one_update_matches_reference(dtype):
+    """One update_meta_embedding_interactions call from the reference's init state.
+    Well-conditioned outputs agree to 1e-5; the polar factors U agree to the reference's
+    own fp32 SVD error, which grows with the conditioning of the per-bin matrices."""
+    z = G.load("als_small.npz")
+    orc = _oracle_from(z, dtype=dtype)
+    U, Y, exU, exV, tn = orc.update(first_iter=True)
+    assert O.rel_err(tn, z["it1_tnorm"]) < 1e-5
+    assert O.rel_err(exU, z["it1_exU"]) < 1e-5
+    assert abs(exV - float(z["it1_exV"])) / abs(float(z["it1_exV"])) < 1e-5
+    errs = [O.rel_err(U[ci][bi], z["it1_U%d_%d" % (ci, bi)])
+            for ci in range(len(U)) for bi in range(len(U[ci]))]
+    assert np.median(errs) < 1e-4 and max(errs) < 1e-2
+    assert O.rel_err(orc.E, z["it1_E"]) < 1e-4
+    for ci in range(len(Y)):
+        assert O.rel_err(Y[ci], z["it1_Y%d" % ci]) < 1e-3
+
+
+# rtol of the trajectory: rec = sqrt(|X|^2 + |core|^2 - 2<X, core>) / |X| cancels ~45x at
+# rec ~ 0.2, and the reference forms |core|^2 in fp32 with a 1.5e-5 relative error on c1
+# (its chr1 value 1102.7616 against 1102.7785 exactly), so its own trajectory is off by
+# ~1e-3 there.  The fp32 and fp64 restatements agree with each other to 2e-6.
+@pytest.mark.parametrize("fixture,n_iter,rtol", [("als_small.npz", 4, 1e-4), ("c1_fit.npz", 10, 2e-3)])
+def test_fit_trajectory_matches_reference(fixture, n_iter, rtol):
+    z = G.load(fixture)
+    orc = _oracle_from(z)
+    orc.fit(n_iter)
+    traj = np.asarray(orc.rec_errors_total)
+    np.testing.assert_allclose(traj, z["fit_rec_total"], rtol=rtol)
+    n = len(orc.datas)
+    A, B, D, E, _ = G.state(z, "fit", n)
+    # the final embedding agrees after orthogonal Procrustes alignment
+    assert O.rel_err(O.procrustes_align(orc.E, E), E) < 1e-3
