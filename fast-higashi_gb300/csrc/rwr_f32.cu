@@ -1,0 +1,365 @@
+// Partial random walk with restart, fp32 CUDA-core path (one CTA per (bin batch, cell)).
+//
+// Reference: fasthigashi/partial_rwr.py:75-138 (do_conv=False, do_col=False) fed by
+// densify_jit (fasthigashi/sparse_for_schic.py:279-320).
+//
+// The tile A (b x n, the cell's rows of one bin batch over its compact columns) is densified
+// straight into shared memory from the cell's packed segment and floored at 1e-8.  Then:
+//   S2 = A A^T with a zero diagonal; S1 = A[:, s0:s0+b]
+//   L  = 0.75 * S1 / colsum(S1) + 0.25 * S2 / colsum(S2);  zero columns get a unit diagonal
+//   P  = L / colsum(L)
+// The reference iterates Q_{t+1} = 0.5 Q_t P + 0.5 I from Q_0 = I and returns Q_n A.  Every
+// Q_t is a polynomial in P, so Q_t P = P Q_t, and Z_t = Q_t A obeys Z_{t+1} = 0.5 P Z_t +
+// 0.5 A.  The kernel runs that recurrence in place (P^T and Z resident in shared memory,
+// the product accumulated in registers), which needs no b x b Q buffer and no final Q A
+// product.  The +0.5 A term is the constant 0.5e-8 floor plus the segment's entries.
+//
+// The auto-stop variant (partial_rwr.py:99-123) runs the same recurrence with A = I, which
+// is Q_t itself, and records ||Q_t - Q_{t+1}||_F per epoch.
+#include "fh_common.cuh"
+
+namespace fh {
+
+constexpr int kRwrThreads = 256;
+constexpr float kFloor = 1e-8f;  // densify floor, sparse_for_schic.py:320
+constexpr float kEps = 1e-15f;   // column-sum guard, partial_rwr.py:90,91,111
+
+enum RwrSource { kSparse = 0, kDense = 1 };
+enum RwrMode { kOutput = 0, kDeltas = 1 };
+
+struct RwrArgs {
+  const fh_tile* tiles;
+  int n_cells;
+  const uint2* entries;
+  const int64_t* offsets;
+  const float* dense;  // dense source: [n_cells][rows][width]
+  int d_rows, d_width, d_s0, d_epochs;
+  int max_rows, max_width;  // extents the shared-memory carve-out was sized for
+  float* out;
+  int64_t cell_stride;
+  double* sumsq;
+  float* deltas;
+  int cap;
+  int* status;
+};
+
+__host__ __device__ inline int rwr_ldp(int b) { return (b + 3) & ~3; }
+
+__host__ __device__ inline size_t rwr_smem_bytes(int b, int n) {
+  const int ldp = rwr_ldp(b), ldz = lds_stride_odd(n > b ? n : b);
+  return (size_t)(b * ldp + b * ldz + 4 * kMaxBinRows) * sizeof(float);
+}
+
+// acc[u][v] += sum_k Z[k][ty + 16u] * Pt[k][tx + 16v]  ==  (P Z)[tx+16v][ty+16u]
+template <int MAXU>
+__device__ __forceinline__ void pz_product(const float* __restrict__ Z, int ldz,
+                                           const float* __restrict__ Pt, int ldp, int b,
+                                           int ty, int tx, float (&acc)[MAXU][8]) {
+#pragma unroll
+  for (int u = 0; u < MAXU; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+  for (int k = 0; k < b; ++k) {
+    float zk[MAXU], pk[8];
+    const float* zr = Z + k * ldz + ty;
+    const float* pr = Pt + k * ldp + tx;
+#pragma unroll
+    for (int u = 0; u < MAXU; ++u) zk[u] = zr[16 * u];
+#pragma unroll
+    for (int v = 0; v < 8; ++v) pk[v] = pr[16 * v];
+#pragma unroll
+    for (int u = 0; u < MAXU; ++u)
+#pragma unroll
+      for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(zk[u], pk[v], acc[u][v]);
+  }
+}
+
+template <int MAXU, int SRC, int MODE>
+__global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ double dred[32];
+  __shared__ float fred[32];
+  const int c = blockIdx.x;
+  const int t = blockIdx.y;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+
+  int b, n, s0, epochs;
+  int64_t xoff = 0;
+  if (SRC == kSparse) {
+    const fh_tile T = a.tiles[t];
+    b = T.rows; n = T.width; s0 = T.s0; epochs = T.n_rwr; xoff = T.xoff;
+    if (b <= 0 || b > a.max_rows || n < b || n > a.max_width || s0 < 0 || s0 + b > n ||
+        epochs < 0) {
+      if (tid == 0) set_status(a.status, FH_ERR_ARG);
+      return;
+    }
+  } else {
+    b = a.d_rows; n = a.d_width; s0 = a.d_s0; epochs = a.d_epochs;
+  }
+  if (MODE == kDeltas) epochs = a.cap;
+  const int ldp = rwr_ldp(b);
+  const int ldz = lds_stride_odd(n > b ? n : b);
+  float* Pt = smem;               // b x ldp : S2, then L, then P^T
+  float* Z = smem + b * ldp;      // b x ldz : A, then Z_t (or Q_t in delta mode)
+  float* cs1 = Z + b * ldz;       // column sums
+  float* cs2 = cs1 + kMaxBinRows;
+  float* csl = cs2 + kMaxBinRows;
+
+  int64_t e0 = 0, e1 = 0;
+  const float* xin = nullptr;
+  if (SRC == kSparse) {
+    e0 = a.offsets[(int64_t)t * a.n_cells + c];
+    e1 = a.offsets[(int64_t)t * a.n_cells + c + 1];
+    for (int i = tid; i < b * ldz; i += kRwrThreads) Z[i] = 0.f;
+    __syncthreads();
+    for (int64_t e = e0 + tid; e < e1; e += kRwrThreads) {
+      const uint2 en = a.entries[e];
+      Z[(en.x & 0xffff) * ldz + (en.x >> 16)] = __uint_as_float(en.y);
+    }
+    __syncthreads();
+    for (int i = tid; i < b * n; i += kRwrThreads) {
+      float* z = Z + (i / n) * ldz + (i % n);
+      *z = fmaxf(*z, kFloor);
+    }
+  } else {
+    xin = a.dense + (int64_t)c * b * n;
+    for (int i = tid; i < b * n; i += kRwrThreads) Z[(i / n) * ldz + (i % n)] = xin[i];
+  }
+  __syncthreads();
+
+  // ---- S2 = Z Z^T (b x b), diagonal zeroed (partial_rwr.py:85-87)
+  {
+    float acc[8][8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+    const float* zp[8];
+    const float* zq[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      zp[u] = Z + min(ty + 16 * u, b - 1) * ldz;
+      zq[u] = Z + min(tx + 16 * u, b - 1) * ldz;
+    }
+    for (int k = 0; k < n; ++k) {
+      float ap[8], aq[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) { ap[u] = zp[u][k]; aq[u] = zq[u][k]; }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(ap[u], aq[v], acc[u][v]);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        const int p = ty + 16 * u, q = tx + 16 * v;
+        if (p < b && q < b) Pt[p * ldp + q] = (p == q) ? 0.f : acc[u][v];
+      }
+  }
+  __syncthreads();
+
+  // ---- column sums of S2 and of the first-order block S1 = Z[:, s0:s0+b]
+  if (tid < b) {
+    float s = 0.f;
+    for (int p = 0; p < b; ++p) s += Pt[p * ldp + tid];
+    cs2[tid] = s;
+  } else if (tid >= 128 && tid - 128 < b) {
+    const int q = tid - 128;
+    float s = 0.f;
+    for (int p = 0; p < b; ++p) s += Z[p * ldz + s0 + q];
+    cs1[q] = s;
+  }
+  __syncthreads();
+  // ---- L = (S1 / (cs1 + eps)) * 0.75 + (S2 / (cs2 + eps)) * 0.25   (partial_rwr.py:90-93)
+  for (int i = tid; i < b * b; i += kRwrThreads) {
+    const int p = i / b, q = i % b;
+    const float l1 = (Z[p * ldz + s0 + q] / (cs1[q] + kEps)) * 0.75f;
+    const float l2 = (Pt[p * ldp + q] / (cs2[q] + kEps)) * 0.25f;
+    Pt[p * ldp + q] = l1 + l2;
+  }
+  __syncthreads();
+  // ---- zero columns get a unit diagonal (:96-97); P = L / (colsum(L) + eps) (:111)
+  if (tid < b) {
+    float s = 0.f;
+    for (int p = 0; p < b; ++p) s += Pt[p * ldp + tid];
+    if (s == 0.f) {
+      Pt[tid * ldp + tid] += 1.f;
+      s = 0.f;
+      for (int p = 0; p < b; ++p) s += Pt[p * ldp + tid];
+    }
+    csl[tid] = s;
+  }
+  __syncthreads();
+  // P stored transposed in place: Pt[q][p] = P[p][q] = L[p][q] / (csl[q] + eps)
+  for (int i = tid; i < b * b; i += kRwrThreads) {
+    const int p = i / b, q = i % b;
+    if (p < q) {
+      const float lpq = Pt[p * ldp + q], lqp = Pt[q * ldp + p];
+      Pt[q * ldp + p] = lpq / (csl[q] + kEps);
+      Pt[p * ldp + q] = lqp / (csl[p] + kEps);
+    } else if (p == q) {
+      Pt[p * ldp + p] = Pt[p * ldp + p] / (csl[p] + kEps);
+    }
+  }
+  __syncthreads();
+
+  int zw = n;  // columns of the recurrence state
+  if (MODE == kDeltas) {
+    zw = b;    // Q_0 = I
+    for (int i = tid; i < b * b; i += kRwrThreads) Z[(i / b) * ldz + (i % b)] = (i / b == i % b);
+    __syncthreads();
+  }
+
+  // ---- Z_{t+1} = 0.5 P Z_t + 0.5 A   (Q_{t+1} = 0.5 P Q_t + 0.5 I in delta mode)
+  for (int ep = 0; ep < epochs; ++ep) {
+    float acc[MAXU][8];
+    pz_product<MAXU>(Z, ldz, Pt, ldp, b, ty, tx, acc);
+    float d2 = 0.f;
+    if (MODE == kDeltas) {
+#pragma unroll
+      for (int u = 0; u < MAXU; ++u)
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+          const int i = ty + 16 * u, j = tx + 16 * v;
+          if (i < zw && j < b) {
+            const float nv = 0.5f * acc[u][v] + (i == j ? 0.5f : 0.f);
+            const float dd = Z[j * ldz + i] - nv;
+            d2 = fmaf(dd, dd, d2);
+          }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < MAXU; ++u)
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        const int i = ty + 16 * u, j = tx + 16 * v;
+        if (i < zw && j < b) {
+          float base;
+          if (MODE == kDeltas) base = (i == j) ? 0.5f : 0.f;
+          else if (SRC == kSparse) base = 0.5f * kFloor;
+          else base = 0.5f * xin[j * n + i];
+          Z[j * ldz + i] = fmaf(0.5f, acc[u][v], base);
+        }
+      }
+    if (MODE == kDeltas) {
+      const float s = block_sum<float>(d2, fred);
+      if (tid == 0) a.deltas[((int64_t)t * a.n_cells + c) * a.cap + ep] = sqrtf(s);
+    }
+    __syncthreads();
+    if (MODE == kOutput && SRC == kSparse) {
+      for (int64_t e = e0 + tid; e < e1; e += kRwrThreads) {
+        const uint2 en = a.entries[e];
+        const float v = __uint_as_float(en.y);
+        if (v > kFloor) Z[(en.x & 0xffff) * ldz + (en.x >> 16)] += 0.5f * (v - kFloor);
+      }
+      __syncthreads();
+    }
+  }
+
+  if (MODE == kOutput) {
+    double ss = 0.0;
+    float* o = a.out + (int64_t)c * a.cell_stride + xoff;
+    for (int i = tid; i < b * n; i += kRwrThreads) {
+      const float v = Z[(i / n) * ldz + (i % n)];
+      o[i] = v;
+      ss += (double)v * v;
+    }
+    if (a.sumsq) {
+      ss = block_sum<double>(ss, dred);
+      if (tid == 0) a.sumsq[(int64_t)t * a.n_cells + c] = ss;
+    }
+  }
+}
+
+template <int U, int SRC, int MODE>
+static int launch_rwr_u(const RwrArgs& a, dim3 grid, size_t smem, cudaStream_t s) {
+  if constexpr (MODE == kDeltas && U != 8) {
+    return FH_ERR_UNSUPPORTED;  // the delta recurrence is b x b, b <= 128
+  } else {
+    auto k = rwr_f32_kernel<U, SRC, MODE>;
+    if (ensure_smem((const void*)k, smem))
+      return FH_ERR_LAUNCH;
+    k<<<grid, kRwrThreads, smem, s>>>(a);
+    FH_CHECK_LAUNCH();
+    return FH_OK;
+  }
+}
+
+template <int SRC, int MODE>
+static int launch_rwr(const RwrArgs& a, int n_tiles, int max_rows, int max_width,
+                      cudaStream_t s) {
+  if (max_rows > kMaxBinRows || max_rows <= 0) return FH_ERR_UNSUPPORTED;
+  const int w = MODE == kDeltas ? (max_width > max_rows ? max_width : max_rows) : max_width;
+  if (w > kMaxWidth) return FH_ERR_UNSUPPORTED;
+  const size_t smem = rwr_smem_bytes(max_rows, w);
+  if (smem > 227 * 1024) return FH_ERR_UNSUPPORTED;
+  dim3 grid(a.n_cells, n_tiles);
+  const int zw = MODE == kDeltas ? max_rows : max_width;
+  if (zw <= 128) return launch_rwr_u<8, SRC, MODE>(a, grid, smem, s);
+  if (zw <= 192) return launch_rwr_u<12, SRC, MODE>(a, grid, smem, s);
+  if (zw <= 256) return launch_rwr_u<16, SRC, MODE>(a, grid, smem, s);
+  return launch_rwr_u<20, SRC, MODE>(a, grid, smem, s);
+}
+
+}  // namespace fh
+
+using namespace fh;
+
+extern "C" int fh_rwr_tiles_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                                int32_t mr, int32_t mw, const fh_entry* entries,
+                                const int64_t* offsets, float* out, int64_t cell_stride,
+                                double* sumsq, int* status, void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !offsets || !out || mr <= 0 || mw < mr)
+    return FH_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  RwrArgs a{};
+  a.max_rows = mr; a.max_width = mw;
+  a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
+  a.offsets = offsets; a.out = out; a.cell_stride = cell_stride; a.sumsq = sumsq;
+  a.status = status;
+  return launch_rwr<kSparse, kOutput>(a, n_tiles, mr, mw, s);
+}
+
+extern "C" int fh_rwr_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width,
+                                int32_t s0, int32_t n_epochs, float* out, int* status,
+                                void* stream) {
+  if (!x || !out || n_cells <= 0 || rows <= 0 || width < rows || s0 < 0 ||
+      s0 + rows > width || n_epochs < 0)
+    return FH_ERR_ARG;
+  RwrArgs a{};
+  a.n_cells = n_cells; a.dense = x; a.d_rows = rows; a.d_width = width; a.d_s0 = s0;
+  a.max_rows = rows; a.max_width = width;
+  a.d_epochs = n_epochs; a.out = out; a.cell_stride = (int64_t)rows * width; a.status = status;
+  return launch_rwr<kDense, kOutput>(a, 1, rows, width, (cudaStream_t)stream);
+}
+
+extern "C" int fh_rwr_dense_deltas(const float* x, int32_t n_cells, int32_t rows, int32_t width,
+                                   int32_t s0, int32_t cap, float* deltas, int* status,
+                                   void* stream) {
+  if (!x || !deltas || n_cells <= 0 || rows <= 0 || width < rows || s0 < 0 ||
+      s0 + rows > width || cap <= 0)
+    return FH_ERR_ARG;
+  RwrArgs a{};
+  a.n_cells = n_cells; a.dense = x; a.d_rows = rows; a.d_width = width; a.d_s0 = s0;
+  a.max_rows = rows; a.max_width = width;
+  a.deltas = deltas; a.cap = cap; a.status = status;
+  return launch_rwr<kDense, kDeltas>(a, 1, rows, width, (cudaStream_t)stream);
+}
+
+extern "C" int fh_rwr_tiles_deltas(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                                   int32_t mr, int32_t mw, const fh_entry* entries,
+                                   const int64_t* offsets, int32_t cap, float* deltas,
+                                   int* status, void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !offsets || !deltas || cap <= 0 || mr <= 0 ||
+      mw < mr)
+    return FH_ERR_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  RwrArgs a{};
+  a.max_rows = mr; a.max_width = mw;
+  a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
+  a.offsets = offsets; a.deltas = deltas; a.cap = cap; a.status = status;
+  return launch_rwr<kSparse, kDeltas>(a, n_tiles, mr, mw, s);
+}

@@ -1,0 +1,141 @@
+"""ctypes binding of libfhgb300.so (the C ABI declared in include/fhgb300.h).
+
+The library is the only compute path: importing works anywhere, but every call raises
+``FHError`` when the shared object is missing or no CUDA device is usable.  There is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libfhgb300.so")
+
+FH_OK = 0
+STATUS_NAMES = {0: "FH_OK", 1: "FH_ERR_ARG", 2: "FH_ERR_UNSUPPORTED", 3: "FH_ERR_NONFINITE",
+                4: "FH_ERR_ILLCOND", 5: "FH_ERR_LAUNCH", 6: "FH_ERR_INDEX", 7: "FH_ERR_TIMEOUT"}
+
+
+class FHError(RuntimeError):
+    def __init__(self, func, status, msg=""):
+        self.status = status
+        super().__init__("%s failed: %s (%d)%s" % (func, STATUS_NAMES.get(status, "?"), status,
+                                                   (": " + msg) if msg else ""))
+
+
+class fh_tile(C.Structure):
+    _fields_ = [("chrom", C.c_int32), ("row0", C.c_int32), ("rows", C.c_int32),
+                ("width", C.c_int32), ("shift", C.c_int32), ("s0", C.c_int32),
+                ("rank", C.c_int32), ("n_rwr", C.c_int32), ("xoff", C.c_int64),
+                ("brow0", C.c_int64), ("uoff", C.c_int64)]
+
+
+TILE_DTYPE = np.dtype([("chrom", "<i4"), ("row0", "<i4"), ("rows", "<i4"), ("width", "<i4"),
+                       ("shift", "<i4"), ("s0", "<i4"), ("rank", "<i4"), ("n_rwr", "<i4"),
+                       ("xoff", "<i8"), ("brow0", "<i8"), ("uoff", "<i8")])
+assert TILE_DTYPE.itemsize == C.sizeof(fh_tile) == 56
+
+P, I32, I64, SZ, D = C.c_void_p, C.c_int32, C.c_int64, C.c_size_t, C.c_double
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "fh_status_string": (C.c_char_p, [C.c_int]),
+    "fh_version": (C.c_int, []),
+    "fh_contacts_count": (C.c_int, [P, P, P, I64, I32, P, I32, I32, I32, P, P, P]),
+    "fh_scan_workspace": (SZ, [I64]),
+    "fh_exclusive_scan": (C.c_int, [P, I64, P, P, SZ, P]),
+    "fh_contacts_scatter": (C.c_int, [P, P, P, P, I64, I32, P, I32, I32, I32, P, P, P, P]),
+    "fh_densify_tile": (C.c_int, [P, I32, I32, I32, I32, P, P, P, P]),
+    "fh_rwr_tiles_f32": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, P, P, P]),
+    "fh_rwr_dense_f32": (C.c_int, [P, I32, I32, I32, I32, I32, P, P, P]),
+    "fh_rwr_dense_deltas": (C.c_int, [P, I32, I32, I32, I32, I32, P, P, P]),
+    "fh_rwr_tiles_deltas": (C.c_int, [P, I32, I32, I32, I32, P, P, I32, P, P, P]),
+    "fh_xe_f32": (C.c_int, [P, I64, I32, I64, P, I32, P, P]),
+    "fh_xg_splits": (C.c_int, [I32, I64]),
+    "fh_xg_f32": (C.c_int, [P, I64, I32, I64, P, I32, I32, P, P, P]),
+    "fh_project_y_f32": (C.c_int, [P, P, I64, P, P, I32, P, I32, P]),
+    "fh_procrustes_smem": (SZ, [I32, I32, I32]),
+    "fh_procrustes_f32": (C.c_int, [P, P, I64, I32, I32, P, P, I32, P, P, I32, I32, I32, P, P,
+                                    P, P, P]),
+    "fh_projection_g_f32": (C.c_int, [P, P, I64, I32, I32, P, I32, P, P, I32, I32, I32, P, P,
+                                      P]),
+    "fh_polar_f32": (C.c_int, [P, I64, I32, I32, P, P, P, P]),
+    "fh_polar_svals_f32": (C.c_int, [P, P, I64, I32, I32, P, P]),
+    "fh_meta_polar_workspace": (SZ, [I32, I32]),
+    "fh_meta_polar": (C.c_int, [P, I32, I32, I32, P, P, P, SZ, P, P]),
+    "fh_cp_workspace": (SZ, [I32, I32, I32, I32]),
+    "fh_cp_als": (C.c_int, [I32, I32, P, P, P, P, P, I32, I32, I32, I32, I32, P, P, P, SZ, P,
+                            P]),
+    "fh_core_norm": (C.c_int, [I32, I32, P, P, P, P, P, I32, I32, I32, I32, P, P, SZ, P, P]),
+}
+
+# kernels each entry point launches (the count the benchmark reports as gpu_launches)
+_KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_contacts_scatter": 1,
+            "fh_densify_tile": 1, "fh_rwr_tiles_f32": 1, "fh_rwr_dense_f32": 1,
+            "fh_rwr_dense_deltas": 1, "fh_rwr_tiles_deltas": 1, "fh_xe_f32": 1, "fh_xg_f32": 2,
+            "fh_project_y_f32": 1, "fh_procrustes_f32": 1, "fh_projection_g_f32": 1,
+            "fh_polar_f32": 1, "fh_polar_svals_f32": 1, "fh_meta_polar": 4, "fh_core_norm": 2}
+launches = 0
+
+
+def _kernel_count(name, args):
+    if name == "fh_cp_als":
+        n_iter = args[11]
+        return 2 if n_iter == 0 else 3 + 5 * n_iter
+    return _KERNELS.get(name, 0)
+
+
+_lib = None
+
+
+def load():
+    """Loads the shared library (building nothing).  Raises FHError if it is absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FHError("load", 5, "%s is missing; run fh_gb300.build.build()" % LIB_PATH)
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def exported_symbols():
+    return sorted(SIGNATURES)
+
+
+def call(name, *args):
+    """Calls an fh_status-returning entry point and raises FHError on failure."""
+    global launches
+    f = getattr(load(), name)
+    st = f(*args)
+    launches += _kernel_count(name, args)
+    if st != FH_OK:
+        raise FHError(name, st, load().fh_status_string(st).decode())
+    return st
+
+
+def value(name, *args):
+    """Calls an entry point that returns a plain value (a size or a count)."""
+    return getattr(load(), name)(*args)
+
+
+def ptr(t):
+    """Device (or host) address of a torch tensor / numpy array, or None."""
+    if t is None:
+        return None
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream

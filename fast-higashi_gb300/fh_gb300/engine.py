@@ -1,0 +1,312 @@
+"""Device-resident fit engine: contact build, RWR once, then the ALS sweep as kernel launches.
+
+Layout in HBM (all on one GPU):
+  entries   packed contacts, one segment per (bin batch, cell)           8 B / contact
+  X         RWR output of every cell: X[cell][band row]                   4 B / element
+            band row = tile.xoff + i * width + j; the row stride is padded to 128
+  W, Gt     [band row][rp]: X^T E and the projection rows U M^T
+  U         projections, tile-major (rows, width, r) as the reference's projection_list
+  Y         [bin row][ld][rp] projected tensors
+  A         [bin row][ld];  B [chrom][ld][ld];  D [chrom][rp][ld];  E [cell][rp]
+Per ALS iteration (parafac2_intergrative.py:635-737): procrustes (per bin row polar) ->
+X G^T (SVD_term) -> meta polar (E) -> X^T E (W) -> Y -> CP-ALS sweeps.  Loss scalars go
+into a device history and are turned into the reference's rec_error values on the host.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib
+from .sparse_for_schic import ContactStore, tile_table
+
+
+def _pad_rank(R):
+    for p in (16, 32, 64, 128):
+        if R <= p:
+            return p
+    raise _lib.FHError("engine", 2, "rank %d > 128" % R)
+
+
+class FitEngine:
+    def __init__(self, schic, rank, chrom2size, n_i, device, do_rwr=True, stream=None):
+        import torch
+        self.torch = torch
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise _lib.FHError("FitEngine", 2, "the fit runs on a CUDA device only")
+        _lib.load()
+        self.schic = schic
+        self.R = int(rank)
+        self.rp = _pad_rank(self.R)
+        self.ld = self.rp
+        self.C = schic[0].num_cell
+        self.Ct = schic[0].total_cell_num
+        for d in schic:
+            if d.num_cell != self.C or d.total_cell_num != self.Ct:
+                raise _lib.FHError("FitEngine", 1, "datasets disagree on the cell count")
+        self.names = []
+        for d in schic:
+            if d.chrom not in self.names:
+                self.names.append(d.chrom)
+        if len(self.names) != len(schic):
+            raise _lib.FHError("FitEngine", 2, "one dataset per chromosome (single resolution)")
+        self.chrom_index = [self.names.index(d.chrom) for d in schic]
+        self.ranks = [int(chrom2size[d.chrom]) for d in schic]
+        if max(self.ranks) > 64 or self.R > 64:
+            raise _lib.FHError("FitEngine", 2, "ranks above 64 are not supported yet")
+        self.do_rwr = do_rwr
+        self.n_rwr = [int(v) if do_rwr else 0 for v in (n_i if n_i is not None else [0] * len(schic))]
+        order = sorted(range(len(schic)), key=lambda k: self.chrom_index[k])
+        self.tiles, self.tile_base = tile_table(schic, self.chrom_index, self.ranks, self.n_rwr, order)
+        t = self.tiles
+        self.n_tiles = len(t)
+        self.rows = int((t["rows"] * t["width"]).sum())
+        self.ldx = int(math.ceil(self.rows / 128) * 128)
+        self.nb = int(t["rows"].sum())
+        self.max_rows = int(t["rows"].max())
+        self.max_width = int(t["width"].max())
+        self.max_rank = int(t["rank"].max())
+        self.u_size = int((t["rows"] * t["width"] * t["rank"]).sum())
+        # bin rows of each dataset and chromosome
+        self.ds_rows = []
+        for k, d in enumerate(schic):
+            t0 = self.tile_base[k]
+            b0 = int(t["brow0"][t0])
+            self.ds_rows.append(slice(b0, b0 + d.num_bin))
+        row_tile = np.repeat(np.arange(self.n_tiles, dtype=np.int32), t["rows"])
+        self.stream = stream
+        dev = self.device
+        f32, f64, i32 = torch.float32, torch.float64, torch.int32
+        self.row_tile = torch.from_numpy(row_tile).to(dev)
+        self.status = torch.zeros(1, dtype=i32, device=dev)
+        # ---- contacts and RWR (once)
+        self.store = ContactStore(schic, dev, self.tiles, self.tile_base, stream)
+        self.tiles_dev = self.store.tiles_dev
+        self.X = torch.zeros((self.Ct, self.ldx), dtype=f32, device=dev)
+        self.sumsq = torch.zeros(self.n_tiles * self.Ct, dtype=f64, device=dev)
+        if n_i is not None:
+            self.run_rwr()
+        # ---- factor state and work buffers
+        nchrom = len(self.names)
+        self.A = torch.zeros((self.nb, self.ld), dtype=f32, device=dev)
+        self.B = torch.zeros((nchrom, self.ld, self.ld), dtype=f32, device=dev)
+        self.D = torch.zeros((nchrom, self.rp, self.ld), dtype=f32, device=dev)
+        self.E = torch.zeros((self.C, self.rp), dtype=f32, device=dev)
+        self.W = torch.zeros((self.ldx, self.rp), dtype=f32, device=dev)
+        self.Gt = torch.zeros((self.ldx, self.rp), dtype=f32, device=dev)
+        self.U = torch.zeros(max(self.u_size, 1), dtype=f32, device=dev)
+        self.Y = torch.zeros((self.nb, self.ld, self.rp), dtype=f32, device=dev)
+        self.S = torch.zeros((self.Ct, self.rp), dtype=f32, device=dev)
+        self.splits = _lib.value("fh_xg_splits", self.Ct, self.rows)
+        self.partial = torch.empty((self.splits, self.Ct, self.rp), dtype=f32, device=dev)
+        self.ssum = torch.zeros(self.nb, dtype=f64, device=dev)
+        self.meta_ssum = torch.zeros(1, dtype=f64, device=dev)
+        self.core = torch.zeros(nchrom, dtype=f64, device=dev)
+        mw = _lib.value("fh_meta_polar_workspace", self.Ct, self.R)
+        self.meta_ws = torch.empty(mw, dtype=torch.uint8, device=dev)
+        # CP-ALS chunk tables (<= 8 rows, inside one chromosome)
+        c_row0, c_nbin, c_rank, c_chunk0, c_nchunk = [], [], [], [], []
+        k_chrom, k_row0, k_nrow = [], [], []
+        for ci, name in enumerate(self.names):
+            k = self.chrom_index.index(ci)
+            rs = self.ds_rows[k]
+            c_row0.append(rs.start); c_nbin.append(rs.stop - rs.start); c_rank.append(self.ranks[k])
+            c_chunk0.append(len(k_chrom))
+            for r0 in range(rs.start, rs.stop, 8):
+                k_chrom.append(ci); k_row0.append(r0); k_nrow.append(min(8, rs.stop - r0))
+            c_nchunk.append(len(k_chrom) - c_chunk0[-1])
+        self.nchunks = len(k_chrom)
+        meta = np.array(c_row0 + c_nbin + c_rank + c_chunk0 + c_nchunk + k_chrom + k_row0 + k_nrow,
+                        dtype=np.int32)
+        self.cp_meta = torch.from_numpy(meta).to(dev)
+        cw = _lib.value("fh_cp_workspace", nchrom, self.nchunks, self.ld, self.rp)
+        self.cp_ws = torch.empty(cw, dtype=torch.uint8, device=dev)
+        self.history = []
+
+    # ------------------------------------------------------------------ helpers
+    def sp(self):
+        return _lib.stream_ptr(self.stream)
+
+    def check_status(self, what):
+        st = int(self.status.item())
+        if st:
+            self.status.zero_()
+            raise _lib.FHError(what, st)
+
+    def set_epochs(self, per_tile):
+        """Sets the RWR epoch count of every tile (force_rwr_epochs) and re-uploads the table."""
+        self.tiles["n_rwr"] = np.asarray(per_tile, dtype=np.int32)
+        self.tiles_dev.copy_(self.torch.from_numpy(self.tiles.view(np.uint8).copy()))
+
+    def set_n_i(self, n_i):
+        self.n_rwr = [int(v) if self.do_rwr else 0 for v in n_i]
+        per_tile = np.zeros(self.n_tiles, dtype=np.int32)
+        for k, d in enumerate(self.schic):
+            per_tile[self.tile_base[k]:self.tile_base[k] + d.num_bin_batch] = self.n_rwr[k]
+        self.set_epochs(per_tile)
+
+    def auto_deltas(self, cap):
+        """||Q_e - Q_{e+1}||_F for e < cap for every (tile, good cell) (partial_rwr.py:99-123)."""
+        P = _lib.ptr
+        out = self.torch.zeros((self.n_tiles, self.Ct, cap), dtype=self.torch.float32,
+                               device=self.device)
+        _lib.call("fh_rwr_tiles_deltas", P(self.tiles_dev), self.n_tiles, self.Ct, self.max_rows,
+                  self.max_width, P(self.store.entries), P(self.store.offsets), cap, P(out),
+                  P(self.status), self.sp())
+        return out[:, :self.C]
+
+    def run_rwr(self):
+        P = _lib.ptr
+        _lib.call("fh_rwr_tiles_f32", P(self.tiles_dev), self.n_tiles, self.Ct, self.max_rows,
+                  self.max_width, P(self.store.entries), P(self.store.offsets), P(self.X),
+                  self.ldx, P(self.sumsq), P(self.status), self.sp())
+
+    def tensor_norms(self):
+        """||X||^2 per dataset over the good-QC cells (parafac2_intergrative.py:369)."""
+        s = self.sumsq.view(self.n_tiles, self.Ct)[:, :self.C].sum(1).cpu().numpy()
+        out = np.zeros(len(self.schic))
+        for k, d in enumerate(self.schic):
+            t0 = self.tile_base[k]
+            out[k] = s[t0:t0 + d.num_bin_batch].sum()
+        return out
+
+    # ------------------------------------------------------------------ state
+    def set_state(self, A_list, B_dict, D_dict, E):
+        """Loads factors (they may be views of this engine's own buffers)."""
+        torch = self.torch
+        dev, f32 = self.device, torch.float32
+        A_in = [torch.as_tensor(a, dtype=f32).to(dev).clone() for a in A_list]
+        B_in = {n: torch.as_tensor(B_dict[n], dtype=f32).to(dev).clone() for n in self.names}
+        D_in = {n: torch.as_tensor(D_dict[n], dtype=f32).to(dev).clone() for n in self.names}
+        E_in = torch.as_tensor(E, dtype=f32).to(dev).clone()
+        self.A.zero_(); self.B.zero_(); self.D.zero_(); self.E.zero_()
+        for k, d in enumerate(self.schic):
+            self.A[self.ds_rows[k], :self.ranks[k]] = A_in[k]
+        for ci, name in enumerate(self.names):
+            r = self.ranks[self.chrom_index.index(ci)]
+            self.B[ci, :r, :r] = B_in[name]
+            self.D[ci, :self.R, :r] = D_in[name]
+        self.E[:, :self.R] = E_in[:self.C]
+
+    def A_views(self):
+        return [self.A[self.ds_rows[k], :self.ranks[k]] for k in range(len(self.schic))]
+
+    def B_views(self):
+        return {n: self.B[ci, :self.ranks[self.chrom_index.index(ci)], :self.ranks[self.chrom_index.index(ci)]]
+                for ci, n in enumerate(self.names)}
+
+    def D_views(self):
+        return {n: self.D[ci, :self.R, :self.ranks[self.chrom_index.index(ci)]]
+                for ci, n in enumerate(self.names)}
+
+    def projection_views(self):
+        """U per dataset and bin batch as (b, n, r) tensors (projection_list)."""
+        out = []
+        for k, d in enumerate(self.schic):
+            lst = []
+            for bi in range(d.num_bin_batch):
+                t = self.tiles[self.tile_base[k] + bi]
+                n = int(t["rows"]) * int(t["width"]) * int(t["rank"])
+                lst.append(self.U[int(t["uoff"]):int(t["uoff"]) + n].view(int(t["rows"]), int(t["width"]), int(t["rank"])))
+            out.append(lst)
+        return out
+
+    def projected_views(self):
+        return {self.schic[k].chrom: self.Y[self.ds_rows[k], :self.ranks[k], :self.R]
+                for k in range(len(self.schic))}
+
+    # ------------------------------------------------------------------ kernels
+    def xe(self):
+        P = _lib.ptr
+        _lib.call("fh_xe_f32", P(self.X), self.ldx, self.C, self.rows, P(self.E), self.rp,
+                  P(self.W), self.sp())
+
+    def procrustes(self):
+        P = _lib.ptr
+        _lib.call("fh_procrustes_f32", P(self.tiles_dev), P(self.row_tile), self.nb,
+                  self.max_width, self.max_rank, P(self.W), P(self.A), self.ld, P(self.B),
+                  P(self.D), self.ld, self.R, self.rp, P(self.U), P(self.Gt), P(self.ssum),
+                  P(self.status), self.sp())
+
+    def xg(self, n_cells):
+        P = _lib.ptr
+        _lib.call("fh_xg_f32", P(self.X), self.ldx, n_cells, self.rows, P(self.Gt), self.rp,
+                  self.splits, P(self.partial), P(self.S), self.sp())
+
+    def meta_polar(self, n_cells, E_out):
+        P = _lib.ptr
+        _lib.call("fh_meta_polar", P(self.S), n_cells, self.R, self.rp, P(E_out),
+                  P(self.meta_ssum), P(self.meta_ws), self.meta_ws.numel(), P(self.status),
+                  self.sp())
+
+    def project_y(self):
+        P = _lib.ptr
+        _lib.call("fh_project_y_f32", P(self.tiles_dev), P(self.row_tile), self.nb, P(self.U),
+                  P(self.W), self.rp, P(self.Y), self.ld, self.sp())
+
+    def cp_als(self, n_iter):
+        P = _lib.ptr
+        _lib.call("fh_cp_als", len(self.names), self.nchunks, P(self.cp_meta), P(self.A),
+                  P(self.B), P(self.D), P(self.Y), self.ld, self.rp, self.R, self.ld, n_iter,
+                  P(self.core), None, P(self.cp_ws), self.cp_ws.numel(), P(self.status), self.sp())
+
+    # ------------------------------------------------------------------ ALS
+    def update(self, first):
+        """update_meta_embedding_interactions (parafac2_intergrative.py:304-540)."""
+        if first:
+            self.xe()
+        self.procrustes()
+        self.xg(self.C)
+        self.meta_polar(self.C, self.E)
+        self.xe()
+        self.project_y()
+
+    def iterate(self, first, n_iter_parafac, hist):
+        """One fit-loop iteration (parafac2_intergrative.py:635-706); hist receives the loss
+        scalars: per-bin-row sum(S), <E, SVD_term^T>, and the core norms before CP-ALS."""
+        self.update(first)
+        hist["ssum"].copy_(self.ssum)
+        hist["meta"].copy_(self.meta_ssum)
+        hist["core"].copy_(self.core)
+        self.cp_als(n_iter_parafac)
+
+    def core_norm(self):
+        P = _lib.ptr
+        _lib.call("fh_core_norm", len(self.names), self.nchunks, P(self.cp_meta), P(self.A),
+                  P(self.B), P(self.D), P(self.Y), self.ld, self.rp, self.R, self.ld,
+                  P(self.core), P(self.cp_ws), self.cp_ws.numel(), P(self.status), self.sp())
+
+    def new_history(self, n):
+        torch = self.torch
+        return [dict(ssum=torch.zeros(self.nb, dtype=torch.float64, device=self.device),
+                     meta=torch.zeros(1, dtype=torch.float64, device=self.device),
+                     core=torch.zeros(len(self.names), dtype=torch.float64, device=self.device))
+                for _ in range(n)]
+
+    def losses(self, hist, tnorm):
+        """rec_error (total) and per-dataset rec_error of the reference (:667-713)."""
+        ssum = hist["ssum"].cpu().numpy()
+        core = hist["core"].cpu().numpy()
+        xU = np.array([ssum[self.ds_rows[k]].sum() for k in range(len(self.schic))])
+        core_ds = np.array([core[self.chrom_index[k]] for k in range(len(self.schic))])
+        by_block = tnorm + core_ds - 2 * xU
+        rec_V = tnorm.sum() + core_ds.sum() - 2 * float(hist["meta"].item())
+        norm_tensor = np.sqrt(tnorm)
+        total = math.sqrt(rec_V) / float(np.linalg.norm(norm_tensor)) if rec_V > 0 else float("nan")
+        with np.errstate(invalid="ignore"):
+            block = np.sqrt(by_block) / norm_tensor
+        return total, block
+
+    def transform(self):
+        """Final SVD_term over good and bad cells with the stored projections and the
+        current factors, and its polar factor (parafac2_intergrative.py:742-834)."""
+        P = _lib.ptr
+        _lib.call("fh_projection_g_f32", P(self.tiles_dev), P(self.row_tile), self.nb,
+                  self.max_width, self.max_rank, P(self.A), self.ld, P(self.B), P(self.D),
+                  self.ld, self.R, self.rp, P(self.U), P(self.Gt), self.sp())
+        self.xg(self.Ct)
+        E_all = self.torch.zeros((self.Ct, self.rp), dtype=self.torch.float32, device=self.device)
+        self.meta_polar(self.Ct, E_all)
+        return E_all[:, :self.R]

@@ -1,0 +1,168 @@
+"""init_params on the GPU (fasthigashi/parafac2_intergrative.py:61-301).
+
+1. A_list = 1 + 0.01 N(0,1) on the host and B = I + 0.01 N (one N(0,1) row added to every
+   row of I, as the reference's broadcast does), drawn from torch's generators in the
+   reference's order.
+2. n_i: the auto-stop rule of partial_rwr.py:99-126 per (bin batch, cell batch), evaluated
+   by the library's delta kernel: the batch stops at the first epoch e where
+   max_cells ||Q_e - Q_{e+1}||_F < 0.01; n_i[chrom] is the largest stopping epoch
+   (:265).  The features use the stopped output Q_{e+1} A as the reference does.
+3. Per chromosome, a randomized truncated SVD of the cells x band features (the
+   reference's sklearn TruncatedSVD(n_components=r, n_iter=2), :257-258) whose tall
+   products F Omega, F^T Q run as the library's X passes; the (r+10)-column QR and SVD
+   factorizations of that sketch run on the host in float64.  The concatenated features'
+   top-R singular triplets give meta_embedding = U[:, :R] and D = (S Vh)[:R] (:283-290),
+   taken from the eigen-decomposition of their Gram matrix.
+At resolutions finer than 1 Mb the reference pools the features to 1 Mb first; this
+restatement sketches the unpooled band features.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib
+from .engine import FitEngine
+
+
+def _stop_epochs(deltas, cap, tol=0.01):
+    """First epoch e with max over cells of delta[e] < tol, or None if none below cap."""
+    m = deltas.max(axis=0)
+    below = np.nonzero(m < tol)[0]
+    return int(below[0]) if below.size else None
+
+
+def auto_epochs(eng, schic):
+    """Per-tile stopping epochs and per-dataset n_i (partial_rwr.py:99-126, :265)."""
+    n_i = np.zeros(len(schic), dtype=np.int64)
+    feat_epochs = np.zeros(eng.n_tiles, dtype=np.int32)
+    for cap in (12, 60):
+        deltas = eng.auto_deltas(cap).cpu().numpy()       # (tiles, cells, cap)
+        ok = True
+        for k, d in enumerate(schic):
+            for bi in range(d.num_bin_batch):
+                t = eng.tile_base[k] + bi
+                fe = 0
+                for cs in d.cell_slice_list[:d.num_cell_batch]:
+                    e = _stop_epochs(deltas[t, cs], cap)
+                    if e is None:
+                        if cap < 60:
+                            ok = False
+                            break
+                        e, out = 60, 60                   # ran all 60 epochs without stopping
+                    else:
+                        out = e + 1                       # Q was advanced once more before break
+                    n_i[k] = max(n_i[k], e)
+                    fe = max(fe, out)
+                feat_epochs[t] = fe
+                if not ok:
+                    break
+            if not ok:
+                break
+        if ok:
+            return n_i, feat_epochs
+        n_i[:] = 0
+    return n_i, feat_epochs
+
+
+def _chrom_band_rows(eng, k):
+    t0 = eng.tile_base[k]
+    d = eng.schic[k]
+    t = eng.tiles
+    x0 = int(t["xoff"][t0])
+    last = t0 + d.num_bin_batch - 1
+    x1 = int(t["xoff"][last] + t["rows"][last] * t["width"][last])
+    return x0, x1
+
+
+def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
+    """U_k S_k (cells x n_comp) of chromosome k's band features F (cells x band rows)."""
+    torch = eng.torch
+    P = _lib.ptr
+    C = eng.C
+    x0, x1 = _chrom_band_rows(eng, k)
+    a0 = (x0 // 128) * 128
+    a1 = min(eng.ldx, int(math.ceil(x1 / 128) * 128))
+    rows = a1 - a0
+    n = n_comp + n_oversamples
+    rp = 128 if n > 64 else (64 if n > 32 else (32 if n > 16 else 16))
+    dev, f32 = eng.device, torch.float32
+    Xk = eng.X[:, a0:]                        # row stride stays ldx
+    W = torch.zeros((rows, rp), dtype=f32, device=dev)
+    S = torch.zeros((C, rp), dtype=f32, device=dev)
+    splits = _lib.value("fh_xg_splits", C, rows)
+    part = torch.empty((splits, C, rp), dtype=f32, device=dev)
+    lo, hi = x0 - a0, x1 - a0
+
+    def ft_times(Ecells):                     # F^T E: (band rows of k) x n
+        E = torch.zeros((C, rp), dtype=f32, device=dev)
+        E[:, :n] = Ecells
+        _lib.call("fh_xe_f32", P(Xk), eng.ldx, C, rows, P(E), rp, P(W), eng.sp())
+        return W[lo:hi, :n].clone()
+
+    def f_times(Qrows):                       # F Q: cells x n
+        G = torch.zeros((rows, rp), dtype=f32, device=dev)
+        G[lo:hi, :n] = Qrows
+        _lib.call("fh_xg_f32", P(Xk), eng.ldx, C, rows, P(G), rp, splits, P(part), P(S), eng.sp())
+        return S[:, :n].clone()
+
+    omega = torch.from_numpy(rng.standard_normal((C, n)).astype(np.float32)).to(dev)
+    Q = ft_times(omega)                       # range of F^T (band rows x n)
+    for _ in range(n_iter):
+        Q = ft_times(f_times(Q))
+    Qh, _ = np.linalg.qr(Q.double().cpu().numpy())
+    Bt = f_times(torch.from_numpy(Qh.astype(np.float32)).to(dev)).double().cpu().numpy()  # (Q^T F^T)^T
+    # F^T = Qh Bt^T  =>  F = Bt Qh^T ; SVD of Bt (cells x n) gives F's left factors
+    Uc, s, _ = np.linalg.svd(Bt, full_matrices=False)
+    return Uc[:, :n_comp] * s[:n_comp]
+
+
+def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
+    import torch
+    if do_conv or do_col:
+        raise NotImplementedError("do_conv / do_col are not supported")
+    rank = model.rank
+    device = model.device
+    sizes = model.chrom2size
+    A_list = [torch.randn([d.shape[0], sizes[d.chrom]], dtype=torch.float32) * 1e-2 + 1
+              for d in schic]
+    B_dict = {c: torch.eye(s, device=device).add_(torch.randn(s, device=device), alpha=1e-2)
+              for c, s in sizes.items()}
+    eng = FitEngine(schic, rank, sizes, None, device, do_rwr=do_rwr)
+    model.engine = eng
+    if do_rwr:
+        n_i, feat_epochs = auto_epochs(eng, schic)
+        eng.set_epochs(feat_epochs)
+    else:
+        n_i = np.zeros(len(schic), dtype=np.int64)
+        eng.set_n_i(n_i)
+    eng.run_rwr()
+    rng = np.random.default_rng(seed)
+    feats, cols = [], []
+    start = 0
+    for k, d in enumerate(schic):
+        f = randomized_features(eng, k, sizes[d.chrom], rng)
+        feats.append(f)
+        cols.append((d.chrom, start, start + f.shape[1]))
+        start += f.shape[1]
+    Call = np.concatenate(feats, axis=1)                   # cells x sum(r)
+    G = Call.T @ Call
+    lam, V = np.linalg.eigh(G)
+    lam, V = lam[::-1], V[:, ::-1]
+    R = min(rank, Call.shape[1])
+    sv = np.sqrt(np.maximum(lam[:R], 1e-300))
+    E = np.zeros((Call.shape[0], rank))
+    E[:, :R] = (Call @ V[:, :R]) / sv
+    SVh = np.zeros((rank, Call.shape[1]))
+    SVh[:R] = sv[:, None] * V[:, :R].T
+    model.meta_embedding = torch.from_numpy(E.astype(np.float32)).to(device)
+    model.D_dict = {c: torch.from_numpy(np.ascontiguousarray(SVh[:, a:b]).astype(np.float32)).to(device)
+                    for c, a, b in cols}
+    model.A_list = A_list
+    model.B_dict = B_dict
+    model.n_i = np.asarray(n_i)
+    model.bin_cov_list = [None] * len(schic)
+    model.bad_bin_cov_list = [0] * len(schic)
+    eng.set_n_i(model.n_i)
+    eng.run_rwr()

@@ -1,0 +1,194 @@
+"""Fast_Higashi_core on one GB300 (drop-in for fasthigashi.parafac2_intergrative).
+
+Same constructor, ``fit`` / ``transform`` / ``fit_transform`` signatures and the attributes
+callers read (A_list, B_dict, D_dict, meta_embedding, projection_list,
+projected_tensor_list, n_i, bin_cov_list, chrom2size), computed by the CUDA kernels of
+libfhgb300.so.  Factor tensors live on the GPU (the reference keeps A_list and the
+projections in pinned host memory); they are torch tensors, so ``.cpu()`` works as before.
+
+Supported options: do_rwr True/False, do_conv=False, do_col=False, one resolution, ranks
+r <= R <= 64.  Anything else raises NotImplementedError.
+"""
+from __future__ import annotations
+
+import math
+import sys
+import time
+
+import numpy as np
+
+from . import _lib
+from .engine import FitEngine
+
+
+class Fast_Higashi_core:
+    def __init__(self, rank, off_diag, res_list):
+        self.rank = rank
+        self.sparse_conv = False
+        self.off_diag = off_diag
+        self.res_list = res_list
+        import torch
+        self.device = torch.device("cpu")
+        self.engine = None
+        self.rec_errors_total = []
+        self.rec_errors = []
+
+    def to(self, device):
+        import torch
+        self.device = torch.device(device)
+        return self
+
+    # ------------------------------------------------------------------ sizes
+    def _sizes(self, schic, size_ratio, size_list):
+        """chrom2size and per-dataset bin offsets (parafac2_intergrative.py:558-590)."""
+        if size_list is None:
+            size_list = [min(int(d.shape[0] * size_ratio * d.resolution / 1000000), self.rank)
+                         for d in schic]
+            chrom2size = {}
+            for d, s in zip(schic, size_list):
+                chrom2size[d.chrom] = min(chrom2size.get(d.chrom, s), s)
+        else:
+            chrom2size = {}
+            for d, s in zip(schic, size_list):
+                if d.chrom in chrom2size and chrom2size[d.chrom] != s:
+                    raise EOFError("size of the same chromosome must be same!")
+                chrom2size[d.chrom] = s
+        self.chrom2size = chrom2size
+        self.chrom2num_bin = {}
+        self.chrom2id = {c: [] for c in chrom2size}
+        for k, d in enumerate(schic):
+            self.chrom2id[d.chrom].append(k)
+            if d.chrom not in self.chrom2num_bin:
+                self.chrom2num_bin[d.chrom] = d.num_bin
+                d.global_slice_bin = slice(0, d.num_bin)
+            else:
+                d.global_slice_bin = slice(self.chrom2num_bin[d.chrom],
+                                           self.chrom2num_bin[d.chrom] + d.num_bin)
+                self.chrom2num_bin[d.chrom] += d.num_bin
+
+    @staticmethod
+    def _check_options(do_conv, do_col):
+        if do_conv:
+            raise NotImplementedError("do_conv=True is not supported")
+        if do_col:
+            raise NotImplementedError("do_col=True is not supported")
+
+    # ------------------------------------------------------------------ init
+    def init_params(self, schic, do_conv, do_rwr, do_col, seed=None):
+        """Initial factors (parafac2_intergrative.py:61-301): A = 1 + 0.01 N(0,1) and
+        B = I + 0.01 N (the same draws as the reference from torch's generators), n_i from
+        the auto-stop RWR rule evaluated on the GPU, and the meta-embedding / D from a
+        randomized SVD of the RWR features computed with the library's X passes."""
+        from .init import init_params
+        init_params(self, schic, do_conv, do_rwr, do_col, seed=seed)
+
+    # ------------------------------------------------------------------ fit
+    def _engine(self, schic, do_rwr):
+        if self.engine is None or self.engine.schic is not schic:
+            self.engine = FitEngine(schic, self.rank, self.chrom2size, self.n_i, self.device,
+                                    do_rwr=do_rwr)
+        return self.engine
+
+    def fit(self, schic, size_ratio=0.3, n_iter_max=2000, n_iter_parafac=5, do_conv=True,
+            do_rwr=False, do_col=False, tol=1e-8, size_list=None, gpu_id=None, verbose=True,
+            run_init=True):
+        self._check_options(do_conv, do_col)
+        self.gpu_id = gpu_id
+        self._sizes(schic, size_ratio, size_list)
+        if verbose:
+            print("empty params initialized")
+        if run_init:
+            self.init_params(schic, do_conv, do_rwr, do_col)
+        eng = self._engine(schic, do_rwr)
+        eng.set_state(self.A_list, self.B_dict, self.D_dict, self.meta_embedding)
+        self.tensor_norm = eng.tensor_norms()
+        eng.core_norm()
+        hist = eng.new_history(n_iter_max)
+        self.rec_errors_total, self.rec_errors = [], []
+        lines = []
+        t_start = time.time()
+        done = n_iter_max
+        for it in range(n_iter_max):
+            if it % 10 == 0 and it > 0 and n_iter_parafac < 10:
+                n_iter_parafac += 1
+            eng.iterate(it == 0, n_iter_parafac, hist[it])
+            if tol > 0:
+                if self._record(eng, hist[it], it, lines, verbose, t_start, tol):
+                    done = it + 1
+                    break
+        if tol <= 0:
+            for it in range(n_iter_max):
+                self._record(eng, hist[it], it, lines, verbose, t_start, tol)
+        eng.check_status("fit")
+        self.n_iter_done = done
+        self._publish(eng)
+        return self
+
+    def _record(self, eng, h, it, lines, verbose, t_start, tol):
+        total, block = eng.losses(h, self.tensor_norm)
+        self.rec_errors_total.append(total)
+        self.rec_errors.append(block)
+        stop = False
+        if it >= 1:
+            r = self.rec_errors
+            t = self.rec_errors_total
+            diff = (r[-2] ** 2 - r[-1] ** 2) / r[-2] ** 2
+            tdiff = (t[-2] ** 2 - t[-1] ** 2) / t[-2] ** 2
+            msg = ("PARAFAC2 re=%.3f %.2e variation min%.1e at chrom %d, max%.1e at chrom %d"
+                   % (total, tdiff, diff.min(), diff.argmin(), diff.max(), diff.argmax()))
+            stop = it >= 3 and tol > 0 and (tdiff < tol or diff.max() < tol * 2)
+        else:
+            msg = "PARAFAC2 re=%.3f" % total
+        if verbose:
+            print(msg, "takes %.1fs" % (time.time() - t_start))
+            if stop:
+                print("converged in {} iterations.".format(it))
+            sys.stdout.flush()
+        lines.append(msg)
+        return stop
+
+    def _publish(self, eng):
+        self.A_list = eng.A_views()
+        self.B_dict = eng.B_views()
+        self.D_dict = eng.D_views()
+        self.meta_embedding = eng.E[:, :self.rank]
+        self.projection_list = eng.projection_views()
+        self.projected_tensor_list = eng.projected_views()
+
+    def update_meta_embedding_interactions(self, schic, projection_list=None,
+                                           projected_tensor_list=None, do_conv=True, do_rwr=True,
+                                           do_col=False, first_iter=False):
+        """One update (parafac2_intergrative.py:304-540) from the current state.  Returns
+        (projection_list, projected_tensor_list, rec_error_x_U, rec_error_x_V
+        [, rec_error_tensor_norm])."""
+        self._check_options(do_conv, do_col)
+        eng = self._engine(schic, do_rwr)
+        eng.set_state(self.A_list, self.B_dict, self.D_dict, self.meta_embedding)
+        eng.update(first=True)
+        eng.check_status("update_meta_embedding_interactions")
+        ssum = eng.ssum.cpu().numpy()
+        xU = np.array([[ssum[eng.ds_rows[k]].sum()] for k in range(len(schic))])
+        xV = float(eng.meta_ssum.item())
+        self.meta_embedding = eng.E[:, :self.rank]
+        out = (eng.projection_views(), eng.projected_views(), xU, xV)
+        if first_iter:
+            return out + (eng.tensor_norms().reshape(-1, 1),)
+        return out
+
+    # ------------------------------------------------------------------ transform
+    def transform(self, schic, do_conv, do_rwr, do_col):
+        self._check_options(do_conv, do_col)
+        eng = self._engine(schic, do_rwr)
+        E = eng.transform()
+        eng.check_status("transform")
+        return (None, (self.A_list, self.B_dict.values(), self.D_dict.values(), E),
+                self.projection_list)
+
+    def fit_transform(self, schic, size_ratio=0.3, n_iter_max=2000, n_iter_parafac=5,
+                      do_conv=True, do_rwr=False, do_col=False, tol=1e-8, size_list=None,
+                      gpu_id=None, verbose=True, run_init=True):
+        if verbose:
+            print("n_iter_parafac", n_iter_parafac)
+        self.fit(schic, size_ratio, n_iter_max, n_iter_parafac, do_conv, do_rwr, do_col, tol,
+                 size_list, gpu_id, verbose, run_init)
+        return self.transform(schic, do_conv, do_rwr, do_col)

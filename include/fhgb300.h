@@ -1,0 +1,205 @@
+/* fhgb300.h - C ABI of the GB300-native Fast-Higashi fit hot path (libfhgb300.so).
+ *
+ * Every entry point takes device pointers, plain sizes and a cudaStream_t passed as
+ * void*, launches on that stream and returns an fh_status (0 = ok).  Nothing here
+ * allocates device memory unless its comment says so; temporary storage is a caller
+ * workspace whose size the matching *_workspace function reports.  The library has no
+ * CPU fallback: without a usable GPU every entry point returns FH_ERR_LAUNCH.
+ *
+ * Reference citations are paths within ma-compbio/Fast-Higashi.
+ */
+#ifndef FHGB300_H
+#define FHGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fh_status {
+  FH_OK = 0,
+  FH_ERR_ARG = 1,          /* bad pointer, shape or count                                   */
+  FH_ERR_UNSUPPORTED = 2,  /* a size or option outside what the kernels handle              */
+  FH_ERR_NONFINITE = 3,    /* NaN/Inf met in an input or produced by a factorisation        */
+  FH_ERR_ILLCOND = 4,      /* a factorisation met a zero or non-positive pivot              */
+  FH_ERR_LAUNCH = 5,       /* a CUDA launch or runtime call failed                          */
+  FH_ERR_INDEX = 6,        /* a contact index lies outside its tile                         */
+  FH_ERR_TIMEOUT = 7       /* a bounded device-side wait ran out                            */
+} fh_status;
+
+/* A packed contact of one (tile, cell) segment: local row in the low 16 bits of rc, local
+ * compact column in the high 16 bits, and its value. */
+typedef struct fh_entry {
+  uint32_t rc;
+  float v;
+} fh_entry;
+
+/* One bin batch of one chromosome in the compact band layout (Chrom_Dataset with
+ * compact=True, fasthigashi/sparse_for_schic.py:401-492). */
+typedef struct fh_tile {
+  int32_t chrom;   /* dataset (chromosome) index                                        */
+  int32_t row0;    /* first row bin of the bin batch within its chromosome              */
+  int32_t rows;    /* b: row bins of the batch                                          */
+  int32_t width;   /* n: compact columns (local_bin_slice / col_bin_slice widths)       */
+  int32_t shift;   /* local column = chromosome column - shift                          */
+  int32_t s0;      /* first compact column holding the batch's own bins (s1 = s0+rows)  */
+  int32_t rank;    /* r of the chromosome (chrom2size)                                  */
+  int32_t n_rwr;   /* RWR epochs (force_rwr_epochs)                                     */
+  int64_t xoff;    /* first band row of the tile: band row = xoff + i*width + j         */
+  int64_t brow0;   /* first bin row of the tile in the all-chromosome bin-row numbering */
+  int64_t uoff;    /* first element of the tile's projection U (rows x width x rank)    */
+} fh_tile;
+
+const char* fh_status_string(int status);
+int fh_version(void);
+
+/* ---- sparse per-cell contact build (sparse_for_schic.py:401-503 tiling + 279-353 densify) */
+
+/* Counts the contacts of one chromosome per (tile, cell).  row/col/cell: int32[nnz] COO of
+ * the chromosome (Sparse.indices); tiles[tile_base .. tile_base+n_tiles) are its bin
+ * batches of bs_bin rows; counts: int32[n_tiles_total * n_cells], accumulated.  Entries
+ * whose compact column falls one step outside the tile are dropped, as the reference's
+ * padded densify crops them; anything farther sets FH_ERR_INDEX in *status. */
+int fh_contacts_count(const int32_t* row, const int32_t* col, const int32_t* cell, int64_t nnz,
+                      int32_t bs_bin, const fh_tile* tiles, int32_t tile_base, int32_t n_tiles,
+                      int32_t n_cells, int32_t* counts, int* status, void* stream);
+
+/* Exclusive prefix sum of int32 counts into int64 offsets[n+1].  workspace: see below. */
+size_t fh_scan_workspace(int64_t n);
+int fh_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* Writes each contact as a packed entry (uint32 local_row | local_col << 16, float value)
+ * into its (tile, cell) segment [offsets[t*n_cells+c], offsets[t*n_cells+c+1]).  cursor:
+ * int32[n_tiles_total * n_cells], zeroed by the caller before the first chromosome. */
+int fh_contacts_scatter(const int32_t* row, const int32_t* col, const int32_t* cell,
+                        const float* val, int64_t nnz, int32_t bs_bin, const fh_tile* tiles,
+                        int32_t tile_base, int32_t n_tiles, int32_t n_cells,
+                        const int64_t* offsets, int32_t* cursor, fh_entry* entries,
+                        void* stream);
+
+/* Densifies cells [c0, c0+ncell) of tile t from its packed segments into
+ * out[ncell][rows][width] with the 1e-8 floor (Fake_Sparse.densify / densify_jit with
+ * transpose=True, sparse_for_schic.py:279-320, 352-353). */
+int fh_densify_tile(const fh_tile* tiles, int32_t t, int32_t n_cells, int32_t c0, int32_t ncell,
+                    const int64_t* offsets, const fh_entry* entries, float* out, void* stream);
+
+/* ---- partial random walk with restart (partial_rwr.py:47-175, do_conv=False, do_col=False)
+ *
+ * fh_rwr_tiles_f32: densifies every (tile, cell) segment (floor 1e-8,
+ * sparse_for_schic.py:320), builds the column-stochastic P (partial_rwr.py:84-111) and
+ * writes out[c * cell_stride + xoff + i*width + j] = (Q_{n_rwr} A)[i][j] with
+ * Q_{t+1} = 0.5 Q_t P + 0.5 I (partial_rwr.py:112-138), all in fp32.  sumsq (optional,
+ * double[n_tiles * n_cells]) receives each (tile, cell)'s squared Frobenius norm of the
+ * output (parafac2_intergrative.py:369).  max_rows / max_width bound every tile's rows and
+ * width (b <= 128, n <= 320); a tile outside them sets FH_ERR_ARG in *status. */
+int fh_rwr_tiles_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                     int32_t max_rows, int32_t max_width, const fh_entry* entries,
+                     const int64_t* offsets, float* out, int64_t cell_stride, double* sumsq,
+                     int* status, void* stream);
+
+/* Same arithmetic on a dense tile x[n_cells][rows][width] (the partial_rwr drop-in: no
+ * floor is applied to x); out[n_cells][rows][width]. */
+int fh_rwr_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width, int32_t s0,
+                     int32_t n_epochs, float* out, int* status, void* stream);
+
+/* Auto-stop rule of partial_rwr.py:99-126: deltas[c * cap + e] = ||Q_e - Q_{e+1}||_F for
+ * e < cap, per cell of a dense tile x[n_cells][rows][width]. */
+int fh_rwr_dense_deltas(const float* x, int32_t n_cells, int32_t rows, int32_t width,
+                        int32_t s0, int32_t cap, float* deltas, int* status, void* stream);
+
+/* Same on the packed segments of every tile (init_params, parafac2_intergrative.py:124-140):
+ * deltas[(t * n_cells + c) * cap + e]. */
+int fh_rwr_tiles_deltas(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                        int32_t max_rows, int32_t max_width, const fh_entry* entries,
+                        const int64_t* offsets, int32_t cap, float* deltas, int* status,
+                        void* stream);
+
+
+/* ---- ALS streaming contractions over the cached RWR output (parafac2_intergrative.py:304-540)
+ *
+ * X: float[n_cells][ldx], band rows [0, rows), ldx a multiple of 128, padding zero.
+ * E: float[n_cells][rp] (meta_embedding, columns >= R zero).  rp in {16, 32, 64, 128}.
+ *
+ * fh_xe_f32:  W[row][m] = sum_c X[c][row] E[c][m]  (W: float[rows][rp]).  W_i = X_i E gives
+ *             temp_i = W_i D diag(A_i) B^T (:336,374-383) and Y_i = U_i^T W_i (:522-529).
+ * fh_xg_f32:  out[c][m] = sum_row X[c][row] Gt[row][m]  (SVD_term^T, :422-477) with
+ *             Gt_i = U_i lhs2_i^T; partial: float[splits][n_cells][rp] workspace, splits from
+ *             fh_xg_splits (the reduction over splits runs in a fixed order). */
+int fh_xe_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const float* E,
+              int32_t rp, float* W, void* stream);
+int fh_xg_splits(int32_t n_cells, int64_t rows);
+int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const float* Gt,
+              int32_t rp, int32_t splits, float* partial, float* out, void* stream);
+
+/* Y[g][l][m] = sum_j U_g[j][l] W[xoff + i*width + j][m] for every bin row g (K16 tail,
+ * parafac2_intergrative.py:522-529); Y: float[n_rows][ldy_l][rp]; row_tile: int32[n_rows]. */
+int fh_project_y_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n_rows,
+                     const float* U, const float* W, int32_t rp, float* Y, int32_t ldy_l,
+                     void* stream);
+
+/* ---- Procrustes step per bin row (parafac2_intergrative.py:336,374-417,422-423;
+ * project2orthogonal.py:6-34).  For bin row g of tile t (local row i):
+ *   M = D_c diag(A_g) B_c^T (R x r); temp = W_g M (n x r); U_g, sum(S) = polar(temp);
+ *   Gt[xoff + i*n + j][m] = sum_l U_g[j][l] M[m][l].
+ * A: float[n_rows][lda]; B: float[nchrom][ldb][ldb]; D: float[nchrom][rp][ldb] (rows >= R
+ * zero); U: float tile-major (rows x width x rank at tile.uoff); ssum: double[n_rows].
+ * r <= 64, rp <= 64, width <= 320. */
+size_t fh_procrustes_smem(int32_t n, int32_t r, int32_t rp);
+int fh_procrustes_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n_rows,
+                      int32_t max_width, int32_t max_rank, const float* W, const float* A,
+                      int32_t lda, const float* B, const float* D, int32_t ldb, int32_t R,
+                      int32_t rp, float* U, float* Gt, double* ssum, int* status, void* stream);
+
+/* Gt rows from stored projections, no polar step: Gt[xoff + i*n + j][m] = sum_l U_g[j][l]
+ * M[m][l] with M = D_c diag(A_g) B_c^T (transform, parafac2_intergrative.py:772-801). */
+int fh_projection_g_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n_rows,
+                        int32_t max_width, int32_t max_rank, const float* A, int32_t lda,
+                        const float* B, const float* D, int32_t ldb, int32_t R, int32_t rp,
+                        const float* U, float* Gt, void* stream);
+
+/* project2orthogonal drop-in (project2orthogonal.py:6-34) for a batch of tall matrices:
+ * M: float[batch][n][r] (n >= r, r <= 64) -> U: float[batch][n][r] = polar factor,
+ * ssum: double[batch] = sum of singular values (optional). */
+int fh_polar_f32(const float* M, int64_t batch, int32_t n, int32_t r, float* U, double* ssum,
+                 int* status, void* stream);
+
+/* Singular values (descending) of each M given its polar factor U: the eigenvalues of
+ * U^T M by cyclic Jacobi (the S output of project2orthogonal.py:6-34). */
+int fh_polar_svals_f32(const float* M, const float* U, int64_t batch, int32_t n, int32_t r,
+                       float* S, void* stream);
+
+/* ---- meta polar (parafac2_intergrative.py:483-486): E = polar(S), S = SVD_term^T
+ * (float[n_cells][rp], R columns used, R <= 64); *ssum = sum of singular values = <E, S>.
+ * fp64 Gram, fp64 Cholesky, Newton polar of the factor, fp64 apply. */
+size_t fh_meta_polar_workspace(int32_t n_cells, int32_t R);
+int fh_meta_polar(const float* S, int32_t n_cells, int32_t R, int32_t rp, float* E,
+                  double* ssum, void* workspace, size_t workspace_bytes, int* status,
+                  void* stream);
+
+/* ---- CP-ALS on every chromosome's projected tensor (parafac_integrative.py:28-112 with
+ * n_iter_max = n_iter; parafac2_intergrative.py:674-706).  A: float[bin rows][ld],
+ * B: float[nchrom][ld][ld], D: float[nchrom][rp][ld], Y: float[bin rows][ldy][rp]; the
+ * factors are updated in place.  meta (device int32): c_row0, c_nbin, c_rank, c_chunk0,
+ * c_nchunk (nchrom each) then k_chrom, k_row0, k_nrow (nchunks each): bin-row chunks of at
+ * most 8 rows, each inside one chromosome.  core: double[nchrom] = ||[[A,B,D]]||^2 after
+ * the sweeps; cross (optional): double[nchrom] = <[[A,B,D]], Y> of the last sweep
+ * (parafac's loss_norm and loss_x).  Requires r <= ld <= 64, R <= rp <= ld. */
+size_t fh_cp_workspace(int32_t nchrom, int32_t nchunks, int32_t ld, int32_t rp);
+int fh_cp_als(int32_t nchrom, int32_t nchunks, const int32_t* meta, float* A, float* B,
+              float* D, const float* Y, int32_t ld, int32_t rp, int32_t R, int32_t ldy,
+              int32_t n_iter, double* core, double* cross, void* workspace,
+              size_t workspace_bytes, int* status, void* stream);
+/* core[chrom] = ||[[A,B,D]]||^2 of the current factors, which stay unchanged
+ * (parafac2_intergrative.py:621-632). */
+int fh_core_norm(int32_t nchrom, int32_t nchunks, const int32_t* meta, float* A, float* B,
+                 float* D, const float* Y, int32_t ld, int32_t rp, int32_t R, int32_t ldy,
+                 double* core, void* workspace, size_t workspace_bytes, int* status,
+                 void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FHGB300_H */

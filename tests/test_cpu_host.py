@@ -1,0 +1,83 @@
+"""CPU-only checks of the host side: the C ABI library, the Sparse container, the tiling."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from fh_gb300 import _lib, synth
+from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset, compact_layout
+from oracle import fh_oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "fhgb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(fh_\w+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    if not os.path.exists(_lib.LIB_PATH):
+        from fh_gb300 import build
+        build.build()
+    lib = _lib.load()
+    declared = header_functions()
+    assert declared, "no declarations parsed"
+    for name in declared:
+        assert hasattr(lib, name), name
+    # the Python binding covers exactly the declared ABI
+    assert sorted(_lib.SIGNATURES) == declared
+    assert lib.fh_version() >= 100
+    assert lib.fh_status_string(0) == b"ok"
+
+
+def test_sparse_known_answers():
+    """The reference's own known-answer test of Sparse (sparse_for_schic.py:634-661)."""
+    def new_obj():
+        return Sparse([[0, 2, 1, 0], [0, 3, 2, 1]], [1, 2, 3, 4.], (3, 4))
+    base = new_obj().to_scipy().todense()
+    o = new_obj(); o.sort_indices()
+    assert (o.to_scipy().todense() == base).all()
+    assert (new_obj().permute(0, 1).to_scipy().todense() == base).all()
+    assert (new_obj().permute(1, 0).to_scipy().todense() == base.T).all()
+    assert (new_obj().reshape(1, 12).to_scipy().todense() == base.reshape(1, 12)).all()
+    assert (new_obj().reshape(4, 3).to_scipy().todense() == base.reshape(4, 3)).all()
+    for s in [slice(2), slice(10), slice(0, None), slice(2, None), slice(1, 3)]:
+        assert (new_obj().slicing(s).to_scipy().todense() == base[s]).all()
+    o = new_obj().permute(1, 0).reshape(6, 2).slicing(slice(1, 3)).permute(1, 0)
+    assert (o.to_scipy().todense() == base.T.reshape(6, 2)[1:3].T).all()
+
+
+@pytest.mark.parametrize("num_bin,bs_bin,flank", [(37, 12, 4), (20, 12, 4), (249, 125, 20),
+                                                  (5, 5, 10), (100, 100, 10), (130, 33, 30)])
+def test_compact_layout_matches_oracle(num_bin, bs_bin, flank):
+    mine = compact_layout(num_bin, bs_bin, flank)
+    ref = O.tile_layout(num_bin, bs_bin, flank)
+    assert len(mine) == len(ref)
+    for a, b in zip(mine, ref):
+        assert (a.start, a.rows, a.local, a.col, a.width, a.shift) == \
+               (b.start, b.rows, b.local, b.col, b.width, b.shift)
+
+
+def test_chrom_dataset_slices():
+    w = synth.workload("tiny")
+    coo, _ = synth.generate(w, seed=3)
+    idx, val, shape = coo[0]
+    d = Chrom_Dataset(Sparse(idx, val, shape), 12, 10, compact=True, flank=w.band)
+    assert d.num_bin_batch == 4 and d.num_cell_batch == 3
+    assert d.cell_slice_list == [slice(0, 10), slice(10, 20), slice(20, 24)]
+    assert d.bin_slice_list[-1] == slice(36, 37)
+
+
+def test_synthetic_generator_is_seeded():
+    w = synth.workload("tiny")
+    a, _ = synth.generate(w, seed=5)
+    b, _ = synth.generate(w, seed=5)
+    for (i1, v1, s1), (i2, v2, s2) in zip(a, b):
+        assert s1 == s2 and (i1 == i2).all() and (v1 == v2).all()
+    i, v, s = a[0]
+    assert (np.abs(i[0] - i[1]) <= w.band).all()
+    key = (i[0].astype(np.int64) * s[1] + i[1]) * s[2] + i[2]
+    assert (np.diff(key) > 0).all()          # sorted by (row, col, cell), unique

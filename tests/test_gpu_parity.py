@@ -1,0 +1,197 @@
+"""GPU parity of the CUDA path against the reference's golden outputs and the oracle.
+
+Tolerances (relative Frobenius error unless stated):
+  contact build / densify  bit-exact
+  RWR output (fp32)        1e-5 against the reference
+  polar factors            against an fp64 SVD of the same fp32 input: within
+                           max(1e-5, 2 x the error of the reference's route, a float32 torch
+                           SVD); fp32 factorizations of these ill-conditioned matrices (the
+                           reference's own have condition numbers up to 5e6) cannot do better
+  singular values          1e-5
+  one ALS update           1e-5 on well-conditioned outputs (sum of singular values, the
+                           meta-embedding error term); U, Y, E within 2x the reference's own
+                           fp32 error
+  loss trajectory          1e-5 against the fp64 oracle, 2e-3 against the reference (its fp32
+                           core norm cancels ~45x in the loss formula)
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import fh_oracle as O
+import golden_io as G
+from gpu_util import datasets_from
+
+pytestmark = pytest.mark.gpu
+
+CUDA = torch.device("cuda")
+
+
+def rel(a, b):
+    return O.rel_err(a.detach().cpu().numpy() if hasattr(a, "detach") else a,
+                     b.detach().cpu().numpy() if hasattr(b, "detach") else b)
+
+
+# ------------------------------------------------------------------ contacts and RWR
+def test_fetch_densify_bit_exact():
+    z = G.load("rwr_tiles.npz")
+    ds = datasets_from(z, resolution=1000000)
+    for k in range(int(z["n_tiles"])):
+        ci, bi, cj, s0, s1, _ = z["t%d_meta" % k]
+        (x, _), kind = ds[ci].fetch(bi, cj, save_context=dict(device=CUDA), transpose=True)
+        np.testing.assert_array_equal(x.cpu().numpy(), z["t%d_x" % k])
+
+
+def test_partial_rwr_dropin_matches_reference():
+    from fh_gb300 import partial_rwr
+    z = G.load("rwr_tiles.npz")
+    for k in range(int(z["n_tiles"])):
+        _, _, _, s0, s1, n_auto = z["t%d_meta" % k]
+        x = torch.from_numpy(z["t%d_x" % k]).to(CUDA)
+        y3, _ = partial_rwr(x, int(s0), int(s1), False, True, False, force_rwr_epochs=3)
+        assert rel(y3, z["t%d_y3" % k]) < 1e-5
+        ya, na = partial_rwr(x, int(s0), int(s1), False, True, False, force_rwr_epochs=-1,
+                             return_rwr_iter=True, final_transpose=False)
+        assert na == n_auto
+        assert rel(ya, z["t%d_yauto" % k]) < 1e-5
+
+
+def test_fused_rwr_tiles_match_reference():
+    """Contact build + fused densify/RWR over every tile at once (force_rwr_epochs=3)."""
+    from fh_gb300.engine import FitEngine
+    z = G.load("rwr_tiles.npz")
+    ds = datasets_from(z, resolution=1000000)
+    eng = FitEngine(ds, 4, {d.chrom: 2 for d in ds}, [3] * len(ds), CUDA)
+    X = eng.X.cpu().numpy()
+    for k in range(int(z["n_tiles"])):
+        ci, bi, cj, s0, s1, _ = z["t%d_meta" % k]
+        t = eng.tiles[eng.tile_base[ci] + bi]
+        cs = ds[ci].cell_slice_list[cj]
+        b, n, x0 = int(t["rows"]), int(t["width"]), int(t["xoff"])
+        got = X[cs, x0:x0 + b * n].reshape(-1, b, n).transpose(1, 2, 0)
+        assert O.rel_err(got, z["t%d_y3" % k]) < 1e-5
+    # squared norms per (tile, cell) agree with the output
+    ss = eng.sumsq.view(eng.n_tiles, eng.Ct).cpu().numpy()
+    t = eng.tiles[0]
+    x = X[:, int(t["xoff"]):int(t["xoff"]) + int(t["rows"]) * int(t["width"])]
+    np.testing.assert_allclose(ss[0], (x.astype(np.float64) ** 2).sum(1), rtol=1e-6)
+
+
+def test_rwr_empty_cell_and_zero_epochs():
+    """A cell without contacts is the 1e-8 floor; zero epochs return the densified tile."""
+    from fh_gb300 import partial_rwr
+    x = torch.full((2, 6, 10), 1e-8, device=CUDA)
+    x[1, 2, 4] = 3.0
+    y, _ = partial_rwr(x, 2, 8, False, True, False, force_rwr_epochs=0, final_transpose=False)
+    assert torch.equal(y, x)
+    y, _ = partial_rwr(x, 2, 8, False, True, False, force_rwr_epochs=4, final_transpose=False)
+    ref, _ = O.partial_rwr(x.cpu().double().numpy(), 2, 8, force_rwr_epochs=4, final_transpose=False)
+    assert rel(y, ref) < 1e-5 and torch.isfinite(y).all()
+
+
+# ------------------------------------------------------------------ polar factors
+def _ill_conditioned(rng, batch, n, r, kappa):
+    out = []
+    for _ in range(batch):
+        U, _ = np.linalg.qr(rng.standard_normal((n, r)))
+        V, _ = np.linalg.qr(rng.standard_normal((r, r)))
+        s = np.logspace(0, -np.log10(kappa), r)
+        out.append((U * s) @ V.T)
+    return np.stack(out).astype(np.float32)
+
+
+def _fp32_svd_polar(M):
+    """The reference's route on the host: a float32 torch SVD, U Vh."""
+    U, S, Vh = torch.linalg.svd(torch.from_numpy(M), full_matrices=False)
+    return (U @ Vh).numpy()
+
+
+@pytest.mark.parametrize("n,r,kappa", [(40, 8, 1e2), (165, 64, 1e4), (188, 64, 1e6), (70, 16, 10.0)])
+def test_polar_factor_against_fp64(n, r, kappa):
+    from fh_gb300 import project2orthogonal
+    rng = np.random.default_rng(n + r)
+    M = _ill_conditioned(rng, 6, n, r, kappa)
+    U, S = project2orthogonal(torch.from_numpy(M).to(CUDA), r, CUDA)
+    Ut, St = O.project2orthogonal(M.astype(np.float64), r)
+    ref_err = O.rel_err(_fp32_svd_polar(M), Ut)
+    assert rel(U, Ut) < max(1e-5, 2 * ref_err)
+    assert rel(S, St) < 1e-5
+    # the meta-embedding route (fp64 Gram / Cholesky / apply): one tall matrix
+    M2 = _ill_conditioned(rng, 1, 900, min(r, 32), kappa)[0]
+    U2, S2 = project2orthogonal(torch.from_numpy(M2).to(CUDA), None, CUDA)
+    Ut2, St2 = O.project2orthogonal(M2.astype(np.float64))
+    assert rel(U2, Ut2) < max(1e-5, 2 * O.rel_err(_fp32_svd_polar(M2), Ut2))
+    assert rel(S2, St2) < 1e-5
+
+
+def test_parafac_dropin_matches_reference():
+    from fh_gb300 import parafac
+    z = G.load("parafac.npz")
+    for n in (1, 3):
+        f, ln, lx = parafac(torch.from_numpy(z["X"]), 6, n_iter_max=n,
+                            init=[torch.from_numpy(z[k]) for k in ("A0", "B0", "D0")])
+        for a, name in zip(f, "ABD"):
+            assert rel(a, z["%s%d" % (name, n)]) < 1e-5
+        assert abs(ln - float(z["ln%d" % n])) < 1e-5 * abs(float(z["ln%d" % n]))
+        assert abs(lx - float(z["lx%d" % n])) < 1e-5 * abs(float(z["lx%d" % n]))
+
+
+# ------------------------------------------------------------------ ALS
+def _model_from(z, n_chrom):
+    from fh_gb300 import Fast_Higashi_core
+    ds = datasets_from(z)
+    A, B, D, E, n_i = G.state(z, "init", n_chrom)
+    m = Fast_Higashi_core(int(z["rank"]), int(z["flank"]), [int(z["resolution"])]).to(CUDA)
+    m._sizes(ds, float(z["dim1"]), None)
+    m.A_list = [torch.from_numpy(a) for a in A]
+    m.B_dict = {k: torch.from_numpy(v) for k, v in B.items()}
+    m.D_dict = {k: torch.from_numpy(v) for k, v in D.items()}
+    m.meta_embedding = torch.from_numpy(E)
+    m.n_i = np.asarray(n_i)
+    m.bin_cov_list = [None] * n_chrom
+    return m, ds
+
+
+def test_one_update_matches_reference_and_oracle():
+    z = G.load("als_small.npz")
+    n = int(z["n_chrom"])
+    m, ds = _model_from(z, n)
+    pl, ptl, xU, xV, tn = m.update_meta_embedding_interactions(ds, do_conv=False, do_rwr=True,
+                                                               do_col=False, first_iter=True)
+    orc = O.ALSOracle(G.chrom_datas(z, O), int(z["rank"]), *G.state(z, "init", n))
+    U_o, Y_o, xU_o, xV_o, tn_o = orc.update(first_iter=True)
+    # well-conditioned scalars: 1e-5 against the reference and the oracle
+    assert O.rel_err(tn.ravel(), z["it1_tnorm"]) < 1e-5
+    assert O.rel_err(xU.ravel(), z["it1_exU"]) < 1e-5 and O.rel_err(xU.ravel(), xU_o) < 1e-5
+    assert abs(xV - float(z["it1_exV"])) < 1e-5 * abs(xV)
+    assert abs(xV - xV_o) < 1e-5 * abs(xV)
+    # polar factors over all bins: within 2x the reference's own fp32 error against fp64
+    cat = lambda xs: np.concatenate([np.ravel(x) for x in xs])
+    U_gpu = cat([pl[ci][bi].cpu().numpy() for ci in range(n) for bi in range(len(pl[ci]))])
+    U_ref = cat([z["it1_U%d_%d" % (ci, bi)] for ci in range(n) for bi in range(len(pl[ci]))])
+    U_fp64 = cat([U_o[ci][bi] for ci in range(n) for bi in range(len(pl[ci]))])
+    assert O.rel_err(U_gpu, U_fp64) < max(1e-5, 2 * O.rel_err(U_ref, U_fp64))
+    assert rel(m.meta_embedding, orc.E) < 1e-4
+    for ci, d in enumerate(ds):
+        assert rel(ptl[d.chrom], Y_o[ci]) < 1e-4
+
+
+@pytest.mark.parametrize("fixture,n_iter,ref_tol", [("als_small.npz", 4, 1e-4), ("c1_fit.npz", 10, 2e-3)])
+def test_fit_trajectory(fixture, n_iter, ref_tol):
+    z = G.load(fixture)
+    n = int(z["n_chrom"])
+    m, ds = _model_from(z, n)
+    m.fit(ds, size_ratio=float(z["dim1"]), n_iter_max=n_iter, n_iter_parafac=1, do_conv=False,
+          do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
+    traj = np.asarray(m.rec_errors_total)
+    orc = O.ALSOracle(G.chrom_datas(z, O), int(z["rank"]), *G.state(z, "init", n)).fit(n_iter)
+    np.testing.assert_allclose(traj, orc.rec_errors_total, rtol=1e-5)
+    np.testing.assert_allclose(traj, z["fit_rec_total"], rtol=ref_tol)
+    E = m.meta_embedding.cpu().numpy()
+    assert O.rel_err(O.procrustes_align(E, orc.E), orc.E) < 1e-4
+    # transform: embedding over all cells, aligned with the reference's
+    res = m.transform(ds, False, True, False)
+    Et = res[1][3].cpu().numpy()
+    Et_ref = z["fit_E_transform"]
+    assert O.rel_err(O.procrustes_align(Et, Et_ref), Et_ref) < 1e-2
