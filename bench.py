@@ -1,0 +1,331 @@
+#!/usr/bin/env python
+"""Benchmark of the Fast-Higashi fit hot path on one GB300: cells/s for RWR + 30 ALS iterations.
+
+A step is one fit of the workload: the contact build, the partial RWR of every tile and 30
+iterations of the PARAFAC2-like ALS (per-bin polar, SVD_term, meta polar, projections,
+CP-ALS), from a fixed initial state (init_params runs once, untimed, as the metric states).
+
+  value  device-timed (CUDA events), contacts already resident in HBM as the COO
+  e2e    the public API (Fast_Higashi_core.fit on host Sparse data) with the COO H2D and the
+         embedding / loss D2H inside the timed region
+  --impl reference   the CPU restatement of the reference (the oracle, fp32, all host threads)
+                     on a bounded cell sample, extrapolated to cells/s
+
+Multi-GPU runs (torchrun) are independent replicas: the fit does not shard (scaling weak).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "fast-higashi_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "cells/sec for RWR + ALS fit, BF16-batched vs plain FP32 on GB300 at stated error"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c2", help="workload: c1..c5 (default c2, 2,000 cells at 1 Mb)")
+    ap.add_argument("--iters", type=int, default=None, help="ALS iterations (default: the workload's 30)")
+    ap.add_argument("--sample-cells", type=int, default=96,
+                    help="cells of the CPU-baseline sample (at least the rank R)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 0, 1
+    import torch
+    import torch.distributed as dist
+    rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, local, ws
+
+
+def make_workload(name, seed=0):
+    from fh_gb300 import synth
+    from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
+    w = synth.workload(name)
+    coo, _ = synth.generate(w, seed=seed)
+    ds = []
+    for (idx, val, shape), cname, nb in zip(coo, w.chrom_names, w.chrom_bins):
+        bsb, bsc = synth.recommend_batches(w, nb, w.n_cells)
+        ds.append(Chrom_Dataset(Sparse(idx, val, shape, copy=False), bsb, bsc, compact=True,
+                                flank=w.band, chrom=cname, resolution=w.resolution))
+    return w, coo, ds
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) of the SM clock and throttle reasons while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.lines, self.proc = gpu, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], p["bf16_tflops"], "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 1900.0, "fallback"
+
+
+# --------------------------------------------------------------------------------------
+def cpu_sample_rate(coo, w, n_cells, iters, threads=None):
+    """Cells/s of the CPU restatement (fp32, the reference's loop structure with its RWR
+    recomputation) on the first n_cells cells: RWR + one warm ALS iteration, extrapolated
+    to RWR + iters iterations.  Returns (cells/s, sample description, seconds spent)."""
+    from oracle import fh_oracle as O
+    from fh_gb300 import synth
+    n_cells = max(n_cells, w.rank)
+    t0 = time.perf_counter()
+    datas = []
+    for k, ((idx, val, shape), nb) in enumerate(zip(coo, w.chrom_bins)):
+        m = idx[2] < n_cells
+        bsb, _ = synth.recommend_batches(w, nb, w.n_cells)
+        datas.append(O.ChromData("chr%d" % (k + 1), idx[:, m], val[m], nb, n_cells, bsb, n_cells, w.band))
+    sizes = O.chrom2size(datas, w.rank, w.dim1, w.resolution)
+    rng = np.random.default_rng(0)
+    A = [1 + 0.01 * rng.standard_normal((d.num_bin, sizes[d.name])) for d in datas]
+    B = {d.name: np.eye(sizes[d.name]) + 0.01 * rng.standard_normal(sizes[d.name]) for d in datas}
+    D = {d.name: rng.standard_normal((w.rank, sizes[d.name])) for d in datas}
+    E, _ = np.linalg.qr(rng.standard_normal((n_cells, w.rank)))
+    orc = O.ALSOracle(datas, w.rank, A, B, D, E, [6] * len(datas), dtype=np.float32, cache_rwr=False)
+    t = time.perf_counter()
+    for ci, d in enumerate(datas):                       # the RWR pass of init / the first fetch
+        for bi in range(len(d.layout())):
+            orc.rwr_tile(ci, bi, 0)
+    t_rwr = time.perf_counter() - t
+    orc.iterate(0, 1)
+    t = time.perf_counter()
+    orc.iterate(1, 1)
+    t_iter = time.perf_counter() - t
+    rate = n_cells / (t_rwr + iters * t_iter)
+    desc = ("%d of %d cells, RWR pass %.2fs + 1 timed ALS iteration %.2fs (3 RWR recomputations "
+            "per bin batch, as the reference), extrapolated to %d iterations" %
+            (n_cells, w.n_cells, t_rwr, t_iter, iters))
+    return rate, desc, time.perf_counter() - t0
+
+
+def reference_arm(args, rank, ws):
+    if rank != 0:
+        return
+    w, coo, _ = make_workload(args.config)
+    iters = args.iters or w.n_iter
+    threads = os.cpu_count()
+    rates, desc = [], ""
+    for i in range(args.warmup + args.steps):
+        r, desc, _ = cpu_sample_rate(coo, w, args.sample_cells, iters)
+        if i >= args.warmup:
+            rates.append(r)
+    v = float(np.mean(rates))
+    line = {"metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * w.n_cells / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, %s)" % args.config, "impl": "reference",
+            "config": {"workload": "%s: %d cells, %d bins, R=%d, band %d, %d ALS iterations" %
+                       (args.config, w.n_cells, sum(w.chrom_bins), w.rank, w.band, iters),
+                       "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------------------
+def gb300_arm(args, rank, local, ws):
+    import torch
+    from fh_gb300 import Fast_Higashi_core, _lib
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    w, coo, ds = make_workload(args.config)
+    iters = args.iters or w.n_iter
+    C = w.n_cells
+    # ---- init (untimed): the GPU init_params, then the state every step starts from
+    torch.manual_seed(0)
+    m = Fast_Higashi_core(w.rank, w.band, [w.resolution]).to(dev)
+    m._sizes(ds, w.dim1, None)
+    m.init_params(ds, False, True, False, seed=0)
+    torch.cuda.synchronize()
+    state = ([a.clone() for a in m.A_list], {k: v.clone() for k, v in m.B_dict.items()},
+             {k: v.clone() for k, v in m.D_dict.items()}, m.meta_embedding.clone())
+    eng = m.engine
+    hist = eng.new_history(iters)
+
+    def device_step():
+        eng.store.rebuild()
+        eng.run_rwr()
+        eng.set_state(*state)
+        eng.core_norm()
+        npar = 1
+        for it in range(iters):
+            if it % 10 == 0 and it > 0 and npar < 10:
+                npar += 1
+            eng.iterate(it == 0, npar, hist[it])
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        device_step()
+    torch.cuda.synchronize()
+    barrier()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = _lib.launches
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        s0.record()
+        for _ in range(args.steps):
+            device_step()
+        s1.record()
+        torch.cuda.synchronize()
+    launches = (_lib.launches - n0) // args.steps
+    ms = s0.elapsed_time(s1) / args.steps
+    t = torch.tensor([ms], device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms = float(t.item())
+    value = ws * C / (ms / 1000.0)
+    eng.check_status("bench")
+    # ---- per-kernel times (one instrumented step) for the roofline
+    eng.timing = {}
+    device_step()
+    torch.cuda.synchronize()
+    kt = eng.timing_summary()
+    eng.timing = None
+    hbm, bf16, peak_kind = peaks()
+    xbytes = C * eng.rows * 4
+    fam = max(("xe", "xg"), key=lambda k: kt.get(k, {}).get("total_ms", 0))
+    dom = max(kt, key=lambda k: kt[k]["total_ms"])
+    ach = xbytes / (kt[fam]["mean_ms"] / 1000.0) / 1e9
+    roof = {"kernel": fam, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+            "frac": ach / hbm, "peak_kind": peak_kind, "traffic": None,
+            "algorithmic_bytes_per_launch": xbytes,
+            "note": ("X pass (%d cells x %d band rows fp32); kernel share of the step: %s; "
+                     "largest family: %s" % (C, eng.rows,
+                                             {k: round(v["total_ms"] / ms, 3) for k, v in kt.items()},
+                                             dom))}
+    # ---- end to end through the public API, host data in and out
+    A0, B0, D0, E0 = [x.cpu() for x in state[0]], {k: v.cpu() for k, v in state[1].items()}, \
+        {k: v.cpu() for k, v in state[2].items()}, state[3].cpu()
+    n_i = m.n_i.copy()
+
+    def e2e_step():
+        mm = Fast_Higashi_core(w.rank, w.band, [w.resolution]).to(dev)
+        mm._sizes(ds, w.dim1, None)
+        mm.A_list, mm.B_dict, mm.D_dict, mm.meta_embedding = A0, B0, D0, E0
+        mm.n_i, mm.bin_cov_list = n_i, [None] * len(ds)
+        mm.fit(ds, size_ratio=w.dim1, n_iter_max=iters, n_iter_parafac=1, do_conv=False,
+               do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
+        emb = mm.meta_embedding.cpu()
+        return mm, emb
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps // 2)):
+        mm, emb = e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 2)
+    h2d = mm.engine.store.h2d_bytes + sum(a.numel() * 4 for a in A0) + E0.numel() * 4 + \
+        sum(v.numel() * 4 for v in B0.values()) + sum(v.numel() * 4 for v in D0.values())
+    d2h = emb.numel() * 4 + iters * (eng.nb + 1 + len(eng.names)) * 8
+    e2e = {"value": ws * C / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1000.0}
+    if rank != 0:
+        return
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        r, desc, _ = cpu_sample_rate(coo, w, args.sample_cells, iters)
+        cpu = {"value": r, "unit": "cells/s", "cores": os.cpu_count(), "kind": "port", "sample": desc}
+    line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, %s)" % args.config,
+            "config": {"workload": "%s: %d cells, %d bins (%d bin batches), R=%d, band %d, %d ALS "
+                                   "iterations, RWR epochs %s" %
+                                   (args.config, C, sum(w.chrom_bins), eng.n_tiles, w.rank, w.band,
+                                    iters, sorted(set(int(v) for v in n_i))),
+                       "precision": "fp32 (plain)", "l2": "inputs larger than L2 (X %.2f GB)" %
+                       (eng.X.numel() * 4 / 1e9), "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clk.summary(), "kernel_ms": {k: round(v["mean_ms"], 4) for k, v in kt.items()},
+            "loss_final": float(m.engine.losses(hist[-1], eng.tensor_norms())[0])}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, local, ws = dist_setup()
+    if args.impl == "reference":
+        reference_arm(args, rank, ws)
+    else:
+        from fh_gb300 import build as _b
+        _b.build()
+        gb300_arm(args, rank, local, ws)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

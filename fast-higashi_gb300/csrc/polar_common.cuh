@@ -1,0 +1,244 @@
+// CTA-wide building blocks of the polar-factor kernels (fp32, shared memory).
+//
+// All routines are called by every thread of the block (blockDim.x a multiple of 32) with
+// uniform arguments.  Loops map lanes to columns and warps to rows, so no loop divides by a
+// runtime extent.
+#pragma once
+#include "fh_common.cuh"
+
+namespace fh {
+
+constexpr int kNewtonMaxIt = 30;
+
+struct PolarScratch {
+  float* vh;     // [kMaxRank] head of each Householder vector
+  float* beta;   // [kMaxRank] 2 / v^T v
+  float* wv;     // [2 * kMaxRank] per-column dot products / pivot row
+  float* fcol;   // [kMaxRank] pivot column
+  float* red;    // [32]
+  double* dred;  // [32]
+  int* ival;     // [4]: [0] a zero pivot was met
+};
+constexpr int kPolarMiscFloats = 5 * kMaxRank + 64;
+
+__device__ __forceinline__ int pc_lane() { return threadIdx.x & 31; }
+__device__ __forceinline__ int pc_warp() { return threadIdx.x >> 5; }
+__device__ __forceinline__ int pc_nwarps() { return blockDim.x >> 5; }
+
+// ---- Householder QR of T (n x r, row stride ldt, n >= r), in place ---------------------
+// On return the upper triangle of T[0:r][0:r] is R, T[i][k] (i > k) holds v_k below the
+// diagonal, vh[k] the head of v_k and beta[k] = 2 / v_k^T v_k (0 for a zero column).
+__device__ inline void householder_qr(float* T, int n, int r, int ldt, PolarScratch& s) {
+  const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
+  for (int k = 0; k < r; ++k) {
+    if (ty == 0) {
+      float ss = 0.f;
+      for (int i = k + 1 + tx; i < n; i += 32) ss = fmaf(T[i * ldt + k], T[i * ldt + k], ss);
+      ss = warp_sum(ss);
+      if (tx == 0) {
+        const float x0 = T[k * ldt + k];
+        const float s2 = fmaf(x0, x0, ss);
+        if (s2 == 0.f) {
+          s.beta[k] = 0.f; s.vh[k] = 0.f; s.wv[2 * kMaxRank - 1] = 0.f;
+        } else {
+          const float nrm = sqrtf(s2);
+          const float alpha = x0 >= 0.f ? -nrm : nrm;
+          s.vh[k] = x0 - alpha;
+          s.beta[k] = 1.f / (s2 - x0 * alpha);
+          s.wv[2 * kMaxRank - 1] = alpha;
+        }
+      }
+    }
+    __syncthreads();
+    const float beta = s.beta[k], vh = s.vh[k];
+    for (int j = k + 1 + ty; j < r; j += nw) {       // w_j = v^T T[k:, j], one warp per column
+      float d = 0.f;
+      for (int i = k + 1 + tx; i < n; i += 32) d = fmaf(T[i * ldt + k], T[i * ldt + j], d);
+      d = warp_sum(d);
+      if (tx == 0) s.wv[j] = fmaf(vh, T[k * ldt + j], d);
+    }
+    __syncthreads();
+    if (beta != 0.f) {
+      for (int i = k + ty; i < n; i += nw) {
+        const float bv = -beta * ((i == k) ? vh : T[i * ldt + k]);
+        for (int j = k + 1 + tx; j < r; j += 32) T[i * ldt + j] = fmaf(bv, s.wv[j], T[i * ldt + j]);
+      }
+    }
+    if (threadIdx.x == 0) T[k * ldt + k] = s.wv[2 * kMaxRank - 1];
+    __syncthreads();
+  }
+}
+
+// ---- U = Q U: apply the stored reflectors in reverse to U (n x r, stride ldu) ----------
+__device__ inline void apply_q(const float* T, int ldt, float* U, int ldu, int n, int r,
+                               PolarScratch& s) {
+  const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
+  for (int k = r - 1; k >= 0; --k) {
+    const float beta = s.beta[k], vh = s.vh[k];
+    if (beta == 0.f) continue;  // uniform across the block
+    for (int j = ty; j < r; j += nw) {
+      float d = 0.f;
+      for (int i = k + 1 + tx; i < n; i += 32) d = fmaf(T[i * ldt + k], U[i * ldu + j], d);
+      d = warp_sum(d);
+      if (tx == 0) s.wv[j] = fmaf(vh, U[k * ldu + j], d);
+    }
+    __syncthreads();
+    for (int i = k + ty; i < n; i += nw) {
+      const float bv = -beta * ((i == k) ? vh : T[i * ldt + k]);
+      for (int j = tx; j < r; j += 32) U[i * ldu + j] = fmaf(bv, s.wv[j], U[i * ldu + j]);
+    }
+    __syncthreads();
+  }
+}
+
+// ---- inverse of an upper-triangular R (r x r, stride ldr) into Xi (stride ldo) ---------
+// Column j of R^{-1} by back substitution; one warp per column, lanes share each dot product.
+__device__ inline void tri_inverse(const float* R, int ldr, float* Xi, int ldo, int r,
+                                   PolarScratch& s) {
+  const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
+  for (int j = ty; j < r; j += nw) {
+    for (int i = tx; i < r; i += 32) Xi[i * ldo + j] = 0.f;
+    __syncwarp();
+    for (int i = j; i >= 0; --i) {
+      float d = 0.f;
+      for (int l = i + 1 + tx; l <= j; l += 32) d = fmaf(R[i * ldr + l], Xi[l * ldo + j], d);
+      d = warp_sum(d);
+      if (tx == 0) {
+        float rii = R[i * ldr + i];
+        if (rii == 0.f) { rii = 1e-30f; s.ival[0] = 1; }
+        Xi[i * ldo + j] = ((i == j ? 1.f : 0.f) - d) / rii;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+}
+
+// ---- inverse of X (r x r, stride ldx) by Gauss-Jordan with partial pivoting ------------
+// Aug: r x (2r+1) scratch; on return its columns [r, 2r) hold X^{-1}.
+__device__ inline void gj_inverse(const float* X, int ldx, float* Aug, int r, PolarScratch& s) {
+  const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
+  const int la = 2 * r + 1, w2 = 2 * r;
+  for (int i = ty; i < r; i += nw)
+    for (int j = tx; j < w2; j += 32)
+      Aug[i * la + j] = j < r ? X[i * ldx + j] : (j - r == i ? 1.f : 0.f);
+  __syncthreads();
+  for (int k = 0; k < r; ++k) {
+    if (ty == 0) {
+      float best = -1.f;
+      int bi = k;
+      for (int i = k + tx; i < r; i += 32) {
+        const float a = fabsf(Aug[i * la + k]);
+        if (a > best) { best = a; bi = i; }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (bi != k)
+        for (int j = k + tx; j < w2; j += 32) {
+          const float a = Aug[k * la + j];
+          Aug[k * la + j] = Aug[bi * la + j];
+          Aug[bi * la + j] = a;
+        }
+      __syncwarp();
+      float piv = Aug[k * la + k];
+      if (piv == 0.f) {
+        piv = 1e-30f;
+        if (tx == 0) s.ival[0] = 1;
+      }
+      for (int i = tx; i < r; i += 32) s.fcol[i] = Aug[i * la + k];
+      const float rp = 1.f / piv;
+      for (int j = k + 1 + tx; j < w2; j += 32) {
+        const float v = Aug[k * la + j] * rp;
+        s.wv[j] = v;
+        Aug[k * la + j] = v;
+      }
+    }
+    __syncthreads();
+    for (int i = ty; i < r; i += nw) {
+      if (i == k) continue;
+      const float f = -s.fcol[i];
+      for (int j = k + 1 + tx; j < w2; j += 32) Aug[i * la + j] = fmaf(f, s.wv[j], Aug[i * la + j]);
+    }
+    __syncthreads();
+  }
+}
+
+// Scratch floats newton_polar needs after X: [X | I] (r x (2r+1)) or two r x (r+1) buffers.
+__host__ __device__ inline size_t newton_scratch_floats(int r) { return 2 * (size_t)r * (r + 1) + 8; }
+
+// ---- polar factor of a square X (r x r, stride ldx) in place ---------------------------
+// Scaled Newton X <- (z X + X^{-T} / z) / 2 (Higham, Frobenius scaling z) while the step is
+// large; once a step moves X by less than 10 % it is close to orthogonal and the pivot-free
+// Newton-Schulz step X <- X (3 I - X^T X) / 2 finishes the convergence.  When X enters
+// upper triangular (the R of a QR), the first inverse is a triangular solve.
+// Aug: newton_scratch_floats(r) floats; ldx must be r + 1.
+__device__ inline void newton_polar(float* X, int ldx, float* Aug, int r, bool upper,
+                                    PolarScratch& s) {
+  const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
+  const int la = 2 * r + 1;
+  bool schulz = false, last = false;
+  for (int it = 0; it < kNewtonMaxIt; ++it) {
+    float dn = 0.f, nn = 0.f;
+    if (!schulz) {
+      // ---- X^{-1}: Xinv[i][j] at Aug[i * la + r + j]
+      if (it == 0 && upper) tri_inverse(X, ldx, Aug + r, la, r, s);
+      else gj_inverse(X, ldx, Aug, r, s);
+      float a = 0.f, b = 0.f;
+      for (int i = ty; i < r; i += nw)
+        for (int j = tx; j < r; j += 32) {
+          a = fmaf(X[i * ldx + j], X[i * ldx + j], a);
+          b = fmaf(Aug[i * la + r + j], Aug[i * la + r + j], b);
+        }
+      a = block_sum<float>(a, s.red);
+      b = block_sum<float>(b, s.red);
+      float zeta = sqrtf(sqrtf(b) / sqrtf(a));
+      if (it >= 1 && fabsf(zeta - 1.f) < 1e-2f) zeta = 1.f;
+      const float iz = 1.f / zeta;
+      for (int i = ty; i < r; i += nw)
+        for (int j = tx; j < r; j += 32) {
+          const float x = X[i * ldx + j];
+          const float xn = 0.5f * (zeta * x + iz * Aug[j * la + r + i]);
+          const float d = xn - x;
+          dn = fmaf(d, d, dn);
+          nn = fmaf(xn, xn, nn);
+          X[i * ldx + j] = xn;
+        }
+    } else {
+      // ---- Newton-Schulz: G = 1.5 I - 0.5 X^T X;  X <- X G
+      float* G = Aug;              // r x ldx
+      float* Xn = Aug + r * ldx;   // r x ldx
+      for (int i = ty; i < r; i += nw)
+        for (int j = tx; j < r; j += 32) {
+          float acc = 0.f;
+          for (int k = 0; k < r; ++k) acc = fmaf(X[k * ldx + i], X[k * ldx + j], acc);
+          G[i * ldx + j] = (i == j ? 1.5f : 0.f) - 0.5f * acc;
+        }
+      __syncthreads();
+      for (int i = ty; i < r; i += nw)
+        for (int j = tx; j < r; j += 32) {
+          float acc = 0.f;
+          for (int k = 0; k < r; ++k) acc = fmaf(X[i * ldx + k], G[k * ldx + j], acc);
+          Xn[i * ldx + j] = acc;
+          const float d = acc - X[i * ldx + j];
+          dn = fmaf(d, d, dn);
+          nn = fmaf(acc, acc, nn);
+        }
+      __syncthreads();
+      for (int i = ty; i < r; i += nw)
+        for (int j = tx; j < r; j += 32) X[i * ldx + j] = Xn[i * ldx + j];
+    }
+    dn = block_sum<float>(dn, s.red);
+    nn = block_sum<float>(nn, s.red);
+    __syncthreads();
+    const float rel = sqrtf(dn / nn);
+    if (last) break;
+    if (schulz && rel < 3e-5f) last = true;     // quadratic: one more step reaches ~1e-9
+    if (!schulz && rel < 0.1f) schulz = true;
+  }
+}
+
+}  // namespace fh

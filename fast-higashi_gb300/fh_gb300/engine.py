@@ -33,6 +33,7 @@ class FitEngine:
     def __init__(self, schic, rank, chrom2size, n_i, device, do_rwr=True, stream=None):
         import torch
         self.torch = torch
+        self.timing = None   # {kernel family: [(start event, end event)]} when enabled
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise _lib.FHError("FitEngine", 2, "the fit runs on a CUDA device only")
@@ -129,6 +130,27 @@ class FitEngine:
     def sp(self):
         return _lib.stream_ptr(self.stream)
 
+    def _timed(self, name, fn):
+        """Runs fn; with timing enabled, brackets it with CUDA events on the launch stream."""
+        if self.timing is None:
+            return fn()
+        torch = self.torch
+        stream = self.stream if self.stream is not None else torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        out = fn()
+        b.record(stream)
+        self.timing.setdefault(name, []).append((a, b))
+        return out
+
+    def timing_summary(self):
+        """Mean milliseconds and launch count per kernel family (after a synchronize)."""
+        out = {}
+        for k, evs in (self.timing or {}).items():
+            ms = [a.elapsed_time(b) for a, b in evs]
+            out[k] = dict(mean_ms=float(np.mean(ms)), total_ms=float(np.sum(ms)), calls=len(ms))
+        return out
+
     def check_status(self, what):
         st = int(self.status.item())
         if st:
@@ -158,6 +180,9 @@ class FitEngine:
         return out[:, :self.C]
 
     def run_rwr(self):
+        self._timed("rwr", self._run_rwr)
+
+    def _run_rwr(self):
         P = _lib.ptr
         _lib.call("fh_rwr_tiles_f32", P(self.tiles_dev), self.n_tiles, self.Ct, self.max_rows,
                   self.max_width, P(self.store.entries), P(self.store.offsets), P(self.X),
@@ -220,37 +245,40 @@ class FitEngine:
     # ------------------------------------------------------------------ kernels
     def xe(self):
         P = _lib.ptr
-        _lib.call("fh_xe_f32", P(self.X), self.ldx, self.C, self.rows, P(self.E), self.rp,
-                  P(self.W), self.sp())
+        self._timed("xe", lambda: _lib.call("fh_xe_f32", P(self.X), self.ldx, self.C, self.rows,
+                                            P(self.E), self.rp, P(self.W), self.sp()))
 
     def procrustes(self):
         P = _lib.ptr
-        _lib.call("fh_procrustes_f32", P(self.tiles_dev), P(self.row_tile), self.nb,
-                  self.max_width, self.max_rank, P(self.W), P(self.A), self.ld, P(self.B),
-                  P(self.D), self.ld, self.R, self.rp, P(self.U), P(self.Gt), P(self.ssum),
-                  P(self.status), self.sp())
+        self._timed("procrustes", lambda: _lib.call(
+            "fh_procrustes_f32", P(self.tiles_dev), P(self.row_tile), self.nb, self.max_width,
+            self.max_rank, P(self.W), P(self.A), self.ld, P(self.B), P(self.D), self.ld, self.R,
+            self.rp, P(self.U), P(self.Gt), P(self.ssum), P(self.status), self.sp()))
 
     def xg(self, n_cells):
         P = _lib.ptr
-        _lib.call("fh_xg_f32", P(self.X), self.ldx, n_cells, self.rows, P(self.Gt), self.rp,
-                  self.splits, P(self.partial), P(self.S), self.sp())
+        self._timed("xg", lambda: _lib.call("fh_xg_f32", P(self.X), self.ldx, n_cells, self.rows,
+                                            P(self.Gt), self.rp, self.splits, P(self.partial),
+                                            P(self.S), self.sp()))
 
     def meta_polar(self, n_cells, E_out):
         P = _lib.ptr
-        _lib.call("fh_meta_polar", P(self.S), n_cells, self.R, self.rp, P(E_out),
-                  P(self.meta_ssum), P(self.meta_ws), self.meta_ws.numel(), P(self.status),
-                  self.sp())
+        self._timed("meta_polar", lambda: _lib.call(
+            "fh_meta_polar", P(self.S), n_cells, self.R, self.rp, P(E_out), P(self.meta_ssum),
+            P(self.meta_ws), self.meta_ws.numel(), P(self.status), self.sp()))
 
     def project_y(self):
         P = _lib.ptr
-        _lib.call("fh_project_y_f32", P(self.tiles_dev), P(self.row_tile), self.nb, P(self.U),
-                  P(self.W), self.rp, P(self.Y), self.ld, self.sp())
+        self._timed("project_y", lambda: _lib.call(
+            "fh_project_y_f32", P(self.tiles_dev), P(self.row_tile), self.nb, P(self.U),
+            P(self.W), self.rp, P(self.Y), self.ld, self.sp()))
 
     def cp_als(self, n_iter):
         P = _lib.ptr
-        _lib.call("fh_cp_als", len(self.names), self.nchunks, P(self.cp_meta), P(self.A),
-                  P(self.B), P(self.D), P(self.Y), self.ld, self.rp, self.R, self.ld, n_iter,
-                  P(self.core), None, P(self.cp_ws), self.cp_ws.numel(), P(self.status), self.sp())
+        self._timed("cp_als", lambda: _lib.call(
+            "fh_cp_als", len(self.names), self.nchunks, P(self.cp_meta), P(self.A), P(self.B),
+            P(self.D), P(self.Y), self.ld, self.rp, self.R, self.ld, n_iter, P(self.core), None,
+            P(self.cp_ws), self.cp_ws.numel(), P(self.status), self.sp()))
 
     # ------------------------------------------------------------------ ALS
     def update(self, first):

@@ -2,9 +2,9 @@
 
 Returns (U Vh, S) of matrix (..., d1, d2) as the reference's thin SVD would
 (project2orthogonal.py:6-34): the orthonormal polar factor and the singular values in
-descending order.  Batches of small tall matrices (d1 <= 320, d2 <= 64) take the
-Householder-QR + scaled-Newton kernel; a single tall matrix with d2 <= 64 (the
-meta-embedding case) takes the fp64-Gram route.  Wide matrices are transposed.
+descending order.  Matrices that fit in shared memory take the Householder-QR + Newton
+kernel; taller ones with d2 <= 64 (the meta-embedding case) take the fp64-Gram route.  S
+comes from a one-sided Jacobi of the symmetric U^T M.  Wide matrices are transposed.
 """
 from __future__ import annotations
 
@@ -15,8 +15,9 @@ def _polar_tall(M):
     import torch
     batch, n, r = M.shape
     U = torch.empty_like(M)
+    S = torch.empty((batch, r), dtype=torch.float32, device=M.device)
     st = torch.zeros(1, dtype=torch.int32, device=M.device)
-    if n <= 320 and r <= 64:
+    if r <= 128 and _lib.value("fh_polar_smem", n, r) <= 227 * 1024:
         _lib.call("fh_polar_f32", _lib.ptr(M), batch, n, r, _lib.ptr(U), None, _lib.ptr(st),
                   _lib.stream_ptr())
     elif r <= 64:
@@ -33,7 +34,6 @@ def _polar_tall(M):
             U[b] = Ep[:, :r]
     else:
         raise _lib.FHError("project2orthogonal", 2, "more than 64 columns")
-    S = torch.empty((batch, r), dtype=torch.float32, device=M.device)
     _lib.call("fh_polar_svals_f32", _lib.ptr(M), _lib.ptr(U), batch, n, r, _lib.ptr(S),
               _lib.stream_ptr())
     return U, S

@@ -292,38 +292,55 @@ class ContactStore:
             tiles, tile_base = tile_table(datasets)
         self.tiles_np = tiles
         self.tiles_dev = torch.from_numpy(tiles.view(np.uint8).copy()).to(device)
-        n_tiles = len(tiles)
-        self.n_tiles = n_tiles
-        sp = _lib.stream_ptr(stream)
-        counts = torch.zeros(n_tiles * self.n_cells, dtype=torch.int32, device=device)
-        status = torch.zeros(1, dtype=torch.int32, device=device)
-        dev_coo = []
-        for d, base in zip(datasets, tile_base):
+        self.n_tiles = len(tiles)
+        self.stream = stream
+        self.meta = [(d.bs_bin, base, d.num_bin_batch) for d, base in zip(datasets, tile_base)]
+        # H2D of the host COO (Sparse.indices int32 x 3, values fp32), once
+        self.coo = []
+        for d in datasets:
             t = d.tensor
             idx = torch.from_numpy(np.ascontiguousarray(t.indices.astype(np.int32))).to(device)
             val = torch.from_numpy(np.ascontiguousarray(t.values.astype(np.float32))).to(device)
-            nnz = int(val.numel())
-            _lib.call("fh_contacts_count", _lib.ptr(idx[0]), _lib.ptr(idx[1]), _lib.ptr(idx[2]),
-                      nnz, d.bs_bin, _lib.ptr(self.tiles_dev), base, d.num_bin_batch,
-                      self.n_cells, _lib.ptr(counts), _lib.ptr(status), sp)
-            dev_coo.append((idx, val, nnz))
-        self.offsets = torch.empty(n_tiles * self.n_cells + 1, dtype=torch.int64, device=device)
-        ws_bytes = _lib.value("fh_scan_workspace", counts.numel())
-        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
-        _lib.call("fh_exclusive_scan", _lib.ptr(counts), counts.numel(), _lib.ptr(self.offsets),
-                  _lib.ptr(ws), ws_bytes, sp)
+            self.coo.append((idx, val, int(val.numel())))
+        self.h2d_bytes = sum(i.numel() * 4 + v.numel() * 4 for i, v, _ in self.coo)
+        self.counts = torch.zeros(self.n_tiles * self.n_cells, dtype=torch.int32, device=device)
+        self.cursor = torch.zeros_like(self.counts)
+        self.status = torch.zeros(1, dtype=torch.int32, device=device)
+        self.offsets = torch.empty(self.n_tiles * self.n_cells + 1, dtype=torch.int64, device=device)
+        ws_bytes = _lib.value("fh_scan_workspace", self.counts.numel())
+        self.scan_ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+        self.count_and_scan()
         total = int(self.offsets[-1].item())
         self.entries = torch.empty(max(total, 1) * 2, dtype=torch.int32, device=device)
-        cursor = torch.zeros_like(counts)
-        for d, base, (idx, val, nnz) in zip(datasets, tile_base, dev_coo):
-            _lib.call("fh_contacts_scatter", _lib.ptr(idx[0]), _lib.ptr(idx[1]), _lib.ptr(idx[2]),
-                      _lib.ptr(val), nnz, d.bs_bin, _lib.ptr(self.tiles_dev), base,
-                      d.num_bin_batch, self.n_cells, _lib.ptr(self.offsets), _lib.ptr(cursor),
-                      _lib.ptr(self.entries), sp)
-        st = int(status.item())
+        self.scatter()
+        st = int(self.status.item())
         if st:
             raise _lib.FHError("contact build", st)
         self.nnz_packed = total
+
+    def count_and_scan(self):
+        sp = _lib.stream_ptr(self.stream)
+        self.counts.zero_()
+        for (bs_bin, base, nbb), (idx, val, nnz) in zip(self.meta, self.coo):
+            _lib.call("fh_contacts_count", _lib.ptr(idx[0]), _lib.ptr(idx[1]), _lib.ptr(idx[2]),
+                      nnz, bs_bin, _lib.ptr(self.tiles_dev), base, nbb, self.n_cells,
+                      _lib.ptr(self.counts), _lib.ptr(self.status), sp)
+        _lib.call("fh_exclusive_scan", _lib.ptr(self.counts), self.counts.numel(),
+                  _lib.ptr(self.offsets), _lib.ptr(self.scan_ws), self.scan_ws.numel(), sp)
+
+    def scatter(self):
+        sp = _lib.stream_ptr(self.stream)
+        self.cursor.zero_()
+        for (bs_bin, base, nbb), (idx, val, nnz) in zip(self.meta, self.coo):
+            _lib.call("fh_contacts_scatter", _lib.ptr(idx[0]), _lib.ptr(idx[1]), _lib.ptr(idx[2]),
+                      _lib.ptr(val), nnz, bs_bin, _lib.ptr(self.tiles_dev), base, nbb,
+                      self.n_cells, _lib.ptr(self.offsets), _lib.ptr(self.cursor),
+                      _lib.ptr(self.entries), sp)
+
+    def rebuild(self):
+        """Re-runs the contact build from the device-resident COO (no host sync)."""
+        self.count_and_scan()
+        self.scatter()
 
 
 def tile_table(datasets, chrom_index=None, ranks=None, n_rwr=None, order=None):

@@ -141,13 +141,13 @@ int fh_project_y_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n_ro
                      void* stream);
 
 /* ---- Procrustes step per bin row (parafac2_intergrative.py:336,374-417,422-423;
- * project2orthogonal.py:6-34).  For bin row g of tile t (local row i):
- *   M = D_c diag(A_g) B_c^T (R x r); temp = W_g M (n x r); U_g, sum(S) = polar(temp);
- *   Gt[xoff + i*n + j][m] = sum_l U_g[j][l] M[m][l].
+ * project2orthogonal.py:6-34), fp32.  For bin row g of tile t (local row i):
+ *   M = D_c diag(A_g) B_c^T (R x r); temp = W_g M (n x r);
+ *   U_g = polar(temp) by Householder QR + scaled Newton / Newton-Schulz on R,
+ *   ssum[g] = sum of the singular values of temp,
+ *   Gt[xoff + i*n + j][m] = sum_l U_g[j][l] M[m][l]  (the rows of lhs2 U^T).
  * A: float[n_rows][lda]; B: float[nchrom][ldb][ldb]; D: float[nchrom][rp][ldb] (rows >= R
- * zero); U: float tile-major (rows x width x rank at tile.uoff); ssum: double[n_rows].
- * r <= 64, rp <= 64, width <= 320. */
-size_t fh_procrustes_smem(int32_t n, int32_t r, int32_t rp);
+ * zero); U: tile-major (rows x width x rank at tile.uoff).  r <= 64, rp <= 64, width <= 320. */
 int fh_procrustes_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n_rows,
                       int32_t max_width, int32_t max_rank, const float* W, const float* A,
                       int32_t lda, const float* B, const float* D, int32_t ldb, int32_t R,
@@ -161,13 +161,15 @@ int fh_projection_g_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n
                         const float* U, float* Gt, void* stream);
 
 /* project2orthogonal drop-in (project2orthogonal.py:6-34) for a batch of tall matrices:
- * M: float[batch][n][r] (n >= r, r <= 64) -> U: float[batch][n][r] = polar factor,
- * ssum: double[batch] = sum of singular values (optional). */
+ * M: float[batch][n][r] (n >= r, r <= 128, fh_polar_smem(n, r) <= 227 KB) -> U: float[batch]
+ * [n][r] polar factor (Householder QR + Newton), ssum (optional): double[batch] the sums of
+ * the singular values. */
+size_t fh_polar_smem(int32_t n, int32_t r);
 int fh_polar_f32(const float* M, int64_t batch, int32_t n, int32_t r, float* U, double* ssum,
                  int* status, void* stream);
 
-/* Singular values (descending) of each M given its polar factor U: the eigenvalues of
- * U^T M by cyclic Jacobi (the S output of project2orthogonal.py:6-34). */
+/* Singular values (descending) of tall matrices M (any n) given their polar factors U: the
+ * one-sided Jacobi of the symmetric U^T M (accumulated in fp64). */
 int fh_polar_svals_f32(const float* M, const float* U, int64_t batch, int32_t n, int32_t r,
                        float* S, void* stream);
 

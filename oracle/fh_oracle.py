@@ -282,8 +282,9 @@ class ALSOracle:
             for bi, bb in enumerate(d.layout()):
                 rs = slice(bb.start, bb.start + bb.rows)
                 temp = None
+                X_last = None
                 for cj, cs in enumerate(d.cells()):
-                    X = self.rwr_tile(ci, bi, cj)
+                    X = X_last = self.rwr_tile(ci, bi, cj)
                     if first_iter:
                         tnorm[ci] += float(np.sum(X.astype(np.float64) ** 2))   # :369
                     lhs = np.einsum("ir,jr,kr->ikj", A[rs], B, C[cs], optimize=True)   # :374
@@ -294,8 +295,10 @@ class ALSOracle:
                 U_list.append(U)
                 err_x_U[ci] += float(np.sum(S))                          # :417
                 lhs2 = np.einsum("ir,jr,kr->kij", A[rs], B, D, optimize=True).reshape(D.shape[0], -1)  # :422-423
+                ncb = len(d.cells())
                 for cj, cs in enumerate(d.cells()):                       # :429-477
-                    X = self.rwr_tile(ci, bi, cj)
+                    # the last cell batch of phase 1 is reused, as the reference does (:429)
+                    X = X_last if cj == ncb - 1 else self.rwr_tile(ci, bi, cj)
                     proj = np.matmul(U.transpose(0, 2, 1), X)
                     SVD_term[:, cs] += lhs2 @ proj.reshape(-1, proj.shape[-1])
             U_all.append(U_list)
