@@ -214,6 +214,56 @@ extern "C" int fh_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offs
   return FH_OK;
 }
 
+// ---------------------------------------------------------------------------------------
+// fh_exclusive_scan_noalloc: the same scan with its scratch in a fixed device array.
+//
+// Some callers cannot hand the library a workspace: host code that owns no CUDA allocator
+// (a binding from another language that only passes the buffers it already has), or code
+// that must not call cudaMalloc because it synchronizes the device and would stall work
+// other streams have in flight.  This variant takes only the input and the output.  Its
+// scratch, the per-block totals of the three-phase scan, lives in the array below, which
+// every GPU that loads the library holds until the process exits.
+// ---------------------------------------------------------------------------------------
+constexpr int64_t kNoAllocScanBlocks = 8191;   // 64 KiB of int64 block totals
+constexpr int64_t kNoAllocScanMax = kNoAllocScanBlocks * kScanTile;   // 16,775,168 counts
+static __device__ __align__(256) int64_t g_scan_scratch[kNoAllocScanBlocks + 1];
+
+// Device address of g_scan_scratch on the current device, looked up once per device.
+static int scan_scratch_address(int64_t** out) {
+  static std::mutex mu;
+  static std::unordered_map<int, int64_t*> addr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return FH_ERR_LAUNCH;
+  std::lock_guard<std::mutex> g(mu);
+  auto it = addr.find(dev);
+  if (it == addr.end()) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_scan_scratch) != cudaSuccess || !p) return FH_ERR_LAUNCH;
+    it = addr.emplace(dev, (int64_t*)p).first;
+  }
+  *out = it->second;
+  return FH_OK;
+}
+
+extern "C" int fh_exclusive_scan_noalloc(const int32_t* counts, int64_t n, int64_t* offsets,
+                                         void* stream) {
+  if (n <= 0 || !counts || !offsets) return FH_ERR_ARG;
+  if (n > kNoAllocScanMax) return FH_ERR_UNSUPPORTED;   // the block totals would not fit
+  int64_t* totals = nullptr;
+  const int st = scan_scratch_address(&totals);
+  if (st) return st;
+  // Every entry the scan reads is written first in the same call (block totals, then their
+  // prefix sums), so the array needs no clearing between calls.
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t nb = ceil_div(n, kScanTile);
+  scan_block_totals<<<(unsigned)nb, kScanThreads, 0, s>>>(counts, n, totals);
+  scan_totals<<<1, 1024, 0, s>>>(totals, nb);
+  scan_blocks<<<(unsigned)nb, kScanThreads, 0, s>>>(counts, n, totals, offsets);
+  cudaMemcpyAsync(offsets + n, totals + nb, sizeof(int64_t), cudaMemcpyDeviceToDevice, s);
+  FH_CHECK_LAUNCH();
+  return FH_OK;
+}
+
 extern "C" int fh_contacts_scatter(const int32_t* row, const int32_t* col, const int32_t* cell,
                                    const float* val, int64_t nnz, int32_t bs_bin,
                                    const fh_tile* tiles, int32_t tile_base, int32_t n_tiles,

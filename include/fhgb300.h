@@ -71,6 +71,17 @@ size_t fh_scan_workspace(int64_t n);
 int fh_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* fh_exclusive_scan without a workspace argument, for callers that cannot allocate device
+ * memory (a foreign-language binding that holds only its own buffers, or code that must not
+ * call cudaMalloc because it synchronizes the device).  No counterpart in the reference.
+ * The scratch is a 64 KiB array in the library's device memory, held by every GPU that
+ * loads the library until exit; n may be at most 16,775,168 (FH_ERR_UNSUPPORTED beyond).
+ * The first call on a device looks up the array's address once; make that first call
+ * before any stream capture.  All calls share the array: calls that overlap on the GPU
+ * (on different streams, or from several threads at once) race and must be serialized by
+ * the caller.  Allocates nothing. */
+int fh_exclusive_scan_noalloc(const int32_t* counts, int64_t n, int64_t* offsets, void* stream);
+
 /* Writes each contact as a packed entry (uint32 local_row | local_col << 16, float value)
  * into its (tile, cell) segment [offsets[t*n_cells+c], offsets[t*n_cells+c+1]).  cursor:
  * int32[n_tiles_total * n_cells], zeroed by the caller before the first chromosome. */
