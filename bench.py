@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--sample-cells", type=int, default=96,
                     help="cells of the CPU-baseline sample (at least the rank R)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16"],
+                    help="fp32: the plain drop-in; bf16: X in bf16, tensor-core X passes")
     return ap.parse_args()
 
 
@@ -201,7 +203,7 @@ def gb300_arm(args, rank, local, ws):
     C = w.n_cells
     # ---- init (untimed): the GPU init_params, then the state every step starts from
     torch.manual_seed(0)
-    m = Fast_Higashi_core(w.rank, w.band, [w.resolution]).to(dev)
+    m = Fast_Higashi_core(w.rank, w.band, [w.resolution], precision=args.precision).to(dev)
     m._sizes(ds, w.dim1, None)
     m.init_params(ds, False, True, False, seed=0)
     torch.cuda.synchronize()
@@ -253,15 +255,16 @@ def gb300_arm(args, rank, local, ws):
     kt = eng.timing_summary()
     eng.timing = None
     hbm, bf16, peak_kind = peaks()
-    xbytes = C * eng.rows * 4
+    xel = 2 if eng.bf16 else 4
+    xbytes = C * eng.rows * xel
     fam = max(("xe", "xg"), key=lambda k: kt.get(k, {}).get("total_ms", 0))
     dom = max(kt, key=lambda k: kt[k]["total_ms"])
     ach = xbytes / (kt[fam]["mean_ms"] / 1000.0) / 1e9
     roof = {"kernel": fam, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
             "frac": ach / hbm, "peak_kind": peak_kind, "traffic": None,
             "algorithmic_bytes_per_launch": xbytes,
-            "note": ("X pass (%d cells x %d band rows fp32); kernel share of the step: %s; "
-                     "largest family: %s" % (C, eng.rows,
+            "note": ("X pass (%d cells x %d band rows %s); kernel share of the step: %s; "
+                     "largest family: %s" % (C, eng.rows, eng.precision,
                                              {k: round(v["total_ms"] / ms, 3) for k, v in kt.items()},
                                              dom))}
     # ---- end to end through the public API, host data in and out
@@ -270,7 +273,7 @@ def gb300_arm(args, rank, local, ws):
     n_i = m.n_i.copy()
 
     def e2e_step():
-        mm = Fast_Higashi_core(w.rank, w.band, [w.resolution]).to(dev)
+        mm = Fast_Higashi_core(w.rank, w.band, [w.resolution], precision=args.precision).to(dev)
         mm._sizes(ds, w.dim1, None)
         mm.A_list, mm.B_dict, mm.D_dict, mm.meta_embedding = A0, B0, D0, E0
         mm.n_i, mm.bin_cov_list = n_i, [None] * len(ds)
@@ -300,13 +303,13 @@ def gb300_arm(args, rank, local, ws):
         cpu = {"value": r, "unit": "cells/s", "cores": os.cpu_count(), "kind": "port", "sample": desc}
     line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, %s)" % args.config,
+            "vs_baseline": None, "dtype": "bf16" if eng.bf16 else "f32", "data": "synthetic (seeded generator, %s)" % args.config,
             "config": {"workload": "%s: %d cells, %d bins (%d bin batches), R=%d, band %d, %d ALS "
                                    "iterations, RWR epochs %s" %
                                    (args.config, C, sum(w.chrom_bins), eng.n_tiles, w.rank, w.band,
                                     iters, sorted(set(int(v) for v in n_i))),
-                       "precision": "fp32 (plain)", "l2": "inputs larger than L2 (X %.2f GB)" %
-                       (eng.X.numel() * 4 / 1e9), "parallelism": "replicas" if ws > 1 else "single GPU"},
+                       "precision": ("bf16 X, tensor-core X passes" if eng.bf16 else "fp32 (plain)"),
+                       "l2": "inputs larger than L2 (X %.2f GB)" % (eng.Ct * eng.ldx * xel / 1e9), "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clk.summary(), "kernel_ms": {k: round(v["mean_ms"], 4) for k, v in kt.items()},
             "loss_final": float(m.engine.losses(hist[-1], eng.tensor_norms())[0])}

@@ -189,16 +189,6 @@ __global__ void __launch_bounds__(256) xg_f32_kernel(const float* __restrict__ X
   }
 }
 
-__global__ void reduce_splits_kernel(const float* __restrict__ partial, int splits, int64_t n,
-                                     float* __restrict__ out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    float s = 0.f;
-    for (int k = 0; k < splits; ++k) s += partial[(int64_t)k * n + i];
-    out[i] = s;
-  }
-}
-
 // ---------------------------------------------------------------------------------------
 // Y[g][l][m] = sum_j U_g[j][l] W[xoff + i*n + j][m]   (K16 tail), one CTA per bin row g.
 // ---------------------------------------------------------------------------------------
@@ -312,7 +302,7 @@ extern "C" int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t r
     default: xg_f32_kernel<128><<<grid, 256, 0, s>>>(X, ldx, n_cells, Gt, rows, per, partial); break;
   }
   const int64_t n = (int64_t)n_cells * rp;
-  reduce_splits_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(partial, splits, n, out);
+  reduce_splits_kernel<float><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(partial, splits, n, out);
   FH_CHECK_LAUNCH();
   return FH_OK;
 }

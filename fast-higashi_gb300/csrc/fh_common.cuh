@@ -46,6 +46,18 @@ __device__ inline T block_sum(T v, T* scratch /* >= 32 */) {
   return s;
 }
 
+// out[i] = sum over k of partial[k][i] in a fixed order (deterministic split-K reduction).
+template <typename T>
+__global__ void reduce_splits_kernel(const T* __restrict__ partial, int splits, int64_t n,
+                                     T* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    T s = 0;
+    for (int k = 0; k < splits; ++k) s += partial[(int64_t)k * n + i];
+    out[i] = s;
+  }
+}
+
 __device__ inline void set_status(int* status, int code) {
   if (status) atomicCAS(status, 0, code);
 }

@@ -16,6 +16,7 @@
 //
 // The auto-stop variant (partial_rwr.py:99-123) runs the same recurrence with A = I, which
 // is Q_t itself, and records ||Q_t - Q_{t+1}||_F per epoch.
+#include <cuda_bf16.h>
 #include "fh_common.cuh"
 
 namespace fh {
@@ -25,7 +26,7 @@ constexpr float kFloor = 1e-8f;  // densify floor, sparse_for_schic.py:320
 constexpr float kEps = 1e-15f;   // column-sum guard, partial_rwr.py:90,91,111
 
 enum RwrSource { kSparse = 0, kDense = 1 };
-enum RwrMode { kOutput = 0, kDeltas = 1 };
+enum RwrMode { kOutput = 0, kDeltas = 1, kOutput16 = 2 };
 
 struct RwrArgs {
   const fh_tile* tiles;
@@ -36,6 +37,7 @@ struct RwrArgs {
   int d_rows, d_width, d_s0, d_epochs;
   int max_rows, max_width;  // extents the shared-memory carve-out was sized for
   float* out;
+  __nv_bfloat16* out16;
   int64_t cell_stride;
   double* sumsq;
   float* deltas;
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
       if (tid == 0) a.deltas[((int64_t)t * a.n_cells + c) * a.cap + ep] = sqrtf(s);
     }
     __syncthreads();
-    if (MODE == kOutput && SRC == kSparse) {
+    if (MODE != kDeltas && SRC == kSparse) {
       for (int64_t e = e0 + tid; e < e1; e += kRwrThreads) {
         const uint2 en = a.entries[e];
         const float v = __uint_as_float(en.y);
@@ -259,12 +261,17 @@ __global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
     }
   }
 
-  if (MODE == kOutput) {
+  if (MODE == kOutput || MODE == kOutput16) {
     double ss = 0.0;
-    float* o = a.out + (int64_t)c * a.cell_stride + xoff;
     for (int i = tid; i < b * n; i += kRwrThreads) {
-      const float v = Z[(i / n) * ldz + (i % n)];
-      o[i] = v;
+      float v = Z[(i / n) * ldz + (i % n)];
+      if (MODE == kOutput) {
+        a.out[(int64_t)c * a.cell_stride + xoff + i] = v;
+      } else {
+        const __nv_bfloat16 h = __float2bfloat16_rn(v);
+        a.out16[(int64_t)c * a.cell_stride + xoff + i] = h;
+        v = __bfloat162float(h);
+      }
       ss += (double)v * v;
     }
     if (a.sumsq) {
@@ -321,6 +328,20 @@ extern "C" int fh_rwr_tiles_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n
   a.offsets = offsets; a.out = out; a.cell_stride = cell_stride; a.sumsq = sumsq;
   a.status = status;
   return launch_rwr<kSparse, kOutput>(a, n_tiles, mr, mw, s);
+}
+
+extern "C" int fh_rwr_tiles_bf16(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                                 int32_t mr, int32_t mw, const fh_entry* entries,
+                                 const int64_t* offsets, uint16_t* out16, int64_t cell_stride,
+                                 double* sumsq, int* status, void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !offsets || !out16 || mr <= 0 || mw < mr)
+    return FH_ERR_ARG;
+  RwrArgs a{};
+  a.max_rows = mr; a.max_width = mw;
+  a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
+  a.offsets = offsets; a.out16 = reinterpret_cast<__nv_bfloat16*>(out16);
+  a.cell_stride = cell_stride; a.sumsq = sumsq; a.status = status;
+  return launch_rwr<kSparse, kOutput16>(a, n_tiles, mr, mw, (cudaStream_t)stream);
 }
 
 extern "C" int fh_rwr_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width,

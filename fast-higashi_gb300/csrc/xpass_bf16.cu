@@ -1,0 +1,394 @@
+// ALS streaming contractions over X in bf16 on the 5th-generation tensor cores.
+//
+// The two passes over the RWR output X of every ALS iteration (the re-associated form of
+// fasthigashi/parafac2_intergrative.py:374-383, 422-477, 522-529; the fp32 kernels in
+// als_f32.cu state the algebra) as persistent TMA -> tcgen05 -> TMEM GEMMs:
+//
+//   W   = X^T [E_hi | E_lo]   M = 128 band rows, N = 2 rp, K = cells      (X read MN-major)
+//   S^T = X   [G_hi | G_lo]   M = 128 cells,     N = 2 rp, K = band rows  (X read K-major),
+//                             split over K with a deterministic reduction
+//
+// X is stored once in bf16 (X16[cell][band row], row pitch ldx, the padding zero).  The
+// small operands E (cells x rp) and G^T (band rows x rp) are split into bf16 hi and lo parts
+// (x = hi + lo to 16 significant bits) and stacked along N, so one MMA per K step produces
+// X*hi and X*lo side by side in TMEM; the epilogue adds them.  The products are exact in the
+// fp32 accumulator, so the error is the bf16 rounding of X alone.
+//
+// CTA (192 threads, one per SM, persistent over work items):
+//   warp 0  TMA producer: per K step one 128 x 64 tile of X (two 64 x 64 boxes) and the
+//           N x 64 slab of the hi|lo operand (N/64 boxes) into an NST-deep smem ring
+//   warp 1  TMEM owner and MMA issuer: 4 x tcgen05.mma (K = 16 each) per K step, commit to
+//           free the stage; two TMEM accumulators so the epilogue of one item overlaps the
+//           main loop of the next
+//   warps 2-5 epilogue: tcgen05.ld of their 32-lane quarter, hi + lo, fp32 stores
+#include "tc_common.cuh"
+
+namespace fh {
+
+enum XPassKind { kPassXE = 0, kPassXG = 1 };
+
+struct XPassArgs {
+  int64_t rows;         // band rows
+  int n_cells;          // xe: cells contracted; xg: output cells
+  int rp;               // output columns (N = 2 rp)
+  int64_t n_items;
+  int64_t k_chunks;     // xe: chunks of 64 cells; xg: chunks of 64 band rows in total
+  int64_t chunks_per_split;  // xg
+  int cell_tiles;       // xg
+  float* out;           // xe: W[rows][rp]; xg: partial[splits][n_cells][rp]
+  int* status;
+};
+
+constexpr int kXpThreads = 192;
+
+template <int N>
+struct XpCfg {
+  static constexpr uint32_t kA = 128 * 64 * 2;          // 16 KB: two 64 x 64 boxes of X
+  static constexpr uint32_t kB = (uint32_t)N * 64 * 2;  // N/64 boxes of the hi|lo operand
+  static constexpr uint32_t kStage = kA + kB;
+  static constexpr int kStages = (int)((192u * 1024u) / kStage);
+  static constexpr uint32_t kCols = 2 * N;              // two accumulators
+  static constexpr size_t kSmem = (size_t)kStages * kStage + 1024 + 256;
+};
+
+struct XpItem {
+  int x0;        // xe: first band row of the tile; xg: first cell of the tile
+  int split;     // xg
+  int64_t k0, k1;
+};
+
+template <int PASS>
+__device__ __forceinline__ XpItem xp_item(const XPassArgs& p, int64_t item) {
+  XpItem it;
+  if (PASS == kPassXE) {
+    it.x0 = (int)(item * 128);
+    it.split = 0;
+    it.k0 = 0;
+    it.k1 = p.k_chunks;
+  } else {
+    const int ct = (int)(item % p.cell_tiles);
+    it.split = (int)(item / p.cell_tiles);
+    it.x0 = ct * 128;
+    it.k0 = (int64_t)it.split * p.chunks_per_split;
+    it.k1 = it.k0 + p.chunks_per_split;
+    if (it.k1 > p.k_chunks) it.k1 = p.k_chunks;
+    if (it.k0 > it.k1) it.k0 = it.k1;
+  }
+  return it;
+}
+
+template <int PASS, int N>
+__global__ void __launch_bounds__(kXpThreads, 1)
+    xpass_bf16_kernel(const __grid_constant__ CUtensorMap amap,
+                      const __grid_constant__ CUtensorMap bmap, XPassArgs p) {
+  using Cfg = XpCfg<N>;
+  constexpr int NST = Cfg::kStages;
+  constexpr uint32_t kIdesc = idesc_bf16(128, N, PASS == kPassXE, true);
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + (base - raw) + NST * Cfg::kStage);
+  // bars: [0, NST) full, [NST, 2 NST) empty, 2 NST + {0,1} acc full, 2 NST + {2,3} acc empty,
+  //       2 NST + 4 drain
+  uint32_t* misc = reinterpret_cast<uint32_t*>(bars + 2 * NST + 5);
+  // misc: [0] TMEM base, [1] abort flag, [2] stages issued, [3] stages consumed
+  volatile int* abort = reinterpret_cast<volatile int*>(misc + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t bar0 = smem_u32(bars);
+  auto full = [&](uint32_t s) { return bar0 + 8u * s; };
+  auto empty = [&](uint32_t s) { return bar0 + 8u * (NST + s); };
+  auto accf = [&](uint32_t a) { return bar0 + 8u * (2 * NST + a); };
+  auto acce = [&](uint32_t a) { return bar0 + 8u * (2 * NST + 2 + a); };
+  const uint32_t drain = bar0 + 8u * (2 * NST + 4);
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NST; ++i) {
+      mbar_init(full(i), 1);
+      mbar_init(empty(i), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(accf(a), 1);
+      mbar_init(acce(a), 4);
+    }
+    mbar_init(drain, 1);
+    misc[1] = 0;
+    misc[2] = 0;
+    misc[3] = 0;
+    mbar_fence_init();
+    tma_prefetch_map(&amap);
+    tma_prefetch_map(&bmap);
+  }
+  if (warp == 1) {
+    tmem_alloc(smem_u32(misc), Cfg::kCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = misc[0];
+
+  if (warp == 0) {
+    // ------------------------------------------------------------- TMA producer
+    if (lane == 0) {
+      uint32_t it = 0;
+      bool ok = true;
+      for (int64_t item = blockIdx.x; ok && item < p.n_items; item += gridDim.x) {
+        const XpItem w = xp_item<PASS>(p, item);
+        for (int64_t kc = w.k0; kc < w.k1; ++kc, ++it) {
+          const uint32_t s = it % NST, ph = (it / NST) & 1u;
+          if (!mbar_wait(empty(s), ph ^ 1u, abort)) { ok = false; break; }
+          const uint32_t sa = base + s * Cfg::kStage, sb = sa + Cfg::kA;
+          const int k = (int)(kc * 64);
+          mbar_expect_tx(full(s), Cfg::kStage);
+          if (PASS == kPassXE) {
+            tma_load_2d(sa, &amap, w.x0, k, full(s));
+            tma_load_2d(sa + 8192, &amap, w.x0 + 64, k, full(s));
+          } else {
+            tma_load_2d(sa, &amap, k, w.x0, full(s));
+            tma_load_2d(sa + 8192, &amap, k, w.x0 + 64, full(s));
+          }
+#pragma unroll
+          for (int b = 0; b < N / 64; ++b) tma_load_2d(sb + 8192u * b, &bmap, 64 * b, k, full(s));
+          misc[2] = it + 1;
+        }
+      }
+      if (!ok) {
+        *abort = 1;
+        set_status(p.status, FH_ERR_TIMEOUT);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ------------------------------------------------------------- MMA issuer
+    if (lane == 0) {
+      uint32_t it = 0, tc = 0;
+      bool ok = true;
+      for (int64_t item = blockIdx.x; ok && item < p.n_items; item += gridDim.x, ++tc) {
+        const XpItem w = xp_item<PASS>(p, item);
+        const uint32_t a = tc & 1u, aph = (tc >> 1) & 1u;
+        if (!mbar_wait(acce(a), aph ^ 1u, abort)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t d = tmem + a * (uint32_t)N;
+        for (int64_t kc = w.k0; kc < w.k1; ++kc, ++it) {
+          const uint32_t s = it % NST, ph = (it / NST) & 1u;
+          if (!mbar_wait(full(s), ph, abort)) { ok = false; break; }
+          tc_fence_after();
+          misc[3] = it + 1;
+          const uint32_t sa = base + s * Cfg::kStage, sb = sa + Cfg::kA;
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t ad = PASS == kPassXE ? sdesc_sw128(sa + 2048u * kk, 8192, 1024)
+                                                : sdesc_sw128(sa + 32u * kk, 16, 1024);
+            const uint64_t bd = sdesc_sw128(sb + 2048u * kk, 8192, 1024);
+            mma_bf16(d, ad, bd, kIdesc, (kc > w.k0 || kk > 0) ? 1u : 0u);
+          }
+          mma_commit(empty(s));
+        }
+        if (!ok) break;
+        mma_commit(accf(a));
+      }
+      if (!ok) {
+        *abort = 1;
+        set_status(p.status, FH_ERR_TIMEOUT);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------- epilogue (warps 2-5)
+    const int q = warp & 3;   // TMEM lane quarter this warp may access
+    uint32_t tc = 0;
+    for (int64_t item = blockIdx.x; item < p.n_items; item += gridDim.x, ++tc) {
+      const XpItem w = xp_item<PASS>(p, item);
+      const uint32_t a = tc & 1u, aph = (tc >> 1) & 1u;
+      const bool got = __all_sync(0xffffffffu, mbar_wait(accf(a), aph, abort));
+      if (!got) {
+        if (lane == 0) {
+          *abort = 1;
+          set_status(p.status, FH_ERR_TIMEOUT);
+        }
+        break;
+      }
+      tc_fence_after();
+      const int64_t r = (int64_t)w.x0 + 32 * q + lane;
+      float* o;
+      bool valid;
+      if (PASS == kPassXE) {
+        valid = r < p.rows;
+        o = p.out + r * p.rp;
+      } else {
+        valid = r < p.n_cells;
+        o = p.out + ((int64_t)w.split * p.n_cells + r) * p.rp;
+      }
+      const bool has = w.k1 > w.k0;
+      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + a * (uint32_t)N;
+#pragma unroll 1
+      for (int c = 0; c < N / 2; c += 16) {
+        float hi[16], lo[16];
+        tmem_ld16x2(ta + c, ta + N / 2 + c, hi, lo);
+        if (valid) {
+          float4* o4 = reinterpret_cast<float4*>(o + c);
+#pragma unroll
+          for (int v = 0; v < 4; ++v)
+            o4[v] = has ? make_float4(hi[4 * v] + lo[4 * v], hi[4 * v + 1] + lo[4 * v + 1],
+                                      hi[4 * v + 2] + lo[4 * v + 2], hi[4 * v + 3] + lo[4 * v + 3])
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce(a));
+    }
+  }
+
+  // ------------------------------------------------------------- teardown
+  tc_fence_before();
+  __syncthreads();
+  if (*abort) {
+    // An aborted CTA still lets its copies and MMAs in flight land before it releases TMEM
+    // and exits; these waits are time-bounded and ignore the abort flag.
+    if (threadIdx.x == 0)
+      for (uint32_t it = misc[3]; it < misc[2]; ++it) mbar_wait(full(it % NST), (it / NST) & 1u, nullptr);
+    if (threadIdx.x == 32) {
+      mma_commit(drain);
+      mbar_wait(drain, 0, nullptr);
+    }
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, Cfg::kCols);
+  }
+}
+
+// x = hi + lo with hi = bf16(x), lo = bf16(x - hi): dst[row][0, rp) = hi, [rp, 2 rp) = lo.
+__global__ void split_bf16_kernel(const float* __restrict__ src, int64_t n_rows, int rp,
+                                  int64_t ld_src, __nv_bfloat16* __restrict__ dst) {
+  const int64_t n = n_rows * rp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = i / rp;
+    const int m = (int)(i - row * rp);
+    const float x = src[row * ld_src + m];
+    const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+    dst[row * 2 * rp + m] = hi;
+    dst[row * 2 * rp + rp + m] = lo;
+  }
+}
+
+template <int PASS, int N>
+static int launch_xpass(const CUtensorMap& am, const CUtensorMap& bm, const XPassArgs& p,
+                        cudaStream_t s) {
+  auto k = xpass_bf16_kernel<PASS, N>;
+  if (ensure_smem((const void*)k, XpCfg<N>::kSmem)) return FH_ERR_LAUNCH;
+  const int sms = sm_count();
+  if (sms <= 0) return FH_ERR_LAUNCH;
+  const int64_t grid = p.n_items < sms ? p.n_items : sms;
+  k<<<(unsigned)grid, kXpThreads, XpCfg<N>::kSmem, s>>>(am, bm, p);
+  FH_CHECK_LAUNCH();
+  return FH_OK;
+}
+
+template <int PASS>
+static int dispatch_xpass(const CUtensorMap& am, const CUtensorMap& bm, const XPassArgs& p,
+                          cudaStream_t s) {
+  switch (p.rp) {
+    case 32: return launch_xpass<PASS, 64>(am, bm, p, s);
+    case 64: return launch_xpass<PASS, 128>(am, bm, p, s);
+    case 128: return launch_xpass<PASS, 256>(am, bm, p, s);
+    default: return FH_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace fh
+
+using namespace fh;
+
+extern "C" int fh_split_bf16(const float* src, int64_t n_rows, int32_t rp, int64_t ld_src,
+                             uint16_t* dst, void* stream) {
+  if (!src || !dst || n_rows <= 0 || rp <= 0 || ld_src < rp) return FH_ERR_ARG;
+  const int64_t n = n_rows * rp;
+  int64_t blocks = ceil_div(n, 256);
+  if (blocks > 4096) blocks = 4096;
+  split_bf16_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
+      src, n_rows, rp, ld_src, reinterpret_cast<__nv_bfloat16*>(dst));
+  FH_CHECK_LAUNCH();
+  return FH_OK;
+}
+
+extern "C" int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total,
+                          int32_t n_cells, int64_t rows, const uint16_t* E2, int32_t rp, float* W,
+                          int* status, void* stream) {
+  if (!X16 || !E2 || !W || n_cells <= 0 || n_cells > n_cells_total || rows <= 0 || ldx < rows ||
+      ldx % 128)
+    return FH_ERR_ARG;
+  if (rp != 32 && rp != 64 && rp != 128) return FH_ERR_UNSUPPORTED;
+  // the map ends at the last 128-row tile, so no box reads past the band rows asked for
+  const uint64_t inner = (uint64_t)ceil_div(rows, 128) * 128;
+  CUtensorMap am, bm;
+  if (!make_map_bf16(&am, X16, inner, (uint64_t)n_cells_total, (uint64_t)ldx, 64) ||
+      !make_map_bf16(&bm, E2, (uint64_t)(2 * rp), (uint64_t)n_cells, (uint64_t)(2 * rp), 64))
+    return FH_ERR_LAUNCH;
+  XPassArgs p{};
+  p.rows = rows;
+  p.n_cells = n_cells;
+  p.rp = rp;
+  p.n_items = ceil_div(rows, 128);
+  p.k_chunks = ceil_div(n_cells, 64);
+  p.out = W;
+  p.status = status;
+  return dispatch_xpass<kPassXE>(am, bm, p, (cudaStream_t)stream);
+}
+
+// Splits of the band-row dimension for fh_xg_bf16: about whole waves of items over the SMs,
+// each split at least 16 chunks of 64 band rows.
+extern "C" int fh_xg_bf16_splits(int32_t n_cells, int64_t rows) {
+  if (n_cells <= 0 || rows <= 0) return 1;
+  const int sms = sm_count() > 0 ? sm_count() : 152;
+  const int64_t ct = ceil_div(n_cells, 128), chunks = ceil_div(rows, 64);
+  int best = 1;
+  double best_cost = 1e300;
+  for (int s = 1; s <= 256; ++s) {
+    if (s > 1 && ceil_div(chunks, s) < 16) break;
+    const int64_t items = ct * s;
+    const double cost = (double)ceil_div(items, sms) / s * (1.0 + 0.002 * s);
+    if (cost < best_cost) { best_cost = cost; best = s; }
+  }
+  return best;
+}
+
+extern "C" int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total,
+                          int32_t n_cells, int64_t rows, const uint16_t* G2, int32_t rp,
+                          int32_t splits, float* partial, float* out, int* status, void* stream) {
+  if (!X16 || !G2 || !partial || !out || n_cells <= 0 || n_cells > n_cells_total || rows <= 0 ||
+      ldx < rows || ldx % 128 || splits <= 0)
+    return FH_ERR_ARG;
+  if (rp != 32 && rp != 64 && rp != 128) return FH_ERR_UNSUPPORTED;
+  const uint64_t inner = (uint64_t)ceil_div(rows, 128) * 128;
+  CUtensorMap am, bm;
+  if (!make_map_bf16(&am, X16, inner, (uint64_t)n_cells_total, (uint64_t)ldx, 64) ||
+      !make_map_bf16(&bm, G2, (uint64_t)(2 * rp), (uint64_t)rows, (uint64_t)(2 * rp), 64))
+    return FH_ERR_LAUNCH;
+  const int64_t chunks = ceil_div(rows, 64);
+  const int64_t per = ceil_div(chunks, splits);
+  const int used = (int)ceil_div(chunks, per);   // every split non-empty
+  XPassArgs p{};
+  p.rows = rows;
+  p.n_cells = n_cells;
+  p.rp = rp;
+  p.cell_tiles = (int)ceil_div(n_cells, 128);
+  p.n_items = (int64_t)p.cell_tiles * used;
+  p.k_chunks = chunks;
+  p.chunks_per_split = per;
+  p.out = partial;
+  p.status = status;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = dispatch_xpass<kPassXG>(am, bm, p, s);
+  if (rc) return rc;
+  const int64_t n = (int64_t)n_cells * rp;
+  int64_t blocks = ceil_div(n, 256);
+  if (blocks > 4096) blocks = 4096;
+  reduce_splits_kernel<float><<<(unsigned)blocks, 256, 0, s>>>(partial, used, n, out);
+  FH_CHECK_LAUNCH();
+  return FH_OK;
+}

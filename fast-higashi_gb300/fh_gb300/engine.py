@@ -1,8 +1,12 @@
 """Device-resident fit engine: contact build, RWR once, then the ALS sweep as kernel launches.
 
+Two forms share everything but X and the two passes over it:
+  precision="fp32"  the plain drop-in: X in fp32, CUDA-core passes (fh_xe_f32 / fh_xg_f32)
+  precision="bf16"  the batched tensor-core form: X in bf16, tcgen05 passes (fh_xe_bf16 /
+                    fh_xg_bf16) with the small operands split hi|lo; every other step fp32
 Layout in HBM (all on one GPU):
   entries   packed contacts, one segment per (bin batch, cell)           8 B / contact
-  X         RWR output of every cell: X[cell][band row]                   4 B / element
+  X / X16   RWR output of every cell: X[cell][band row]              4 B / 2 B per element
             band row = tile.xoff + i * width + j; the row stride is padded to 128
   W, Gt     [band row][rp]: X^T E and the projection rows U M^T
   U         projections, tile-major (rows, width, r) as the reference's projection_list
@@ -30,9 +34,14 @@ def _pad_rank(R):
 
 
 class FitEngine:
-    def __init__(self, schic, rank, chrom2size, n_i, device, do_rwr=True, stream=None):
+    def __init__(self, schic, rank, chrom2size, n_i, device, do_rwr=True, stream=None,
+                 precision="fp32"):
         import torch
         self.torch = torch
+        if precision not in ("fp32", "bf16"):
+            raise _lib.FHError("FitEngine", 1, "precision must be 'fp32' or 'bf16'")
+        self.precision = precision
+        self.bf16 = precision == "bf16"
         self.timing = None   # {kernel family: [(start event, end event)]} when enabled
         self.device = torch.device(device)
         if self.device.type != "cuda":
@@ -41,6 +50,8 @@ class FitEngine:
         self.schic = schic
         self.R = int(rank)
         self.rp = _pad_rank(self.R)
+        if self.bf16:
+            self.rp = max(self.rp, 32)   # the tensor-core passes take N = 2 rp >= 64
         self.ld = self.rp
         self.C = schic[0].num_cell
         self.Ct = schic[0].total_cell_num
@@ -85,7 +96,12 @@ class FitEngine:
         # ---- contacts and RWR (once)
         self.store = ContactStore(schic, dev, self.tiles, self.tile_base, stream)
         self.tiles_dev = self.store.tiles_dev
-        self.X = torch.zeros((self.Ct, self.ldx), dtype=f32, device=dev)
+        if self.bf16:
+            self.X = None
+            self.X16 = torch.zeros((self.Ct, self.ldx), dtype=torch.bfloat16, device=dev)
+        else:
+            self.X = torch.zeros((self.Ct, self.ldx), dtype=f32, device=dev)
+            self.X16 = None
         self.sumsq = torch.zeros(self.n_tiles * self.Ct, dtype=f64, device=dev)
         if n_i is not None:
             self.run_rwr()
@@ -100,7 +116,10 @@ class FitEngine:
         self.U = torch.zeros(max(self.u_size, 1), dtype=f32, device=dev)
         self.Y = torch.zeros((self.nb, self.ld, self.rp), dtype=f32, device=dev)
         self.S = torch.zeros((self.Ct, self.rp), dtype=f32, device=dev)
-        self.splits = _lib.value("fh_xg_splits", self.Ct, self.rows)
+        self.splits = max(self.xg_splits(self.C, self.rows), self.xg_splits(self.Ct, self.rows))
+        if self.bf16:
+            self.E2 = torch.zeros((self.Ct, 2 * self.rp), dtype=torch.bfloat16, device=dev)
+            self.G2 = torch.zeros((self.rows, 2 * self.rp), dtype=torch.bfloat16, device=dev)
         self.partial = torch.empty((self.splits, self.Ct, self.rp), dtype=f32, device=dev)
         self.ssum = torch.zeros(self.nb, dtype=f64, device=dev)
         self.meta_ssum = torch.zeros(1, dtype=f64, device=dev)
@@ -184,9 +203,50 @@ class FitEngine:
 
     def _run_rwr(self):
         P = _lib.ptr
-        _lib.call("fh_rwr_tiles_f32", P(self.tiles_dev), self.n_tiles, self.Ct, self.max_rows,
-                  self.max_width, P(self.store.entries), P(self.store.offsets), P(self.X),
-                  self.ldx, P(self.sumsq), P(self.status), self.sp())
+        if self.bf16:
+            _lib.call("fh_rwr_tiles_bf16", P(self.tiles_dev), self.n_tiles, self.Ct,
+                      self.max_rows, self.max_width, P(self.store.entries),
+                      P(self.store.offsets), P(self.X16), self.ldx, P(self.sumsq),
+                      P(self.status), self.sp())
+        else:
+            _lib.call("fh_rwr_tiles_f32", P(self.tiles_dev), self.n_tiles, self.Ct,
+                      self.max_rows, self.max_width, P(self.store.entries),
+                      P(self.store.offsets), P(self.X), self.ldx, P(self.sumsq),
+                      P(self.status), self.sp())
+
+    # ------------------------------------------------------------------ X passes
+    def xg_splits(self, n_cells, rows):
+        name = "fh_xg_bf16_splits" if self.bf16 else "fh_xg_splits"
+        return _lib.value(name, n_cells, rows)
+
+    def x_times_e(self, a0, rows, n_cells, E, rp, W, E2=None):
+        """W[row][m] = sum_{c < n_cells} X[c][a0 + row] E[c][m]  (E: [n_cells][rp] fp32,
+        W: [rows][rp]); a0 is a multiple of 128."""
+        P = _lib.ptr
+        if self.bf16:
+            if E2 is None:
+                E2 = self.torch.empty((n_cells, 2 * rp), dtype=self.torch.bfloat16,
+                                      device=self.device)
+            _lib.call("fh_split_bf16", P(E), n_cells, rp, rp, P(E2), self.sp())
+            _lib.call("fh_xe_bf16", P(self.X16[:, a0:]), self.ldx, self.Ct, n_cells, rows, P(E2),
+                      rp, P(W), P(self.status), self.sp())
+        else:
+            _lib.call("fh_xe_f32", P(self.X[:, a0:]), self.ldx, n_cells, rows, P(E), rp, P(W),
+                      self.sp())
+
+    def x_times_g(self, a0, rows, n_cells, Gt, rp, splits, partial, out, G2=None):
+        """out[c][m] = sum_row X[c][a0 + row] Gt[row][m] for c < n_cells (Gt: [rows][rp])."""
+        P = _lib.ptr
+        if self.bf16:
+            if G2 is None:
+                G2 = self.torch.empty((rows, 2 * rp), dtype=self.torch.bfloat16,
+                                      device=self.device)
+            _lib.call("fh_split_bf16", P(Gt), rows, rp, rp, P(G2), self.sp())
+            _lib.call("fh_xg_bf16", P(self.X16[:, a0:]), self.ldx, self.Ct, n_cells, rows, P(G2),
+                      rp, splits, P(partial), P(out), P(self.status), self.sp())
+        else:
+            _lib.call("fh_xg_f32", P(self.X[:, a0:]), self.ldx, n_cells, rows, P(Gt), rp, splits,
+                      P(partial), P(out), self.sp())
 
     def tensor_norms(self):
         """||X||^2 per dataset over the good-QC cells (parafac2_intergrative.py:369)."""
@@ -244,9 +304,8 @@ class FitEngine:
 
     # ------------------------------------------------------------------ kernels
     def xe(self):
-        P = _lib.ptr
-        self._timed("xe", lambda: _lib.call("fh_xe_f32", P(self.X), self.ldx, self.C, self.rows,
-                                            P(self.E), self.rp, P(self.W), self.sp()))
+        self._timed("xe", lambda: self.x_times_e(0, self.rows, self.C, self.E, self.rp, self.W,
+                                                 self.E2[:self.C] if self.bf16 else None))
 
     def procrustes(self):
         P = _lib.ptr
@@ -256,10 +315,10 @@ class FitEngine:
             self.rp, P(self.U), P(self.Gt), P(self.ssum), P(self.status), self.sp()))
 
     def xg(self, n_cells):
-        P = _lib.ptr
-        self._timed("xg", lambda: _lib.call("fh_xg_f32", P(self.X), self.ldx, n_cells, self.rows,
-                                            P(self.Gt), self.rp, self.splits, P(self.partial),
-                                            P(self.S), self.sp()))
+        self._timed("xg", lambda: self.x_times_g(0, self.rows, n_cells, self.Gt, self.rp,
+                                                 self.xg_splits(n_cells, self.rows),
+                                                 self.partial, self.S,
+                                                 self.G2 if self.bf16 else None))
 
     def meta_polar(self, n_cells, E_out):
         P = _lib.ptr

@@ -86,25 +86,24 @@ def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
     a1 = min(eng.ldx, int(math.ceil(x1 / 128) * 128))
     rows = a1 - a0
     n = n_comp + n_oversamples
-    rp = 128 if n > 64 else (64 if n > 32 else (32 if n > 16 else 16))
+    rp = 128 if n > 64 else (64 if n > 32 else (32 if n > 16 or eng.bf16 else 16))
     dev, f32 = eng.device, torch.float32
-    Xk = eng.X[:, a0:]                        # row stride stays ldx
     W = torch.zeros((rows, rp), dtype=f32, device=dev)
     S = torch.zeros((C, rp), dtype=f32, device=dev)
-    splits = _lib.value("fh_xg_splits", C, rows)
+    splits = eng.xg_splits(C, rows)
     part = torch.empty((splits, C, rp), dtype=f32, device=dev)
     lo, hi = x0 - a0, x1 - a0
 
     def ft_times(Ecells):                     # F^T E: (band rows of k) x n
         E = torch.zeros((C, rp), dtype=f32, device=dev)
         E[:, :n] = Ecells
-        _lib.call("fh_xe_f32", P(Xk), eng.ldx, C, rows, P(E), rp, P(W), eng.sp())
+        eng.x_times_e(a0, rows, C, E, rp, W)
         return W[lo:hi, :n].clone()
 
     def f_times(Qrows):                       # F Q: cells x n
         G = torch.zeros((rows, rp), dtype=f32, device=dev)
         G[lo:hi, :n] = Qrows
-        _lib.call("fh_xg_f32", P(Xk), eng.ldx, C, rows, P(G), rp, splits, P(part), P(S), eng.sp())
+        eng.x_times_g(a0, rows, C, G, rp, splits, part, S)
         return S[:, :n].clone()
 
     omega = torch.from_numpy(rng.standard_normal((C, n)).astype(np.float32)).to(dev)
@@ -129,7 +128,8 @@ def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
               for d in schic]
     B_dict = {c: torch.eye(s, device=device).add_(torch.randn(s, device=device), alpha=1e-2)
               for c, s in sizes.items()}
-    eng = FitEngine(schic, rank, sizes, None, device, do_rwr=do_rwr)
+    eng = FitEngine(schic, rank, sizes, None, device, do_rwr=do_rwr,
+                    precision=getattr(model, "precision", "fp32"))
     model.engine = eng
     if do_rwr:
         n_i, feat_epochs = auto_epochs(eng, schic)

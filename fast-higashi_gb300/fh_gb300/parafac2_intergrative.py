@@ -22,8 +22,11 @@ from .engine import FitEngine
 
 
 class Fast_Higashi_core:
-    def __init__(self, rank, off_diag, res_list):
+    def __init__(self, rank, off_diag, res_list, precision="fp32"):
+        """precision: "fp32" is the plain drop-in (the reference's arithmetic on CUDA cores);
+        "bf16" keeps the RWR output in bf16 and runs the passes over it on the tensor cores."""
         self.rank = rank
+        self.precision = precision
         self.sparse_conv = False
         self.off_diag = off_diag
         self.res_list = res_list
@@ -86,7 +89,7 @@ class Fast_Higashi_core:
     def _engine(self, schic, do_rwr):
         if self.engine is None or self.engine.schic is not schic:
             self.engine = FitEngine(schic, self.rank, self.chrom2size, self.n_i, self.device,
-                                    do_rwr=do_rwr)
+                                    do_rwr=do_rwr, precision=self.precision)
         return self.engine
 
     def fit(self, schic, size_ratio=0.3, n_iter_max=2000, n_iter_parafac=5, do_conv=True,

@@ -111,6 +111,13 @@ int fh_rwr_tiles_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
                      const int64_t* offsets, float* out, int64_t cell_stride, double* sumsq,
                      int* status, void* stream);
 
+/* fh_rwr_tiles_f32 with the output rounded to bf16 (out16: bf16 bits, same indexing); the
+ * sumsq entries are taken over the rounded values.  Feeds fh_xe_bf16 / fh_xg_bf16. */
+int fh_rwr_tiles_bf16(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                      int32_t max_rows, int32_t max_width, const fh_entry* entries,
+                      const int64_t* offsets, uint16_t* out16, int64_t cell_stride,
+                      double* sumsq, int* status, void* stream);
+
 /* Same arithmetic on a dense tile x[n_cells][rows][width] (the partial_rwr drop-in: no
  * floor is applied to x); out[n_cells][rows][width]. */
 int fh_rwr_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width, int32_t s0,
@@ -144,6 +151,30 @@ int fh_xe_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const 
 int fh_xg_splits(int32_t n_cells, int64_t rows);
 int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const float* Gt,
               int32_t rp, int32_t splits, float* partial, float* out, void* stream);
+
+/* ---- the same two passes over X held in bf16, on the tcgen05 tensor cores (no reference
+ * counterpart: the reference's passes are fp32 torch.bmm / opt_einsum calls at
+ * parafac2_intergrative.py:374-383, 422-430 and 522-529).
+ * X16: bf16[n_cells_total][ldx] (ldx % 128 == 0, columns >= rows zero), written by
+ * fh_rwr_tiles_bf16.  The small operand is passed split, hi | lo = fh_split_bf16(x), so
+ * the products carry it to 16 significant bits; the error is X's bf16 rounding.
+ * fh_split_bf16: dst[row][0, rp) = bf16(x), dst[row][rp, 2 rp) = bf16(x - bf16(x)) for
+ *                x = src[row * ld_src + m].
+ * fh_xe_bf16:    W[row][m] = sum_{c < n_cells} X16[c][row] E[c][m];  E2 = split of E
+ *                (bf16[n_cells][2 rp]).  rp in {32, 64, 128}.
+ * fh_xg_bf16:    out[c][m] = sum_row X16[c][row] Gt[row][m] for c < n_cells;  G2 = split of
+ *                Gt (bf16[rows][2 rp]); partial: float[splits][n_cells][rp] with splits from
+ *                fh_xg_bf16_splits (fixed-order reduction).
+ * status: int32 device word; a device-side wait that runs out sets FH_ERR_TIMEOUT. */
+int fh_split_bf16(const float* src, int64_t n_rows, int32_t rp, int64_t ld_src, uint16_t* dst,
+                  void* stream);
+int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t n_cells,
+               int64_t rows, const uint16_t* E2, int32_t rp, float* W, int* status,
+               void* stream);
+int fh_xg_bf16_splits(int32_t n_cells, int64_t rows);
+int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t n_cells,
+               int64_t rows, const uint16_t* G2, int32_t rp, int32_t splits, float* partial,
+               float* out, int* status, void* stream);
 
 /* Y[g][l][m] = sum_j U_g[j][l] W[xoff + i*width + j][m] for every bin row g (K16 tail,
  * parafac2_intergrative.py:522-529); Y: float[n_rows][ldy_l][rp]; row_tile: int32[n_rows]. */
