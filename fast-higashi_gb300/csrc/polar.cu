@@ -71,8 +71,7 @@ __global__ void __launch_bounds__(kPolThreads) meta_small_kernel(const double* _
   float* X = fbase;
   float* Aug = X + (size_t)R * ldt;
   float* misc = Aug + newton_scratch_floats(R);
-  PolarScratch s{misc, misc + kMaxRank, misc + 2 * kMaxRank, misc + 4 * kMaxRank, red, dred,
-                 ival};
+  PolarScratch s = polar_scratch(misc, red, dred, ival);
   if (tid == 0) ival[0] = 0;
   for (int idx = tid; idx < R * R; idx += kPolThreads) G[idx] = Gg[idx];
   __syncthreads();

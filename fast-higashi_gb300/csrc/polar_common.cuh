@@ -18,8 +18,62 @@ struct PolarScratch {
   float* red;    // [32]
   double* dred;  // [32]
   int* ival;     // [4]: [0] a zero pivot was met
+  float* gcol;   // [2][64]  register Gauss-Jordan: pivot column (double-buffered)
+  float* grow;   // [2][128] scaled pivot row
+  float* grp;    // [2]      1 / pivot
+  int* gi;       // [0, 64) row used as a pivot, [64, 128) step that pivoted the row, [128, 130) pivot
 };
-constexpr int kPolarMiscFloats = 5 * kMaxRank + 64;
+constexpr int kPolarMiscFloats = 5 * kMaxRank + 64 + 128 + 256 + 4 + 132;
+
+// Carves the scratch out of kPolarMiscFloats floats of shared memory.
+__device__ inline PolarScratch polar_scratch(float* misc, float* red, double* dred, int* ival) {
+  PolarScratch s;
+  s.vh = misc;
+  s.beta = misc + kMaxRank;
+  s.wv = misc + 2 * kMaxRank;
+  s.fcol = misc + 4 * kMaxRank;
+  s.red = red;
+  s.dred = dred;
+  s.ival = ival;
+  float* g = misc + 5 * kMaxRank + 64;
+  s.gcol = g;
+  s.grow = g + 128;
+  s.grp = g + 384;
+  s.gi = reinterpret_cast<int*>(g + 388);
+  return s;
+}
+
+// ---- register-tiled CTA matrix product (512 threads) -----------------------------------
+// acc[u][v] = sum_k fa(i_u, k) fb(k, j_v) for the thread's outputs i_u = warp + 16 u,
+// j_v = lane + 32 v (u < TM, v < TN), k in increasing order.  Rows / columns past M / N are
+// clamped to the last one (their results are to be discarded).  fa is read with one address
+// per warp (a broadcast), fb with consecutive or odd-strided addresses across the lanes.
+template <int TM, int TN, class FA, class FB>
+__device__ __forceinline__ void cta_mm(int M, int N, int K, int row0, FA fa, FB fb,
+                                       float (&acc)[TM][TN]) {
+  const int rt = threadIdx.x >> 5, ct = threadIdx.x & 31;
+  int ri[TM], cj[TN];
+#pragma unroll
+  for (int u = 0; u < TM; ++u) ri[u] = min(row0 + rt + 16 * u, M - 1);
+#pragma unroll
+  for (int v = 0; v < TN; ++v) cj[v] = min(ct + 32 * v, N - 1);
+#pragma unroll
+  for (int u = 0; u < TM; ++u)
+#pragma unroll
+    for (int v = 0; v < TN; ++v) acc[u][v] = 0.f;
+#pragma unroll 2
+  for (int k = 0; k < K; ++k) {
+    float av[TM], bv[TN];
+#pragma unroll
+    for (int u = 0; u < TM; ++u) av[u] = fa(ri[u], k);
+#pragma unroll
+    for (int v = 0; v < TN; ++v) bv[v] = fb(k, cj[v]);
+#pragma unroll
+    for (int u = 0; u < TM; ++u)
+#pragma unroll
+      for (int v = 0; v < TN; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+  }
+}
 
 __device__ __forceinline__ int pc_lane() { return threadIdx.x & 31; }
 __device__ __forceinline__ int pc_warp() { return threadIdx.x >> 5; }
@@ -167,6 +221,112 @@ __device__ inline void gj_inverse(const float* X, int ldx, float* Aug, int r, Po
   }
 }
 
+// ---- inverse of X (r x r, r <= 64, stride ldx) into Xi (stride ldo), 512 threads -------
+// Gauss-Jordan with partial pivoting on [X | I] held in registers: thread (warp w, lane l)
+// owns rows w + 16 u (u < 4) and columns l + 32 v (v < 4).  Rows are not swapped: each step
+// picks the largest |entry| of the column among the rows not yet used as pivots, so every
+// element sees the same operations as in gj_inverse; row p_k of the right block is row k of
+// X^{-1}.  Three barriers per column, no shared-memory traffic for the matrix itself.
+__device__ inline void gj_inverse_reg(const float* X, int ldx, float* Xi, int ldo, int r,
+                                      PolarScratch& s) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  int* used = s.gi;
+  int* kof = s.gi + 64;
+  int* pidx = s.gi + 128;
+  float a[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = w + 16 * u;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int j = l + 32 * v;
+      float x = 0.f;
+      if (i < r) {
+        if (j < r) x = X[i * ldx + j];
+        else if (j - r == i) x = 1.f;
+      }
+      a[u][v] = x;
+    }
+  }
+  if (threadIdx.x < 64) used[threadIdx.x] = threadIdx.x < r ? 0 : 1;
+  for (int k = 0; k < r; ++k) {
+    const int b = k & 1;
+    float* colk = s.gcol + 64 * b;
+    float* prow = s.grow + 128 * b;
+    if (l == (k & 31)) {
+      const bool hi = (k >> 5) != 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) colk[w + 16 * u] = hi ? a[u][1] : a[u][0];
+    }
+    __syncthreads();
+    if (w == 0) {
+      float best = -1.f;
+      int bi = 64;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int i = l + 32 * h;
+        if (!used[i]) {
+          const float v = fabsf(colk[i]);
+          if (v > best) { best = v; bi = i; }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (l == 0) {
+        float pv = colk[bi];
+        if (pv == 0.f) { pv = 1e-30f; s.ival[0] = 1; }
+        pidx[b] = bi;
+        s.grp[b] = 1.f / pv;
+        used[bi] = 1;
+        kof[bi] = k;
+      }
+    }
+    __syncthreads();
+    const int p = pidx[b];
+    if (w == (p & 15)) {
+      const int pu = p >> 4;
+      const float rp = s.grp[b];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (u == pu) {
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            a[u][v] *= rp;
+            prow[l + 32 * v] = a[u][v];
+          }
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = w + 16 * u;
+      if (i != p) {
+        const float f = -colk[i];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) a[u][v] = fmaf(f, prow[l + 32 * v], a[u][v]);
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = w + 16 * u;
+    if (i < r) {
+      const int kk = kof[i];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int j = l + 32 * v;
+        if (j >= r && j < 2 * r) Xi[kk * ldo + (j - r)] = a[u][v];
+      }
+    }
+  }
+  __syncthreads();
+}
+
 // Scratch floats newton_polar needs after X: [X | I] (r x (2r+1)) or two r x (r+1) buffers.
 __host__ __device__ inline size_t newton_scratch_floats(int r) { return 2 * (size_t)r * (r + 1) + 8; }
 
@@ -237,6 +397,77 @@ __device__ inline void newton_polar(float* X, int ldx, float* Aug, int r, bool u
     const float rel = sqrtf(dn / nn);
     if (last) break;
     if (schulz && rel < 3e-5f) last = true;     // quadratic: one more step reaches ~1e-9
+    if (!schulz && rel < 0.1f) schulz = true;
+  }
+}
+
+// ---- newton_polar for r <= 64 on 512 threads ------------------------------------------
+// The same iteration with the Gauss-Jordan inverse in registers and the Newton-Schulz
+// products register-tiled; every element sees the same arithmetic as newton_polar.
+// Sc: r x ldx scratch (X^{-1}, then 1.5 I - 0.5 X^T X); ldx odd.
+__device__ inline void newton_polar_r64(float* X, int ldx, float* Sc, int r, bool upper,
+                                        PolarScratch& s) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  bool schulz = false, last = false;
+  for (int it = 0; it < kNewtonMaxIt; ++it) {
+    float dn = 0.f, nn = 0.f;
+    if (!schulz) {
+      if (it == 0 && upper) tri_inverse(X, ldx, Sc, ldx, r, s);
+      else gj_inverse_reg(X, ldx, Sc, ldx, r, s);
+      float a = 0.f, b = 0.f;
+      for (int i = w; i < r; i += 16)
+        for (int j = l; j < r; j += 32) {
+          a = fmaf(X[i * ldx + j], X[i * ldx + j], a);
+          b = fmaf(Sc[i * ldx + j], Sc[i * ldx + j], b);
+        }
+      a = block_sum<float>(a, s.red);
+      b = block_sum<float>(b, s.red);
+      float zeta = sqrtf(sqrtf(b) / sqrtf(a));
+      if (it >= 1 && fabsf(zeta - 1.f) < 1e-2f) zeta = 1.f;
+      const float iz = 1.f / zeta;
+      for (int i = w; i < r; i += 16)
+        for (int j = l; j < r; j += 32) {
+          const float x = X[i * ldx + j];
+          const float xn = 0.5f * (zeta * x + iz * Sc[j * ldx + i]);
+          const float d = xn - x;
+          dn = fmaf(d, d, dn);
+          nn = fmaf(xn, xn, nn);
+          X[i * ldx + j] = xn;
+        }
+    } else {
+      float acc[4][2];
+      cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return X[k * ldx + i]; },
+                   [&](int k, int j) { return X[k * ldx + j]; }, acc);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const int i = w + 16 * u, j = l + 32 * v;
+          if (i < r && j < r) Sc[i * ldx + j] = (i == j ? 1.5f : 0.f) - 0.5f * acc[u][v];
+        }
+      __syncthreads();
+      cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return X[i * ldx + k]; },
+                   [&](int k, int j) { return Sc[k * ldx + j]; }, acc);
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const int i = w + 16 * u, j = l + 32 * v;
+          if (i < r && j < r) {
+            const float d = acc[u][v] - X[i * ldx + j];
+            dn = fmaf(d, d, dn);
+            nn = fmaf(acc[u][v], acc[u][v], nn);
+            X[i * ldx + j] = acc[u][v];
+          }
+        }
+    }
+    dn = block_sum<float>(dn, s.red);
+    nn = block_sum<float>(nn, s.red);
+    __syncthreads();
+    const float rel = sqrtf(dn / nn);
+    if (last) break;
+    if (schulz && rel < 3e-5f) last = true;
     if (!schulz && rel < 0.1f) schulz = true;
   }
 }

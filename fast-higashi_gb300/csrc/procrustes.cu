@@ -36,23 +36,71 @@ struct ProcArgs {
   int mode;          // 0 fit step, 1 Gt from the stored U (transform)
 };
 
-__host__ __device__ inline size_t proc_region_floats(int n, int r, int rp) {
-  const int ldt = r + 1;
-  size_t region = (size_t)n * ldt;                                  // U
-  const size_t newton = (size_t)r * ldt + newton_scratch_floats(r); // X + scratch
-  if (newton > region) region = newton;
-  const size_t stage = (size_t)rp * ldt + (size_t)r * ldt;          // D diag(A), B
-  if (stage > region) region = stage;
-  return region;
+// Shared memory: two regions of row stride ldt = r + 1 and the polar scratch.
+//   region 0 (max(n, RP + r) rows): D diag(A_g) and B staging, then temp -> R and the
+//            Householder vectors, then the staging and M again for the Gt product
+//   region 1 (max(n, 2 r, RP) rows): M, then the Newton iterate X (rows < r) with its
+//            scratch (rows r .. 2r), then U = Q [polar(R); 0]
+__host__ __device__ inline int proc_r0_rows(int n, int r, int rp) { return n > rp + r ? n : rp + r; }
+__host__ __device__ inline int proc_r1_rows(int n, int r, int rp) {
+  int m = n > 2 * r ? n : 2 * r;
+  return m > rp ? m : rp;
+}
+__host__ __device__ inline size_t proc_smem_floats(int n, int r, int rp) {
+  return (size_t)(proc_r0_rows(n, r, rp) + proc_r1_rows(n, r, rp)) * (r + 1) + kPolarMiscFloats;
 }
 
-__host__ __device__ inline size_t proc_smem_floats(int n, int r, int rp) {
-  const int ldt = r + 1;
-  return (size_t)rp * ldt + (size_t)n * ldt + proc_region_floats(n, r, rp) + kPolarMiscFloats;
+// M[m][l] = sum_rho D[m][rho] A_g[rho] B[l][rho] (m < RP, rows m >= R zero) into dst (stride
+// ldt); stage: (RP + r) x ldt floats, may overlap dst.  Called by the whole CTA.
+template <int RP>
+__device__ inline void form_m(const ProcArgs& a, int64_t g, int ci, int r, int ldt, float* stage,
+                              float* dst) {
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  float* DA = stage;
+  float* Bs = stage + (size_t)RP * ldt;
+  const float* Ag = a.A + g * a.lda;
+  const float* Dc = a.D + (size_t)ci * RP * a.ldb;
+  const float* Bc = a.B + (size_t)ci * a.ldb * a.ldb;
+  for (int m = ty; m < RP; m += 16)
+    for (int rho = tx; rho < r; rho += 32)
+      DA[m * ldt + rho] = m < a.R ? Dc[m * a.ldb + rho] * Ag[rho] : 0.f;
+  for (int l = ty; l < r; l += 16)
+    for (int rho = tx; rho < r; rho += 32) Bs[l * ldt + rho] = Bc[l * a.ldb + rho];
+  __syncthreads();
+  float acc[4][2];
+  cta_mm<4, 2>(RP, r, r, 0, [&](int m, int rho) { return DA[m * ldt + rho]; },
+               [&](int rho, int l) { return Bs[l * ldt + rho]; }, acc);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int m = ty + 16 * u, l = tx + 32 * v;
+      if (m < RP && l < r) dst[m * ldt + l] = acc[u][v];
+    }
+  __syncthreads();
+}
+
+// Gg[i][m] = sum_l U[i][l] M[m][l] for i < n, m < RP (U read through fu(i, l)).
+template <int RP, class FU>
+__device__ inline void gt_rows(int n, int r, int ldt, FU fu, const float* M, float* Gg) {
+  constexpr int TN = RP >= 64 ? 2 : 1;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int row0 = 0; row0 < n; row0 += 96) {
+    float acc[6][TN];
+    cta_mm<6, TN>(n, RP, r, row0, fu, [&](int l, int m) { return M[m * ldt + l]; }, acc);
+#pragma unroll
+    for (int u = 0; u < 6; ++u)
+#pragma unroll
+      for (int v = 0; v < TN; ++v) {
+        const int i = row0 + ty + 16 * u, m = tx + 32 * v;
+        if (i < n && m < RP) Gg[(int64_t)i * RP + m] = acc[u][v];
+      }
+  }
 }
 
 template <int RP>
-__global__ void __launch_bounds__(kProcThreads) procrustes_qr_kernel(ProcArgs a) {
+__global__ void __launch_bounds__(kProcThreads, 2) procrustes_qr_kernel(ProcArgs a) {
   extern __shared__ __align__(16) float sm[];
   __shared__ float red[32];
   __shared__ double dred[32];
@@ -61,92 +109,64 @@ __global__ void __launch_bounds__(kProcThreads) procrustes_qr_kernel(ProcArgs a)
   const int64_t g = blockIdx.x;
   const fh_tile T = a.tiles[a.row_tile[g]];
   const int i0 = (int)(g - T.brow0);
-  const int n = T.width, r = T.rank, ci = T.chrom, R = a.R;
+  const int n = T.width, r = T.rank, ci = T.chrom;
   const int ldt = r + 1;
-  float* Ms = sm;                        // RP x ldt: M[m][l]
-  float* Tm = Ms + (size_t)RP * ldt;     // n x ldt: temp, then R and the reflectors
-  float* reg = Tm + (size_t)n * ldt;     // reused region
-  float* misc = reg + proc_region_floats(n, r, RP);
-  PolarScratch s{misc, misc + kMaxRank, misc + 2 * kMaxRank, misc + 4 * kMaxRank, red, dred,
-                 ival};
+  float* R0 = sm;
+  float* R1 = R0 + (size_t)proc_r0_rows(n, r, RP) * ldt;
+  float* misc = R1 + (size_t)proc_r1_rows(n, r, RP) * ldt;
+  PolarScratch s = polar_scratch(misc, red, dred, ival);
   if (tid == 0) ival[0] = 0;
-  // ---- M[m][l] = sum_rho D[m][rho] A_g[rho] B[l][rho]
-  {
-    float* DA = reg;
-    float* Bs = reg + (size_t)RP * ldt;
-    const float* Ag = a.A + g * a.lda;
-    const float* Dc = a.D + (size_t)ci * RP * a.ldb;
-    const float* Bc = a.B + (size_t)ci * a.ldb * a.ldb;
-    for (int m = ty; m < RP; m += nw)
-      for (int rho = tx; rho < r; rho += 32)
-        DA[m * ldt + rho] = m < R ? Dc[m * a.ldb + rho] * Ag[rho] : 0.f;
-    for (int l = ty; l < r; l += nw)
-      for (int rho = tx; rho < r; rho += 32) Bs[l * ldt + rho] = Bc[l * a.ldb + rho];
-    __syncthreads();
-    for (int m = ty; m < RP; m += nw)
-      for (int l = tx; l < r; l += 32) {
-        float acc = 0.f;
-        for (int rho = 0; rho < r; ++rho) acc = fmaf(DA[m * ldt + rho], Bs[l * ldt + rho], acc);
-        Ms[m * ldt + l] = acc;
-      }
-    __syncthreads();
-  }
   const int64_t brow = T.xoff + (int64_t)i0 * n;
   float* Gg = a.Gt + brow * RP;
+  form_m<RP>(a, g, ci, r, ldt, R0, R1);   // M in region 1
   if (a.mode == 1) {
     // transform: Gt_g = U_g M^T with the stored projection (parafac2_intergrative.py:772-801)
     const float* Ug = a.U + T.uoff + (int64_t)i0 * n * r;
-    for (int i = ty; i < n; i += nw)
-      for (int m = tx; m < RP; m += 32) {
-        float acc = 0.f;
-        for (int l = 0; l < r; ++l) acc = fmaf(__ldg(Ug + (int64_t)i * r + l), Ms[m * ldt + l], acc);
-        Gg[(int64_t)i * RP + m] = acc;
-      }
+    gt_rows<RP>(n, r, ldt, [&](int i, int l) { return __ldg(Ug + (int64_t)i * r + l); }, R1, Gg);
     return;
   }
-  // ---- temp[i][l] = sum_m W_g[i][m] M[m][l]
+  // ---- temp[i][l] = sum_m W_g[i][m] M[m][l] into region 0
   {
     const float* Wg = a.W + brow * RP;
-    for (int i = ty; i < n; i += nw) {
-      const float* wr = Wg + (int64_t)i * RP;
-      for (int l = tx; l < r; l += 32) {
-        float acc = 0.f;
-#pragma unroll 8
-        for (int m = 0; m < RP; ++m) acc = fmaf(__ldg(wr + m), Ms[m * ldt + l], acc);
-        Tm[i * ldt + l] = acc;
-      }
+    for (int row0 = 0; row0 < n; row0 += 96) {
+      float acc[6][2];
+      cta_mm<6, 2>(n, r, RP, row0, [&](int i, int m) { return __ldg(Wg + (int64_t)i * RP + m); },
+                   [&](int m, int l) { return R1[m * ldt + l]; }, acc);
+#pragma unroll
+      for (int u = 0; u < 6; ++u)
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const int i = row0 + ty + 16 * u, l = tx + 32 * v;
+          if (i < n && l < r) R0[i * ldt + l] = acc[u][v];
+        }
     }
     __syncthreads();
   }
   // ---- QR, polar factor of R, sum(S)
-  householder_qr(Tm, n, r, ldt, s);
-  float* X = reg;
+  householder_qr(R0, n, r, ldt, s);
+  float* X = R1;
   for (int p = ty; p < r; p += nw)
-    for (int q = tx; q < r; q += 32) X[p * ldt + q] = q >= p ? Tm[p * ldt + q] : 0.f;
+    for (int q = tx; q < r; q += 32) X[p * ldt + q] = q >= p ? R0[p * ldt + q] : 0.f;
   __syncthreads();
-  newton_polar(X, ldt, reg + (size_t)r * ldt, r, true, s);
+  newton_polar_r64(X, ldt, R1 + (size_t)r * ldt, r, true, s);
   {
     double acc = 0.0;
     for (int p = ty; p < r; p += nw)
-      for (int q = p + tx; q < r; q += 32) acc += (double)X[p * ldt + q] * (double)Tm[p * ldt + q];
+      for (int q = p + tx; q < r; q += 32) acc += (double)X[p * ldt + q] * (double)R0[p * ldt + q];
     acc = block_sum<double>(acc, dred);
     if (tid == 0) a.ssum[g] = acc;
   }
   // ---- U = Q [P; 0]: U's first r rows are X (same storage and stride)
-  float* Uu = reg;
   for (int j = r + ty; j < n; j += nw)
-    for (int l = tx; l < r; l += 32) Uu[j * ldt + l] = 0.f;
+    for (int l = tx; l < r; l += 32) R1[j * ldt + l] = 0.f;
   __syncthreads();
-  apply_q(Tm, ldt, Uu, ldt, n, r, s);
+  apply_q(R0, ldt, R1, ldt, n, r, s);
   float* Ug = a.U + T.uoff + (int64_t)i0 * n * r;
-  for (int j = ty; j < n; j += nw) {
-    for (int l = tx; l < r; l += 32) Ug[(int64_t)j * r + l] = Uu[j * ldt + l];
-    for (int m = tx; m < RP; m += 32) {
-      float acc = 0.f;
-      for (int l = 0; l < r; ++l) acc = fmaf(Uu[j * ldt + l], Ms[m * ldt + l], acc);
-      Gg[(int64_t)j * RP + m] = acc;
-    }
-  }
+  for (int j = ty; j < n; j += nw)
+    for (int l = tx; l < r; l += 32) Ug[(int64_t)j * r + l] = R1[j * ldt + l];
+  // ---- Gt = U M^T (M formed again in region 0)
+  form_m<RP>(a, g, ci, r, ldt, R0, R0);
+  gt_rows<RP>(n, r, ldt, [&](int i, int l) { return R1[i * ldt + l]; }, R0, Gg);
   if (tid == 0 && ival[0]) set_status(a.status, FH_ERR_ILLCOND);
 }
 
@@ -168,8 +188,7 @@ __global__ void __launch_bounds__(kProcThreads) polar_qr_kernel(const float* __r
   const size_t newton = (size_t)r * ldt + newton_scratch_floats(r);
   if (newton > regsz) regsz = newton;
   float* misc = reg + regsz;
-  PolarScratch s{misc, misc + kMaxRank, misc + 2 * kMaxRank, misc + 4 * kMaxRank, red, dred,
-                 ival};
+  PolarScratch s = polar_scratch(misc, red, dred, ival);
   if (tid == 0) ival[0] = 0;
   const float* Mb = M + b * (int64_t)n * r;
   for (int i = ty; i < n; i += nw)
@@ -180,7 +199,8 @@ __global__ void __launch_bounds__(kProcThreads) polar_qr_kernel(const float* __r
   for (int p = ty; p < r; p += nw)
     for (int q = tx; q < r; q += 32) X[p * ldt + q] = q >= p ? Tm[p * ldt + q] : 0.f;
   __syncthreads();
-  newton_polar(X, ldt, reg + (size_t)r * ldt, r, true, s);
+  if (r <= 64) newton_polar_r64(X, ldt, reg + (size_t)r * ldt, r, true, s);
+  else newton_polar(X, ldt, reg + (size_t)r * ldt, r, true, s);
   double acc = 0.0;
   for (int p = ty; p < r; p += nw)
     for (int q = p + tx; q < r; q += 32) acc += (double)X[p * ldt + q] * (double)Tm[p * ldt + q];
