@@ -43,8 +43,11 @@ def parse():
     ap.add_argument("--sample-cells", type=int, default=96,
                     help="cells of the CPU-baseline sample (at least the rank R)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "bf16"],
-                    help="fp32: the plain drop-in; bf16: X in bf16, tensor-core X passes")
+    ap.add_argument("--precision", default="bf16x2", choices=["fp32", "bf16x2", "bf16"],
+                    help="form timed for the headline: bf16x2 (default) the tensor-core form, X "
+                         "as two bf16 planes; bf16 one plane; fp32 the plain drop-in")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip timing the plain fp32 form beside the headline form")
     return ap.parse_args()
 
 
@@ -71,6 +74,23 @@ def make_workload(name, seed=0):
         ds.append(Chrom_Dataset(Sparse(idx, val, shape, copy=False), bsb, bsc, compact=True,
                                 flank=w.band, chrom=cname, resolution=w.resolution))
     return w, coo, ds
+
+
+class _Null:
+    def __enter__(self):
+        return None
+
+    def __exit__(self, *a):
+        return False
+
+
+def aligned_diff(E, Eref):
+    """Relative Frobenius difference of E after the orthogonal Procrustes rotation onto Eref
+    (two fits' embeddings agree up to a rotation)."""
+    import torch
+    E, Eref = E.double(), Eref.double()
+    U, _, Vh = torch.linalg.svd(E.T @ Eref)
+    return float(torch.linalg.norm(E @ (U @ Vh) - Eref) / torch.linalg.norm(Eref))
 
 
 class Clocks:
@@ -212,50 +232,68 @@ def gb300_arm(args, rank, local, ws):
     eng = m.engine
     hist = eng.new_history(iters)
 
-    def device_step():
-        eng.store.rebuild()
-        eng.run_rwr()
-        eng.set_state(*state)
-        eng.core_norm()
-        npar = 1
-        for it in range(iters):
-            if it % 10 == 0 and it > 0 and npar < 10:
-                npar += 1
-            eng.iterate(it == 0, npar, hist[it])
+    def device_step(e, h, graph=True):
+        e.store.rebuild()
+        e.run_rwr()
+        e.set_state(*state)
+        e.core_norm()
+        e.run_iterations(iters, 1, h, graph=graph)
 
     def barrier():
         if ws > 1:
             torch.distributed.barrier()
 
-    for _ in range(args.warmup):
-        device_step()
-    torch.cuda.synchronize()
-    barrier()
-    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    n0 = _lib.launches
-    with Clocks(local) as clk:
+    def timed(e, h, clocks):
+        """W warm-up fits, then K fits bracketed by a barrier and synchronizes; max over ranks."""
+        for _ in range(args.warmup):
+            device_step(e, h)
         torch.cuda.synchronize()
-        s0.record()
-        for _ in range(args.steps):
-            device_step()
-        s1.record()
-        torch.cuda.synchronize()
-    launches = (_lib.launches - n0) // args.steps
-    ms = s0.elapsed_time(s1) / args.steps
-    t = torch.tensor([ms], device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms = float(t.item())
+        barrier()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = _lib.launches
+        with Clocks(local) if clocks else _Null() as clk:
+            torch.cuda.synchronize()
+            s0.record()
+            for _ in range(args.steps):
+                device_step(e, h)
+            s1.record()
+            torch.cuda.synchronize()
+        n_launch = (_lib.launches - n0) // args.steps
+        t = torch.tensor([s0.elapsed_time(s1) / args.steps], device=dev)
+        if ws > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e.check_status("bench")
+        return float(t.item()), n_launch, clk
+
+    ms, launches, clk = timed(eng, hist, True)
     value = ws * C / (ms / 1000.0)
-    eng.check_status("bench")
+    # ---- the plain fp32 form on the same state, for the BF16-batched vs plain FP32 ratio
+    plain = None
+    if args.precision != "fp32" and not args.no_plain:
+        from fh_gb300.engine import FitEngine
+        peng = FitEngine(ds, w.rank, m.chrom2size, m.n_i, dev, precision="fp32")
+        phist = peng.new_history(iters)
+        pms, plaunch, _ = timed(peng, phist, False)
+        peng.timing = {}
+        device_step(peng, phist, graph=False)
+        torch.cuda.synchronize()
+        pkt = peng.timing_summary()
+        plain = {"value": ws * C / (pms / 1000.0), "unit": "cells/s", "ms_per_step": pms,
+                 "gpu_launches": int(plaunch),
+                 "kernel_ms": {k: round(v["mean_ms"], 4) for k, v in pkt.items()},
+                 "speedup_of_headline": (ws * C / (ms / 1000.0)) / (ws * C / (pms / 1000.0)),
+                 "embedding_aligned_rel_diff": aligned_diff(eng.E[:, :w.rank], peng.E[:, :w.rank]),
+                 "loss_final": float(peng.losses(phist[-1], peng.tensor_norms())[0])}
+        del peng
+        torch.cuda.empty_cache()
     # ---- per-kernel times (one instrumented step) for the roofline
     eng.timing = {}
-    device_step()
+    device_step(eng, hist, graph=False)
     torch.cuda.synchronize()
     kt = eng.timing_summary()
     eng.timing = None
     hbm, bf16, peak_kind = peaks()
-    xel = 2 if eng.bf16 else 4
+    xel = 2 * eng.planes if eng.bf16 else 4
     xbytes = C * eng.rows * xel
     fam = max(("xe", "xg"), key=lambda k: kt.get(k, {}).get("total_ms", 0))
     dom = max(kt, key=lambda k: kt[k]["total_ms"])
@@ -308,9 +346,12 @@ def gb300_arm(args, rank, local, ws):
                                    "iterations, RWR epochs %s" %
                                    (args.config, C, sum(w.chrom_bins), eng.n_tiles, w.rank, w.band,
                                     iters, sorted(set(int(v) for v in n_i))),
-                       "precision": ("bf16 X, tensor-core X passes" if eng.bf16 else "fp32 (plain)"),
+                       "precision": ({"bf16": "X in one bf16 plane, tensor-core X passes",
+                                      "bf16x2": "X in two bf16 planes (hi+lo), tensor-core X passes"}
+                                     .get(eng.precision, "fp32 (plain)")),
                        "l2": "inputs larger than L2 (X %.2f GB)" % (eng.Ct * eng.ldx * xel / 1e9), "parallelism": "replicas" if ws > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+            "plain_fp32": plain,
             "clocks": clk.summary(), "kernel_ms": {k: round(v["mean_ms"], 4) for k, v in kt.items()},
             "loss_final": float(m.engine.losses(hist[-1], eng.tensor_norms())[0])}
     print(json.dumps(line), flush=True)

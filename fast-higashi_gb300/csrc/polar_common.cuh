@@ -82,9 +82,12 @@ __device__ __forceinline__ int pc_nwarps() { return blockDim.x >> 5; }
 // ---- Householder QR of T (n x r, row stride ldt, n >= r), in place ---------------------
 // On return the upper triangle of T[0:r][0:r] is R, T[i][k] (i > k) holds v_k below the
 // diagonal, vh[k] the head of v_k and beta[k] = 2 / v_k^T v_k (0 for a zero column).
-__device__ inline void householder_qr(float* T, int n, int r, int ldt, PolarScratch& s) {
+// householder_panel factors columns [k0, k1) and applies each reflector to the columns
+// below k1 only; householder_qr is the whole matrix as one panel.
+__device__ inline void householder_panel(float* T, int n, int k0, int k1, int ldt,
+                                         PolarScratch& s) {
   const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
-  for (int k = 0; k < r; ++k) {
+  for (int k = k0; k < k1; ++k) {
     if (ty == 0) {
       float ss = 0.f;
       for (int i = k + 1 + tx; i < n; i += 32) ss = fmaf(T[i * ldt + k], T[i * ldt + k], ss);
@@ -105,7 +108,7 @@ __device__ inline void householder_qr(float* T, int n, int r, int ldt, PolarScra
     }
     __syncthreads();
     const float beta = s.beta[k], vh = s.vh[k];
-    for (int j = k + 1 + ty; j < r; j += nw) {       // w_j = v^T T[k:, j], one warp per column
+    for (int j = k + 1 + ty; j < k1; j += nw) {       // w_j = v^T T[k:, j], one warp per column
       float d = 0.f;
       for (int i = k + 1 + tx; i < n; i += 32) d = fmaf(T[i * ldt + k], T[i * ldt + j], d);
       d = warp_sum(d);
@@ -115,12 +118,16 @@ __device__ inline void householder_qr(float* T, int n, int r, int ldt, PolarScra
     if (beta != 0.f) {
       for (int i = k + ty; i < n; i += nw) {
         const float bv = -beta * ((i == k) ? vh : T[i * ldt + k]);
-        for (int j = k + 1 + tx; j < r; j += 32) T[i * ldt + j] = fmaf(bv, s.wv[j], T[i * ldt + j]);
+        for (int j = k + 1 + tx; j < k1; j += 32) T[i * ldt + j] = fmaf(bv, s.wv[j], T[i * ldt + j]);
       }
     }
     if (threadIdx.x == 0) T[k * ldt + k] = s.wv[2 * kMaxRank - 1];
     __syncthreads();
   }
+}
+
+__device__ inline void householder_qr(float* T, int n, int r, int ldt, PolarScratch& s) {
+  householder_panel(T, n, 0, r, ldt, s);
 }
 
 // ---- U = Q U: apply the stored reflectors in reverse to U (n x r, stride ldu) ----------
@@ -219,6 +226,176 @@ __device__ inline void gj_inverse(const float* X, int ldx, float* Aug, int r, Po
     }
     __syncthreads();
   }
+}
+
+// ---- blocked Householder QR (512 threads, r <= 64, n <= 192) ---------------------------
+// Panels of 16 columns are factored by householder_panel; the columns to their right are
+// updated once per panel with the UT form of the panel's reflectors,
+//   A2 <- (I - Vp Tp Vp^T)^T A2 = A2 - Vp (Tp^T (Vp^T A2)),  Tp^{-1} = diag(1/beta) + striu(Vp^T Vp),
+// as register-tiled products.  Same reflectors as householder_qr; Sc: >= 2600 floats.
+__device__ inline void householder_qr_blocked(float* T, int n, int r, int ldt, float* Sc,
+                                              PolarScratch& s) {
+  constexpr int NB = 16;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  float* Wm = Sc;            // NB x 64: Vp^T [Vp | A2]
+  float* Tp = Sc + NB * 64;  // NB x NB (stride NB + 1)
+  float* W2 = Tp + NB * (NB + 1);  // NB x 64
+  const float* vh = s.vh;
+  const float* beta = s.beta;
+  for (int k0 = 0; k0 < r; k0 += NB) {
+    const int k1 = min(k0 + NB, r), nb = k1 - k0, m2 = r - k1;
+    householder_panel(T, n, k0, k1, ldt, s);
+    if (m2 == 0) break;
+    auto V = [&](int i, int c) -> float {   // column k0 + c of the panel's reflectors
+      const int k = k0 + c;
+      return i > k ? T[i * ldt + k] : (i == k ? vh[k] : 0.f);
+    };
+    // Wm = Vp^T [Vp | A2] over rows k0 .. n-1
+    {
+      float acc[1][2];
+      cta_mm<1, 2>(nb, nb + m2, n - k0, 0, [&](int c, int kk) { return V(k0 + kk, c); },
+                   [&](int kk, int j) {
+                     return j < nb ? V(k0 + kk, j) : T[(k0 + kk) * ldt + k1 + (j - nb)];
+                   },
+                   acc);
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int j = l + 32 * v;
+        if (w < nb && j < nb + m2) Wm[w * 64 + j] = acc[0][v];
+      }
+    }
+    __syncthreads();
+    // Tp = (diag(1/beta) + striu(Vp^T Vp))^{-1}, one warp per column
+    if (w < nb) {
+      const int j = w;
+      for (int i = j; i >= 0; --i) {
+        float d = 0.f;
+        for (int q = i + 1 + l; q <= j; q += 32) d = fmaf(Wm[i * 64 + q], Tp[q * (NB + 1) + j], d);
+        d = warp_sum(d);
+        if (l == 0) {
+          const float bi = beta[k0 + i];
+          const float dii = bi != 0.f ? 1.f / bi : 1.f;
+          Tp[i * (NB + 1) + j] = ((i == j ? 1.f : 0.f) - d) / dii;
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    // W2 = Tp^T (Vp^T A2)
+    for (int idx = threadIdx.x; idx < nb * m2; idx += 512) {
+      const int c = idx / m2, j = idx - c * m2;
+      float acc = 0.f;
+      for (int cp = 0; cp <= c; ++cp) acc = fmaf(Tp[cp * (NB + 1) + c], Wm[cp * 64 + nb + j], acc);
+      W2[c * 64 + j] = acc;
+    }
+    __syncthreads();
+    // A2 -= Vp W2 (rows k0 .. n-1; each thread updates the elements it computed)
+    for (int row0 = k0; row0 < n; row0 += 96) {
+      float acc[6][2];
+      cta_mm<6, 2>(n, m2, nb, row0, [&](int i, int c) { return V(i, c); },
+                   [&](int c, int j) { return W2[c * 64 + j]; }, acc);
+#pragma unroll
+      for (int u = 0; u < 6; ++u)
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const int i = row0 + w + 16 * u, j = l + 32 * v;
+          if (i < n && j < m2) T[i * ldt + k1 + j] -= acc[u][v];
+        }
+    }
+    __syncthreads();
+  }
+}
+
+// ---- U = Q [X; 0] from the compact UT form of the reflectors (512 threads) ------------
+// Q = H_0 ... H_{r-1} = I - V T V^T with T^{-1} = diag(1/beta) + striu(V^T V) (the UT
+// transform of the Householder product), so U = [X; 0] - V (T (V_top^T X)), V_top = V's first
+// r rows: three register-tiled products, one triangular inverse, no per-reflector steps.
+// T: n x ldt reflector storage of householder_qr (its upper triangle, no longer needed after
+// the Newton iteration, receives T); U: rows < r hold X on entry, n rows of U on return;
+// Sc: r x ldt scratch.  n <= 192, r <= 64.
+__device__ inline void apply_q_ut(float* T, int ldt, float* U, int ldu, float* Sc, int n, int r,
+                                  PolarScratch& s) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const float* vh = s.vh;
+  const float* beta = s.beta;
+  auto V = [&](int k, int c) -> float {
+    return k > c ? T[k * ldt + c] : (k == c ? vh[c] : 0.f);
+  };
+  float acc[4][2];
+  // Sc = diag(1/beta) + striu(V^T V)
+  cta_mm<4, 2>(r, r, n, 0, [&](int i, int k) { return V(k, i); },
+               [&](int k, int j) { return V(k, j); }, acc);
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int i = w + 16 * u, j = l + 32 * v;
+      if (i < r && j < r)
+        Sc[i * ldt + j] = i < j ? acc[u][v] : (i == j ? (beta[i] != 0.f ? 1.f / beta[i] : 1.f) : 0.f);
+    }
+  __syncthreads();
+  // T = Sc^{-1} into the upper triangle of the reflector storage
+  for (int j = w; j < r; j += 16) {
+    for (int i = j; i >= 0; --i) {
+      float d = 0.f;
+      for (int q = i + 1 + l; q <= j; q += 32) d = fmaf(Sc[i * ldt + q], T[q * ldt + j], d);
+      d = warp_sum(d);
+      if (l == 0) T[i * ldt + j] = ((i == j ? 1.f : 0.f) - d) / Sc[i * ldt + i];
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // Sc = V_top^T X
+  cta_mm<4, 2>(r, r, r, 0, [&](int c, int k) { return V(k, c); },
+               [&](int k, int j) { return U[k * ldu + j]; }, acc);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int i = w + 16 * u, j = l + 32 * v;
+      if (i < r && j < r) Sc[i * ldt + j] = acc[u][v];
+    }
+  __syncthreads();
+  // Sc = T Sc
+  cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return k >= i ? T[i * ldt + k] : 0.f; },
+               [&](int k, int j) { return Sc[k * ldt + j]; }, acc);
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int i = w + 16 * u, j = l + 32 * v;
+      if (i < r && j < r) Sc[i * ldt + j] = acc[u][v];
+    }
+  __syncthreads();
+  // U = [X; 0] - V Sc, both 96-row tiles held in registers until every thread has read X
+  float a0[6][2], a1[6][2];
+  cta_mm<6, 2>(n, r, r, 0, [&](int i, int c) { return V(i, c); },
+               [&](int c, int j) { return Sc[c * ldt + j]; }, a0);
+  cta_mm<6, 2>(n, r, r, 96, [&](int i, int c) { return V(i, c); },
+               [&](int c, int j) { return Sc[c * ldt + j]; }, a1);
+  float x0[6][2];
+#pragma unroll
+  for (int u = 0; u < 6; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int i = w + 16 * u, j = l + 32 * v;
+      x0[u][v] = (i < r && j < r) ? U[i * ldu + j] : 0.f;
+    }
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 6; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int j = l + 32 * v;
+      const int i0 = w + 16 * u, i1 = 96 + w + 16 * u;
+      if (j < r) {
+        if (i0 < n) U[i0 * ldu + j] = x0[u][v] - a0[u][v];
+        if (i1 < n) U[i1 * ldu + j] = -a1[u][v];
+      }
+    }
+  __syncthreads();
 }
 
 // ---- inverse of X (r x r, r <= 64, stride ldx) into Xi (stride ldo), 512 threads -------

@@ -143,7 +143,8 @@ __global__ void __launch_bounds__(kProcThreads, 2) procrustes_qr_kernel(ProcArgs
     __syncthreads();
   }
   // ---- QR, polar factor of R, sum(S)
-  householder_qr(R0, n, r, ldt, s);
+  if (n <= 192) householder_qr_blocked(R0, n, r, ldt, R1, s);
+  else householder_qr(R0, n, r, ldt, s);
   float* X = R1;
   for (int p = ty; p < r; p += nw)
     for (int q = tx; q < r; q += 32) X[p * ldt + q] = q >= p ? R0[p * ldt + q] : 0.f;
@@ -157,10 +158,14 @@ __global__ void __launch_bounds__(kProcThreads, 2) procrustes_qr_kernel(ProcArgs
     if (tid == 0) a.ssum[g] = acc;
   }
   // ---- U = Q [P; 0]: U's first r rows are X (same storage and stride)
-  for (int j = r + ty; j < n; j += nw)
-    for (int l = tx; l < r; l += 32) R1[j * ldt + l] = 0.f;
-  __syncthreads();
-  apply_q(R0, ldt, R1, ldt, n, r, s);
+  if (n <= 192) {
+    apply_q_ut(R0, ldt, R1, ldt, R1 + (size_t)r * ldt, n, r, s);
+  } else {
+    for (int j = r + ty; j < n; j += nw)
+      for (int l = tx; l < r; l += 32) R1[j * ldt + l] = 0.f;
+    __syncthreads();
+    apply_q(R0, ldt, R1, ldt, n, r, s);
+  }
   float* Ug = a.U + T.uoff + (int64_t)i0 * n * r;
   for (int j = ty; j < n; j += nw)
     for (int l = tx; l < r; l += 32) Ug[(int64_t)j * r + l] = R1[j * ldt + l];

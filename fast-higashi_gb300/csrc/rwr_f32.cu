@@ -38,6 +38,7 @@ struct RwrArgs {
   int max_rows, max_width;  // extents the shared-memory carve-out was sized for
   float* out;
   __nv_bfloat16* out16;
+  int64_t plane_stride;  // > 0: a second bf16 plane with the rounding residual
   int64_t cell_stride;
   double* sumsq;
   float* deltas;
@@ -268,9 +269,16 @@ __global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
       if (MODE == kOutput) {
         a.out[(int64_t)c * a.cell_stride + xoff + i] = v;
       } else {
+        const int64_t o = (int64_t)c * a.cell_stride + xoff + i;
         const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        a.out16[(int64_t)c * a.cell_stride + xoff + i] = h;
-        v = __bfloat162float(h);
+        a.out16[o] = h;
+        if (a.plane_stride > 0) {
+          const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+          a.out16[a.plane_stride + o] = l;
+          v = __bfloat162float(h) + __bfloat162float(l);
+        } else {
+          v = __bfloat162float(h);
+        }
       }
       ss += (double)v * v;
     }
@@ -333,14 +341,16 @@ extern "C" int fh_rwr_tiles_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n
 extern "C" int fh_rwr_tiles_bf16(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
                                  int32_t mr, int32_t mw, const fh_entry* entries,
                                  const int64_t* offsets, uint16_t* out16, int64_t cell_stride,
-                                 double* sumsq, int* status, void* stream) {
-  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !offsets || !out16 || mr <= 0 || mw < mr)
+                                 int64_t plane_stride, double* sumsq, int* status, void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !offsets || !out16 || mr <= 0 || mw < mr ||
+      plane_stride < 0)
     return FH_ERR_ARG;
   RwrArgs a{};
   a.max_rows = mr; a.max_width = mw;
   a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
   a.offsets = offsets; a.out16 = reinterpret_cast<__nv_bfloat16*>(out16);
-  a.cell_stride = cell_stride; a.sumsq = sumsq; a.status = status;
+  a.cell_stride = cell_stride; a.plane_stride = plane_stride; a.sumsq = sumsq;
+  a.status = status;
   return launch_rwr<kSparse, kOutput16>(a, n_tiles, mr, mw, (cudaStream_t)stream);
 }
 

@@ -1,0 +1,432 @@
+// Partial random walk with restart on the 5th-generation tensor cores (tcgen05), writing the
+// bf16 planes of X that the tensor-core X passes read.
+//
+// Reference: fasthigashi/partial_rwr.py:75-138 (do_conv=False, do_col=False) fed by
+// densify_jit (fasthigashi/sparse_for_schic.py:279-320); rwr_f32.cu states the algebra:
+//   S2 = A A^T (diagonal zeroed), S1 = A[:, s0:s0+b]
+//   L  = 0.75 S1 / colsum(S1) + 0.25 S2 / colsum(S2),  P = L / colsum(L)
+//   Z_0 = A,  Z_{t+1} = 0.5 P Z_t + 0.5 A,  X = Z_epochs  (= Q_epochs A of the reference)
+//
+// One CTA (8 warps, one per SM, persistent over (tile, cell) items) per item at a time:
+//   smem   Z as bf16 hi and lo planes (128 rows x npad columns, 128-byte swizzled, the
+//          layout tcgen05 reads), P as hi and lo planes (128 x 128)
+//   TMEM   D (the fp32 accumulator, npad columns) and A in fp32 (npad columns)
+//   S2     = A_hi A_hi^T + A_hi A_lo^T + A_lo A_hi^T   (K = npad)        -> D
+//   P      from D row by row: colsum(S2) is a row sum (S2 is symmetric), colsum(S1) a
+//          column sum of the smem tile, colsum(L) = 0.75 c1/(c1+eps) + 0.25 c2/(c2+eps)
+//          in closed form (the reference sums L's columns numerically; they agree to
+//          rounding).  With the 1e-8 floor every column sum is positive, so the reference's
+//          zero-column rule (partial_rwr.py:96-97) never applies; it is kept for c1 = c2 = 0.
+//   epoch  D = P_hi Z_hi + P_hi Z_lo + P_lo Z_hi  (K = 128, N = npad), then each thread
+//          turns its row of D and A into Z_{t+1} = 0.5 D + 0.5 A and writes the hi/lo planes
+//          back in place (the MMA that read them has completed)
+//   out    the last epoch's fp32 Z is rounded to the output planes (one: bf16(Z); two: hi and
+//          the residual lo) through a staging copy in smem, then stored contiguously.
+// The split products carry every operand to 16 significant bits, so the result is fp32-class.
+// Thread (warp w, lane l) serves row p = 32 (w % 4) + l (the TMEM lane quarter its warp may
+// read) and the column half w / 4.  Tiles wider than 256 columns use rwr_f32.cu.
+#include "tc_common.cuh"
+
+namespace fh {
+
+constexpr int kRtThreads = 256;
+constexpr float kRtFloor = 1e-8f;  // densify floor, sparse_for_schic.py:320
+constexpr float kRtEps = 1e-15f;   // column-sum guard, partial_rwr.py:90,91,111
+constexpr int kRtMaxPad = 256;     // npad: columns rounded up to 64, at most one MMA's N
+
+struct RtArgs {
+  const fh_tile* tiles;
+  int n_tiles;
+  int n_cells;
+  int max_rows, max_width, npad_max;
+  const uint2* entries;
+  const int64_t* offsets;
+  __nv_bfloat16* out16;
+  int64_t cell_stride;
+  int64_t plane_stride;  // > 0: write the lo plane too
+  double* sumsq;
+  int* status;
+};
+
+// Byte offset of element (row p, column j) in a 128-row operand of 64-column blocks with the
+// 128-byte swizzle (16-byte chunk index XOR row mod 8), the layout TMA's SWIZZLE_128B writes.
+__device__ __forceinline__ uint32_t sw_off(int p, int j) {
+  return (uint32_t)((j >> 6) * 16384 + p * 128 + ((((j & 63) >> 3) ^ (p & 7)) << 4) + (j & 7) * 2);
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t ta, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(ta),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+      "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+      "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+      "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+      "r"(__float_as_uint(v[15]))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
+  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+// Splits 8 values into bf16 hi and lo and stores both 16-byte chunks.
+__device__ __forceinline__ void store_split8(uint8_t* hi, uint8_t* lo, uint32_t off,
+                                             const float* v) {
+  __nv_bfloat16 h[8], l[8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e) {
+    h[e] = __float2bfloat16_rn(v[e]);
+    l[e] = __float2bfloat16_rn(v[e] - __bfloat162float(h[e]));
+  }
+  *reinterpret_cast<uint4*>(hi + off) =
+      make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
+  *reinterpret_cast<uint4*>(lo + off) =
+      make_uint4(pack2(l[0], l[1]), pack2(l[2], l[3]), pack2(l[4], l[5]), pack2(l[6], l[7]));
+}
+
+__device__ __forceinline__ float ld_split(const uint8_t* hi, const uint8_t* lo, uint32_t off) {
+  return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(hi + off)) +
+         __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(lo + off));
+}
+
+__host__ __device__ inline size_t rt_smem_bytes(int npad_max) {
+  return (size_t)npad_max / 64 * 16384 * 2 + 65536 + 4 * 128 * sizeof(float) + 64 * sizeof(double) +
+         64 + 1024;
+}
+
+__global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;
+  uint8_t* g = smem_raw + (base - raw);
+  const uint32_t zbytes = (uint32_t)(a.npad_max / 64) * 16384u;
+  uint8_t* Zhi = g;
+  uint8_t* Zlo = g + zbytes;
+  uint8_t* Phi = g + 2 * zbytes;
+  uint8_t* Plo = Phi + 32768;
+  float* cs1p = reinterpret_cast<float*>(Plo + 32768);  // [2][128] partial column sums of S1
+  float* cs2p = cs1p + 256;                              // [2][128] partial row sums of S2
+  double* dred = reinterpret_cast<double*>(cs2p + 256);  // [64]
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(dred + 64);
+  uint32_t* misc = reinterpret_cast<uint32_t*>(mbar + 1);  // [0] TMEM base
+  const uint32_t sZhi = base, sZlo = base + zbytes, sPhi = base + 2 * zbytes,
+                 sPlo = sPhi + 32768;
+
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int q4 = w & 3, h = w >> 2;
+  const int p = 32 * q4 + lane;
+  const uint32_t bar = smem_u32(mbar);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  if (w == 0) {
+    tmem_alloc(smem_u32(misc), 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = misc[0];
+  const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
+  const uint32_t tD = tmem + lane_off, tA = tmem + 256 + lane_off;
+  const __nv_bfloat16 fl_hi = __float2bfloat16_rn(kRtFloor);
+  const __nv_bfloat16 fl_lo = __float2bfloat16_rn(kRtFloor - __bfloat162float(fl_hi));
+  uint32_t phase = 0;
+  bool ok = true;
+
+  // Issues the MMAs of one product group (thread 0) and waits for them (all threads).
+  auto mma_wait = [&]() -> bool {
+    if (tid == 0) mma_commit(bar);
+    const bool got = mbar_wait(bar, phase, nullptr);
+    phase ^= 1u;
+    const bool any_fail = __syncthreads_or(!got);
+    tc_fence_after();
+    return !any_fail;
+  };
+
+  const int64_t items = (int64_t)a.n_tiles * a.n_cells;
+  for (int64_t item = blockIdx.x; ok && item < items; item += gridDim.x) {
+    const int t = (int)(item / a.n_cells), c = (int)(item - (int64_t)t * a.n_cells);
+    const fh_tile T = a.tiles[t];
+    const int b = T.rows, n = T.width, s0 = T.s0, epochs = T.n_rwr;
+    if (b <= 0 || b > a.max_rows || b > 128 || n < b || n > a.max_width || n > a.npad_max ||
+        s0 < 0 || s0 + b > n || epochs < 0) {
+      if (tid == 0) set_status(a.status, FH_ERR_ARG);
+      continue;
+    }
+    const int npad = (n + 63) & ~63;
+    const int hw = npad / 2;  // columns per half
+    // ---- 1. Z = floor on the tile, zero on the padding (both planes)
+    {
+      const int cpr = npad / 8;  // 16-byte chunks per row
+      for (int idx = tid; idx < 128 * cpr; idx += kRtThreads) {
+        const int row = idx / cpr, j0 = (idx - row * cpr) * 8;
+        uint32_t hv[4], lv[4];
+#pragma unroll
+        for (int e = 0; e < 8; e += 2) {
+          const bool in0 = row < b && j0 + e < n, in1 = row < b && j0 + e + 1 < n;
+          const __nv_bfloat16 z = __float2bfloat16_rn(0.f);
+          hv[e / 2] = pack2(in0 ? fl_hi : z, in1 ? fl_hi : z);
+          lv[e / 2] = pack2(in0 ? fl_lo : z, in1 ? fl_lo : z);
+        }
+        const uint32_t off = sw_off(row, j0);
+        *reinterpret_cast<uint4*>(Zhi + off) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
+        *reinterpret_cast<uint4*>(Zlo + off) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+      }
+    }
+    __syncthreads();
+    // ---- 2. the cell's contacts (floored at 1e-8)
+    {
+      const int64_t e0 = a.offsets[(int64_t)t * a.n_cells + c];
+      const int64_t e1 = a.offsets[(int64_t)t * a.n_cells + c + 1];
+      for (int64_t e = e0 + tid; e < e1; e += kRtThreads) {
+        const uint2 en = a.entries[e];
+        const int r = (int)(en.x & 0xffffu), j = (int)(en.x >> 16);
+        if (r >= b || j >= n) {
+          set_status(a.status, FH_ERR_INDEX);
+          continue;
+        }
+        const float v = fmaxf(__uint_as_float(en.y), kRtFloor);
+        const __nv_bfloat16 hv = __float2bfloat16_rn(v);
+        const uint32_t off = sw_off(r, j);
+        *reinterpret_cast<__nv_bfloat16*>(Zhi + off) = hv;
+        *reinterpret_cast<__nv_bfloat16*>(Zlo + off) = __float2bfloat16_rn(v - __bfloat162float(hv));
+      }
+    }
+    __syncthreads();
+    // ---- 3. row p of A into TMEM (this thread's column half); column sums of S1
+    for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
+      float v[16];
+#pragma unroll
+      for (int e = 0; e < 16; e += 8) {
+        const uint32_t off = sw_off(p, j0 + e);
+        const uint4 hv = *reinterpret_cast<const uint4*>(Zhi + off);
+        const uint4 lv = *reinterpret_cast<const uint4*>(Zlo + off);
+        const uint32_t hw4[4] = {hv.x, hv.y, hv.z, hv.w}, lw4[4] = {lv.x, lv.y, lv.z, lv.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          v[e + 2 * k] = __uint_as_float(hw4[k] << 16) + __uint_as_float(lw4[k] << 16);
+          v[e + 2 * k + 1] = __uint_as_float(hw4[k] & 0xffff0000u) +
+                             __uint_as_float(lw4[k] & 0xffff0000u);
+        }
+      }
+      tmem_st16(tA + j0, v);
+    }
+    {
+      const int q = tid & 127, half = tid >> 7;
+      float s = 0.f;
+      if (q < b) {
+        const int pe = min(b, 64 * half + 64);
+        for (int pp = 64 * half; pp < pe; ++pp) s += ld_split(Zhi, Zlo, sw_off(pp, s0 + q));
+      }
+      cs1p[half * 128 + q] = s;
+    }
+    tmem_wait_st();
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    // ---- 4. S2 = A A^T (split products) into D
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t idesc = idesc_bf16(128, 128, false, false);
+      for (int ks = 0; ks < npad / 16; ++ks) {
+        const uint32_t ko = (uint32_t)(ks >> 2) * 16384u + (uint32_t)(ks & 3) * 32u;
+        const uint64_t ah = sdesc_sw128(sZhi + ko, 16, 1024), al = sdesc_sw128(sZlo + ko, 16, 1024);
+        mma_bf16(tmem, ah, ah, idesc, ks > 0 ? 1u : 0u);
+        mma_bf16(tmem, ah, al, idesc, 1u);
+        mma_bf16(tmem, al, ah, idesc, 1u);
+      }
+    }
+    if (!mma_wait()) { ok = false; break; }
+    // ---- 5. P: row sums of S2 (diagonal excluded) = its column sums, then P row by row
+    {
+      float s = 0.f;
+      for (int q0 = 64 * h; q0 < 64 * h + 64; q0 += 16) {
+        float d[16], unused[16];
+        tmem_ld16x2(tD + q0, tD + q0, d, unused);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+          const int q = q0 + e;
+          if (q != p && q < b) s += d[e];
+        }
+      }
+      cs2p[h * 128 + p] = s;
+    }
+    __syncthreads();
+    for (int q0 = 64 * h; q0 < 64 * h + 64; q0 += 16) {
+      float d[16], unused[16], pv[16];
+      tmem_ld16x2(tD + q0, tD + q0, d, unused);
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const int q = q0 + e;
+        float v = 0.f;
+        if (p < b && q < b) {
+          const float c1 = cs1p[q] + cs1p[128 + q];
+          const float c2 = cs2p[q] + cs2p[128 + q];
+          if (c1 == 0.f && c2 == 0.f) {
+            v = (p == q) ? 1.f / (1.f + kRtEps) : 0.f;
+          } else {
+            const float s2 = (p == q) ? 0.f : d[e];
+            const float a1 = ld_split(Zhi, Zlo, sw_off(p, s0 + q));
+            const float l = (a1 / (c1 + kRtEps)) * 0.75f + (s2 / (c2 + kRtEps)) * 0.25f;
+            const float csl = (c1 / (c1 + kRtEps)) * 0.75f + (c2 / (c2 + kRtEps)) * 0.25f;
+            v = l / (csl + kRtEps);
+          }
+        }
+        pv[e] = v;
+      }
+      store_split8(Phi, Plo, sw_off(p, q0), pv);
+      store_split8(Phi, Plo, sw_off(p, q0 + 8), pv + 8);
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    // ---- 6. Z_{t+1} = 0.5 P Z_t + 0.5 A; the last epoch writes the output staging
+    uint8_t* stage = Zhi;                    // free once the last MMA has completed
+    const int64_t g0 = (int64_t)c * a.cell_stride + T.xoff;
+    const int mis = (int)(g0 & 7);           // staging shares the global 16-byte phase
+    double ss = 0.0;
+    const bool two = a.plane_stride > 0;
+    const int64_t tot = (int64_t)b * n;
+    auto emit = [&](int j0, const float (&z)[16]) {
+      if (p >= b) return;
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const int j = j0 + e;
+        if (j < n) {
+          const int64_t k = (int64_t)p * n + j + mis;
+          const __nv_bfloat16 hv = __float2bfloat16_rn(z[e]);
+          float sv = __bfloat162float(hv);
+          reinterpret_cast<__nv_bfloat16*>(stage)[k] = hv;
+          if (two) {
+            const __nv_bfloat16 lv = __float2bfloat16_rn(z[e] - sv);
+            reinterpret_cast<__nv_bfloat16*>(stage)[tot + 8 + k] = lv;
+            sv += __bfloat162float(lv);
+          }
+          ss += (double)sv * sv;
+        }
+      }
+    };
+    for (int ep = 0; ep < epochs; ++ep) {
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t idesc = idesc_bf16(128, npad, false, true);
+        for (int ks = 0; ks < 8; ++ks) {
+          const uint32_t pk = (uint32_t)(ks >> 2) * 16384u + (uint32_t)(ks & 3) * 32u;
+          const uint32_t zk = (uint32_t)ks * 2048u;
+          const uint64_t ph = sdesc_sw128(sPhi + pk, 16, 1024), pl = sdesc_sw128(sPlo + pk, 16, 1024);
+          const uint64_t zh = sdesc_sw128(sZhi + zk, 16384, 1024),
+                         zl = sdesc_sw128(sZlo + zk, 16384, 1024);
+          mma_bf16(tmem, ph, zh, idesc, ks > 0 ? 1u : 0u);
+          mma_bf16(tmem, ph, zl, idesc, 1u);
+          mma_bf16(tmem, pl, zh, idesc, 1u);
+        }
+      }
+      if (!mma_wait()) { ok = false; break; }
+      const bool last = ep == epochs - 1;
+      if (last) __syncthreads();   // nobody reads Z any more: the staging may overwrite it
+      for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
+        float d[16], av[16], z[16];
+        tmem_ld16x2(tD + j0, tA + j0, d, av);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) z[e] = fmaf(0.5f, d[e], 0.5f * av[e]);
+        if (last) {
+          emit(j0, z);
+        } else {
+          store_split8(Zhi, Zlo, sw_off(p, j0), z);
+          store_split8(Zhi, Zlo, sw_off(p, j0 + 8), z + 8);
+        }
+      }
+      if (!last) fence_proxy_async();
+      tc_fence_before();
+      __syncthreads();
+    }
+    if (!ok) break;
+    if (epochs == 0) {
+      for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
+        float av[16], unused[16];
+        tmem_ld16x2(tA + j0, tA + j0, av, unused);
+        emit(j0, av);
+      }
+      tc_fence_before();
+      __syncthreads();
+    }
+    // ---- 7. staging -> X16 (contiguous b x n run of the cell's row), squared norm
+    {
+      const __nv_bfloat16* st = reinterpret_cast<const __nv_bfloat16*>(stage);
+      __nv_bfloat16* o = a.out16 + g0;
+      for (int64_t k = tid; k < tot; k += kRtThreads) o[k] = st[k + mis];
+      if (two) {
+        __nv_bfloat16* o2 = o + a.plane_stride;
+        for (int64_t k = tid; k < tot; k += kRtThreads) o2[k] = st[tot + 8 + k + mis];
+      }
+      ss = block_sum<double>(ss, dred);
+      if (tid == 0 && a.sumsq) a.sumsq[(int64_t)t * a.n_cells + c] = ss;
+      __syncthreads();
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (!ok) {
+    if (tid == 0) set_status(a.status, FH_ERR_TIMEOUT);
+    if (tid == 0) {
+      mma_commit(bar);
+      mbar_wait(bar, phase, nullptr);
+    }
+    __syncthreads();
+  }
+  if (w == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+}  // namespace fh
+
+using namespace fh;
+
+extern "C" int fh_rwr_tiles_tc(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                               int32_t mr, int32_t mw, const fh_entry* entries,
+                               const int64_t* offsets, uint16_t* out16, int64_t cell_stride,
+                               int64_t plane_stride, double* sumsq, int* status, void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !offsets || !out16 || mr <= 0 || mw < mr ||
+      plane_stride < 0)
+    return FH_ERR_ARG;
+  if (mr > 128 || mw > kRtMaxPad) return FH_ERR_UNSUPPORTED;
+  RtArgs a{};
+  a.tiles = tiles;
+  a.n_tiles = n_tiles;
+  a.n_cells = n_cells;
+  a.max_rows = mr;
+  a.max_width = mw;
+  a.npad_max = (mw + 63) & ~63;
+  a.entries = reinterpret_cast<const uint2*>(entries);
+  a.offsets = offsets;
+  a.out16 = reinterpret_cast<__nv_bfloat16*>(out16);
+  a.cell_stride = cell_stride;
+  a.plane_stride = plane_stride;
+  a.sumsq = sumsq;
+  a.status = status;
+  // at least 120 KB so that one CTA (and one 512-column TMEM allocation) sits on an SM
+  size_t smem = rt_smem_bytes(a.npad_max);
+  if (smem < 120 * 1024) smem = 120 * 1024;
+  if (smem > 227 * 1024) return FH_ERR_UNSUPPORTED;
+  if (ensure_smem((const void*)rwr_tc_kernel, smem)) return FH_ERR_LAUNCH;
+  const int sms = sm_count();
+  if (sms <= 0) return FH_ERR_LAUNCH;
+  const int64_t items = (int64_t)n_tiles * n_cells;
+  const int64_t grid = items < sms ? items : sms;
+  rwr_tc_kernel<<<(unsigned)grid, kRtThreads, smem, (cudaStream_t)stream>>>(a);
+  FH_CHECK_LAUNCH();
+  return FH_OK;
+}

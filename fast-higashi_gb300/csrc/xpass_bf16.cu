@@ -8,11 +8,12 @@
 //   S^T = X   [G_hi | G_lo]   M = 128 cells,     N = 2 rp, K = band rows  (X read K-major),
 //                             split over K with a deterministic reduction
 //
-// X is stored once in bf16 (X16[cell][band row], row pitch ldx, the padding zero).  The
-// small operands E (cells x rp) and G^T (band rows x rp) are split into bf16 hi and lo parts
-// (x = hi + lo to 16 significant bits) and stacked along N, so one MMA per K step produces
-// X*hi and X*lo side by side in TMEM; the epilogue adds them.  The products are exact in the
-// fp32 accumulator, so the error is the bf16 rounding of X alone.
+// X is stored in bf16 planes X16[plane][cell][band row] (row pitch ldx, the padding zero):
+// one plane (bf16(X)) or two (hi = bf16(X), lo = bf16(X - hi), X to 16 significant bits).
+// The small operands E (cells x rp) and G^T (band rows x rp) are split the same way and
+// stacked along N, so one MMA per plane and K step produces X*hi and X*lo side by side in
+// TMEM; the epilogue adds them.  The products are exact in the fp32 accumulator, so the
+// error is that of X's planes: 2^-9 relative with one plane, 2^-17 with two.
 //
 // CTA (192 threads, one per SM, persistent over work items):
 //   warp 0  TMA producer: per K step one 128 x 64 tile of X (two 64 x 64 boxes) and the
@@ -35,15 +36,16 @@ struct XPassArgs {
   int64_t k_chunks;     // xe: chunks of 64 cells; xg: chunks of 64 band rows in total
   int64_t chunks_per_split;  // xg
   int cell_tiles;       // xg
+  int plane_rows;       // rows of the X map between planes (the cells of a plane)
   float* out;           // xe: W[rows][rp]; xg: partial[splits][n_cells][rp]
   int* status;
 };
 
 constexpr int kXpThreads = 192;
 
-template <int N>
+template <int N, int PLANES>
 struct XpCfg {
-  static constexpr uint32_t kA = 128 * 64 * 2;          // 16 KB: two 64 x 64 boxes of X
+  static constexpr uint32_t kA = PLANES * 128 * 64 * 2; // 16 KB per plane: two 64 x 64 boxes
   static constexpr uint32_t kB = (uint32_t)N * 64 * 2;  // N/64 boxes of the hi|lo operand
   static constexpr uint32_t kStage = kA + kB;
   static constexpr int kStages = (int)((192u * 1024u) / kStage);
@@ -77,11 +79,11 @@ __device__ __forceinline__ XpItem xp_item(const XPassArgs& p, int64_t item) {
   return it;
 }
 
-template <int PASS, int N>
+template <int PASS, int N, int PLANES>
 __global__ void __launch_bounds__(kXpThreads, 1)
     xpass_bf16_kernel(const __grid_constant__ CUtensorMap amap,
                       const __grid_constant__ CUtensorMap bmap, XPassArgs p) {
-  using Cfg = XpCfg<N>;
+  using Cfg = XpCfg<N, PLANES>;
   constexpr int NST = Cfg::kStages;
   constexpr uint32_t kIdesc = idesc_bf16(128, N, PASS == kPassXE, true);
   extern __shared__ uint8_t smem_raw[];
@@ -140,12 +142,17 @@ __global__ void __launch_bounds__(kXpThreads, 1)
           const uint32_t sa = base + s * Cfg::kStage, sb = sa + Cfg::kA;
           const int k = (int)(kc * 64);
           mbar_expect_tx(full(s), Cfg::kStage);
-          if (PASS == kPassXE) {
-            tma_load_2d(sa, &amap, w.x0, k, full(s));
-            tma_load_2d(sa + 8192, &amap, w.x0 + 64, k, full(s));
-          } else {
-            tma_load_2d(sa, &amap, k, w.x0, full(s));
-            tma_load_2d(sa + 8192, &amap, k, w.x0 + 64, full(s));
+#pragma unroll
+          for (int pl = 0; pl < PLANES; ++pl) {
+            const uint32_t d = sa + 16384u * pl;
+            const int y = pl * p.plane_rows;
+            if (PASS == kPassXE) {
+              tma_load_2d(d, &amap, w.x0, y + k, full(s));
+              tma_load_2d(d + 8192, &amap, w.x0 + 64, y + k, full(s));
+            } else {
+              tma_load_2d(d, &amap, k, y + w.x0, full(s));
+              tma_load_2d(d + 8192, &amap, k, y + w.x0 + 64, full(s));
+            }
           }
 #pragma unroll
           for (int b = 0; b < N / 64; ++b) tma_load_2d(sb + 8192u * b, &bmap, 64 * b, k, full(s));
@@ -176,12 +183,15 @@ __global__ void __launch_bounds__(kXpThreads, 1)
           misc[3] = it + 1;
           const uint32_t sa = base + s * Cfg::kStage, sb = sa + Cfg::kA;
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const uint64_t ad = PASS == kPassXE ? sdesc_sw128(sa + 2048u * kk, 8192, 1024)
-                                                : sdesc_sw128(sa + 32u * kk, 16, 1024);
-            const uint64_t bd = sdesc_sw128(sb + 2048u * kk, 8192, 1024);
-            mma_bf16(d, ad, bd, kIdesc, (kc > w.k0 || kk > 0) ? 1u : 0u);
-          }
+          for (int pl = 0; pl < PLANES; ++pl)
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint32_t ap = sa + 16384u * pl;
+              const uint64_t ad = PASS == kPassXE ? sdesc_sw128(ap + 2048u * kk, 8192, 1024)
+                                                  : sdesc_sw128(ap + 32u * kk, 16, 1024);
+              const uint64_t bd = sdesc_sw128(sb + 2048u * kk, 8192, 1024);
+              mma_bf16(d, ad, bd, kIdesc, (kc > w.k0 || kk > 0 || pl > 0) ? 1u : 0u);
+            }
           mma_commit(empty(s));
         }
         if (!ok) break;
@@ -276,28 +286,36 @@ __global__ void split_bf16_kernel(const float* __restrict__ src, int64_t n_rows,
   }
 }
 
-template <int PASS, int N>
+template <int PASS, int N, int PLANES>
 static int launch_xpass(const CUtensorMap& am, const CUtensorMap& bm, const XPassArgs& p,
                         cudaStream_t s) {
-  auto k = xpass_bf16_kernel<PASS, N>;
-  if (ensure_smem((const void*)k, XpCfg<N>::kSmem)) return FH_ERR_LAUNCH;
+  auto k = xpass_bf16_kernel<PASS, N, PLANES>;
+  using Cfg = XpCfg<N, PLANES>;
+  if (ensure_smem((const void*)k, Cfg::kSmem)) return FH_ERR_LAUNCH;
   const int sms = sm_count();
   if (sms <= 0) return FH_ERR_LAUNCH;
   const int64_t grid = p.n_items < sms ? p.n_items : sms;
-  k<<<(unsigned)grid, kXpThreads, XpCfg<N>::kSmem, s>>>(am, bm, p);
+  k<<<(unsigned)grid, kXpThreads, Cfg::kSmem, s>>>(am, bm, p);
   FH_CHECK_LAUNCH();
   return FH_OK;
 }
 
-template <int PASS>
-static int dispatch_xpass(const CUtensorMap& am, const CUtensorMap& bm, const XPassArgs& p,
-                          cudaStream_t s) {
+template <int PASS, int PLANES>
+static int dispatch_xpass_p(const CUtensorMap& am, const CUtensorMap& bm, const XPassArgs& p,
+                            cudaStream_t s) {
   switch (p.rp) {
-    case 32: return launch_xpass<PASS, 64>(am, bm, p, s);
-    case 64: return launch_xpass<PASS, 128>(am, bm, p, s);
-    case 128: return launch_xpass<PASS, 256>(am, bm, p, s);
+    case 32: return launch_xpass<PASS, 64, PLANES>(am, bm, p, s);
+    case 64: return launch_xpass<PASS, 128, PLANES>(am, bm, p, s);
+    case 128: return launch_xpass<PASS, 256, PLANES>(am, bm, p, s);
     default: return FH_ERR_UNSUPPORTED;
   }
+}
+
+template <int PASS>
+static int dispatch_xpass(const CUtensorMap& am, const CUtensorMap& bm, const XPassArgs& p,
+                          int planes, cudaStream_t s) {
+  return planes == 2 ? dispatch_xpass_p<PASS, 2>(am, bm, p, s)
+                     : dispatch_xpass_p<PASS, 1>(am, bm, p, s);
 }
 
 }  // namespace fh
@@ -317,19 +335,20 @@ extern "C" int fh_split_bf16(const float* src, int64_t n_rows, int32_t rp, int64
 }
 
 extern "C" int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total,
-                          int32_t n_cells, int64_t rows, const uint16_t* E2, int32_t rp, float* W,
-                          int* status, void* stream) {
+                          int32_t planes, int32_t n_cells, int64_t rows, const uint16_t* E2,
+                          int32_t rp, float* W, int* status, void* stream) {
   if (!X16 || !E2 || !W || n_cells <= 0 || n_cells > n_cells_total || rows <= 0 || ldx < rows ||
-      ldx % 128)
+      ldx % 128 || (planes != 1 && planes != 2))
     return FH_ERR_ARG;
   if (rp != 32 && rp != 64 && rp != 128) return FH_ERR_UNSUPPORTED;
   // the map ends at the last 128-row tile, so no box reads past the band rows asked for
   const uint64_t inner = (uint64_t)ceil_div(rows, 128) * 128;
   CUtensorMap am, bm;
-  if (!make_map_bf16(&am, X16, inner, (uint64_t)n_cells_total, (uint64_t)ldx, 64) ||
+  if (!make_map_bf16(&am, X16, inner, (uint64_t)n_cells_total * planes, (uint64_t)ldx, 64) ||
       !make_map_bf16(&bm, E2, (uint64_t)(2 * rp), (uint64_t)n_cells, (uint64_t)(2 * rp), 64))
     return FH_ERR_LAUNCH;
   XPassArgs p{};
+  p.plane_rows = n_cells_total;
   p.rows = rows;
   p.n_cells = n_cells;
   p.rp = rp;
@@ -337,7 +356,7 @@ extern "C" int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_tota
   p.k_chunks = ceil_div(n_cells, 64);
   p.out = W;
   p.status = status;
-  return dispatch_xpass<kPassXE>(am, bm, p, (cudaStream_t)stream);
+  return dispatch_xpass<kPassXE>(am, bm, p, planes, (cudaStream_t)stream);
 }
 
 // Splits of the band-row dimension for fh_xg_bf16: about whole waves of items over the SMs,
@@ -358,15 +377,16 @@ extern "C" int fh_xg_bf16_splits(int32_t n_cells, int64_t rows) {
 }
 
 extern "C" int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total,
-                          int32_t n_cells, int64_t rows, const uint16_t* G2, int32_t rp,
-                          int32_t splits, float* partial, float* out, int* status, void* stream) {
+                          int32_t planes, int32_t n_cells, int64_t rows, const uint16_t* G2,
+                          int32_t rp, int32_t splits, float* partial, float* out, int* status,
+                          void* stream) {
   if (!X16 || !G2 || !partial || !out || n_cells <= 0 || n_cells > n_cells_total || rows <= 0 ||
-      ldx < rows || ldx % 128 || splits <= 0)
+      ldx < rows || ldx % 128 || splits <= 0 || (planes != 1 && planes != 2))
     return FH_ERR_ARG;
   if (rp != 32 && rp != 64 && rp != 128) return FH_ERR_UNSUPPORTED;
   const uint64_t inner = (uint64_t)ceil_div(rows, 128) * 128;
   CUtensorMap am, bm;
-  if (!make_map_bf16(&am, X16, inner, (uint64_t)n_cells_total, (uint64_t)ldx, 64) ||
+  if (!make_map_bf16(&am, X16, inner, (uint64_t)n_cells_total * planes, (uint64_t)ldx, 64) ||
       !make_map_bf16(&bm, G2, (uint64_t)(2 * rp), (uint64_t)rows, (uint64_t)(2 * rp), 64))
     return FH_ERR_LAUNCH;
   const int64_t chunks = ceil_div(rows, 64);
@@ -377,13 +397,14 @@ extern "C" int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_tota
   p.n_cells = n_cells;
   p.rp = rp;
   p.cell_tiles = (int)ceil_div(n_cells, 128);
+  p.plane_rows = n_cells_total;
   p.n_items = (int64_t)p.cell_tiles * used;
   p.k_chunks = chunks;
   p.chunks_per_split = per;
   p.out = partial;
   p.status = status;
   cudaStream_t s = (cudaStream_t)stream;
-  int rc = dispatch_xpass<kPassXG>(am, bm, p, s);
+  int rc = dispatch_xpass<kPassXG>(am, bm, p, planes, s);
   if (rc) return rc;
   const int64_t n = (int64_t)n_cells * rp;
   int64_t blocks = ceil_div(n, 256);

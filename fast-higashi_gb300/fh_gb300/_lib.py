@@ -58,11 +58,12 @@ SIGNATURES = {
     "fh_xg_splits": (C.c_int, [I32, I64]),
     "fh_xg_f32": (C.c_int, [P, I64, I32, I64, P, I32, I32, P, P, P]),
     "fh_project_y_f32": (C.c_int, [P, P, I64, P, P, I32, P, I32, P]),
-    "fh_rwr_tiles_bf16": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, P, P, P]),
+    "fh_rwr_tiles_bf16": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, I64, P, P, P]),
+    "fh_rwr_tiles_tc": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, I64, P, P, P]),
     "fh_split_bf16": (C.c_int, [P, I64, I32, I64, P, P]),
-    "fh_xe_bf16": (C.c_int, [P, I64, I32, I32, I64, P, I32, P, P, P]),
+    "fh_xe_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, P, P, P]),
     "fh_xg_bf16_splits": (C.c_int, [I32, I64]),
-    "fh_xg_bf16": (C.c_int, [P, I64, I32, I32, I64, P, I32, I32, P, P, P, P]),
+    "fh_xg_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, I32, P, P, P, P]),
     "fh_procrustes_f32": (C.c_int, [P, P, I64, I32, I32, P, P, I32, P, P, I32, I32, I32, P, P,
                                     P, P, P]),
     "fh_projection_g_f32": (C.c_int, [P, P, I64, I32, I32, P, I32, P, P, I32, I32, I32, P, P,
@@ -83,7 +84,7 @@ _KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_exclusive_scan_n
             "fh_densify_tile": 1, "fh_rwr_tiles_f32": 1, "fh_rwr_dense_f32": 1,
             "fh_rwr_dense_deltas": 1, "fh_rwr_tiles_deltas": 1, "fh_xe_f32": 1, "fh_xg_f32": 2,
             "fh_project_y_f32": 1, "fh_procrustes_f32": 1, "fh_projection_g_f32": 1,
-            "fh_rwr_tiles_bf16": 1, "fh_split_bf16": 1, "fh_xe_bf16": 1, "fh_xg_bf16": 2,
+            "fh_rwr_tiles_bf16": 1, "fh_rwr_tiles_tc": 1, "fh_split_bf16": 1, "fh_xe_bf16": 1, "fh_xg_bf16": 2,
             "fh_polar_f32": 1, "fh_polar_svals_f32": 1, "fh_meta_polar": 5, "fh_core_norm": 2}
 launches = 0
 

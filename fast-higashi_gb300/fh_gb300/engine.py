@@ -1,9 +1,11 @@
 """Device-resident fit engine: contact build, RWR once, then the ALS sweep as kernel launches.
 
-Two forms share everything but X and the two passes over it:
-  precision="fp32"  the plain drop-in: X in fp32, CUDA-core passes (fh_xe_f32 / fh_xg_f32)
-  precision="bf16"  the batched tensor-core form: X in bf16, tcgen05 passes (fh_xe_bf16 /
-                    fh_xg_bf16) with the small operands split hi|lo; every other step fp32
+The forms share everything but X and the two passes over it:
+  precision="fp32"    the plain drop-in: X in fp32, CUDA-core passes (fh_xe_f32 / fh_xg_f32)
+  precision="bf16x2"  the tensor-core form: X as two bf16 planes (hi, lo: 16 significant
+                      bits), tcgen05 passes (fh_xe_bf16 / fh_xg_bf16) with the small operands
+                      split hi|lo as well, so the products are fp32-class; every other step fp32
+  precision="bf16"    the same with one bf16 plane (half the X traffic, X rounded to 2^-9)
 Layout in HBM (all on one GPU):
   entries   packed contacts, one segment per (bin batch, cell)           8 B / contact
   X / X16   RWR output of every cell: X[cell][band row]              4 B / 2 B per element
@@ -38,10 +40,11 @@ class FitEngine:
                  precision="fp32"):
         import torch
         self.torch = torch
-        if precision not in ("fp32", "bf16"):
-            raise _lib.FHError("FitEngine", 1, "precision must be 'fp32' or 'bf16'")
+        if precision not in ("fp32", "bf16", "bf16x2"):
+            raise _lib.FHError("FitEngine", 1, "precision must be 'fp32', 'bf16' or 'bf16x2'")
         self.precision = precision
-        self.bf16 = precision == "bf16"
+        self.bf16 = precision != "fp32"
+        self.planes = 2 if precision == "bf16x2" else 1
         self.timing = None   # {kernel family: [(start event, end event)]} when enabled
         self.device = torch.device(device)
         if self.device.type != "cuda":
@@ -98,7 +101,8 @@ class FitEngine:
         self.tiles_dev = self.store.tiles_dev
         if self.bf16:
             self.X = None
-            self.X16 = torch.zeros((self.Ct, self.ldx), dtype=torch.bfloat16, device=dev)
+            self.X16 = torch.zeros((self.planes, self.Ct, self.ldx), dtype=torch.bfloat16,
+                                   device=dev)
         else:
             self.X = torch.zeros((self.Ct, self.ldx), dtype=f32, device=dev)
             self.X16 = None
@@ -203,10 +207,17 @@ class FitEngine:
 
     def _run_rwr(self):
         P = _lib.ptr
-        if self.bf16:
+        if self.bf16 and self.max_rows <= 128 and self.max_width <= 256:
+            _lib.call("fh_rwr_tiles_tc", P(self.tiles_dev), self.n_tiles, self.Ct,
+                      self.max_rows, self.max_width, P(self.store.entries),
+                      P(self.store.offsets), P(self.X16), self.ldx,
+                      self.Ct * self.ldx if self.planes == 2 else 0, P(self.sumsq),
+                      P(self.status), self.sp())
+        elif self.bf16:
             _lib.call("fh_rwr_tiles_bf16", P(self.tiles_dev), self.n_tiles, self.Ct,
                       self.max_rows, self.max_width, P(self.store.entries),
-                      P(self.store.offsets), P(self.X16), self.ldx, P(self.sumsq),
+                      P(self.store.offsets), P(self.X16), self.ldx,
+                      self.Ct * self.ldx if self.planes == 2 else 0, P(self.sumsq),
                       P(self.status), self.sp())
         else:
             _lib.call("fh_rwr_tiles_f32", P(self.tiles_dev), self.n_tiles, self.Ct,
@@ -228,8 +239,8 @@ class FitEngine:
                 E2 = self.torch.empty((n_cells, 2 * rp), dtype=self.torch.bfloat16,
                                       device=self.device)
             _lib.call("fh_split_bf16", P(E), n_cells, rp, rp, P(E2), self.sp())
-            _lib.call("fh_xe_bf16", P(self.X16[:, a0:]), self.ldx, self.Ct, n_cells, rows, P(E2),
-                      rp, P(W), P(self.status), self.sp())
+            _lib.call("fh_xe_bf16", P(self.X16[0, :, a0:]), self.ldx, self.Ct, self.planes,
+                      n_cells, rows, P(E2), rp, P(W), P(self.status), self.sp())
         else:
             _lib.call("fh_xe_f32", P(self.X[:, a0:]), self.ldx, n_cells, rows, P(E), rp, P(W),
                       self.sp())
@@ -242,8 +253,9 @@ class FitEngine:
                 G2 = self.torch.empty((rows, 2 * rp), dtype=self.torch.bfloat16,
                                       device=self.device)
             _lib.call("fh_split_bf16", P(Gt), rows, rp, rp, P(G2), self.sp())
-            _lib.call("fh_xg_bf16", P(self.X16[:, a0:]), self.ldx, self.Ct, n_cells, rows, P(G2),
-                      rp, splits, P(partial), P(out), P(self.status), self.sp())
+            _lib.call("fh_xg_bf16", P(self.X16[0, :, a0:]), self.ldx, self.Ct, self.planes,
+                      n_cells, rows, P(G2), rp, splits, P(partial), P(out), P(self.status),
+                      self.sp())
         else:
             _lib.call("fh_xg_f32", P(self.X[:, a0:]), self.ldx, n_cells, rows, P(Gt), rp, splits,
                       P(partial), P(out), self.sp())
@@ -358,6 +370,53 @@ class FitEngine:
         hist["meta"].copy_(self.meta_ssum)
         hist["core"].copy_(self.core)
         self.cp_als(n_iter_parafac)
+
+    @staticmethod
+    def parafac_schedule(n_iter, n_iter_parafac):
+        """CP-ALS sweeps per fit iteration: one more every 10 iterations, at most 10
+        (parafac2_intergrative.py:636-637)."""
+        out = []
+        for it in range(n_iter):
+            if it % 10 == 0 and it > 0 and n_iter_parafac < 10:
+                n_iter_parafac += 1
+            out.append(n_iter_parafac)
+        return out
+
+    def run_iterations(self, n_iter, n_iter_parafac, hist, graph=True):
+        """n_iter fit iterations with no host synchronisation.  With graph=True the whole
+        sequence is captured once into a CUDA graph (per schedule and history buffers) and
+        replayed: every launch, buffer and tensor map in it is fixed, so replays are exact
+        repeats of the eager launches.  The capture runs after one eager pass has set every
+        kernel's shared-memory attribute."""
+        torch = self.torch
+        sched = self.parafac_schedule(n_iter, n_iter_parafac)
+        if not graph:
+            for it in range(n_iter):
+                self.iterate(it == 0, sched[it], hist[it])
+            return
+        key = (tuple(sched), tuple(h["ssum"].data_ptr() for h in hist[:n_iter]))
+        if key not in getattr(self, "_graphs", {}):
+            if not getattr(self, "_warm", False):
+                for it in range(n_iter):             # eager pass: attributes, lazy init
+                    self.iterate(it == 0, sched[it], hist[it])
+                self._warm = True
+                return
+            g = torch.cuda.CUDAGraph()
+            cap = torch.cuda.Stream(device=self.device)
+            cap.wait_stream(torch.cuda.current_stream(self.device))
+            n0 = _lib.launches
+            with torch.cuda.graph(g, stream=cap):
+                for it in range(n_iter):
+                    self.iterate(it == 0, sched[it], hist[it])
+            torch.cuda.current_stream(self.device).wait_stream(cap)
+            n_kernels = _lib.launches - n0          # captured, not yet launched
+            _lib.launches = n0
+            if not hasattr(self, "_graphs"):
+                self._graphs = {}
+            self._graphs[key] = (g, n_kernels)
+        g, n_kernels = self._graphs[key]
+        g.replay()
+        _lib.launches += n_kernels                  # the kernels each replay runs
 
     def core_norm(self):
         P = _lib.ptr

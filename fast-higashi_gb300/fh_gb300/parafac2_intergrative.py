@@ -24,9 +24,11 @@ from .engine import FitEngine
 class Fast_Higashi_core:
     def __init__(self, rank, off_diag, res_list, precision="fp32"):
         """precision: "fp32" is the plain drop-in (the reference's arithmetic on CUDA cores);
-        "bf16" keeps the RWR output in bf16 and runs the passes over it on the tensor cores."""
+        "bf16x2" keeps the RWR output as two bf16 planes (16 significant bits) and runs the
+        passes over it on the tensor cores; "bf16" keeps one plane (X rounded to bf16)."""
         self.rank = rank
         self.precision = precision
+        self.use_graph = True
         self.sparse_conv = False
         self.off_diag = off_diag
         self.res_list = res_list
@@ -111,15 +113,18 @@ class Fast_Higashi_core:
         lines = []
         t_start = time.time()
         done = n_iter_max
-        for it in range(n_iter_max):
-            if it % 10 == 0 and it > 0 and n_iter_parafac < 10:
-                n_iter_parafac += 1
-            eng.iterate(it == 0, n_iter_parafac, hist[it])
-            if tol > 0:
+        if tol > 0:
+            for it in range(n_iter_max):
+                if it % 10 == 0 and it > 0 and n_iter_parafac < 10:
+                    n_iter_parafac += 1
+                eng.iterate(it == 0, n_iter_parafac, hist[it])
                 if self._record(eng, hist[it], it, lines, verbose, t_start, tol):
                     done = it + 1
                     break
-        if tol <= 0:
+        else:
+            # no stopping rule: the iterations need no host round trip and run as one CUDA
+            # graph once the engine has run them eagerly
+            eng.run_iterations(n_iter_max, n_iter_parafac, hist, graph=self.use_graph)
             for it in range(n_iter_max):
                 self._record(eng, hist[it], it, lines, verbose, t_start, tol)
         eng.check_status("fit")

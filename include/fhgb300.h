@@ -111,12 +111,24 @@ int fh_rwr_tiles_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
                      const int64_t* offsets, float* out, int64_t cell_stride, double* sumsq,
                      int* status, void* stream);
 
-/* fh_rwr_tiles_f32 with the output rounded to bf16 (out16: bf16 bits, same indexing); the
- * sumsq entries are taken over the rounded values.  Feeds fh_xe_bf16 / fh_xg_bf16. */
+/* fh_rwr_tiles_f32 with the output stored as bf16 planes (out16: bf16 bits, same indexing):
+ * plane 0 = bf16(x); with plane_stride > 0 a second plane at out16 + plane_stride holds
+ * bf16(x - plane 0), which carries x to 16 significant bits.  The sumsq entries are taken
+ * over the stored value.  Feeds fh_xe_bf16 / fh_xg_bf16. */
 int fh_rwr_tiles_bf16(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
                       int32_t max_rows, int32_t max_width, const fh_entry* entries,
                       const int64_t* offsets, uint16_t* out16, int64_t cell_stride,
-                      double* sumsq, int* status, void* stream);
+                      int64_t plane_stride, double* sumsq, int* status, void* stream);
+
+/* The same partial RWR on the tcgen05 tensor cores (no reference counterpart: the reference
+ * runs torch.bmm in fp32, partial_rwr.py:85-138): S2 = A A^T and every P Z_t product with
+ * bf16 operands split hi|lo (three products, fp32 accumulators in TMEM), the recurrence
+ * Z_{t+1} = 0.5 P Z_t + 0.5 A of fh_rwr_tiles_f32, and the same output planes as
+ * fh_rwr_tiles_bf16.  max_rows <= 128 and max_width <= 256 (FH_ERR_UNSUPPORTED otherwise). */
+int fh_rwr_tiles_tc(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells, int32_t max_rows,
+                    int32_t max_width, const fh_entry* entries, const int64_t* offsets,
+                    uint16_t* out16, int64_t cell_stride, int64_t plane_stride, double* sumsq,
+                    int* status, void* stream);
 
 /* Same arithmetic on a dense tile x[n_cells][rows][width] (the partial_rwr drop-in: no
  * floor is applied to x); out[n_cells][rows][width]. */
@@ -155,9 +167,10 @@ int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const 
 /* ---- the same two passes over X held in bf16, on the tcgen05 tensor cores (no reference
  * counterpart: the reference's passes are fp32 torch.bmm / opt_einsum calls at
  * parafac2_intergrative.py:374-383, 422-430 and 522-529).
- * X16: bf16[n_cells_total][ldx] (ldx % 128 == 0, columns >= rows zero), written by
- * fh_rwr_tiles_bf16.  The small operand is passed split, hi | lo = fh_split_bf16(x), so
- * the products carry it to 16 significant bits; the error is X's bf16 rounding.
+ * X16: bf16[planes][n_cells_total][ldx] (ldx % 128 == 0, columns >= rows zero), written by
+ * fh_rwr_tiles_bf16; planes = 1 (bf16(X)) or 2 (X to 16 significant bits).  The small
+ * operand is passed split, hi | lo = fh_split_bf16(x), so the products carry it to 16
+ * significant bits; the error is that of X's planes.
  * fh_split_bf16: dst[row][0, rp) = bf16(x), dst[row][rp, 2 rp) = bf16(x - bf16(x)) for
  *                x = src[row * ld_src + m].
  * fh_xe_bf16:    W[row][m] = sum_{c < n_cells} X16[c][row] E[c][m];  E2 = split of E
@@ -168,13 +181,13 @@ int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const 
  * status: int32 device word; a device-side wait that runs out sets FH_ERR_TIMEOUT. */
 int fh_split_bf16(const float* src, int64_t n_rows, int32_t rp, int64_t ld_src, uint16_t* dst,
                   void* stream);
-int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t n_cells,
-               int64_t rows, const uint16_t* E2, int32_t rp, float* W, int* status,
-               void* stream);
+int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t planes,
+               int32_t n_cells, int64_t rows, const uint16_t* E2, int32_t rp, float* W,
+               int* status, void* stream);
 int fh_xg_bf16_splits(int32_t n_cells, int64_t rows);
-int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t n_cells,
-               int64_t rows, const uint16_t* G2, int32_t rp, int32_t splits, float* partial,
-               float* out, int* status, void* stream);
+int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t planes,
+               int32_t n_cells, int64_t rows, const uint16_t* G2, int32_t rp, int32_t splits,
+               float* partial, float* out, int* status, void* stream);
 
 /* Y[g][l][m] = sum_j U_g[j][l] W[xoff + i*width + j][m] for every bin row g (K16 tail,
  * parafac2_intergrative.py:522-529); Y: float[n_rows][ldy_l][rp]; row_tile: int32[n_rows]. */

@@ -5,7 +5,8 @@ Tolerances (relative Frobenius error):
   fh_xe_bf16, fh_xg_bf16 1e-5 against an fp64 product of the same bf16 X and the exact fp32
                          small operand (the split carries it to 2^-16, the fp32 accumulator
                          adds ~1e-7 sqrt(K))
-  fh_rwr_tiles_bf16      bit-identical to bf16(fh_rwr_tiles_f32)
+  fh_rwr_tiles_bf16      plane 0 bit-identical to bf16(fh_rwr_tiles_f32), plane 1 to the bf16
+                         of the residual
 """
 import math
 
@@ -41,12 +42,18 @@ def split(x):
     return out
 
 
-def make_x16(ct, rows, seed):
+def make_x16(ct, rows, seed, planes=1):
+    """X as bf16 planes [planes][ct][ldx] and its exact value (the sum of the planes)."""
     g = torch.Generator(device="cpu").manual_seed(seed)
     ldx = int(math.ceil(rows / 128) * 128)
     X = torch.zeros((ct, ldx), dtype=torch.float32)
     X[:, :rows] = torch.rand((ct, rows), generator=g) * torch.rand((ct, 1), generator=g)
-    return X.to(torch.bfloat16).to(CUDA), ldx
+    hi = X.to(torch.bfloat16)
+    pl = [hi]
+    if planes == 2:
+        pl.append((X - hi.float()).to(torch.bfloat16))
+    X16 = torch.stack(pl).contiguous().to(CUDA)
+    return X16, ldx, X16.double().sum(0)
 
 
 def test_split_bf16_exact_to_16_bits():
@@ -57,25 +64,27 @@ def test_split_bf16_exact_to_16_bits():
     assert float(err.max()) <= 2.0 ** -16
 
 
+@pytest.mark.parametrize("planes", [1, 2])
 @pytest.mark.parametrize("rp,ct,c,rows", [(64, 300, 260, 1000), (64, 2000, 2000, 40000),
                                           (32, 190, 130, 777), (128, 400, 333, 3001)])
-def test_xe_bf16(rp, ct, c, rows):
-    X16, ldx = make_x16(ct, rows, 1 + rp)
+def test_xe_bf16(rp, ct, c, rows, planes):
+    X16, ldx, Xv = make_x16(ct, rows, 1 + rp, planes)
     E = torch.randn((c, rp), device=CUDA)
     E2 = split(E)
     W = torch.full((rows, rp), float("nan"), device=CUDA)
     st = torch.zeros(1, dtype=torch.int32, device=CUDA)
-    _lib.call("fh_xe_bf16", P(X16), ldx, ct, c, rows, P(E2), rp, P(W), P(st), sp())
+    _lib.call("fh_xe_bf16", P(X16), ldx, ct, planes, c, rows, P(E2), rp, P(W), P(st), sp())
     torch.cuda.synchronize()
     assert int(st.item()) == 0
-    ref = X16[:c, :rows].double().T @ E.double()
+    ref = Xv[:c, :rows].T @ E.double()
     assert rel64(W, ref) < 1e-5
 
 
+@pytest.mark.parametrize("planes", [1, 2])
 @pytest.mark.parametrize("rp,ct,n,rows", [(64, 300, 300, 1000), (64, 2000, 1900, 40000),
                                           (32, 190, 130, 20000), (128, 400, 400, 3001)])
-def test_xg_bf16(rp, ct, n, rows):
-    X16, ldx = make_x16(ct, rows, 7 + rp)
+def test_xg_bf16(rp, ct, n, rows, planes):
+    X16, ldx, Xv = make_x16(ct, rows, 7 + rp, planes)
     Gt = torch.randn((rows, rp), device=CUDA)
     G2 = split(Gt)
     splits = _lib.value("fh_xg_bf16_splits", n, rows)
@@ -83,16 +92,16 @@ def test_xg_bf16(rp, ct, n, rows):
     partial = torch.empty((splits, n, rp), device=CUDA)
     out = torch.full((n, rp), float("nan"), device=CUDA)
     st = torch.zeros(1, dtype=torch.int32, device=CUDA)
-    _lib.call("fh_xg_bf16", P(X16), ldx, ct, n, rows, P(G2), rp, splits, P(partial), P(out),
-              P(st), sp())
+    _lib.call("fh_xg_bf16", P(X16), ldx, ct, planes, n, rows, P(G2), rp, splits, P(partial),
+              P(out), P(st), sp())
     torch.cuda.synchronize()
     assert int(st.item()) == 0
-    ref = X16[:n, :rows].double() @ Gt.double()
+    ref = Xv[:n, :rows] @ Gt.double()
     assert rel64(out, ref) < 1e-5
 
 
 def test_xpass_bf16_deterministic():
-    X16, ldx = make_x16(1000, 30000, 3)
+    X16, ldx, _ = make_x16(1000, 30000, 3, 2)
     Gt = torch.randn((30000, 64), device=CUDA)
     G2 = split(Gt)
     splits = _lib.value("fh_xg_bf16_splits", 1000, 30000)
@@ -101,23 +110,71 @@ def test_xpass_bf16_deterministic():
     st = torch.zeros(1, dtype=torch.int32, device=CUDA)
     for _ in range(2):
         out = torch.empty((1000, 64), device=CUDA)
-        _lib.call("fh_xg_bf16", P(X16), ldx, 1000, 1000, 30000, P(G2), 64, splits, P(partial),
-                  P(out), P(st), sp())
+        _lib.call("fh_xg_bf16", P(X16), ldx, 1000, 2, 1000, 30000, P(G2), 64, splits,
+                  P(partial), P(out), P(st), sp())
         outs.append(out)
     torch.cuda.synchronize()
     assert torch.equal(outs[0], outs[1])
 
 
-def test_rwr_tiles_bf16_is_rounded_fp32():
+def test_rwr_tiles_bf16_planes_are_split_fp32():
     from fh_gb300.engine import FitEngine
     z = G.load("rwr_tiles.npz")
     ds = datasets_from(z, resolution=1000000)
     eng = FitEngine(ds, 4, {d.chrom: 2 for d in ds}, [3] * len(ds), CUDA)
-    X16 = torch.zeros((eng.Ct, eng.ldx), dtype=torch.bfloat16, device=CUDA)
+    X16 = torch.zeros((2, eng.Ct, eng.ldx), dtype=torch.bfloat16, device=CUDA)
     ss = torch.zeros_like(eng.sumsq)
     _lib.call("fh_rwr_tiles_bf16", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
-              eng.max_width, P(eng.store.entries), P(eng.store.offsets), P(X16), eng.ldx, P(ss),
-              P(eng.status), sp())
+              eng.max_width, P(eng.store.entries), P(eng.store.offsets), P(X16), eng.ldx,
+              eng.Ct * eng.ldx, P(ss), P(eng.status), sp())
     torch.cuda.synchronize()
-    assert torch.equal(X16, eng.X.to(torch.bfloat16))
-    np.testing.assert_allclose(ss.cpu().numpy(), eng.sumsq.cpu().numpy(), rtol=1e-2)
+    hi = eng.X.to(torch.bfloat16)
+    assert torch.equal(X16[0], hi)
+    assert torch.equal(X16[1], (eng.X - hi.float()).to(torch.bfloat16))
+    np.testing.assert_allclose(ss.cpu().numpy(), eng.sumsq.cpu().numpy(), rtol=1e-4)
+
+
+@pytest.mark.parametrize("planes", [1, 2])
+def test_rwr_tiles_tc_matches_fp32(planes):
+    """tcgen05 RWR (split bf16 products) against the fp32 CUDA-core RWR on the golden tiles."""
+    from fh_gb300.engine import FitEngine
+    z = G.load("rwr_tiles.npz")
+    ds = datasets_from(z, resolution=1000000)
+    eng = FitEngine(ds, 4, {d.chrom: 2 for d in ds}, [3] * len(ds), CUDA)
+    X16 = torch.zeros((planes, eng.Ct, eng.ldx), dtype=torch.bfloat16, device=CUDA)
+    ss = torch.zeros_like(eng.sumsq)
+    _lib.call("fh_rwr_tiles_tc", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
+              eng.max_width, P(eng.store.entries), P(eng.store.offsets), P(X16), eng.ldx,
+              eng.Ct * eng.ldx if planes == 2 else 0, P(ss), P(eng.status), sp())
+    torch.cuda.synchronize()
+    assert int(eng.status.item()) == 0
+    got = X16.double().sum(0)
+    tol = 1e-4 if planes == 2 else 4e-3
+    assert rel64(got, eng.X.double()) < tol
+    np.testing.assert_allclose(ss.cpu().numpy(), eng.sumsq.cpu().numpy(), rtol=10 * tol)
+
+
+@pytest.mark.parametrize("epochs", [0, 1, 6])
+def test_rwr_tiles_tc_full_tiles(epochs):
+    """125-row bin batches of a 1 Mb genome-like chromosome (widths 145-165), 300 cells."""
+    from fh_gb300 import synth
+    from fh_gb300.engine import FitEngine
+    from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
+    w = synth.workload("c2")
+    w.n_cells = 300
+    w.chrom_bins = w.chrom_bins[:2]
+    w.chrom_names = w.chrom_names[:2]
+    coo, _ = synth.generate(w, seed=3)
+    ds = [Chrom_Dataset(Sparse(i, v, s, copy=False), *synth.recommend_batches(w, nb, w.n_cells),
+                        compact=True, flank=w.band, chrom=nm, resolution=w.resolution)
+          for (i, v, s), nm, nb in zip(coo, w.chrom_names, w.chrom_bins)]
+    eng = FitEngine(ds, 64, {d.chrom: 64 for d in ds}, [epochs] * len(ds), CUDA)
+    X16 = torch.zeros((2, eng.Ct, eng.ldx), dtype=torch.bfloat16, device=CUDA)
+    ss = torch.zeros_like(eng.sumsq)
+    _lib.call("fh_rwr_tiles_tc", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
+              eng.max_width, P(eng.store.entries), P(eng.store.offsets), P(X16), eng.ldx,
+              eng.Ct * eng.ldx, P(ss), P(eng.status), sp())
+    torch.cuda.synchronize()
+    assert int(eng.status.item()) == 0
+    assert rel64(X16.double().sum(0), eng.X.double()) < 1e-4
+    assert float(X16[:, :, eng.rows:].abs().max()) == 0.0

@@ -1,0 +1,147 @@
+"""Precision of the fp32 (plain) and bf16 (tensor-core) forms against an FP64 fit.
+
+The yardstick is tests/fp64_reference.py (the oracle's algorithm in torch float64, so it can
+run full-size fits on the GPU); the CPU test below pins it to the numpy oracle first.
+
+Error measure: relative Frobenius error of the final meta embedding E (cells x R) after the
+orthogonal Procrustes rotation onto the FP64 one (embeddings are defined up to a rotation),
+from the same initial state, and the largest relative difference of the loss trajectory.
+Bounds at 200 cells (c1): fp32 form 5e-4, bf16x2 form (X as two bf16 planes) 1e-3 (the target),
+bf16 form (one plane) 1e-2, losses 1e-3.
+
+FH_PRECISION_WORKLOAD=c2|c3 adds a full-size report (written to
+gpurun_out/precision_<workload>.json when that folder exists) to the GPU run.
+"""
+import json
+import math
+import os
+import time
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import fh_oracle as O
+import fp64_reference as F
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _workload(name, seed=0):
+    from fh_gb300 import synth
+    from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
+    w = synth.workload(name)
+    coo, _ = synth.generate(w, seed=seed)
+    ds, bsb, bsc = [], [], []
+    for (idx, val, shape), cname, nb in zip(coo, w.chrom_names, w.chrom_bins):
+        b, c = synth.recommend_batches(w, nb, w.n_cells)
+        bsb.append(b)
+        bsc.append(c)
+        ds.append(Chrom_Dataset(Sparse(idx, val, shape, copy=False), b, c, compact=True,
+                                flank=w.band, chrom=cname, resolution=w.resolution))
+    datas = F.chrom_datas(coo, w.chrom_names, bsb, bsc, w.band)
+    return w, ds, datas
+
+
+def _random_state(datas, sizes, R, C, seed):
+    rng = np.random.default_rng(seed)
+    A = [1 + 0.01 * rng.standard_normal((d.num_bin, sizes[d.name])) for d in datas]
+    B = {d.name: np.eye(sizes[d.name]) + 0.01 * rng.standard_normal((sizes[d.name],) * 2) for d in datas}
+    D = {d.name: rng.standard_normal((R, sizes[d.name])) for d in datas}
+    E, _ = np.linalg.qr(rng.standard_normal((C, R)))
+    return A, B, D, E
+
+
+def test_fp64_reference_matches_oracle():
+    """The torch float64 restatement reproduces the numpy oracle (4 iterations, 'small')."""
+    w, ds, datas = _workload("small", seed=5)
+    sizes = O.chrom2size(datas, w.rank, w.dim1, w.resolution)
+    A, B, D, E = _random_state(datas, sizes, w.rank, w.n_cells, 1)
+    n_i = [3] * len(datas)
+    orc = O.ALSOracle(datas, w.rank, A, B, D, E, n_i).fit(4)
+    ref = F.FP64Fit(datas, w.rank, A, B, D, E, n_i, "cpu").fit(4)
+    np.testing.assert_allclose(ref.rec_errors_total, orc.rec_errors_total, rtol=1e-10)
+    assert O.rel_err(ref.E.numpy(), orc.E) < 1e-9
+
+
+def _ours(w, ds, precision, state, n_i, iters, dev):
+    from fh_gb300 import Fast_Higashi_core
+    A0, B0, D0, E0 = state
+    m = Fast_Higashi_core(w.rank, w.band, [w.resolution], precision=precision).to(dev)
+    m._sizes(ds, w.dim1, None)
+    m.A_list = [torch.from_numpy(np.asarray(a, dtype=np.float32)) for a in A0]
+    m.B_dict = {k: torch.from_numpy(np.asarray(v, dtype=np.float32)) for k, v in B0.items()}
+    m.D_dict = {k: torch.from_numpy(np.asarray(v, dtype=np.float32)) for k, v in D0.items()}
+    m.meta_embedding = torch.from_numpy(np.asarray(E0, dtype=np.float32))
+    m.n_i = np.asarray(n_i)
+    m.bin_cov_list = [None] * len(ds)
+    m.fit(ds, size_ratio=w.dim1, n_iter_max=iters, n_iter_parafac=1, do_conv=False, do_rwr=True,
+          do_col=False, tol=0, run_init=False, verbose=False)
+    torch.cuda.synchronize()
+    E = m.meta_embedding.detach().cpu().numpy()
+    losses = np.asarray(m.rec_errors_total)
+    del m
+    torch.cuda.empty_cache()
+    return E, losses
+
+
+def precision_report(name, iters=None, seed=0):
+    """Runs the GPU init once (fp32), then the fp32 form, the bf16 form and the FP64
+    restatement from that state; returns the errors."""
+    from fh_gb300 import Fast_Higashi_core
+    dev = torch.device("cuda")
+    w, ds, datas = _workload(name, seed=seed)
+    iters = iters or w.n_iter
+    torch.manual_seed(0)
+    m = Fast_Higashi_core(w.rank, w.band, [w.resolution]).to(dev)
+    m._sizes(ds, w.dim1, None)
+    m.init_params(ds, False, True, False, seed=0)
+    state = ([a.cpu().numpy() for a in m.A_list], {k: v.cpu().numpy() for k, v in m.B_dict.items()},
+             {k: v.cpu().numpy() for k, v in m.D_dict.items()}, m.meta_embedding.cpu().numpy())
+    n_i = [int(v) for v in m.n_i]
+    del m
+    torch.cuda.empty_cache()
+    out = {"workload": name, "iterations": iters, "n_i": sorted(set(n_i))}
+    got = {}
+    for prec in ("fp32", "bf16x2", "bf16"):
+        t0 = time.time()
+        got[prec] = _ours(w, ds, prec, state, n_i, iters, dev)
+        out["%s_seconds" % prec] = time.time() - t0
+    t0 = time.time()
+    ref = F.FP64Fit(datas, w.rank, *state, n_i, dev).fit(iters)
+    out["fp64_seconds"] = time.time() - t0
+    E64 = ref.E.cpu().numpy()
+    L64 = np.asarray(ref.rec_errors_total)
+    del ref
+    torch.cuda.empty_cache()
+    for prec, (E, L) in got.items():
+        out["%s_aligned_embedding_error" % prec] = F.aligned_error(E, E64)
+        out["%s_loss_max_rel_diff" % prec] = float(np.max(np.abs(L - L64) / np.abs(L64)))
+    out["fp64_loss_final"] = float(L64[-1])
+    return out
+
+
+@pytest.mark.gpu
+def test_aligned_embedding_error_c1():
+    r = precision_report("c1")
+    print(json.dumps(r))
+    assert r["fp32_aligned_embedding_error"] < 5e-4
+    assert r["bf16x2_aligned_embedding_error"] < 1e-3
+    assert r["bf16_aligned_embedding_error"] < 1e-2
+    assert r["fp32_loss_max_rel_diff"] < 1e-3
+    assert r["bf16x2_loss_max_rel_diff"] < 1e-3
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(not os.environ.get("FH_PRECISION_WORKLOAD"),
+                    reason="full-size precision report on request (FH_PRECISION_WORKLOAD)")
+def test_precision_report_full_size():
+    name = os.environ["FH_PRECISION_WORKLOAD"]
+    r = precision_report(name)
+    print(json.dumps(r))
+    d = os.path.join(ROOT, "gpurun_out")
+    if os.path.isdir(d):
+        with open(os.path.join(d, "precision_%s.json" % name), "w") as f:
+            json.dump(r, f, indent=1)
+    assert math.isfinite(r["bf16x2_aligned_embedding_error"])
