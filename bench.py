@@ -310,6 +310,8 @@ def gb300_arm(args, rank, local, ws):
         {k: v.cpu() for k, v in state[2].items()}, state[3].cpu()
     n_i = m.n_i.copy()
 
+    store_h2d = [0]
+
     def e2e_step():
         mm = Fast_Higashi_core(w.rank, w.band, [w.resolution], precision=args.precision).to(dev)
         mm._sizes(ds, w.dim1, None)
@@ -318,17 +320,19 @@ def gb300_arm(args, rank, local, ws):
         mm.fit(ds, size_ratio=w.dim1, n_iter_max=iters, n_iter_parafac=1, do_conv=False,
                do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
         emb = mm.meta_embedding.cpu()
-        return mm, emb
+        store_h2d[0] = mm.engine.store.h2d_bytes
+        del mm                       # the next step's engine reuses the freed device memory
+        return emb
 
     e2e_step()
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
     for _ in range(max(1, args.steps // 2)):
-        mm, emb = e2e_step()
+        emb = e2e_step()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 2)
-    h2d = mm.engine.store.h2d_bytes + sum(a.numel() * 4 for a in A0) + E0.numel() * 4 + \
+    h2d = store_h2d[0] + sum(a.numel() * 4 for a in A0) + E0.numel() * 4 + \
         sum(v.numel() * 4 for v in B0.values()) + sum(v.numel() * 4 for v in D0.values())
     d2h = emb.numel() * 4 + iters * (eng.nb + 1 + len(eng.names)) * 8
     e2e = {"value": ws * C / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),

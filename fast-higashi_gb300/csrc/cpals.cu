@@ -8,9 +8,11 @@
 //     A <- MTTKRP_A (B^T B * D^T D + 1e-10 I)^{-1}   (and likewise for B, D)
 //     MTTKRP_A[i] = sum_j B[j] * (Y_i D)[j],   MTTKRP_B = sum_i A_i (x) (Y_i D),
 //     MTTKRP_D   = sum_i A_i (x) (Y_i^T B)      ((x): column-wise product).
-// The r x r systems are solved by Cholesky in fp32, the reference's own precision
-// (parafac_integrative.py:12-15 solves in fp32): this GB300 runs fp64 at ~0.33 TFLOP/s, so
-// fp64 is kept to the scalar sums (loss, core norm).  The reconstruction loss needs no Xhat:
+// The r x r systems are factored by Cholesky in fp32, the reference's own precision
+// (parafac_integrative.py:12-15 solves in fp32), and applied through the inverse
+// (L L^T)^{-1} = L^{-T} L^{-1} formed once per chromosome, so every right-hand side is a
+// register-tiled product instead of a serial substitution: this GB300 runs fp64 at
+// ~0.33 TFLOP/s, so fp64 is kept to the scalar sums (loss, core norm).  The reconstruction loss needs no Xhat:
 // ||Xhat||^2 = sum(A^TA * B^TB * D^TD) and <Xhat, Y> = sum(D * MTTKRP_D) with the final
 // A, B.  balance_norm (unit columns, the product of the column norms folded into D) follows
 // each sweep unless the relative loss change fell below 1e-5, as the reference breaks before
@@ -41,7 +43,7 @@ struct CpArgs {
   float* D;        // [chrom][RP][ld]
   const float* Y;  // [bin rows][ldy][RP]
   int ld, RP, R, ldy;
-  float* L;        // [chrom][ld][ld]    Cholesky factor for the A rows
+  float* L;        // [chrom][ld][ld]    inverse of the A-row system (B^T B * D^T D + 1e-10 I)
   float* part;     // [chunk][pstride]
   float* gAA;      // [chrom][ld*ld]
   float* gBB;
@@ -60,6 +62,31 @@ enum CpSmallMode { kSmallInit = 0, kSmallB = 1, kSmallD = 2, kSmallCore = 3 };
 
 __host__ __device__ inline size_t cp_pstride(int ld) { return (size_t)2 * ld * ld + 2; }
 constexpr size_t kCpRowsSmem = 4 * (size_t)kCpMaxR * kCpLz * sizeof(float);
+
+// acc[u][v] = sum_k fa(w + 8u, k) fb(k, lane + 32v) over k < K for 256 threads (rows w + 8u,
+// u < 8; columns lane + 32 v, v < 2), rows / columns clamped to M-1 / N-1.
+template <class FA, class FB>
+__device__ __forceinline__ void cp_mm(int M, int N, int K, FA fa, FB fb, float (&acc)[8][2]) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  int ri[8], cj[2];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) ri[u] = min(w + 8 * u, M - 1);
+#pragma unroll
+  for (int v = 0; v < 2; ++v) cj[v] = min(l + 32 * v, N - 1);
+#pragma unroll
+  for (int u = 0; u < 8; ++u) acc[u][0] = acc[u][1] = 0.f;
+  for (int k = 0; k < K; ++k) {
+    float av[8], bv[2];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) av[u] = fa(ri[u], k);
+#pragma unroll
+    for (int v = 0; v < 2; ++v) bv[v] = fb(k, cj[v]);
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+  }
+}
 
 __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode) {
   extern __shared__ __align__(16) float cps[];
@@ -131,12 +158,18 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
     __syncthreads();
     if (mode == kRowsAB) {
       // Z[j][q] = sum_m Y[j][m] D[m][q]
-      for (int j = ty; j < r; j += 8)
-        for (int q = tx; q < r; q += 32) {
-          float s = 0.f;
-          for (int m = 0; m < R; ++m) s = fmaf(Ys[j * lz + m], Fs[m * lz + q], s);
-          Zs[j * lz + q] = s;
-        }
+      {
+        float zc[8][2];
+        cp_mm(r, r, R, [&](int j, int m) { return Ys[j * lz + m]; },
+              [&](int m, int q) { return Fs[m * lz + q]; }, zc);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+          for (int v = 0; v < 2; ++v) {
+            const int j = ty + 8 * u, q = tx + 32 * v;
+            if (j < r && q < r) Zs[j * lz + q] = zc[u][v];
+          }
+      }
       __syncthreads();
       if (tid < r) {
         float s = 0.f;
@@ -144,23 +177,12 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
         rhs[tid] = s;
       }
       __syncthreads();
-      // A_g = (L L^T)^{-1} rhs, one warp
-      if (ty == 0) {
-        for (int p = 0; p < r; ++p) {
-          float s = 0.f;
-          for (int q = tx; q < p; q += 32) s = fmaf(Lc[p * ld + q], ysol[q], s);
-          s = warp_sum(s);
-          if (tx == 0) ysol[p] = (rhs[p] - s) / Lc[p * ld + p];
-          __syncwarp();
-        }
-        for (int p = r - 1; p >= 0; --p) {
-          float s = 0.f;
-          for (int q = p + 1 + tx; q < r; q += 32) s = fmaf(Lc[q * ld + p], ysol[q], s);
-          s = warp_sum(s);
-          if (tx == 0) ysol[p] = (ysol[p] - s) / Lc[p * ld + p];
-          __syncwarp();
-        }
-        for (int p = tx; p < r; p += 32) a.A[g * ld + p] = ysol[p];
+      // A_g = G_A^{-1} rhs with the inverse the per-chromosome kernel left in L
+      if (tid < r) {
+        float s = 0.f;
+        for (int q = 0; q < r; ++q) s = fmaf(Lc[tid * ld + q], rhs[q], s);
+        ysol[tid] = s;
+        a.A[g * ld + tid] = s;
       }
       __syncthreads();
 #pragma unroll
@@ -181,6 +203,9 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
     } else {
       // MTTKRP_D[m][q] += A[q] * sum_j Y[j][m] B[j][q]
       const float* Ag = a.A + g * ld;
+      float yb[8][2];
+      cp_mm(R, r, r, [&](int m, int j) { return Ys[j * lz + m]; },
+            [&](int j, int q) { return Fs[j * lz + q]; }, yb);
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int m = ty + 8 * u;
@@ -188,11 +213,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
 #pragma unroll
           for (int v = 0; v < 2; ++v) {
             const int q = tx + 32 * v;
-            if (q < r) {
-              float s = 0.f;
-              for (int j = 0; j < r; ++j) s = fmaf(Ys[j * lz + m], Fs[j * lz + q], s);
-              pA[v][u] = fmaf(Ag[q], s, pA[v][u]);
-            }
+            if (q < r) pA[v][u] = fmaf(Ag[q], yb[u][v], pA[v][u]);
           }
         }
       }
@@ -217,48 +238,74 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
   }
 }
 
-// Cholesky of G (r x r, stride ld) in place into its lower triangle (fp32).
-__device__ bool cp_cholesky(float* G, int r, int ld) {
+// Cholesky of G (r x r, stride lg, odd) in place into its lower triangle (fp32).
+__device__ bool cp_cholesky(float* G, int r, int lg) {
   __shared__ int bad;
   if (threadIdx.x == 0) bad = 0;
   __syncthreads();
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int k = 0; k < r; ++k) {
     if (threadIdx.x == 0) {
-      float d = G[k * ld + k];
+      float d = G[k * lg + k];
       if (!(d > 0.f)) { bad = 1; d = 1e-30f; }
-      G[k * ld + k] = sqrtf(d);
+      G[k * lg + k] = sqrtf(d);
     }
     __syncthreads();
-    const float dk = G[k * ld + k];
-    for (int p = k + 1 + threadIdx.x; p < r; p += blockDim.x) G[p * ld + k] /= dk;
+    const float dk = G[k * lg + k];
+    for (int p = k + 1 + threadIdx.x; p < r; p += blockDim.x) G[p * lg + k] /= dk;
     __syncthreads();
     for (int p = k + 1 + ty; p < r; p += 8) {
-      const float gp = G[p * ld + k];
-      for (int q = k + 1 + tx; q <= p; q += 32) G[p * ld + q] = fmaf(-gp, G[q * ld + k], G[p * ld + q]);
+      const float gp = G[p * lg + k];
+      for (int q = k + 1 + tx; q <= p; q += 32) G[p * lg + q] = fmaf(-gp, G[q * lg + k], G[p * lg + q]);
     }
     __syncthreads();
   }
   return bad == 0;
 }
 
-// rows of RHS (nrhs x r, stride ld) -> out rows = (L L^T)^{-1} rhs, one thread per row.
-__device__ void cp_solve_rows(const float* L, int r, int ld, const float* RHS, int nrhs,
-                              float* out, int ldo) {
-  for (int row = threadIdx.x; row < nrhs; row += blockDim.x) {
-    float y[kCpMaxR];
-    for (int p = 0; p < r; ++p) {
-      float s = RHS[(size_t)row * ld + p];
-      for (int q = 0; q < p; ++q) s = fmaf(-L[p * ld + q], y[q], s);
-      y[p] = s / L[p * ld + p];
+// Gi = (L L^T)^{-1} from the Cholesky factor L (lower, stride lg): Li = L^{-1} by forward
+// substitution (one warp per column), then Gi = Li^T Li.  Li, Gi: r x lg scratch.
+__device__ void cp_chol_inverse(const float* L, int r, int lg, float* Li, float* Gi) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  for (int j = w; j < r; j += 8) {
+    for (int i = l; i < r; i += 32) Li[i * lg + j] = 0.f;
+    __syncwarp();
+    for (int i = j; i < r; ++i) {
+      float d = 0.f;
+      for (int q = j + l; q < i; q += 32) d = fmaf(L[i * lg + q], Li[q * lg + j], d);
+      d = warp_sum(d);
+      if (l == 0) Li[i * lg + j] = ((i == j ? 1.f : 0.f) - d) / L[i * lg + i];
+      __syncwarp();
     }
-    for (int p = r - 1; p >= 0; --p) {
-      float s = y[p];
-      for (int q = p + 1; q < r; ++q) s = fmaf(-L[q * ld + p], y[q], s);
-      y[p] = s / L[p * ld + p];
-    }
-    for (int p = 0; p < r; ++p) out[(size_t)row * ldo + p] = y[p];
   }
+  __syncthreads();
+  float acc[8][2];
+  cp_mm(r, r, r, [&](int p, int i) { return Li[i * lg + p]; },
+        [&](int i, int q) { return Li[i * lg + q]; }, acc);
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int p = w + 8 * u, q = l + 32 * v;
+      if (p < r && q < r) Gi[p * lg + q] = acc[u][v];
+    }
+  __syncthreads();
+}
+
+// out rows = RHS rows G^{-1} (RHS: nrhs x r, stride ldr, nrhs <= 64; Gi symmetric, stride lg).
+__device__ void cp_apply_inverse(const float* RHS, int ldr, int nrhs, const float* Gi, int r,
+                                 int lg, float* out, int ldo) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  float acc[8][2];
+  cp_mm(nrhs, r, r, [&](int row, int p) { return RHS[(size_t)row * ldr + p]; },
+        [&](int p, int q) { return Gi[p * lg + q]; }, acc);
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int row = w + 8 * u, q = l + 32 * v;
+      if (row < nrhs && q < r) out[(size_t)row * ldo + q] = acc[u][v];
+    }
 }
 
 // Gram F^T F of an (nrows x r, stride ld) factor into G (stride ld), fp32.
@@ -277,8 +324,11 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
   const int ci = blockIdx.x;
   const int r = a.c_rank[ci], R = a.R, ld = a.ld;
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
-  float* G = sf;                          // ld*ld
-  float* work = G + ld * ld;              // RP*ld
+  const int lg = ld + 1;                  // odd stride: column walks hit distinct banks
+  float* G = sf;                          // ld x lg: the system, then its Cholesky factor
+  float* Li = G + ld * lg;                // ld x lg: L^{-1}
+  float* Gi = Li + ld * lg;               // ld x lg: the system's inverse
+  float* work = Gi + ld * lg;             // RP*ld
   __shared__ double dred[32];
   __shared__ float nA[kCpMaxR], nB[kCpMaxR], nD[kCpMaxR];
   __shared__ int stop;
@@ -343,12 +393,13 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
         }
         gAA[p * ld + q] = s;
         work[p * ld + q] = t;
-        G[p * ld + q] = s * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
+        G[p * lg + q] = s * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
       }
     __syncthreads();
-    if (!cp_cholesky(G, r, ld) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+    if (!cp_cholesky(G, r, lg) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
     __syncthreads();
-    cp_solve_rows(G, r, ld, work, r, Bc, ld);
+    cp_chol_inverse(G, r, lg, Li, Gi);
+    cp_apply_inverse(work, ld, r, Gi, r, lg, Bc, ld);
     __syncthreads();
     cp_gram(Bc, r, r, ld, gBB);
     return;
@@ -363,11 +414,12 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
       }
     for (int p = ty; p < r; p += 8)
       for (int q = tx; q < r; q += 32)
-        G[p * ld + q] = gAA[p * ld + q] * gBB[p * ld + q] + (p == q ? 1e-10f : 0.f);
+        G[p * lg + q] = gAA[p * ld + q] * gBB[p * ld + q] + (p == q ? 1e-10f : 0.f);
     __syncthreads();
-    if (!cp_cholesky(G, r, ld) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+    if (!cp_cholesky(G, r, lg) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
     __syncthreads();
-    cp_solve_rows(G, r, ld, work, R, Dc, ld);
+    cp_chol_inverse(G, r, lg, Li, Gi);
+    cp_apply_inverse(work, ld, R, Gi, r, lg, Dc, ld);
     __syncthreads();
     cp_gram(Dc, R, r, ld, gDD);
     __syncthreads();
@@ -418,12 +470,13 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
   __syncthreads();
   for (int p = ty; p < r; p += 8)
     for (int q = tx; q < r; q += 32)
-      G[p * ld + q] = gBB[p * ld + q] * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
+      G[p * lg + q] = gBB[p * ld + q] * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
   __syncthreads();
-  if (!cp_cholesky(G, r, ld) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+  if (!cp_cholesky(G, r, lg) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
   __syncthreads();
+  cp_chol_inverse(G, r, lg, Li, Gi);
   for (int p = ty; p < r; p += 8)
-    for (int q = tx; q < r; q += 32) Lc[p * ld + q] = G[p * ld + q];
+    for (int q = tx; q < r; q += 32) Lc[p * ld + q] = Gi[p * lg + q];
 }
 
 }  // namespace fh
@@ -475,7 +528,7 @@ extern "C" int fh_cp_als(int32_t nchrom, int32_t nchunks, const int32_t* meta, f
   a.core = core;
   a.cross = cross;
   a.status = status;
-  const size_t small_smem = (l + (size_t)rp * ld) * sizeof(float);
+  const size_t small_smem = (3 * (size_t)ld * (ld + 1) + (size_t)rp * ld) * sizeof(float);
   if (ensure_smem((const void*)cp_small_kernel, small_smem) ||
       ensure_smem((const void*)cp_rows_kernel, kCpRowsSmem))
     return FH_ERR_LAUNCH;

@@ -83,7 +83,8 @@ __device__ __forceinline__ int pc_nwarps() { return blockDim.x >> 5; }
 // On return the upper triangle of T[0:r][0:r] is R, T[i][k] (i > k) holds v_k below the
 // diagonal, vh[k] the head of v_k and beta[k] = 2 / v_k^T v_k (0 for a zero column).
 // householder_panel factors columns [k0, k1) and applies each reflector to the columns
-// below k1 only; householder_qr is the whole matrix as one panel.
+// below k1 only; householder_qr is the whole matrix as one panel.  (A blocked variant with
+// UT-form trailing updates measured 9 % slower here: the panel steps keep their barriers.)
 __device__ inline void householder_panel(float* T, int n, int k0, int k1, int ldt,
                                          PolarScratch& s) {
   const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
@@ -228,84 +229,6 @@ __device__ inline void gj_inverse(const float* X, int ldx, float* Aug, int r, Po
   }
 }
 
-// ---- blocked Householder QR (512 threads, r <= 64, n <= 192) ---------------------------
-// Panels of 16 columns are factored by householder_panel; the columns to their right are
-// updated once per panel with the UT form of the panel's reflectors,
-//   A2 <- (I - Vp Tp Vp^T)^T A2 = A2 - Vp (Tp^T (Vp^T A2)),  Tp^{-1} = diag(1/beta) + striu(Vp^T Vp),
-// as register-tiled products.  Same reflectors as householder_qr; Sc: >= 2600 floats.
-__device__ inline void householder_qr_blocked(float* T, int n, int r, int ldt, float* Sc,
-                                              PolarScratch& s) {
-  constexpr int NB = 16;
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  float* Wm = Sc;            // NB x 64: Vp^T [Vp | A2]
-  float* Tp = Sc + NB * 64;  // NB x NB (stride NB + 1)
-  float* W2 = Tp + NB * (NB + 1);  // NB x 64
-  const float* vh = s.vh;
-  const float* beta = s.beta;
-  for (int k0 = 0; k0 < r; k0 += NB) {
-    const int k1 = min(k0 + NB, r), nb = k1 - k0, m2 = r - k1;
-    householder_panel(T, n, k0, k1, ldt, s);
-    if (m2 == 0) break;
-    auto V = [&](int i, int c) -> float {   // column k0 + c of the panel's reflectors
-      const int k = k0 + c;
-      return i > k ? T[i * ldt + k] : (i == k ? vh[k] : 0.f);
-    };
-    // Wm = Vp^T [Vp | A2] over rows k0 .. n-1
-    {
-      float acc[1][2];
-      cta_mm<1, 2>(nb, nb + m2, n - k0, 0, [&](int c, int kk) { return V(k0 + kk, c); },
-                   [&](int kk, int j) {
-                     return j < nb ? V(k0 + kk, j) : T[(k0 + kk) * ldt + k1 + (j - nb)];
-                   },
-                   acc);
-#pragma unroll
-      for (int v = 0; v < 2; ++v) {
-        const int j = l + 32 * v;
-        if (w < nb && j < nb + m2) Wm[w * 64 + j] = acc[0][v];
-      }
-    }
-    __syncthreads();
-    // Tp = (diag(1/beta) + striu(Vp^T Vp))^{-1}, one warp per column
-    if (w < nb) {
-      const int j = w;
-      for (int i = j; i >= 0; --i) {
-        float d = 0.f;
-        for (int q = i + 1 + l; q <= j; q += 32) d = fmaf(Wm[i * 64 + q], Tp[q * (NB + 1) + j], d);
-        d = warp_sum(d);
-        if (l == 0) {
-          const float bi = beta[k0 + i];
-          const float dii = bi != 0.f ? 1.f / bi : 1.f;
-          Tp[i * (NB + 1) + j] = ((i == j ? 1.f : 0.f) - d) / dii;
-        }
-        __syncwarp();
-      }
-    }
-    __syncthreads();
-    // W2 = Tp^T (Vp^T A2)
-    for (int idx = threadIdx.x; idx < nb * m2; idx += 512) {
-      const int c = idx / m2, j = idx - c * m2;
-      float acc = 0.f;
-      for (int cp = 0; cp <= c; ++cp) acc = fmaf(Tp[cp * (NB + 1) + c], Wm[cp * 64 + nb + j], acc);
-      W2[c * 64 + j] = acc;
-    }
-    __syncthreads();
-    // A2 -= Vp W2 (rows k0 .. n-1; each thread updates the elements it computed)
-    for (int row0 = k0; row0 < n; row0 += 96) {
-      float acc[6][2];
-      cta_mm<6, 2>(n, m2, nb, row0, [&](int i, int c) { return V(i, c); },
-                   [&](int c, int j) { return W2[c * 64 + j]; }, acc);
-#pragma unroll
-      for (int u = 0; u < 6; ++u)
-#pragma unroll
-        for (int v = 0; v < 2; ++v) {
-          const int i = row0 + w + 16 * u, j = l + 32 * v;
-          if (i < n && j < m2) T[i * ldt + k1 + j] -= acc[u][v];
-        }
-    }
-    __syncthreads();
-  }
-}
-
 // ---- U = Q [X; 0] from the compact UT form of the reflectors (512 threads) ------------
 // Q = H_0 ... H_{r-1} = I - V T V^T with T^{-1} = diag(1/beta) + striu(V^T V) (the UT
 // transform of the Householder product), so U = [X; 0] - V (T (V_top^T X)), V_top = V's first
@@ -401,15 +324,13 @@ __device__ inline void apply_q_ut(float* T, int ldt, float* U, int ldu, float* S
 // ---- inverse of X (r x r, r <= 64, stride ldx) into Xi (stride ldo), 512 threads -------
 // Gauss-Jordan with partial pivoting on [X | I] held in registers: thread (warp w, lane l)
 // owns rows w + 16 u (u < 4) and columns l + 32 v (v < 4).  Rows are not swapped: each step
-// picks the largest |entry| of the column among the rows not yet used as pivots, so every
+// picks the largest |entry| of the column among the rows not yet used as pivots (every warp
+// finds it from the published column, so no thread waits for a pivot broadcast), so every
 // element sees the same operations as in gj_inverse; row p_k of the right block is row k of
-// X^{-1}.  Three barriers per column, no shared-memory traffic for the matrix itself.
+// X^{-1}.  Two barriers per column: the eliminating step also publishes the next column.
 __device__ inline void gj_inverse_reg(const float* X, int ldx, float* Xi, int ldo, int r,
                                       PolarScratch& s) {
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  int* used = s.gi;
-  int* kof = s.gi + 64;
-  int* pidx = s.gi + 128;
   float a[4][4];
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
@@ -425,51 +346,48 @@ __device__ inline void gj_inverse_reg(const float* X, int ldx, float* Xi, int ld
       a[u][v] = x;
     }
   }
-  if (threadIdx.x < 64) used[threadIdx.x] = threadIdx.x < r ? 0 : 1;
+  uint64_t used = r >= 64 ? 0ull : (~0ull << r);   // rows taken as pivots (and rows >= r)
+  int kof[4] = {0, 0, 0, 0};                       // step that pivoted each owned row
+  if (l == 0) {                                    // publish column 0
+#pragma unroll
+    for (int u = 0; u < 4; ++u) s.gcol[w + 16 * u] = a[u][0];
+  }
   for (int k = 0; k < r; ++k) {
     const int b = k & 1;
-    float* colk = s.gcol + 64 * b;
+    const float* colk = s.gcol + 64 * b;
     float* prow = s.grow + 128 * b;
-    if (l == (k & 31)) {
-      const bool hi = (k >> 5) != 0;
-#pragma unroll
-      for (int u = 0; u < 4; ++u) colk[w + 16 * u] = hi ? a[u][1] : a[u][0];
-    }
     __syncthreads();
-    if (w == 0) {
-      float best = -1.f;
-      int bi = 64;
+    // every warp: argmax |colk[i]| over the unused rows (ties to the lower row)
+    float best = -1.f;
+    int bi = 64;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int i = l + 32 * h;
-        if (!used[i]) {
-          const float v = fabsf(colk[i]);
-          if (v > best) { best = v; bi = i; }
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-      }
-      if (l == 0) {
-        float pv = colk[bi];
-        if (pv == 0.f) { pv = 1e-30f; s.ival[0] = 1; }
-        pidx[b] = bi;
-        s.grp[b] = 1.f / pv;
-        used[bi] = 1;
-        kof[bi] = k;
+    for (int h = 0; h < 2; ++h) {
+      const int i = l + 32 * h;
+      if (!((used >> i) & 1ull)) {
+        const float v = fabsf(colk[i]);
+        if (v > best) { best = v; bi = i; }
       }
     }
-    __syncthreads();
-    const int p = pidx[b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    const int p = bi;
+    used |= 1ull << p;
+    float pv = colk[p];
+    if (pv == 0.f) {
+      pv = 1e-30f;
+      if (threadIdx.x == 0) s.ival[0] = 1;
+    }
+    const float rp = 1.f / pv;
     if (w == (p & 15)) {
       const int pu = p >> 4;
-      const float rp = s.grp[b];
 #pragma unroll
       for (int u = 0; u < 4; ++u)
         if (u == pu) {
+          kof[u] = k;
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
             a[u][v] *= rp;
@@ -478,6 +396,8 @@ __device__ inline void gj_inverse_reg(const float* X, int ldx, float* Xi, int ld
         }
     }
     __syncthreads();
+    const int kn = k + 1;
+    float* coln = s.gcol + 64 * (b ^ 1);
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int i = w + 16 * u;
@@ -486,6 +406,7 @@ __device__ inline void gj_inverse_reg(const float* X, int ldx, float* Xi, int ld
 #pragma unroll
         for (int v = 0; v < 4; ++v) a[u][v] = fmaf(f, prow[l + 32 * v], a[u][v]);
       }
+      if (l == (kn & 31) && kn < r) coln[i] = (kn >> 5) ? a[u][1] : a[u][0];
     }
   }
   __syncthreads();
@@ -493,7 +414,7 @@ __device__ inline void gj_inverse_reg(const float* X, int ldx, float* Xi, int ld
   for (int u = 0; u < 4; ++u) {
     const int i = w + 16 * u;
     if (i < r) {
-      const int kk = kof[i];
+      const int kk = kof[u];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const int j = l + 32 * v;

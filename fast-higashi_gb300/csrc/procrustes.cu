@@ -143,8 +143,7 @@ __global__ void __launch_bounds__(kProcThreads, 2) procrustes_qr_kernel(ProcArgs
     __syncthreads();
   }
   // ---- QR, polar factor of R, sum(S)
-  if (n <= 192) householder_qr_blocked(R0, n, r, ldt, R1, s);
-  else householder_qr(R0, n, r, ldt, s);
+  householder_qr(R0, n, r, ldt, s);
   float* X = R1;
   for (int p = ty; p < r; p += nw)
     for (int q = tx; q < r; q += 32) X[p * ldt + q] = q >= p ? R0[p * ldt + q] : 0.f;

@@ -77,19 +77,23 @@ __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
+// Rounds a pair to bf16 (one packed conversion) and returns the residuals' pair too.
+__device__ __forceinline__ void split2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  const float ra = a - __uint_as_float(hi << 16), rb = b - __uint_as_float(hi & 0xffff0000u);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(ra, rb);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
 // Splits 8 values into bf16 hi and lo and stores both 16-byte chunks.
 __device__ __forceinline__ void store_split8(uint8_t* hi, uint8_t* lo, uint32_t off,
                                              const float* v) {
-  __nv_bfloat16 h[8], l[8];
+  uint32_t h[4], l[4];
 #pragma unroll
-  for (int e = 0; e < 8; ++e) {
-    h[e] = __float2bfloat16_rn(v[e]);
-    l[e] = __float2bfloat16_rn(v[e] - __bfloat162float(h[e]));
-  }
-  *reinterpret_cast<uint4*>(hi + off) =
-      make_uint4(pack2(h[0], h[1]), pack2(h[2], h[3]), pack2(h[4], h[5]), pack2(h[6], h[7]));
-  *reinterpret_cast<uint4*>(lo + off) =
-      make_uint4(pack2(l[0], l[1]), pack2(l[2], l[3]), pack2(l[4], l[5]), pack2(l[6], l[7]));
+  for (int e = 0; e < 4; ++e) split2(v[2 * e], v[2 * e + 1], h[e], l[e]);
+  *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+  *reinterpret_cast<uint4*>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
 __device__ __forceinline__ float ld_split(const uint8_t* hi, const uint8_t* lo, uint32_t off) {
@@ -98,7 +102,7 @@ __device__ __forceinline__ float ld_split(const uint8_t* hi, const uint8_t* lo, 
 }
 
 __host__ __device__ inline size_t rt_smem_bytes(int npad_max) {
-  return (size_t)npad_max / 64 * 16384 * 2 + 65536 + 4 * 128 * sizeof(float) + 64 * sizeof(double) +
+  return (size_t)npad_max / 64 * 16384 * 2 + 65536 + 7 * 128 * sizeof(float) + 64 * sizeof(double) +
          64 + 1024;
 }
 
@@ -114,7 +118,8 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
   uint8_t* Plo = Phi + 32768;
   float* cs1p = reinterpret_cast<float*>(Plo + 32768);  // [2][128] partial column sums of S1
   float* cs2p = cs1p + 256;                              // [2][128] partial row sums of S2
-  double* dred = reinterpret_cast<double*>(cs2p + 256);  // [64]
+  float* fac = cs2p + 256;                               // [3][128] per-column P factors
+  double* dred = reinterpret_cast<double*>(fac + 384);   // [64]
   uint64_t* mbar = reinterpret_cast<uint64_t*>(dred + 64);
   uint32_t* misc = reinterpret_cast<uint32_t*>(mbar + 1);  // [0] TMEM base
   const uint32_t sZhi = base, sZlo = base + zbytes, sPhi = base + 2 * zbytes,
@@ -262,6 +267,17 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
       cs2p[h * 128 + p] = s;
     }
     __syncthreads();
+    // per column q: f1 = 0.75 / (c1 + eps), f2 = 0.25 / (c2 + eps), fl = 1 / (colsum(L) + eps)
+    if (tid < 128) {
+      const int q = tid;
+      const float c1 = cs1p[q] + cs1p[128 + q];
+      const float c2 = cs2p[q] + cs2p[128 + q];
+      const float f1 = 0.75f / (c1 + kRtEps), f2 = 0.25f / (c2 + kRtEps);
+      fac[q] = f1;
+      fac[128 + q] = f2;
+      fac[256 + q] = (c1 == 0.f && c2 == 0.f) ? -1.f : 1.f / (fmaf(c1, f1, c2 * f2) + kRtEps);
+    }
+    __syncthreads();
     for (int q0 = 64 * h; q0 < 64 * h + 64; q0 += 16) {
       float d[16], unused[16], pv[16];
       tmem_ld16x2(tD + q0, tD + q0, d, unused);
@@ -270,16 +286,13 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
         const int q = q0 + e;
         float v = 0.f;
         if (p < b && q < b) {
-          const float c1 = cs1p[q] + cs1p[128 + q];
-          const float c2 = cs2p[q] + cs2p[128 + q];
-          if (c1 == 0.f && c2 == 0.f) {
-            v = (p == q) ? 1.f / (1.f + kRtEps) : 0.f;
+          const float fl = fac[256 + q];
+          if (fl < 0.f) {
+            v = (p == q) ? 1.f / (1.f + kRtEps) : 0.f;   // zero column: unit diagonal
           } else {
             const float s2 = (p == q) ? 0.f : d[e];
             const float a1 = ld_split(Zhi, Zlo, sw_off(p, s0 + q));
-            const float l = (a1 / (c1 + kRtEps)) * 0.75f + (s2 / (c2 + kRtEps)) * 0.25f;
-            const float csl = (c1 / (c1 + kRtEps)) * 0.75f + (c2 / (c2 + kRtEps)) * 0.25f;
-            v = l / (csl + kRtEps);
+            v = fmaf(a1, fac[q], s2 * fac[128 + q]) * fl;
           }
         }
         pv[e] = v;
@@ -294,9 +307,10 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     uint8_t* stage = Zhi;                    // free once the last MMA has completed
     const int64_t g0 = (int64_t)c * a.cell_stride + T.xoff;
     const int mis = (int)(g0 & 7);           // staging shares the global 16-byte phase
-    double ss = 0.0;
+    float ss = 0.f;
     const bool two = a.plane_stride > 0;
     const int64_t tot = (int64_t)b * n;
+    const int64_t lo_base = (tot + 15) & ~(int64_t)7;   // lo plane staging, 16-byte aligned
     auto emit = [&](int j0, const float (&z)[16]) {
       if (p >= b) return;
 #pragma unroll
@@ -309,10 +323,10 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
           reinterpret_cast<__nv_bfloat16*>(stage)[k] = hv;
           if (two) {
             const __nv_bfloat16 lv = __float2bfloat16_rn(z[e] - sv);
-            reinterpret_cast<__nv_bfloat16*>(stage)[tot + 8 + k] = lv;
+            reinterpret_cast<__nv_bfloat16*>(stage)[lo_base + k] = lv;
             sv += __bfloat162float(lv);
           }
-          ss += (double)sv * sv;
+          ss = fmaf(sv, sv, ss);
         }
       }
     };
@@ -362,15 +376,23 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     }
     // ---- 7. staging -> X16 (contiguous b x n run of the cell's row), squared norm
     {
-      const __nv_bfloat16* st = reinterpret_cast<const __nv_bfloat16*>(stage);
-      __nv_bfloat16* o = a.out16 + g0;
-      for (int64_t k = tid; k < tot; k += kRtThreads) o[k] = st[k + mis];
-      if (two) {
-        __nv_bfloat16* o2 = o + a.plane_stride;
-        for (int64_t k = tid; k < tot; k += kRtThreads) o2[k] = st[tot + 8 + k + mis];
+      // the staging holds element k at index k + mis, and X16's planes start 16-byte aligned
+      // with every plane a multiple of 8 elements long, so element k and its staging copy
+      // share the 16-byte phase: the middle of the run moves as 16-byte vectors
+      for (int pl = 0; pl < (two ? 2 : 1); ++pl) {
+        const __nv_bfloat16* st = reinterpret_cast<const __nv_bfloat16*>(stage) + pl * lo_base;
+        __nv_bfloat16* o = a.out16 + g0 + pl * a.plane_stride;
+        const int64_t head = (8 - mis) & 7;                  // elements before the first vector
+        const int64_t nvec = tot > head ? (tot - head) >> 3 : 0;
+        const int64_t tail0 = head + (nvec << 3);
+        for (int64_t k = tid; k < head && k < tot; k += kRtThreads) o[k] = st[k + mis];
+        const uint4* sv = reinterpret_cast<const uint4*>(st + head + mis);
+        uint4* ov = reinterpret_cast<uint4*>(o + head);
+        for (int64_t k = tid; k < nvec; k += kRtThreads) ov[k] = sv[k];
+        for (int64_t k = tail0 + tid; k < tot; k += kRtThreads) o[k] = st[k + mis];
       }
-      ss = block_sum<double>(ss, dred);
-      if (tid == 0 && a.sumsq) a.sumsq[(int64_t)t * a.n_cells + c] = ss;
+      const double sst = block_sum<double>((double)ss, dred);
+      if (tid == 0 && a.sumsq) a.sumsq[(int64_t)t * a.n_cells + c] = sst;
       __syncthreads();
     }
   }

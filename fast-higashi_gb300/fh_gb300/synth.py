@@ -123,9 +123,56 @@ def _band_rowmajor(nbin, band):
     return rows[ok], cols[ok]
 
 
-def generate(w: Workload, seed: int = 0, cell_chunk: int = 4096):
-    """Returns (list of (indices int32[3,nnz], values float32[nnz], shape), meta dict)."""
-    rng = np.random.default_rng(seed)
+def _chromosome(w, nbin, rng, totals, alpha, types, genome, cell_chunk):
+    """COO (indices, values, shape) of one chromosome for every cell."""
+    C = w.n_cells
+    s = _compartments(rng, w.n_types, nbin)
+    ui, ud = _upper_band(nbin, w.band)
+    P_up = len(ui)
+    w_sym = np.where(ud > 0, 2.0, 1.0)
+    rows, cols = _band_rowmajor(nbin, w.band)
+    # index of each both-triangle band position in the upper-band enumeration
+    doff = np.concatenate([[0], np.cumsum([nbin - d for d in range(min(w.band, nbin - 1) + 1)])])
+    up_idx = doff[np.abs(cols - rows)] + np.minimum(rows, cols)
+    counts = np.empty((C, P_up), dtype=np.uint16)
+    logd = np.log(ud + 1.0)
+    for c0 in range(0, C, cell_chunk):
+        c1 = min(C, c0 + cell_chunk)
+        lam = np.exp(-alpha[c0:c1, None] * logd[None, :])
+        if w.n_types > 0:
+            st = s[types[c0:c1]]                      # (chunk, nbin)
+            lam *= np.exp(w.gamma * st[:, ui] * st[:, ui + ud])
+        lam *= (totals[c0:c1, None] * nbin / genome) / lam.sum(1, keepdims=True)
+        counts[c0:c1] = np.minimum(rng.poisson(lam), 65535).astype(np.uint16)
+    cell_sum = counts.astype(np.float64) @ w_sym                 # both triangles
+    scale = nbin / (cell_sum + 1e-15)
+    band_counts = counts[:, up_idx].T                            # (P_band, C), rows sorted
+    del counts
+    p, cell = np.nonzero(band_counts)
+    cnt = band_counts[p, cell].astype(np.float32)
+    del band_counts
+    vals = np.log1p(cnt * scale[cell].astype(np.float32)).astype(np.float32)
+    if vals.size:
+        m, sd = np.mean(vals), np.std(vals)
+        vals = np.clip(vals, None, m + 15 * sd).astype(np.float32)
+    idx = np.empty((3, p.size), dtype=np.int32)
+    idx[0] = rows[p]
+    idx[1] = cols[p]
+    idx[2] = cell
+    return idx, vals, (nbin, nbin, C)
+
+
+def generate(w: Workload, seed: int = 0, cell_chunk: int = 2048, threads: int = 0):
+    """Returns (list of (indices int32[3,nnz], values float32[nnz], shape), meta dict).
+
+    The per-cell quantities come from one generator, each chromosome from its own child of
+    the seed, so chromosomes are generated in parallel threads (NumPy's samplers release the
+    GIL) with a result that does not depend on the thread count."""
+    import concurrent.futures as cf
+    import os
+    ss = np.random.SeedSequence(seed)
+    cell_ss, *chrom_ss = ss.spawn(1 + len(w.chrom_bins))
+    rng = np.random.default_rng(cell_ss)
     C = w.n_cells
     totals = np.exp(rng.normal(math.log(w.median_total), w.sigma, C))
     if w.ultra_sparse_frac > 0:
@@ -138,40 +185,11 @@ def generate(w: Workload, seed: int = 0, cell_chunk: int = 4096):
         alpha = np.full(C, float(w.alpha))
     types = rng.integers(0, max(w.n_types, 1), C)
     genome = float(sum(w.chrom_bins))
-    out = []
-    for nbin in w.chrom_bins:
-        s = _compartments(rng, w.n_types, nbin)
-        ui, ud = _upper_band(nbin, w.band)
-        P_up = len(ui)
-        w_sym = np.where(ud > 0, 2.0, 1.0)
-        rows, cols = _band_rowmajor(nbin, w.band)
-        # index of each both-triangle band position in the upper-band enumeration
-        doff = np.concatenate([[0], np.cumsum([nbin - d for d in range(min(w.band, nbin - 1) + 1)])])
-        up_idx = doff[np.abs(cols - rows)] + np.minimum(rows, cols)
-        counts = np.empty((C, P_up), dtype=np.uint16)
-        logd = np.log(ud + 1.0)
-        for c0 in range(0, C, cell_chunk):
-            c1 = min(C, c0 + cell_chunk)
-            lam = np.exp(-alpha[c0:c1, None] * logd[None, :])
-            if w.n_types > 0:
-                st = s[types[c0:c1]]                      # (chunk, nbin)
-                lam *= np.exp(w.gamma * st[:, ui] * st[:, ui + ud])
-            lam *= (totals[c0:c1, None] * nbin / genome) / lam.sum(1, keepdims=True)
-            counts[c0:c1] = np.minimum(rng.poisson(lam), 65535).astype(np.uint16)
-        cell_sum = counts.astype(np.float64) @ w_sym                 # both triangles
-        scale = nbin / (cell_sum + 1e-15)
-        band_counts = counts[:, up_idx].T                            # (P_band, C), rows sorted
-        p, cell = np.nonzero(band_counts)
-        cnt = band_counts[p, cell].astype(np.float32)
-        vals = np.log1p(cnt * scale[cell].astype(np.float32)).astype(np.float32)
-        if vals.size:
-            m, sd = np.mean(vals), np.std(vals)
-            vals = np.clip(vals, None, m + 15 * sd).astype(np.float32)
-        idx = np.empty((3, p.size), dtype=np.int32)
-        idx[0] = rows[p]
-        idx[1] = cols[p]
-        idx[2] = cell
-        out.append((idx, vals, (nbin, nbin, C)))
+    n_thr = threads or min(len(w.chrom_bins), os.cpu_count() or 1)
+    jobs = [(nbin, np.random.default_rng(cs)) for nbin, cs in zip(w.chrom_bins, chrom_ss)]
+    with cf.ThreadPoolExecutor(max_workers=n_thr) as ex:
+        out = list(ex.map(lambda j: _chromosome(w, j[0], j[1], totals, alpha, types, genome,
+                                                cell_chunk), jobs))
     meta = dict(totals=totals, alpha=alpha, types=types)
     return out, meta
 
