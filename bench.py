@@ -1,13 +1,17 @@
 #!/usr/bin/env python
 """Benchmark of the Fast-Higashi fit hot path on one GB300: cells/s for RWR + 30 ALS iterations.
 
-A step is one fit of the workload: the contact build, the partial RWR of every tile and 30
-iterations of the PARAFAC2-like ALS (per-bin polar, SVD_term, meta polar, projections,
-CP-ALS), from a fixed initial state (init_params runs once, untimed, as the metric states).
+A step is one fit of the workload (default c3: 10,000 cells, 22 autosomes at 500 kb, R=64,
+band 30): the contact build, the partial RWR of every tile and 30 iterations of the
+PARAFAC2-like ALS (per-bin polar, SVD_term, meta polar, projections, CP-ALS), from a fixed
+initial state (init_params runs once, untimed, as the metric states).
 
-  value  device-timed (CUDA events), contacts already resident in HBM as the COO
-  e2e    the public API (Fast_Higashi_core.fit on host Sparse data) with the COO H2D and the
-         embedding / loss D2H inside the timed region
+  value       the tensor-core form (precision="bf16x2": tcgen05 RWR and X passes, X as two
+              bf16 planes), device-timed with CUDA events, contacts resident in HBM
+  plain_fp32  the plain fp32 drop-in on the same GPU and state, timed the same way, with
+              the speed-up of the headline form over it
+  e2e         the public API (Fast_Higashi_core.fit on host Sparse data) with the COO H2D and
+              the embedding / loss D2H inside the timed region
   --impl reference   the CPU restatement of the reference (the oracle, fp32, all host threads)
                      on a bounded cell sample, extrapolated to cells/s
 
@@ -38,7 +42,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c2", help="workload: c1..c5 (default c2, 2,000 cells at 1 Mb)")
+    ap.add_argument("--config", default="c3",
+                    help="workload: c1..c5 (default c3, 10,000 cells at 500 kb, the one the "
+                         "BF16-batched vs plain FP32 target is set on)")
     ap.add_argument("--iters", type=int, default=None, help="ALS iterations (default: the workload's 30)")
     ap.add_argument("--sample-cells", type=int, default=96,
                     help="cells of the CPU-baseline sample (at least the rank R)")

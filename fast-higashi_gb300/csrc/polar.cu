@@ -14,7 +14,7 @@
 
 namespace fh {
 
-constexpr int kPolThreads = 256;
+constexpr int kPolThreads = 512;
 
 // =========================================================================================
 // Meta polar: E = polar(S), S = SVD_term^T (cells x R, stride RP).
@@ -101,7 +101,8 @@ __global__ void __launch_bounds__(kPolThreads) meta_small_kernel(const double* _
     X[p * ldt + q] = q >= p ? (float)G[p * R + q] : 0.f;
   }
   __syncthreads();
-  newton_polar(X, ldt, Aug, R, true, s);
+  if (R <= 64) newton_polar_r64(X, ldt, Aug, R, true, s);
+  else newton_polar(X, ldt, Aug, R, true, s);
   double acc = 0.0;
   for (int idx = tid; idx < R * R; idx += kPolThreads) {
     const int p = idx / R, q = idx % R;
