@@ -186,6 +186,28 @@ def chrom_datas(coo, names, bs_bins, bs_cells, flank):
     return out
 
 
+def cell_embedding(E, D_list):
+    """The user-facing cell embedding before its final TruncatedSVD (FastHigashi_Wrapper.py:
+    750-761): E times each chromosome's D with unit columns, concatenated (cells x sum r)."""
+    E = np.asarray(E, dtype=np.float64)
+    parts = []
+    for D in D_list:
+        D = np.asarray(D, dtype=np.float64)
+        parts.append(E @ (D / np.linalg.norm(D, axis=0, keepdims=True)))
+    return np.concatenate(parts, axis=1)
+
+
+def gram_error(F, F_ref):
+    """||F F^T - G G^T||_F / ||G G^T||_F (cell-cell similarities; invariant to any rotation
+    of the embedding's columns), from the small Gram products only."""
+    F = np.asarray(F, dtype=np.float64)
+    G = np.asarray(F_ref, dtype=np.float64)
+    a = np.linalg.norm(F.T @ F) ** 2
+    b = np.linalg.norm(G.T @ G) ** 2
+    c = np.linalg.norm(F.T @ G) ** 2
+    return float(math.sqrt(max(a + b - 2 * c, 0.0)) / math.sqrt(b))
+
+
 def aligned_error(E, E_ref):
     """Relative Frobenius error of E after the orthogonal Procrustes rotation onto E_ref."""
     E = np.asarray(E, dtype=np.float64)

@@ -3,9 +3,12 @@
 The yardstick is tests/fp64_reference.py (the oracle's algorithm in torch float64, so it can
 run full-size fits on the GPU); the CPU test below pins it to the numpy oracle first.
 
-Error measure: relative Frobenius error of the final meta embedding E (cells x R) after the
-orthogonal Procrustes rotation onto the FP64 one (embeddings are defined up to a rotation),
-from the same initial state, and the largest relative difference of the loss trajectory.
+Error measures, from the same initial state: the relative Frobenius error of the final meta
+embedding E (cells x R) after the orthogonal Procrustes rotation onto the FP64 one (embeddings
+are defined up to a rotation); the relative error of the cell-cell similarities of the
+user-facing cell embedding (E times each chromosome's unit-column D, concatenated, as
+FastHigashi_Wrapper.py:750-761 builds it before its final SVD), which weights E's directions as
+the user sees them; and the largest relative difference of the loss trajectory.
 Bounds at 200 cells (c1): fp32 form 5e-4, bf16x2 form (X as two bf16 planes) 1e-3 (the target),
 bf16 form (one plane) 1e-2, losses 1e-3.
 
@@ -81,9 +84,10 @@ def _ours(w, ds, precision, state, n_i, iters, dev):
     torch.cuda.synchronize()
     E = m.meta_embedding.detach().cpu().numpy()
     losses = np.asarray(m.rec_errors_total)
+    D = [m.D_dict[d.chrom].detach().cpu().numpy() for d in ds]
     del m
     torch.cuda.empty_cache()
-    return E, losses
+    return E, losses, D
 
 
 def precision_report(name, iters=None, seed=0):
@@ -113,10 +117,12 @@ def precision_report(name, iters=None, seed=0):
     out["fp64_seconds"] = time.time() - t0
     E64 = ref.E.cpu().numpy()
     L64 = np.asarray(ref.rec_errors_total)
+    C64 = F.cell_embedding(E64, [ref.D[d.name].cpu().numpy() for d in datas])
     del ref
     torch.cuda.empty_cache()
-    for prec, (E, L) in got.items():
+    for prec, (E, L, D) in got.items():
         out["%s_aligned_embedding_error" % prec] = F.aligned_error(E, E64)
+        out["%s_cell_embedding_gram_error" % prec] = F.gram_error(F.cell_embedding(E, D), C64)
         out["%s_loss_max_rel_diff" % prec] = float(np.max(np.abs(L - L64) / np.abs(L64)))
     out["fp64_loss_final"] = float(L64[-1])
     return out
