@@ -539,16 +539,18 @@ extern "C" int fh_cp_als(int32_t nchrom, int32_t nchunks, const int32_t* meta, f
     FH_CHECK_LAUNCH();
     return FH_OK;
   }
+  // Each sweep recomputes every A row from Y, B and D, so the A scaling of a balance only
+  // matters after the last sweep: the initial balance and the intermediate ones rescale B
+  // and D (in place) and leave A to the next sweep.
   cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsNorm);
   cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, kSmallInit);
-  cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsScale);
   for (int it = 0; it < n_iter; ++it) {
     cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsAB);
     cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, kSmallB);
     cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsD);
     cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, kSmallD);
-    cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsScale);
   }
+  cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsScale);
   FH_CHECK_LAUNCH();
   return FH_OK;
 }

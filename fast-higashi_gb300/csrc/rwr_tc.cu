@@ -17,12 +17,11 @@
 //          in closed form (the reference sums L's columns numerically; they agree to
 //          rounding).  With the 1e-8 floor every column sum is positive, so the reference's
 //          zero-column rule (partial_rwr.py:96-97) never applies; it is kept for c1 = c2 = 0.
-//   epoch  D = P_hi Z_hi + P_hi Z_lo + P_lo Z_hi  (K = 128) per 64-column block, then each
-//          thread turns its row of D and A into Z_{t+1} = 0.5 D + 0.5 A and writes the hi/lo
-//          planes back in place (the MMA that read them has completed); the MMAs of the next
-//          block overlap that epilogue
-//   out    the final hi/lo planes are the output planes (one: hi = bf16(Z); two: hi and the
-//          residual lo), copied to the cell's contiguous run of X16.
+//   epoch  D = P_hi Z_hi + P_hi Z_lo + P_lo Z_hi  (K = 128, N = npad), then each thread
+//          turns its row of D and A into Z_{t+1} = 0.5 D + 0.5 A and writes the hi/lo planes
+//          back in place (the MMA that read them has completed)
+//   out    the last epoch's fp32 Z is rounded to the output planes (one: bf16(Z); two: hi and
+//          the residual lo) through a staging copy in smem, then stored contiguously.
 // The split products carry every operand to 16 significant bits, so the result is fp32-class.
 // Thread (warp w, lane l) serves row p = 32 (w % 4) + l (the TMEM lane quarter its warp may
 // read) and the column half w / 4.  Tiles wider than 256 columns use rwr_f32.cu.
@@ -104,7 +103,7 @@ __device__ __forceinline__ float ld_split(const uint8_t* hi, const uint8_t* lo, 
 
 __host__ __device__ inline size_t rt_smem_bytes(int npad_max) {
   return (size_t)npad_max / 64 * 16384 * 2 + 65536 + 7 * 128 * sizeof(float) + 64 * sizeof(double) +
-         128 + 1024;
+         64 + 1024;
 }
 
 __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
@@ -121,8 +120,8 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
   float* cs2p = cs1p + 256;                              // [2][128] partial row sums of S2
   float* fac = cs2p + 256;                               // [3][128] per-column P factors
   double* dred = reinterpret_cast<double*>(fac + 384);   // [64]
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(dred + 64);  // [0] S2, [1..4] column blocks
-  uint32_t* misc = reinterpret_cast<uint32_t*>(mbar + 5);  // [0] TMEM base
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(dred + 64);
+  uint32_t* misc = reinterpret_cast<uint32_t*>(mbar + 1);  // [0] TMEM base
   const uint32_t sZhi = base, sZlo = base + zbytes, sPhi = base + 2 * zbytes,
                  sPlo = sPhi + 32768;
 
@@ -131,7 +130,7 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
   const int p = 32 * q4 + lane;
   const uint32_t bar = smem_u32(mbar);
   if (tid == 0) {
-    for (int i = 0; i < 5; ++i) mbar_init(bar + 8u * i, 1);
+    mbar_init(bar, 1);
     mbar_fence_init();
   }
   if (w == 0) {
@@ -146,8 +145,7 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
   const uint32_t tD = tmem + lane_off, tA = tmem + 256 + lane_off;
   const __nv_bfloat16 fl_hi = __float2bfloat16_rn(kRtFloor);
   const __nv_bfloat16 fl_lo = __float2bfloat16_rn(kRtFloor - __bfloat162float(fl_hi));
-  uint32_t phase = 0;     // parity of the S2 barrier
-  uint32_t bphase = 0;    // parity of each column block's barrier (bit per block)
+  uint32_t phase = 0;
   bool ok = true;
 
   // Issues the MMAs of one product group (thread 0) and waits for them (all threads).
@@ -305,76 +303,93 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     fence_proxy_async();
     tc_fence_before();
     __syncthreads();
-    // ---- 6. Z_{t+1} = 0.5 P Z_t + 0.5 A, pipelined over 64-column blocks: the columns of Z
-    // evolve independently (P acts on the rows), so the MMAs of block k + 1 run on the tensor
-    // core while the threads turn block k's accumulator into its next hi/lo planes.  Each
-    // block has its own accumulator columns and mbarrier.
-    {
-      const int nblk = npad / 64;
-      const int total = epochs * nblk;
-      auto issue = [&](int st) {
-        const int blk = st % nblk;
+    // ---- 6. Z_{t+1} = 0.5 P Z_t + 0.5 A; the last epoch writes the output staging
+    uint8_t* stage = Zhi;                    // free once the last MMA has completed
+    const int64_t g0 = (int64_t)c * a.cell_stride + T.xoff;
+    const int mis = (int)(g0 & 7);           // staging shares the global 16-byte phase
+    float ss = 0.f;
+    const bool two = a.plane_stride > 0;
+    const int64_t tot = (int64_t)b * n;
+    const int64_t lo_base = (tot + 15) & ~(int64_t)7;   // lo plane staging, 16-byte aligned
+    auto emit = [&](int j0, const float (&z)[16]) {
+      if (p >= b) return;
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const int j = j0 + e;
+        if (j < n) {
+          const int64_t k = (int64_t)p * n + j + mis;
+          const __nv_bfloat16 hv = __float2bfloat16_rn(z[e]);
+          float sv = __bfloat162float(hv);
+          reinterpret_cast<__nv_bfloat16*>(stage)[k] = hv;
+          if (two) {
+            const __nv_bfloat16 lv = __float2bfloat16_rn(z[e] - sv);
+            reinterpret_cast<__nv_bfloat16*>(stage)[lo_base + k] = lv;
+            sv += __bfloat162float(lv);
+          }
+          ss = fmaf(sv, sv, ss);
+        }
+      }
+    };
+    for (int ep = 0; ep < epochs; ++ep) {
+      if (tid == 0) {
         tc_fence_after();
-        const uint32_t idesc = idesc_bf16(128, 64, false, true);
-        const uint32_t dcol = tmem + 64u * (uint32_t)blk;
+        const uint32_t idesc = idesc_bf16(128, npad, false, true);
         for (int ks = 0; ks < 8; ++ks) {
           const uint32_t pk = (uint32_t)(ks >> 2) * 16384u + (uint32_t)(ks & 3) * 32u;
-          const uint32_t zk = 16384u * (uint32_t)blk + (uint32_t)ks * 2048u;
+          const uint32_t zk = (uint32_t)ks * 2048u;
           const uint64_t ph = sdesc_sw128(sPhi + pk, 16, 1024), pl = sdesc_sw128(sPlo + pk, 16, 1024);
           const uint64_t zh = sdesc_sw128(sZhi + zk, 16384, 1024),
                          zl = sdesc_sw128(sZlo + zk, 16384, 1024);
-          mma_bf16(dcol, ph, zh, idesc, ks > 0 ? 1u : 0u);
-          mma_bf16(dcol, ph, zl, idesc, 1u);
-          mma_bf16(dcol, pl, zh, idesc, 1u);
+          mma_bf16(tmem, ph, zh, idesc, ks > 0 ? 1u : 0u);
+          mma_bf16(tmem, ph, zl, idesc, 1u);
+          mma_bf16(tmem, pl, zh, idesc, 1u);
         }
-        mma_commit(bar + 8u * (1u + (uint32_t)blk));
-      };
-      if (total > 0 && tid == 0) issue(0);
-      for (int st = 0; st < total; ++st) {
-        const int blk = st % nblk;
-        // the next block's inputs were written (and its accumulator read) nblk - 1 steps ago
-        if (nblk > 1 && st + 1 < total && tid == 0) issue(st + 1);
-        const bool got = mbar_wait(bar + 8u * (1u + (uint32_t)blk), (bphase >> blk) & 1u, nullptr);
-        bphase ^= 1u << blk;
-        if (__syncthreads_or(!got)) { ok = false; break; }
-        tc_fence_after();
-        for (int j0 = 64 * blk + 32 * h; j0 < 64 * blk + 32 * h + 32; j0 += 16) {
-          float d[16], av[16], z[16];
-          tmem_ld16x2(tD + j0, tA + j0, d, av);
+      }
+      if (!mma_wait()) { ok = false; break; }
+      const bool last = ep == epochs - 1;
+      if (last) __syncthreads();   // nobody reads Z any more: the staging may overwrite it
+      for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
+        float d[16], av[16], z[16];
+        tmem_ld16x2(tD + j0, tA + j0, d, av);
 #pragma unroll
-          for (int e = 0; e < 16; ++e) z[e] = fmaf(0.5f, d[e], 0.5f * av[e]);
+        for (int e = 0; e < 16; ++e) z[e] = fmaf(0.5f, d[e], 0.5f * av[e]);
+        if (last) {
+          emit(j0, z);
+        } else {
           store_split8(Zhi, Zlo, sw_off(p, j0), z);
           store_split8(Zhi, Zlo, sw_off(p, j0 + 8), z + 8);
         }
-        fence_proxy_async();
-        tc_fence_before();
-        __syncthreads();
-        if (nblk == 1 && st + 1 < total && tid == 0) issue(st + 1);
       }
+      if (!last) fence_proxy_async();
+      tc_fence_before();
+      __syncthreads();
     }
     if (!ok) break;
-    // ---- 7. the Z planes (hi, lo: X to 16 significant bits) -> X16 (the cell's contiguous
-    // b x n run), and the squared norm of what is stored
+    if (epochs == 0) {
+      for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
+        float av[16], unused[16];
+        tmem_ld16x2(tA + j0, tA + j0, av, unused);
+        emit(j0, av);
+      }
+      tc_fence_before();
+      __syncthreads();
+    }
+    // ---- 7. staging -> X16 (contiguous b x n run of the cell's row), squared norm
     {
-      const bool two = a.plane_stride > 0;
-      const int64_t g0 = (int64_t)c * a.cell_stride + T.xoff;
-      const int64_t tot = (int64_t)b * n;
-      __nv_bfloat16* o = a.out16 + g0;
-      float ss = 0.f;
-      int pr = tid / n, jr = tid - pr * n;     // (row, column) of element k = tid
-      for (int64_t k = tid; k < tot; k += kRtThreads) {
-        const uint32_t off = sw_off(pr, jr);
-        const __nv_bfloat16 hv = *reinterpret_cast<const __nv_bfloat16*>(Zhi + off);
-        float sv = __bfloat162float(hv);
-        o[k] = hv;
-        if (two) {
-          const __nv_bfloat16 lv = *reinterpret_cast<const __nv_bfloat16*>(Zlo + off);
-          o[a.plane_stride + k] = lv;
-          sv += __bfloat162float(lv);
-        }
-        ss = fmaf(sv, sv, ss);
-        jr += kRtThreads;
-        while (jr >= n) { jr -= n; ++pr; }
+      // the staging holds element k at index k + mis, and X16's planes start 16-byte aligned
+      // with every plane a multiple of 8 elements long, so element k and its staging copy
+      // share the 16-byte phase: the middle of the run moves as 16-byte vectors
+      for (int pl = 0; pl < (two ? 2 : 1); ++pl) {
+        const __nv_bfloat16* st = reinterpret_cast<const __nv_bfloat16*>(stage) + pl * lo_base;
+        __nv_bfloat16* o = a.out16 + g0 + pl * a.plane_stride;
+        const int64_t head = (8 - mis) & 7;                  // elements before the first vector
+        const int64_t nvec = tot > head ? (tot - head) >> 3 : 0;
+        const int64_t tail0 = head + (nvec << 3);
+        for (int64_t k = tid; k < head && k < tot; k += kRtThreads) o[k] = st[k + mis];
+        const uint4* sv = reinterpret_cast<const uint4*>(st + head + mis);
+        uint4* ov = reinterpret_cast<uint4*>(o + head);
+        for (int64_t k = tid; k < nvec; k += kRtThreads) ov[k] = sv[k];
+        for (int64_t k = tail0 + tid; k < tot; k += kRtThreads) o[k] = st[k + mis];
       }
       const double sst = block_sum<double>((double)ss, dred);
       if (tid == 0 && a.sumsq) a.sumsq[(int64_t)t * a.n_cells + c] = sst;

@@ -92,7 +92,7 @@ launches = 0
 def _kernel_count(name, args):
     if name == "fh_cp_als":
         n_iter = args[11]
-        return 2 if n_iter == 0 else 3 + 5 * n_iter
+        return 2 if n_iter == 0 else 3 + 4 * n_iter
     return _KERNELS.get(name, 0)
 
 
