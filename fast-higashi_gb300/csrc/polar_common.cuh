@@ -22,8 +22,9 @@ struct PolarScratch {
   float* grow;   // [2][128] scaled pivot row
   float* grp;    // [2]      1 / pivot
   int* gi;       // [0, 64) row used as a pivot, [64, 128) step that pivoted the row, [128, 130) pivot
+  float* tri;    // [3][16][16] off-diagonal block products of the blocked triangular inverse
 };
-constexpr int kPolarMiscFloats = 5 * kMaxRank + 64 + 128 + 256 + 4 + 132;
+constexpr int kPolarMiscFloats = 5 * kMaxRank + 64 + 128 + 256 + 4 + 132 + 768;
 
 // Carves the scratch out of kPolarMiscFloats floats of shared memory.
 __device__ inline PolarScratch polar_scratch(float* misc, float* red, double* dred, int* ival) {
@@ -40,6 +41,7 @@ __device__ inline PolarScratch polar_scratch(float* misc, float* red, double* dr
   s.grow = g + 128;
   s.grp = g + 384;
   s.gi = reinterpret_cast<int*>(g + 388);
+  s.tri = g + 388 + 132;
   return s;
 }
 
@@ -176,6 +178,73 @@ __device__ inline void tri_inverse(const float* R, int ldr, float* Xi, int ldo, 
   __syncthreads();
 }
 
+// ---- inverse of an upper-triangular R (r <= 64, stride ldr) into Xi (stride ldo), 512 threads
+// Blocked: the 16 x 16 diagonal blocks are inverted by one warp each (a lane per column, the
+// column in registers, no synchronisation), then the off-diagonal blocks by block diagonals,
+// X_ij = -X_ii sum_{k=i+1..j} R_ik X_kj, as small products over all threads: six barriers in
+// all instead of a serial chain of r dependent steps.  Writes the upper triangle of Xi (and
+// zeroes the strictly lower part when zero_lower is set).
+__device__ inline void tri_inverse_blocked(const float* R, int ldr, float* Xi, int ldo, int r,
+                                           bool zero_lower, PolarScratch& s) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int nb = (r + 15) >> 4;
+  if (w < nb && l < 16) {
+    const int b0 = 16 * w;
+    const int c = b0 + l;              // this lane's column
+    float x[16];
+#pragma unroll
+    for (int ii = 15; ii >= 0; --ii) {
+      const int i = b0 + ii;
+      float v = 0.f;
+      if (ii <= l && c < r) {
+        float d = (ii == l) ? 1.f : 0.f;
+#pragma unroll
+        for (int ll = ii + 1; ll < 16; ++ll)
+          if (ll <= l) d = fmaf(-R[i * ldr + b0 + ll], x[ll], d);
+        float rii = R[i * ldr + i];
+        if (rii == 0.f) { rii = 1e-30f; s.ival[0] = 1; }
+        v = d / rii;
+      }
+      x[ii] = v;
+    }
+    if (c < r) {
+#pragma unroll
+      for (int ii = 0; ii < 16; ++ii)
+        if (b0 + ii < r && ii <= l) Xi[(b0 + ii) * ldo + c] = x[ii];
+    }
+  }
+  if (zero_lower)
+    for (int idx = threadIdx.x; idx < r * r; idx += blockDim.x) {
+      const int i = idx / r, j = idx - i * r;
+      if (i > j) Xi[i * ldo + j] = 0.f;
+    }
+  __syncthreads();
+  for (int d = 1; d < nb; ++d) {
+    const int nblk = nb - d;
+    // T_i = sum_{k=i+1..i+d} R_ik X_k,i+d  (16 x 16 each), into the scratch
+    for (int idx = threadIdx.x; idx < nblk * 256; idx += blockDim.x) {
+      const int bi = idx >> 8, p = (idx >> 4) & 15, q = idx & 15;
+      const int row = 16 * bi + p, col = 16 * (bi + d) + q;
+      float acc = 0.f;
+      if (row < r && col < r)
+        for (int k = 16 * (bi + 1); k <= col; ++k) acc = fmaf(R[row * ldr + k], Xi[k * ldo + col], acc);
+      s.tri[idx] = acc;
+    }
+    __syncthreads();
+    // X_i,i+d = -X_ii T_i
+    for (int idx = threadIdx.x; idx < nblk * 256; idx += blockDim.x) {
+      const int bi = idx >> 8, p = (idx >> 4) & 15, q = idx & 15;
+      const int row = 16 * bi + p, col = 16 * (bi + d) + q;
+      if (row < r && col < r) {
+        float acc = 0.f;
+        for (int m = p; m < 16; ++m) acc = fmaf(Xi[row * ldo + 16 * bi + m], s.tri[(bi << 8) + (m << 4) + q], acc);
+        Xi[row * ldo + col] = -acc;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---- inverse of X (r x r, stride ldx) by Gauss-Jordan with partial pivoting ------------
 // Aug: r x (2r+1) scratch; on return its columns [r, 2r) hold X^{-1}.
 __device__ inline void gj_inverse(const float* X, int ldx, float* Aug, int r, PolarScratch& s) {
@@ -257,17 +326,8 @@ __device__ inline void apply_q_ut(float* T, int ldt, float* U, int ldu, float* S
         Sc[i * ldt + j] = i < j ? acc[u][v] : (i == j ? (beta[i] != 0.f ? 1.f / beta[i] : 1.f) : 0.f);
     }
   __syncthreads();
-  // T = Sc^{-1} into the upper triangle of the reflector storage
-  for (int j = w; j < r; j += 16) {
-    for (int i = j; i >= 0; --i) {
-      float d = 0.f;
-      for (int q = i + 1 + l; q <= j; q += 32) d = fmaf(Sc[i * ldt + q], T[q * ldt + j], d);
-      d = warp_sum(d);
-      if (l == 0) T[i * ldt + j] = ((i == j ? 1.f : 0.f) - d) / Sc[i * ldt + i];
-      __syncwarp();
-    }
-  }
-  __syncthreads();
+  // T = Sc^{-1} into the upper triangle of the reflector storage (its lower part holds V)
+  tri_inverse_blocked(Sc, ldt, T, ldt, r, false, s);
   // Sc = V_top^T X
   cta_mm<4, 2>(r, r, r, 0, [&](int c, int k) { return V(k, c); },
                [&](int k, int j) { return U[k * ldu + j]; }, acc);
@@ -513,7 +573,7 @@ __device__ inline void newton_polar_r64(float* X, int ldx, float* Sc, int r, boo
   for (int it = 0; it < kNewtonMaxIt; ++it) {
     float dn = 0.f, nn = 0.f;
     if (!schulz) {
-      if (it == 0 && upper) tri_inverse(X, ldx, Sc, ldx, r, s);
+      if (it == 0 && upper) tri_inverse_blocked(X, ldx, Sc, ldx, r, true, s);
       else gj_inverse_reg(X, ldx, Sc, ldx, r, s);
       float a = 0.f, b = 0.f;
       for (int i = w; i < r; i += 16)
