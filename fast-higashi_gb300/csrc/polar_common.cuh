@@ -559,77 +559,139 @@ __device__ inline void newton_polar(float* X, int ldx, float* Aug, int r, bool u
   }
 }
 
-// ---- newton_polar for r <= 64 on 512 threads ------------------------------------------
-// The same iteration with the Gauss-Jordan inverse in registers and the Newton-Schulz
-// products register-tiled.  Newton-Schulz takes over once a Newton step moves X by less than
-// 30 % (newton_polar waits for 10 %): on the per-bin matrices of a 2,000-cell fit this saves
-// 4 % of the kernel and leaves the error against an fp64 SVD unchanged (median, 99th
-// percentile and maximum alike).
-// Sc: r x ldx scratch (X^{-1}, then 1.5 I - 0.5 X^T X); ldx odd.
+// ---- polar factor of X (r <= 64, stride ldx odd) in place, 512 threads -----------------
+// One scaled Newton step X <- (zeta X + X^{-T} / zeta) / 2 (the triangular inverse when X is
+// the R of a QR) maps every singular value into [1, m]; dividing by
+// U = sqrt(||X^T X||_inf) >= sigma_max puts them into [1/U, 1].  Then k quintic steps
+// X <- X (a I + b A + c A^2), A = X^T X, with (a, b, c) = (3.4445, -4.7750, 2.0315) raise
+// small singular values about 3.2-fold per step (k = ceil(log(0.6 U) / log 3.2)) into
+// [0.6, 1.2], and cubic Newton-Schulz steps X <- X (3 I - A) / 2 finish the convergence
+// (until a step moves X by less than 3e-5, then one more).  Every step after the first is
+// three or two register-tiled r x r products: on the per-bin matrices of a 2,000-cell fit
+// (condition numbers 2e7 to 3e12) this replaces 4 Gauss-Jordan inverses per matrix and errs
+// against an fp64 polar factor of the same fp32 R by a median 6e-7 (max 3e-6).
+// Sc: r x ldx scratch.
 __device__ inline void newton_polar_r64(float* X, int ldx, float* Sc, int r, bool upper,
                                         PolarScratch& s) {
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  bool schulz = false, last = false;
-  for (int it = 0; it < kNewtonMaxIt; ++it) {
+  // ---- 1. scaled Newton step
+  if (upper) tri_inverse_blocked(X, ldx, Sc, ldx, r, true, s);
+  else gj_inverse_reg(X, ldx, Sc, ldx, r, s);
+  {
+    float a = 0.f, b = 0.f;
+    for (int i = w; i < r; i += 16)
+      for (int j = l; j < r; j += 32) {
+        a = fmaf(X[i * ldx + j], X[i * ldx + j], a);
+        b = fmaf(Sc[i * ldx + j], Sc[i * ldx + j], b);
+      }
+    a = block_sum<float>(a, s.red);
+    b = block_sum<float>(b, s.red);
+    const float zeta = sqrtf(sqrtf(b) / sqrtf(a));
+    const float iz = 1.f / zeta;
+    for (int i = w; i < r; i += 16)
+      for (int j = l; j < r; j += 32)
+        X[i * ldx + j] = 0.5f * (zeta * X[i * ldx + j] + iz * Sc[j * ldx + i]);
+    __syncthreads();
+  }
+  // ---- 2. scale into [1/U, 1]
+  float acc[4][2];
+  cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return X[k * ldx + i]; },
+               [&](int k, int j) { return X[k * ldx + j]; }, acc);
+  float rmax = 0.f;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    float rs = 0.f;
+#pragma unroll
+    for (int v = 0; v < 2; ++v)
+      if (l + 32 * v < r) rs += fabsf(acc[u][v]);
+    rs = warp_sum(rs);
+    if (w + 16 * u < r) rmax = fmaxf(rmax, rs);
+  }
+  if (l == 0) s.red[w] = rmax;
+  __syncthreads();
+  float Ub = 0.f;
+  for (int q = 0; q < 16; ++q) Ub = fmaxf(Ub, s.red[q]);
+  Ub = sqrtf(Ub);
+  __syncthreads();
+  {
+    const float iu = Ub > 0.f ? 1.f / Ub : 1.f;
+    for (int i = w; i < r; i += 16)
+      for (int j = l; j < r; j += 32) X[i * ldx + j] *= iu;
+    __syncthreads();
+  }
+  // ---- 3. quintic boost of the small singular values
+  int kq = (Ub > 0.f) ? (int)ceilf(logf(0.6f * Ub) / logf(3.2f)) : 0;
+  kq = kq < 0 ? 0 : (kq > 16 ? 16 : kq);
+  for (int q = 0; q < kq; ++q) {
+    cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return X[k * ldx + i]; },
+                 [&](int k, int j) { return X[k * ldx + j]; }, acc);     // A = X^T X
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int i = w + 16 * u, j = l + 32 * v;
+        if (i < r && j < r) Sc[i * ldx + j] = acc[u][v];
+      }
+    __syncthreads();
+    float a2[4][2];
+    cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return Sc[i * ldx + k]; },
+                 [&](int k, int j) { return Sc[k * ldx + j]; }, a2);      // A^2
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int i = w + 16 * u, j = l + 32 * v;
+        if (i < r && j < r)
+          Sc[i * ldx + j] = (i == j ? 3.4445f : 0.f) - 4.7750f * acc[u][v] + 2.0315f * a2[u][v];
+      }
+    __syncthreads();
+    cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return X[i * ldx + k]; },
+                 [&](int k, int j) { return Sc[k * ldx + j]; }, acc);     // X P
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int i = w + 16 * u, j = l + 32 * v;
+        if (i < r && j < r) X[i * ldx + j] = acc[u][v];
+      }
+    __syncthreads();
+  }
+  // ---- 4. cubic Newton-Schulz to convergence
+  bool last = false;
+  for (int it = 0; it < 16; ++it) {
     float dn = 0.f, nn = 0.f;
-    if (!schulz) {
-      if (it == 0 && upper) tri_inverse_blocked(X, ldx, Sc, ldx, r, true, s);
-      else gj_inverse_reg(X, ldx, Sc, ldx, r, s);
-      float a = 0.f, b = 0.f;
-      for (int i = w; i < r; i += 16)
-        for (int j = l; j < r; j += 32) {
-          a = fmaf(X[i * ldx + j], X[i * ldx + j], a);
-          b = fmaf(Sc[i * ldx + j], Sc[i * ldx + j], b);
-        }
-      a = block_sum<float>(a, s.red);
-      b = block_sum<float>(b, s.red);
-      float zeta = sqrtf(sqrtf(b) / sqrtf(a));
-      if (it >= 1 && fabsf(zeta - 1.f) < 1e-2f) zeta = 1.f;
-      const float iz = 1.f / zeta;
-      for (int i = w; i < r; i += 16)
-        for (int j = l; j < r; j += 32) {
-          const float x = X[i * ldx + j];
-          const float xn = 0.5f * (zeta * x + iz * Sc[j * ldx + i]);
-          const float d = xn - x;
+    cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return X[k * ldx + i]; },
+                 [&](int k, int j) { return X[k * ldx + j]; }, acc);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int i = w + 16 * u, j = l + 32 * v;
+        if (i < r && j < r) Sc[i * ldx + j] = (i == j ? 1.5f : 0.f) - 0.5f * acc[u][v];
+      }
+    __syncthreads();
+    cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return X[i * ldx + k]; },
+                 [&](int k, int j) { return Sc[k * ldx + j]; }, acc);
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 2; ++v) {
+        const int i = w + 16 * u, j = l + 32 * v;
+        if (i < r && j < r) {
+          const float d = acc[u][v] - X[i * ldx + j];
           dn = fmaf(d, d, dn);
-          nn = fmaf(xn, xn, nn);
-          X[i * ldx + j] = xn;
+          nn = fmaf(acc[u][v], acc[u][v], nn);
+          X[i * ldx + j] = acc[u][v];
         }
-    } else {
-      float acc[4][2];
-      cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return X[k * ldx + i]; },
-                   [&](int k, int j) { return X[k * ldx + j]; }, acc);
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 2; ++v) {
-          const int i = w + 16 * u, j = l + 32 * v;
-          if (i < r && j < r) Sc[i * ldx + j] = (i == j ? 1.5f : 0.f) - 0.5f * acc[u][v];
-        }
-      __syncthreads();
-      cta_mm<4, 2>(r, r, r, 0, [&](int i, int k) { return X[i * ldx + k]; },
-                   [&](int k, int j) { return Sc[k * ldx + j]; }, acc);
-      __syncthreads();
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 2; ++v) {
-          const int i = w + 16 * u, j = l + 32 * v;
-          if (i < r && j < r) {
-            const float d = acc[u][v] - X[i * ldx + j];
-            dn = fmaf(d, d, dn);
-            nn = fmaf(acc[u][v], acc[u][v], nn);
-            X[i * ldx + j] = acc[u][v];
-          }
-        }
-    }
+      }
     dn = block_sum<float>(dn, s.red);
     nn = block_sum<float>(nn, s.red);
     __syncthreads();
-    const float rel = sqrtf(dn / nn);
     if (last) break;
-    if (schulz && rel < 3e-5f) last = true;
-    if (!schulz && rel < 0.3f) schulz = true;
+    if (sqrtf(dn / nn) < 3e-5f) last = true;
   }
 }
 
