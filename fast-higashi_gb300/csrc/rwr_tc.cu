@@ -24,12 +24,12 @@
 //          the residual lo) through a staging copy in smem, then stored contiguously.
 // The split products carry every operand to 16 significant bits, so the result is fp32-class.
 // Thread (warp w, lane l) serves row p = 32 (w % 4) + l (the TMEM lane quarter its warp may
-// read) and the column half w / 4.  Tiles wider than 256 columns use rwr_f32.cu.
+// read) and the column quarter w / 4 (16 warps).  Tiles wider than 256 columns use rwr_f32.cu.
 #include "tc_common.cuh"
 
 namespace fh {
 
-constexpr int kRtThreads = 256;
+constexpr int kRtThreads = 512;   // 16 warps: four per TMEM lane quarter
 constexpr float kRtFloor = 1e-8f;  // densify floor, sparse_for_schic.py:320
 constexpr float kRtEps = 1e-15f;   // column-sum guard, partial_rwr.py:90,91,111
 constexpr int kRtMaxPad = 256;     // npad: columns rounded up to 64, at most one MMA's N
@@ -102,7 +102,7 @@ __device__ __forceinline__ float ld_split(const uint8_t* hi, const uint8_t* lo, 
 }
 
 __host__ __device__ inline size_t rt_smem_bytes(int npad_max) {
-  return (size_t)npad_max / 64 * 16384 * 2 + 65536 + 7 * 128 * sizeof(float) + 64 * sizeof(double) +
+  return (size_t)npad_max / 64 * 16384 * 2 + 65536 + 11 * 128 * sizeof(float) + 64 * sizeof(double) +
          64 + 1024;
 }
 
@@ -116,9 +116,9 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
   uint8_t* Zlo = g + zbytes;
   uint8_t* Phi = g + 2 * zbytes;
   uint8_t* Plo = Phi + 32768;
-  float* cs1p = reinterpret_cast<float*>(Plo + 32768);  // [2][128] partial column sums of S1
-  float* cs2p = cs1p + 256;                              // [2][128] partial row sums of S2
-  float* fac = cs2p + 256;                               // [3][128] per-column P factors
+  float* cs1p = reinterpret_cast<float*>(Plo + 32768);  // [4][128] partial column sums of S1
+  float* cs2p = cs1p + 512;                              // [4][128] partial row sums of S2
+  float* fac = cs2p + 512;                               // [3][128] per-column P factors
   double* dred = reinterpret_cast<double*>(fac + 384);   // [64]
   uint64_t* mbar = reinterpret_cast<uint64_t*>(dred + 64);
   uint32_t* misc = reinterpret_cast<uint32_t*>(mbar + 1);  // [0] TMEM base
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
       continue;
     }
     const int npad = (n + 63) & ~63;
-    const int hw = npad / 2;  // columns per half
+    const int hw = npad / 4;  // columns per quarter (a multiple of 16)
     // ---- 1. Z = floor on the tile, zero on the padding (both planes)
     {
       const int cpr = npad / 8;  // 16-byte chunks per row
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
       }
     }
     __syncthreads();
-    // ---- 3. row p of A into TMEM (this thread's column half); column sums of S1
+    // ---- 3. row p of A into TMEM (this thread's column quarter); column sums of S1
     for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
       float v[16];
 #pragma unroll
@@ -227,13 +227,13 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
       tmem_st16(tA + j0, v);
     }
     {
-      const int q = tid & 127, half = tid >> 7;
+      const int q = tid & 127, part = tid >> 7;
       float s = 0.f;
       if (q < b) {
-        const int pe = min(b, 64 * half + 64);
-        for (int pp = 64 * half; pp < pe; ++pp) s += ld_split(Zhi, Zlo, sw_off(pp, s0 + q));
+        const int pe = min(b, 32 * part + 32);
+        for (int pp = 32 * part; pp < pe; ++pp) s += ld_split(Zhi, Zlo, sw_off(pp, s0 + q));
       }
-      cs1p[half * 128 + q] = s;
+      cs1p[part * 128 + q] = s;
     }
     tmem_wait_st();
     fence_proxy_async();
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     // ---- 5. P: row sums of S2 (diagonal excluded) = its column sums, then P row by row
     {
       float s = 0.f;
-      for (int q0 = 64 * h; q0 < 64 * h + 64; q0 += 16) {
+      for (int q0 = 32 * h; q0 < 32 * h + 32; q0 += 16) {
         float d[16], unused[16];
         tmem_ld16x2(tD + q0, tD + q0, d, unused);
 #pragma unroll
@@ -270,15 +270,15 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     // per column q: f1 = 0.75 / (c1 + eps), f2 = 0.25 / (c2 + eps), fl = 1 / (colsum(L) + eps)
     if (tid < 128) {
       const int q = tid;
-      const float c1 = cs1p[q] + cs1p[128 + q];
-      const float c2 = cs2p[q] + cs2p[128 + q];
+      const float c1 = (cs1p[q] + cs1p[128 + q]) + (cs1p[256 + q] + cs1p[384 + q]);
+      const float c2 = (cs2p[q] + cs2p[128 + q]) + (cs2p[256 + q] + cs2p[384 + q]);
       const float f1 = 0.75f / (c1 + kRtEps), f2 = 0.25f / (c2 + kRtEps);
       fac[q] = f1;
       fac[128 + q] = f2;
       fac[256 + q] = (c1 == 0.f && c2 == 0.f) ? -1.f : 1.f / (fmaf(c1, f1, c2 * f2) + kRtEps);
     }
     __syncthreads();
-    for (int q0 = 64 * h; q0 < 64 * h + 64; q0 += 16) {
+    for (int q0 = 32 * h; q0 < 32 * h + 32; q0 += 16) {
       float d[16], unused[16], pv[16];
       tmem_ld16x2(tD + q0, tD + q0, d, unused);
 #pragma unroll
