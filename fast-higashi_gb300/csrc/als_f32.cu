@@ -18,15 +18,6 @@
 
 namespace fh {
 
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, bool valid) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-  const int n = valid ? 16 : 0;
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gsrc), "r"(n));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
 // ---------------------------------------------------------------------------------------
 // W[row][m] = sum_c X[c][row] * E[c][m]; CTA = 128 band rows x RP, K = cells in steps of 32.
 // ---------------------------------------------------------------------------------------

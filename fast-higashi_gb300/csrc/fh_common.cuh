@@ -58,6 +58,16 @@ __global__ void reduce_splits_kernel(const T* __restrict__ partial, int splits, 
   }
 }
 
+// 16-byte global -> shared copy (cp.async, L2 only); valid = false fills zeros.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  const int n = valid ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gsrc), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
 __device__ inline void set_status(int* status, int code) {
   if (status) atomicCAS(status, 0, code);
 }

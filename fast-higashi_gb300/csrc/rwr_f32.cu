@@ -17,13 +17,10 @@
 // The auto-stop variant (partial_rwr.py:99-123) runs the same recurrence with A = I, which
 // is Q_t itself, and records ||Q_t - Q_{t+1}||_F per epoch.
 #include <cuda_bf16.h>
-#include "fh_common.cuh"
+#include "rwr_common.cuh"
 
 namespace fh {
 
-constexpr int kRwrThreads = 256;
-constexpr float kFloor = 1e-8f;  // densify floor, sparse_for_schic.py:320
-constexpr float kEps = 1e-15f;   // column-sum guard, partial_rwr.py:90,91,111
 
 enum RwrSource { kSparse = 0, kDense = 1 };
 enum RwrMode { kOutput = 0, kDeltas = 1, kOutput16 = 2 };
@@ -43,10 +40,9 @@ struct RwrArgs {
   double* sumsq;
   float* deltas;
   int cap;
+  float rp;  // walk weight: Q_{t+1} = rp Q_t P + (1 - rp) I (partial_rwr.py:109,116-118)
   int* status;
 };
-
-__host__ __device__ inline int rwr_ldp(int b) { return (b + 3) & ~3; }
 
 __host__ __device__ inline size_t rwr_smem_bytes(int b, int n) {
   const int ldp = rwr_ldp(b), ldz = lds_stride_odd(n > b ? n : b);
@@ -130,84 +126,9 @@ __global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
   }
   __syncthreads();
 
-  // ---- S2 = Z Z^T (b x b), diagonal zeroed (partial_rwr.py:85-87)
-  {
-    float acc[8][8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u)
-#pragma unroll
-      for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
-    const float* zp[8];
-    const float* zq[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      zp[u] = Z + min(ty + 16 * u, b - 1) * ldz;
-      zq[u] = Z + min(tx + 16 * u, b - 1) * ldz;
-    }
-    for (int k = 0; k < n; ++k) {
-      float ap[8], aq[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) { ap[u] = zp[u][k]; aq[u] = zq[u][k]; }
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-#pragma unroll
-        for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(ap[u], aq[v], acc[u][v]);
-    }
-#pragma unroll
-    for (int u = 0; u < 8; ++u)
-#pragma unroll
-      for (int v = 0; v < 8; ++v) {
-        const int p = ty + 16 * u, q = tx + 16 * v;
-        if (p < b && q < b) Pt[p * ldp + q] = (p == q) ? 0.f : acc[u][v];
-      }
-  }
-  __syncthreads();
+  rwr_transition(Z, ldz, Pt, ldp, b, n, s0, cs1, cs2, csl);
 
-  // ---- column sums of S2 and of the first-order block S1 = Z[:, s0:s0+b]
-  if (tid < b) {
-    float s = 0.f;
-    for (int p = 0; p < b; ++p) s += Pt[p * ldp + tid];
-    cs2[tid] = s;
-  } else if (tid >= 128 && tid - 128 < b) {
-    const int q = tid - 128;
-    float s = 0.f;
-    for (int p = 0; p < b; ++p) s += Z[p * ldz + s0 + q];
-    cs1[q] = s;
-  }
-  __syncthreads();
-  // ---- L = (S1 / (cs1 + eps)) * 0.75 + (S2 / (cs2 + eps)) * 0.25   (partial_rwr.py:90-93)
-  for (int i = tid; i < b * b; i += kRwrThreads) {
-    const int p = i / b, q = i % b;
-    const float l1 = (Z[p * ldz + s0 + q] / (cs1[q] + kEps)) * 0.75f;
-    const float l2 = (Pt[p * ldp + q] / (cs2[q] + kEps)) * 0.25f;
-    Pt[p * ldp + q] = l1 + l2;
-  }
-  __syncthreads();
-  // ---- zero columns get a unit diagonal (:96-97); P = L / (colsum(L) + eps) (:111)
-  if (tid < b) {
-    float s = 0.f;
-    for (int p = 0; p < b; ++p) s += Pt[p * ldp + tid];
-    if (s == 0.f) {
-      Pt[tid * ldp + tid] += 1.f;
-      s = 0.f;
-      for (int p = 0; p < b; ++p) s += Pt[p * ldp + tid];
-    }
-    csl[tid] = s;
-  }
-  __syncthreads();
-  // P stored transposed in place: Pt[q][p] = P[p][q] = L[p][q] / (csl[q] + eps)
-  for (int i = tid; i < b * b; i += kRwrThreads) {
-    const int p = i / b, q = i % b;
-    if (p < q) {
-      const float lpq = Pt[p * ldp + q], lqp = Pt[q * ldp + p];
-      Pt[q * ldp + p] = lpq / (csl[q] + kEps);
-      Pt[p * ldp + q] = lqp / (csl[p] + kEps);
-    } else if (p == q) {
-      Pt[p * ldp + p] = Pt[p * ldp + p] / (csl[p] + kEps);
-    }
-  }
-  __syncthreads();
-
+  const float om = a.rp, al = 1.f - a.rp;   // walk and restart weights
   int zw = n;  // columns of the recurrence state
   if (MODE == kDeltas) {
     zw = b;    // Q_0 = I
@@ -227,7 +148,7 @@ __global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
         for (int v = 0; v < 8; ++v) {
           const int i = ty + 16 * u, j = tx + 16 * v;
           if (i < zw && j < b) {
-            const float nv = 0.5f * acc[u][v] + (i == j ? 0.5f : 0.f);
+            const float nv = om * acc[u][v] + (i == j ? al : 0.f);
             const float dd = Z[j * ldz + i] - nv;
             d2 = fmaf(dd, dd, d2);
           }
@@ -241,10 +162,10 @@ __global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
         const int i = ty + 16 * u, j = tx + 16 * v;
         if (i < zw && j < b) {
           float base;
-          if (MODE == kDeltas) base = (i == j) ? 0.5f : 0.f;
-          else if (SRC == kSparse) base = 0.5f * kFloor;
-          else base = 0.5f * xin[j * n + i];
-          Z[j * ldz + i] = fmaf(0.5f, acc[u][v], base);
+          if (MODE == kDeltas) base = (i == j) ? al : 0.f;
+          else if (SRC == kSparse) base = al * kFloor;
+          else base = al * xin[j * n + i];
+          Z[j * ldz + i] = fmaf(om, acc[u][v], base);
         }
       }
     if (MODE == kDeltas) {
@@ -256,7 +177,7 @@ __global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
       for (int64_t e = e0 + tid; e < e1; e += kRwrThreads) {
         const uint2 en = a.entries[e];
         const float v = __uint_as_float(en.y);
-        if (v > kFloor) Z[(en.x & 0xffff) * ldz + (en.x >> 16)] += 0.5f * (v - kFloor);
+        if (v > kFloor) Z[(en.x & 0xffff) * ldz + (en.x >> 16)] += al * (v - kFloor);
       }
       __syncthreads();
     }
@@ -331,6 +252,7 @@ extern "C" int fh_rwr_tiles_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n
     return FH_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   RwrArgs a{};
+  a.rp = 0.5f;   // partial_rwr.py:109
   a.max_rows = mr; a.max_width = mw;
   a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
   a.offsets = offsets; a.out = out; a.cell_stride = cell_stride; a.sumsq = sumsq;
@@ -346,12 +268,30 @@ extern "C" int fh_rwr_tiles_bf16(const fh_tile* tiles, int32_t n_tiles, int32_t 
       plane_stride < 0)
     return FH_ERR_ARG;
   RwrArgs a{};
+  a.rp = 0.5f;   // partial_rwr.py:109
   a.max_rows = mr; a.max_width = mw;
   a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
   a.offsets = offsets; a.out16 = reinterpret_cast<__nv_bfloat16*>(out16);
   a.cell_stride = cell_stride; a.plane_stride = plane_stride; a.sumsq = sumsq;
   a.status = status;
   return launch_rwr<kSparse, kOutput16>(a, n_tiles, mr, mw, (cudaStream_t)stream);
+}
+
+extern "C" int fh_rwr_tiles_rp_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                                   int32_t mr, int32_t mw, const fh_entry* entries,
+                                   const int64_t* offsets, float rp, float* out,
+                                   int64_t cell_stride, double* sumsq, int* status,
+                                   void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !offsets || !out || mr <= 0 || mw < mr ||
+      !(rp >= 0.f && rp < 1.f))
+    return FH_ERR_ARG;
+  RwrArgs a{};
+  a.rp = rp;
+  a.max_rows = mr; a.max_width = mw;
+  a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
+  a.offsets = offsets; a.out = out; a.cell_stride = cell_stride; a.sumsq = sumsq;
+  a.status = status;
+  return launch_rwr<kSparse, kOutput>(a, n_tiles, mr, mw, (cudaStream_t)stream);
 }
 
 extern "C" int fh_rwr_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width,
@@ -361,6 +301,7 @@ extern "C" int fh_rwr_dense_f32(const float* x, int32_t n_cells, int32_t rows, i
       s0 + rows > width || n_epochs < 0)
     return FH_ERR_ARG;
   RwrArgs a{};
+  a.rp = 0.5f;   // partial_rwr.py:109
   a.n_cells = n_cells; a.dense = x; a.d_rows = rows; a.d_width = width; a.d_s0 = s0;
   a.max_rows = rows; a.max_width = width;
   a.d_epochs = n_epochs; a.out = out; a.cell_stride = (int64_t)rows * width; a.status = status;
@@ -374,6 +315,7 @@ extern "C" int fh_rwr_dense_deltas(const float* x, int32_t n_cells, int32_t rows
       s0 + rows > width || cap <= 0)
     return FH_ERR_ARG;
   RwrArgs a{};
+  a.rp = 0.5f;   // partial_rwr.py:109
   a.n_cells = n_cells; a.dense = x; a.d_rows = rows; a.d_width = width; a.d_s0 = s0;
   a.max_rows = rows; a.max_width = width;
   a.deltas = deltas; a.cap = cap; a.status = status;
@@ -389,6 +331,7 @@ extern "C" int fh_rwr_tiles_deltas(const fh_tile* tiles, int32_t n_tiles, int32_
     return FH_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   RwrArgs a{};
+  a.rp = 0.5f;   // partial_rwr.py:109
   a.max_rows = mr; a.max_width = mw;
   a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
   a.offsets = offsets; a.deltas = deltas; a.cap = cap; a.status = status;

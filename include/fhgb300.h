@@ -130,6 +130,25 @@ int fh_rwr_tiles_tc(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells, int3
                     uint16_t* out16, int64_t cell_stride, int64_t plane_stride, double* sumsq,
                     int* status, void* stream);
 
+/* fh_rwr_tiles_f32 with the walk weight free: Q_{t+1} = rp Q_t P + (1 - rp) I, the form of
+ * partial_rwr.py:109,116-118 where rp is fixed at 0.5 (0 <= rp < 1).  The forward of the
+ * differentiable reconstruction loss. */
+int fh_rwr_tiles_rp_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                        int32_t max_rows, int32_t max_width, const fh_entry* entries,
+                        const int64_t* offsets, float rp, float* out, int64_t cell_stride,
+                        double* sumsq, int* status, void* stream);
+
+/* Derivative of the RWR output with respect to rp, recomputing each tile (no reference
+ * counterpart: the reference has no backward pass).  With Z_0 = A, Z_{t+1} = rp P Z_t +
+ * (1 - rp) A and Z'_{t+1} = rp P Z'_t + P Z_t - A, writes dx = Z'_{n_rwr} and, when x is not
+ * null, x = Z_{n_rwr} (bit-identical to fh_rwr_tiles_rp_f32), in the layout of
+ * fh_rwr_tiles_f32.  max_rows <= 128, and 4 * (b*((b+3)&~3) + b*(n|1) + 130 b + 384) bytes
+ * of shared memory must fit in 227 KB (n <= 203 at b = 125). */
+int fh_rwr_grad_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells, int32_t max_rows,
+                    int32_t max_width, const fh_entry* entries, const int64_t* offsets,
+                    float rp, float* x, float* dx, int64_t cell_stride, int* status,
+                    void* stream);
+
 /* Same arithmetic on a dense tile x[n_cells][rows][width] (the partial_rwr drop-in: no
  * floor is applied to x); out[n_cells][rows][width]. */
 int fh_rwr_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width, int32_t s0,
@@ -214,6 +233,39 @@ int fh_projection_g_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n
                         int32_t max_width, int32_t max_rank, const float* A, int32_t lda,
                         const float* B, const float* D, int32_t ldb, int32_t R, int32_t rp,
                         const float* U, float* Gt, void* stream);
+
+/* ---- Fused per-cell reconstruction loss and its backward pass (no reference counterpart;
+ * the loss is the reference's reconstruction error, parafac2_intergrative.py:336-383,
+ * 667-713, split by cell).  With Gt from fh_projection_g_f32 (Gt_g = U_g B diag(A_g) D^T),
+ *   L_c = sum_rows (X[c][row] - sum_m E[c][m] Gt[row][m])^2,   rows < `rows`, c < n_cells,
+ * the residual formed in shared memory and never stored.  X: float[n_cells][ldx] (ldx a
+ * multiple of 64; entries past `rows` are ignored), Gt: float[rows][rp], E: float[n_cells]
+ * [rp], rp in {16, 32, 64}.  ws: fh_recon_workspace bytes of device memory.
+ * fh_recon_loss_f32: loss = double[n_cells].
+ * fh_recon_loss_bwd_f32, for w = dOut/dL (double[n_cells]) and Xp = dX/drp
+ * (fh_rwr_grad_f32; same layout as X):
+ *   dE[c] = -2 w_c sum_rows Res[c] Gt,   dGt[row] = -2 sum_c w_c Res[c][row] E[c],
+ *   *drp = 2 sum_c w_c <Res[c], Xp[c]>,  and loss (optional) as above. */
+size_t fh_recon_workspace(int32_t n_cells, int64_t rows, int32_t rp);
+int fh_recon_loss_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows,
+                      const float* Gt, const float* E, int32_t rp, double* loss, void* ws,
+                      size_t ws_bytes, void* stream);
+int fh_recon_loss_bwd_f32(const float* X, const float* Xp, int64_t ldx, int32_t n_cells,
+                          int64_t rows, const float* Gt, const float* E, int32_t rp,
+                          const double* w, double* loss, float* dE, float* dGt, double* drp,
+                          void* ws, size_t ws_bytes, void* stream);
+
+/* Factor gradients from H_g = U_g^T dGt_g (fh_project_y_f32 applied to dGt; H: float[n_rows]
+ * [ldh][rp]), for Gt_g = U_g B_c diag(A_g) D_c^T:
+ *   dA[g][p] = sum_l B_c[l][p] (H_g D_c)[l][p],   dB_c = sum_g (H_g D_c) diag(A_g),
+ *   dD_c = sum_g H_g^T B_c diag(A_g).
+ * meta: the chunk table of fh_cp_als; A, dA: float[n_rows][ld]; B, dB: float[nchrom][ld][ld];
+ * D, dD: float[nchrom][rp][ld]; ld, rp <= 64.  ws: fh_factor_grad_workspace bytes. */
+size_t fh_factor_grad_workspace(int32_t nchunks, int32_t ld, int32_t rp);
+int fh_factor_grad_f32(int32_t nchrom, int32_t nchunks, const int32_t* meta, const float* H,
+                       int32_t ldh, const float* A, const float* B, const float* D, int32_t ld,
+                       int32_t rp, int32_t R, float* dA, float* dB, float* dD, void* ws,
+                       size_t ws_bytes, void* stream);
 
 /* project2orthogonal drop-in (project2orthogonal.py:6-34) for a batch of tall matrices:
  * M: float[batch][n][r] (n >= r, r <= 128, fh_polar_smem(n, r) <= 227 KB) -> U: float[batch]

@@ -31,9 +31,9 @@ def polar(m):
     return U @ Vh, S
 
 
-def rwr_tile(A, s0, s1, epochs):
-    """partial_rwr.py:84-138 (do_conv=False, do_col=False, force_rwr_epochs=epochs) on a
-    (cells, b, n) float64 tile; returns Q_epochs A."""
+def transition(A, s0, s1):
+    """The column-stochastic P of partial_rwr.py:84-111 (do_conv=False) for a (cells, b, n)
+    float64 tile."""
     b = A.shape[1]
     ar = torch.arange(b, device=A.device)
     S2 = A @ A.transpose(1, 2)
@@ -43,12 +43,43 @@ def rwr_tile(A, s0, s1, epochs):
     S1 = (S1 / (S1.sum(1, keepdim=True) + 1e-15)) * 0.75
     L = S1 + S2
     L[:, ar, ar] += (L.sum(1) == 0).to(F64)
-    P = L / (L.sum(1, keepdim=True) + 1e-15)
-    Q = torch.eye(b, dtype=F64, device=A.device).expand_as(P).clone()
+    return L / (L.sum(1, keepdim=True) + 1e-15)
+
+
+def rwr_tile(A, s0, s1, epochs, rp=0.5):
+    """partial_rwr.py:84-138 (do_conv=False, do_col=False, force_rwr_epochs=epochs) on a
+    (cells, b, n) float64 tile: Q_{t+1} = rp Q_t P + (1 - rp) I from Q_0 = I (:109,116-118;
+    rp may be a tensor that requires grad); returns Q_epochs A."""
+    b = A.shape[1]
+    P = transition(A, s0, s1)
+    eye = torch.eye(b, dtype=F64, device=A.device)
+    Q = eye.expand_as(P).clone()
     for _ in range(epochs):
-        Q = 0.5 * (Q @ P)
-        Q[:, ar, ar] += 0.5
+        Q = rp * (Q @ P) + (1 - rp) * eye
     return Q @ A
+
+
+def dense_tiles(datas, C, device, cell_chunk=2048):
+    """(dataset index, bin batch index, layout, floored dense tile (C, b, n) float64) for every
+    bin batch: densify_jit's +1 padding ring, crop and 1e-8 floor (sparse_for_schic.py:
+    279-320) from the oracle's ChromData records."""
+    dev = torch.device(device)
+    for ci, d in enumerate(datas):
+        r, c, k = (torch.as_tensor(np.asarray(v, dtype=np.int64)).to(dev) for v in d.indices)
+        v = torch.as_tensor(np.asarray(d.values)).to(dev).to(F64)
+        for bi, bb in enumerate(d.layout()):
+            m = (r >= bb.start) & (r < bb.start + bb.rows)
+            rr, cc, kk, vv = r[m] - bb.start, c[m] - bb.shift, k[m], v[m]
+            keep = (cc >= -1) & (cc <= bb.width)          # the +1 padding ring
+            rr, cc, kk, vv = rr[keep], cc[keep], kk[keep], vv[keep]
+            out = torch.empty((C, bb.rows, bb.width), dtype=F64, device=dev)
+            for c0 in range(0, C, cell_chunk):
+                c1 = min(C, c0 + cell_chunk)
+                sel = (kk >= c0) & (kk < c1)
+                dense = torch.zeros((c1 - c0, bb.rows + 2, bb.width + 2), dtype=F64, device=dev)
+                dense[kk[sel] - c0, rr[sel] + 1, cc[sel] + 1] = vv[sel]
+                out[c0:c1] = torch.clamp(dense[:, 1:-1, 1:-1], min=1e-8)
+            yield ci, bi, bb, out
 
 
 def balance_norm(f):
@@ -101,24 +132,10 @@ class FP64Fit:
         self.size = {d.name: self.B[d.name].shape[0] for d in datas}
         self.X = {}
         self.tnorm = np.zeros(len(datas))
-        for ci, d in enumerate(datas):
-            r, c, k = (torch.as_tensor(np.asarray(v, dtype=np.int64)).to(dev) for v in d.indices)
-            v = torch.as_tensor(np.asarray(d.values)).to(dev).to(F64)
-            for bi, bb in enumerate(d.layout()):
-                m = (r >= bb.start) & (r < bb.start + bb.rows)
-                rr, cc, kk, vv = r[m] - bb.start, c[m] - bb.shift, k[m], v[m]
-                keep = (cc >= -1) & (cc <= bb.width)          # the +1 padding ring
-                rr, cc, kk, vv = rr[keep], cc[keep], kk[keep], vv[keep]
-                out = torch.empty((self.C, bb.rows, bb.width), dtype=F64, device=dev)
-                for c0 in range(0, self.C, cell_chunk):
-                    c1 = min(self.C, c0 + cell_chunk)
-                    sel = (kk >= c0) & (kk < c1)
-                    dense = torch.zeros((c1 - c0, bb.rows + 2, bb.width + 2), dtype=F64, device=dev)
-                    dense[kk[sel] - c0, rr[sel] + 1, cc[sel] + 1] = vv[sel]
-                    A = torch.clamp(dense[:, 1:-1, 1:-1], min=1e-8)
-                    out[c0:c1] = rwr_tile(A, bb.local.start, bb.local.stop, int(n_i[ci]))
-                self.X[(ci, bi)] = out
-                self.tnorm[ci] += float((out ** 2).sum())
+        for ci, bi, bb, A in dense_tiles(datas, self.C, dev, cell_chunk):
+            out = rwr_tile(A, bb.local.start, bb.local.stop, int(n_i[ci]))
+            self.X[(ci, bi)] = out
+            self.tnorm[ci] += float((out ** 2).sum())
         self.norm_tensor = np.sqrt(self.tnorm)
         self.norm_all = float(np.linalg.norm(self.norm_tensor))
         self.core = self._core_norm()
