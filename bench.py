@@ -42,9 +42,12 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c3",
+    ap.add_argument("--config", default=None,
                     help="workload: c1..c5 (default c3, 10,000 cells at 500 kb, the one the "
-                         "BF16-batched vs plain FP32 target is set on)")
+                         "BF16-batched vs plain FP32 target is set on; c4 with --grad)")
+    ap.add_argument("--grad", action="store_true",
+                    help="time the differentiable reconstruction loss (forward + backward) "
+                         "instead of the fit; prints its own JSON line")
     ap.add_argument("--iters", type=int, default=None, help="ALS iterations (default: the workload's 30)")
     ap.add_argument("--sample-cells", type=int, default=96,
                     help="cells of the CPU-baseline sample (at least the rank R)")
@@ -54,7 +57,9 @@ def parse():
                          "as two bf16 planes; bf16 one plane; fp32 the plain drop-in")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip timing the plain fp32 form beside the headline form")
-    return ap.parse_args()
+    args = ap.parse_args()
+    args.config = args.config or ("c4" if args.grad else "c3")
+    return args
 
 
 def dist_setup():
@@ -367,10 +372,96 @@ def gb300_arm(args, rank, local, ws):
     print(json.dumps(line), flush=True)
 
 
+def grad_arm(args, rank, local, ws):
+    """Forward + backward of the per-cell reconstruction loss (fh_gb300.differentiable) on a
+    fitted state: the RWR at rp, the Gt rows and the fused loss; then the recomputed RWR with
+    its rp-derivative, the fused residual backward, U^T dGt and the factor gradients."""
+    import torch
+    from fh_gb300 import Fast_Higashi_core, _lib
+    from fh_gb300.differentiable import ReconstructionLoss
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    w, coo, ds = make_workload(args.config)
+    torch.manual_seed(0)
+    m = Fast_Higashi_core(w.rank, w.band, [w.resolution]).to(dev)
+    m.fit(ds, size_ratio=w.dim1, n_iter_max=args.iters or 3, n_iter_parafac=1, do_conv=False,
+          do_rwr=True, do_col=False, tol=0, verbose=False)
+    eng = m.engine
+    layer = ReconstructionLoss(m)
+    leaves = [m.meta_embedding.detach().clone()] + [a.detach().clone() for a in m.A_list] + \
+        [m.B_dict[d.chrom].detach().clone() for d in ds] + [m.D_dict[d.chrom].detach().clone() for d in ds]
+    for t in leaves:
+        t.requires_grad_()
+    n = len(ds)
+    rp = torch.tensor(0.5, dtype=torch.float64, device=dev, requires_grad=True)
+
+    def step():
+        loss = layer(rp, leaves[0], leaves[1:1 + n], leaves[1 + n:1 + 2 * n], leaves[1 + 2 * n:])
+        loss.sum().backward()
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = _lib.launches
+    with Clocks(local) as clk:
+        s0.record()
+        for _ in range(args.steps):
+            step()
+        s1.record()
+        torch.cuda.synchronize()
+    ms = s0.elapsed_time(s1) / args.steps
+    launches = (_lib.launches - n0) // args.steps
+    layer.timing = {}
+    step()
+    torch.cuda.synchronize()
+    kt = layer.timing_summary()
+    layer.timing = None
+    # algorithmic flops (fp32 FMA work) per kernel family
+    t = eng.tiles
+    b, nw, ep = t["rows"].astype(float), t["width"].astype(float), t["n_rwr"].astype(float)
+    C, Ct, R = eng.C, eng.Ct, w.rank
+    fl = {"rwr_rp": Ct * float((2 * b * b * nw * (1 + ep)).sum()),
+          "rwr_grad": Ct * float((2 * b * b * nw * (1 + 2 * ep)).sum()),
+          "recon_loss": 2.0 * eng.rows * C * R,
+          "recon_bwd": 8.0 * eng.rows * C * R}
+    clock = clk.summary()
+    mhz = clock.get("sm_max_mhz") or 2070.0
+    fp32_peak = 2 * 128 * 152 * mhz * 1e6 / 1e12    # nominal fp32 CUDA-core TFLOP/s
+    fam = max(fl, key=lambda k: kt.get(k, {}).get("total_ms", 0))
+    ach = fl[fam] / (kt[fam]["mean_ms"] / 1000.0) / 1e12
+    kernels = {k: {"ms": round(v["mean_ms"], 3),
+                   "tflops": round(fl[k] / (v["mean_ms"] / 1000.0) / 1e12, 2) if k in fl else None}
+               for k, v in kt.items()}
+    if rank != 0:
+        return
+    line = {"metric": "differentiable reconstruction loss, forward + backward (rp, E, A, B, D)",
+            "value": ms, "unit": "ms per forward+backward", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, %s)" % args.config,
+            "config": {"workload": "%s: %d cells, %d bins (%d bin batches), R=%d, band %d, fitted "
+                                   "state after %d ALS iterations" %
+                                   (args.config, C, sum(w.chrom_bins), eng.n_tiles, R, w.band,
+                                    args.iters or 3),
+                       "l2": "inputs larger than L2 (X %.2f GB fp32)" % (Ct * eng.ldx * 4 / 1e9)},
+            "roofline": {"kernel": fam, "bound": "fp32", "achieved": ach, "peak": fp32_peak,
+                         "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                         "peak_kind": "nominal fp32 CUDA-core rate at the sampled maximum clock",
+                         "traffic": None},
+            "kernels": kernels, "gpu_launches": int(launches), "clocks": clock}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, local, ws = dist_setup()
-    if args.impl == "reference":
+    if args.grad:
+        from fh_gb300 import build as _b
+        _b.build()
+        grad_arm(args, rank, local, ws)
+    elif args.impl == "reference":
         reference_arm(args, rank, ws)
     else:
         from fh_gb300 import build as _b

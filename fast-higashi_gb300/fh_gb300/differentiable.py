@@ -44,6 +44,7 @@ class ReconstructionLoss:
         self.eng = eng
         self.torch = torch
         self._ws = {}
+        self.timing = None   # {step: [(start event, end event)]} when enabled
 
     def __call__(self, rp, E, A_list, B_list, D_list):
         torch = self.torch
@@ -55,6 +56,22 @@ class ReconstructionLoss:
         return ReconFn.apply(self, rp, E, *A_list, *B_list, *D_list)
 
     # ------------------------------------------------------------------ helpers
+    def _timed(self, name, fn):
+        """Runs fn; with timing enabled, brackets it with CUDA events on the current stream."""
+        if self.timing is None:
+            return fn()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        out = fn()
+        e.record()
+        self.timing.setdefault(name, []).append((s, e))
+        return out
+
+    def timing_summary(self):
+        return {k: {"launches": len(v), "total_ms": sum(a.elapsed_time(b) for a, b in v),
+                    "mean_ms": sum(a.elapsed_time(b) for a, b in v) / len(v)}
+                for k, v in (self.timing or {}).items()}
+
     def _buf(self, key, nbytes):
         t = self._ws.get(key)
         if t is None or t.numel() < nbytes:
@@ -86,22 +103,25 @@ class ReconstructionLoss:
         X = torch.empty((eng.Ct, eng.ldx), dtype=torch.float32, device=eng.device)
         if grad:
             Xp = torch.empty_like(X)
-            _lib.call("fh_rwr_grad_f32", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
-                      eng.max_width, P(eng.store.entries), P(eng.store.offsets), rp, P(X),
-                      P(Xp), eng.ldx, P(eng.status), _lib.stream_ptr())
+            self._timed("rwr_grad", lambda: _lib.call(
+                "fh_rwr_grad_f32", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
+                eng.max_width, P(eng.store.entries), P(eng.store.offsets), rp, P(X), P(Xp),
+                eng.ldx, P(eng.status), _lib.stream_ptr()))
             return X, Xp
-        _lib.call("fh_rwr_tiles_rp_f32", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
-                  eng.max_width, P(eng.store.entries), P(eng.store.offsets), rp, P(X), eng.ldx,
-                  None, P(eng.status), _lib.stream_ptr())
+        self._timed("rwr_rp", lambda: _lib.call(
+            "fh_rwr_tiles_rp_f32", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
+            eng.max_width, P(eng.store.entries), P(eng.store.offsets), rp, P(X), eng.ldx, None,
+            P(eng.status), _lib.stream_ptr()))
         return X
 
     def gt(self, Ap, Bp, Dp):
         torch, eng = self.torch, self.eng
         Gt = torch.empty((eng.rows, eng.rp), dtype=torch.float32, device=eng.device)
         P = _lib.ptr
-        _lib.call("fh_projection_g_f32", P(eng.tiles_dev), P(eng.row_tile), eng.nb,
-                  eng.max_width, eng.max_rank, P(Ap), eng.ld, P(Bp), P(Dp), eng.ld, eng.R,
-                  eng.rp, P(eng.U), P(Gt), _lib.stream_ptr())
+        self._timed("projection_g", lambda: _lib.call(
+            "fh_projection_g_f32", P(eng.tiles_dev), P(eng.row_tile), eng.nb, eng.max_width,
+            eng.max_rank, P(Ap), eng.ld, P(Bp), P(Dp), eng.ld, eng.R, eng.rp, P(eng.U), P(Gt),
+            _lib.stream_ptr()))
         return Gt
 
     def recon_ws(self):
@@ -128,8 +148,9 @@ class ReconFn(torch.autograd.Function):
         Gt = op.gt(Ap, Bp, Dp)
         loss = torch.empty(eng.C, dtype=torch.float64, device=eng.device)
         ws, nbytes = op.recon_ws()
-        _lib.call("fh_recon_loss_f32", P(X), eng.ldx, eng.C, eng.rows, P(Gt), P(Ep), eng.rp,
-                  P(loss), P(ws), nbytes, _lib.stream_ptr())
+        op._timed("recon_loss", lambda: _lib.call(
+            "fh_recon_loss_f32", P(X), eng.ldx, eng.C, eng.rows, P(Gt), P(Ep), eng.rp, P(loss),
+            P(ws), nbytes, _lib.stream_ptr()))
         del X
         eng.check_status("ReconstructionLoss.forward")
         ctx.op, ctx.rpv, ctx.n = op, rpv, n
@@ -150,18 +171,20 @@ class ReconFn(torch.autograd.Function):
         dGt = torch.empty_like(Gt)
         drp = torch.empty(1, dtype=torch.float64, device=eng.device)
         ws, nbytes = op.recon_ws()
-        _lib.call("fh_recon_loss_bwd_f32", P(X), P(Xp), eng.ldx, eng.C, eng.rows, P(Gt), P(Ep),
-                  eng.rp, P(w), None, P(dE), P(dGt), P(drp), P(ws), nbytes, sp)
+        op._timed("recon_bwd", lambda: _lib.call(
+            "fh_recon_loss_bwd_f32", P(X), P(Xp), eng.ldx, eng.C, eng.rows, P(Gt), P(Ep), eng.rp,
+            P(w), None, P(dE), P(dGt), P(drp), P(ws), nbytes, sp))
         del X, Xp
         H = torch.empty((eng.nb, eng.ld, eng.rp), dtype=torch.float32, device=eng.device)
-        _lib.call("fh_project_y_f32", P(eng.tiles_dev), P(eng.row_tile), eng.nb, P(eng.U),
-                  P(dGt), eng.rp, P(H), eng.ld, sp)
+        op._timed("project_h", lambda: _lib.call(
+            "fh_project_y_f32", P(eng.tiles_dev), P(eng.row_tile), eng.nb, P(eng.U), P(dGt),
+            eng.rp, P(H), eng.ld, sp))
         dA, dB, dD = torch.empty_like(Ap), torch.empty_like(Bp), torch.empty_like(Dp)
         fw = _lib.value("fh_factor_grad_workspace", eng.nchunks, eng.ld, eng.rp)
         fws = op._buf("factor", fw)
-        _lib.call("fh_factor_grad_f32", len(eng.names), eng.nchunks, P(eng.cp_meta), P(H),
-                  eng.ld, P(Ap), P(Bp), P(Dp), eng.ld, eng.rp, eng.R, P(dA), P(dB), P(dD),
-                  P(fws), fw, sp)
+        op._timed("factor_grad", lambda: _lib.call(
+            "fh_factor_grad_f32", len(eng.names), eng.nchunks, P(eng.cp_meta), P(H), eng.ld,
+            P(Ap), P(Bp), P(Dp), eng.ld, eng.rp, eng.R, P(dA), P(dB), P(dD), P(fws), fw, sp))
         eng.check_status("ReconstructionLoss.backward")
         meta = ctx.in_meta
         out = [None, _as(drp.reshape(()), meta[0]), _as(dE[:, :eng.R], meta[1])]
