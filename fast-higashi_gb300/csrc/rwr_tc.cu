@@ -201,10 +201,11 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
           continue;
         }
         const float v = fmaxf(__uint_as_float(en.y), kRtFloor);
-        const __nv_bfloat16 hv = __float2bfloat16_rn(v);
+        uint32_t hv, lv;
+        split2(v, 0.f, hv, lv);                 // packed conversions (low halves used)
         const uint32_t off = sw_off(r, j);
-        *reinterpret_cast<__nv_bfloat16*>(Zhi + off) = hv;
-        *reinterpret_cast<__nv_bfloat16*>(Zlo + off) = __float2bfloat16_rn(v - __bfloat162float(hv));
+        *reinterpret_cast<uint16_t*>(Zhi + off) = (uint16_t)(hv & 0xffffu);
+        *reinterpret_cast<uint16_t*>(Zlo + off) = (uint16_t)(lv & 0xffffu);
       }
     }
     __syncthreads();
@@ -313,20 +314,26 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     const int64_t lo_base = (tot + 15) & ~(int64_t)7;   // lo plane staging, 16-byte aligned
     auto emit = [&](int j0, const float (&z)[16]) {
       if (p >= b) return;
+      uint16_t* st16 = reinterpret_cast<uint16_t*>(stage);
 #pragma unroll
-      for (int e = 0; e < 16; ++e) {
-        const int j = j0 + e;
-        if (j < n) {
-          const int64_t k = (int64_t)p * n + j + mis;
-          const __nv_bfloat16 hv = __float2bfloat16_rn(z[e]);
-          float sv = __bfloat162float(hv);
-          reinterpret_cast<__nv_bfloat16*>(stage)[k] = hv;
-          if (two) {
-            const __nv_bfloat16 lv = __float2bfloat16_rn(z[e] - sv);
-            reinterpret_cast<__nv_bfloat16*>(stage)[lo_base + k] = lv;
-            sv += __bfloat162float(lv);
+      for (int e = 0; e < 16; e += 2) {
+        uint32_t hv, lv;
+        split2(z[e], z[e + 1], hv, lv);        // packed conversions of the pair
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int j = j0 + e + u;
+          if (j < n) {
+            const uint32_t hb = u ? (hv >> 16) : (hv & 0xffffu);
+            const uint32_t lb = u ? (lv >> 16) : (lv & 0xffffu);
+            const int64_t k = (int64_t)p * n + j + mis;
+            st16[k] = (uint16_t)hb;
+            float sv = __uint_as_float(hb << 16);
+            if (two) {
+              st16[lo_base + k] = (uint16_t)lb;
+              sv += __uint_as_float(lb << 16);
+            }
+            ss = fmaf(sv, sv, ss);
           }
-          ss = fmaf(sv, sv, ss);
         }
       }
     };
