@@ -152,6 +152,15 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def autotune_summary():
+    """The schedules the autotuner timed in this process: {knob and shape: candidate -> ms,
+    choice}."""
+    from fh_gb300 import autotune
+    return {k.split("|", 1)[1]: {"ms": {str(c): round(t, 4) for c, t in times.items()},
+                                  "choice": best}
+            for k, times, best in autotune.default_tuner().log}
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -337,17 +346,20 @@ def gb300_arm(args, rank, local, ws):
 
     e2e_step()
     torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(max(1, args.steps // 2)):
+    e2e_times = []
+    for _ in range(max(2, args.steps)):
+        barrier()
+        t0 = time.perf_counter()
         emb = e2e_step()
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 2)
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.median(e2e_times))     # each step is a whole fit through the public API
     h2d = store_h2d[0] + sum(a.numel() * 4 for a in A0) + E0.numel() * 4 + \
         sum(v.numel() * 4 for v in B0.values()) + sum(v.numel() * 4 for v in D0.values())
     d2h = emb.numel() * 4 + iters * (eng.nb + 1 + len(eng.names)) * 8
     e2e = {"value": ws * C / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1000.0}
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1000.0,
+           "ms_steps": [round(t * 1000.0, 1) for t in e2e_times], "statistic": "median"}
     if rank != 0:
         return
     cpu = None
@@ -368,6 +380,7 @@ def gb300_arm(args, rank, local, ws):
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "plain_fp32": plain,
             "clocks": clk.summary(), "kernel_ms": {k: round(v["mean_ms"], 4) for k, v in kt.items()},
+            "autotune": autotune_summary(),
             "loss_final": float(m.engine.losses(hist[-1], eng.tensor_norms())[0])}
     print(json.dumps(line), flush=True)
 

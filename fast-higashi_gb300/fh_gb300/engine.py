@@ -120,7 +120,9 @@ class FitEngine:
         self.U = torch.zeros(max(self.u_size, 1), dtype=f32, device=dev)
         self.Y = torch.zeros((self.nb, self.ld, self.rp), dtype=f32, device=dev)
         self.S = torch.zeros((self.Ct, self.rp), dtype=f32, device=dev)
-        self.splits = max(self.xg_splits(self.C, self.rows), self.xg_splits(self.Ct, self.rows))
+        # room for the autotuner's largest split candidate (four times the heuristic)
+        self.splits = 4 * max(self.xg_splits(self.C, self.rows), self.xg_splits(self.Ct, self.rows))
+        self._tuned = {}
         if self.bf16:
             self.E2 = torch.zeros((self.Ct, 2 * self.rp), dtype=torch.bfloat16, device=dev)
             self.G2 = torch.zeros((self.rows, 2 * self.rp), dtype=torch.bfloat16, device=dev)
@@ -326,10 +328,26 @@ class FitEngine:
             self.max_rank, P(self.W), P(self.A), self.ld, P(self.B), P(self.D), self.ld, self.R,
             self.rp, P(self.U), P(self.Gt), P(self.ssum), P(self.status), self.sp()))
 
+    def tuned_splits(self, n_cells):
+        """Split count of the X G^T pass over n_cells: the autotuner's pick among the
+        heuristic, half, twice and four times it (autotune.py), timed on this engine's own
+        buffers at the first call (an eager one: graph capture comes after the first pass)."""
+        if n_cells not in self._tuned:
+            from . import autotune
+            h = self.xg_splits(n_cells, self.rows)
+            cands = [h] + [v for v in (max(1, h // 2), 2 * h, 4 * h) if v <= self.partial.shape[0]]
+            sig = (self.precision, n_cells, self.rows, self.rp)
+            dev = self.torch.cuda.get_device_name(self.device)
+            self._tuned[n_cells] = autotune.default_tuner().choose(
+                dev, "xg_splits", sig, cands,
+                lambda v: self.x_times_g(0, self.rows, n_cells, self.Gt, self.rp, v, self.partial,
+                                         self.S, self.G2 if self.bf16 else None))
+        return self._tuned[n_cells]
+
     def xg(self, n_cells):
+        splits = self.tuned_splits(n_cells)
         self._timed("xg", lambda: self.x_times_g(0, self.rows, n_cells, self.Gt, self.rp,
-                                                 self.xg_splits(n_cells, self.rows),
-                                                 self.partial, self.S,
+                                                 splits, self.partial, self.S,
                                                  self.G2 if self.bf16 else None))
 
     def meta_polar(self, n_cells, E_out):

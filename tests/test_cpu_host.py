@@ -81,3 +81,40 @@ def test_synthetic_generator_is_seeded():
     assert (np.abs(i[0] - i[1]) <= w.band).all()
     key = (i[0].astype(np.int64) * s[1] + i[1]) * s[2] + i[2]
     assert (np.diff(key) > 0).all()          # sorted by (row, col, cell), unique
+
+
+def test_autotuner_picks_fastest_and_caches(tmp_path):
+    from fh_gb300.autotune import Tuner
+    cost = {4: 3.0, 2: 1.0, 8: 2.0}
+    calls = []
+
+    def timer(fn, reps):
+        fn()
+        return cost[calls[-1]]
+
+    def run(c):
+        calls.append(c)
+
+    path = str(tmp_path / "tune.json")
+    t = Tuner(path=path, enabled=True, timer=timer)
+    assert t.choose("dev", "xg_splits", (10, 20), [4, 2, 8, 2], run) == 2
+    assert sorted(set(calls)) == [2, 4, 8]
+    n = len(calls)
+    assert t.choose("dev", "xg_splits", (10, 20), [4, 2, 8], run) == 2   # memory cache
+    assert len(calls) == n
+    t2 = Tuner(path=path, enabled=True, timer=timer)                     # file cache
+    assert t2.choose("dev", "xg_splits", (10, 20), [4, 2, 8], run) == 2
+    assert len(calls) == n
+    # ties keep the earlier candidate (the heuristic is listed first)
+    cost.update({4: 1.0})
+    assert Tuner(path="", enabled=True, timer=timer).choose("dev", "k", (1,), [4, 2], run) == 4
+
+
+def test_autotuner_disabled_keeps_heuristic():
+    from fh_gb300.autotune import Tuner
+
+    def run(c):
+        raise AssertionError("no timing when tuning is off")
+
+    t = Tuner(path="", enabled=False, timer=lambda fn, reps: fn())
+    assert t.choose("dev", "xg_splits", (1,), [7, 3, 14], run) == 7
