@@ -152,6 +152,12 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM traffic per launch / algorithmic X bytes of the tensor-core X passes, from an ncu capture
+# of the 2,000-cell workload (profiles/xpass_bf16_kernel_c2.md); the bench scales it by the X
+# bytes of its own workload (traffic grows with cells x band rows).
+XPASS_TRAFFIC_RATIO = {"xe": (2.447e9 + 74.7e6) / 2.412e9, "xg": (2.497e9 + 8.7e6) / 2.412e9}
+
+
 def autotune_summary():
     """The schedules the autotuner timed in this process: {knob and shape: candidate -> ms,
     choice}."""
@@ -318,8 +324,10 @@ def gb300_arm(args, rank, local, ws):
     fam = max(("xe", "xg"), key=lambda k: kt.get(k, {}).get("total_ms", 0))
     dom = max(kt, key=lambda k: kt[k]["total_ms"])
     ach = xbytes / (kt[fam]["mean_ms"] / 1000.0) / 1e9
+    traffic = (XPASS_TRAFFIC_RATIO[fam] * xbytes / 1e9) if eng.precision == "bf16x2" else None
     roof = {"kernel": fam, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-            "frac": ach / hbm, "peak_kind": peak_kind, "traffic": None,
+            "frac": ach / hbm, "peak_kind": peak_kind, "traffic": traffic,
+            "traffic_unit": "GB per launch (ncu at 2,000 cells, scaled by cells x band rows)",
             "algorithmic_bytes_per_launch": xbytes,
             "note": ("X pass (%d cells x %d band rows %s); kernel share of the step: %s; "
                      "largest family: %s" % (C, eng.rows, eng.precision,
