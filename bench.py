@@ -153,8 +153,8 @@ class Clocks:
 
 
 # DRAM traffic per launch / algorithmic X bytes of the tensor-core X passes, from an ncu capture
-# of the 2,000-cell workload (profiles/xpass_bf16_kernel_c2.md); the bench scales it by the X
-# bytes of its own workload (traffic grows with cells x band rows).
+# (dram__bytes_read.sum + dram__bytes_write.sum) of the fit's passes at 2,000 cells x 301,461
+# band rows; the bench scales it by the X bytes of its own workload (cells x band rows).
 XPASS_TRAFFIC_RATIO = {"xe": (2.447e9 + 74.7e6) / 2.412e9, "xg": (2.497e9 + 8.7e6) / 2.412e9}
 
 
