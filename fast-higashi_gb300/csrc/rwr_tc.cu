@@ -352,6 +352,19 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
           mma_bf16(tmem, pl, zh, idesc, 1u);
         }
       }
+      if (ep == 0) {
+        // the next item's contact segment into L2 while this item's first
+        // epoch runs on the tensor cores (issued above)
+        const int64_t nitem = item + gridDim.x;
+        if (nitem < items) {
+          const int tn = (int)(nitem / a.n_cells), cn = (int)(nitem - (int64_t)tn * a.n_cells);
+          const int64_t f0 = a.offsets[(int64_t)tn * a.n_cells + cn];
+          const int64_t f1 = a.offsets[(int64_t)tn * a.n_cells + cn + 1];
+          const char* seg = reinterpret_cast<const char*>(a.entries + f0);
+          for (int64_t off = (int64_t)tid * 128; off < (f1 - f0) * 8; off += kRtThreads * 128)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(seg + off));
+        }
+      }
       if (!mma_wait()) { ok = false; break; }
       const bool last = ep == epochs - 1;
       if (last) __syncthreads();   // nobody reads Z any more: the staging may overwrite it
