@@ -341,3 +341,66 @@ def test_recon_grad_central_differences_2000_cells():
     for name, g, fd, scale in checks:
         assert abs(g - fd) <= 1e-5 * scale, (name, g, fd, scale)
     assert math.isfinite(worst)
+
+
+@pytest.mark.parametrize("rp,C,rows", [(16, 70, 1013), (32, 64, 4096), (64, 129, 777)])
+def test_recon_kernels_on_ragged_shapes(rp, C, rows):
+    """fh_recon_loss_f32 / fh_recon_loss_bwd_f32 against float64 torch on random inputs whose
+    cells and band rows are not multiples of the 64 x 64 tile (padding past `rows` is NaN)."""
+    g = torch.Generator(device="cpu").manual_seed(rp + C)
+    ldx = ((rows + 127) // 128) * 128
+    X = torch.full((C, ldx), float("nan"))
+    X[:, :rows] = torch.rand((C, rows), generator=g)
+    Xp = torch.full((C, ldx), float("nan"))
+    Xp[:, :rows] = torch.randn((C, rows), generator=g)
+    Gt = torch.randn((rows, rp), generator=g) * 0.1
+    E = torch.randn((C, rp), generator=g) * 0.1
+    w = torch.rand(C, dtype=F64, generator=g)
+    X, Xp, Gt, E, w = (t.to(CUDA) for t in (X, Xp, Gt, E, w))
+    nbytes = _lib.value("fh_recon_workspace", C, rows, rp)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=CUDA)
+    loss = torch.empty(C, dtype=F64, device=CUDA)
+    _lib.call("fh_recon_loss_f32", P(X), ldx, C, rows, P(Gt), P(E), rp, P(loss), P(ws), nbytes, sp())
+    dE = torch.empty((C, rp), device=CUDA)
+    dGt = torch.empty((rows, rp), device=CUDA)
+    drp = torch.empty(1, dtype=F64, device=CUDA)
+    loss2 = torch.empty(C, dtype=F64, device=CUDA)
+    _lib.call("fh_recon_loss_bwd_f32", P(X), P(Xp), ldx, C, rows, P(Gt), P(E), rp, P(w), P(loss2),
+              P(dE), P(dGt), P(drp), P(ws), nbytes, sp())
+    torch.cuda.synchronize()
+    X64, Xp64 = X[:, :rows].double(), Xp[:, :rows].double()
+    Res = X64 - E.double() @ Gt.double().T
+    assert rel(loss, (Res ** 2).sum(1)) < 1e-6
+    assert torch.equal(loss, loss2)
+    assert rel(dE, -2 * w[:, None] * (Res @ Gt.double())) < 1e-5
+    assert rel(dGt, -2 * (Res * w[:, None]).T @ E.double()) < 1e-5
+    ref = 2 * (w * (Res * Xp64).sum(1)).sum()
+    assert abs(float(drp) - float(ref)) <= 1e-5 * float(2 * (w * (Res.abs() * Xp64.abs()).sum(1)).sum())
+
+
+def test_rwr_grad_zero_epochs_and_zero_walk_weight():
+    """With no epochs X = A and dX/drp = 0; with rp = 0 one epoch gives X = A and
+    dX/drp = P A - A."""
+    from fh_gb300.engine import FitEngine
+    z = G.load("rwr_tiles.npz")
+    ds = datasets_from(z, resolution=1000000)
+    for epochs in (0, 1):
+        eng = FitEngine(ds, 4, {d.chrom: 2 for d in ds}, [epochs] * len(ds), CUDA)
+        X = torch.empty((eng.Ct, eng.ldx), device=CUDA)
+        Xp = torch.empty_like(X)
+        rp = 0.0 if epochs else 0.5
+        _lib.call("fh_rwr_grad_f32", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
+                  eng.max_width, P(eng.store.entries), P(eng.store.offsets), rp, P(X), P(Xp),
+                  eng.ldx, P(eng.status), sp())
+        X0 = rwr_rp(eng, 0.0) if epochs else eng.X
+        torch.cuda.synchronize()
+        eng.check_status("rwr_grad")
+        assert torch.equal(X[:, :eng.rows], X0[:, :eng.rows])
+        if epochs == 0:
+            assert float(Xp[:, :eng.rows].abs().max()) == 0.0
+        else:
+            # dX/drp at rp = 0 after one epoch: P A - A = (X(rp) - A) / rp for any rp (linear)
+            Xh = rwr_rp(eng, 0.25)
+            torch.cuda.synchronize()
+            ref = (Xh[:, :eng.rows].double() - X0[:, :eng.rows].double()) / 0.25
+            assert rel(Xp[:, :eng.rows], ref) < 1e-5
