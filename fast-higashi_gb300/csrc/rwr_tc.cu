@@ -280,8 +280,11 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     }
     __syncthreads();
     for (int q0 = 32 * h; q0 < 32 * h + 32; q0 += 16) {
-      float d[16], unused[16], pv[16];
-      tmem_ld16x2(tD + q0, tD + q0, d, unused);
+      // S2 from D; S1 = A[p][s0 + q] from A's fp32 copy in TMEM when the 16-column window
+      // lies inside A's 256 columns (else from the smem planes, same values)
+      const bool in_tm = s0 + q0 + 16 <= kRtMaxPad;
+      float d[16], a1v[16], pv[16];
+      tmem_ld16x2(tD + q0, in_tm ? tA + s0 + q0 : tA, d, a1v);
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
         const int q = q0 + e;
@@ -292,7 +295,7 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
             v = (p == q) ? 1.f / (1.f + kRtEps) : 0.f;   // zero column: unit diagonal
           } else {
             const float s2 = (p == q) ? 0.f : d[e];
-            const float a1 = ld_split(Zhi, Zlo, sw_off(p, s0 + q));
+            const float a1 = in_tm ? a1v[e] : ld_split(Zhi, Zlo, sw_off(p, s0 + q));
             v = fmaf(a1, fac[q], s2 * fac[128 + q]) * fl;
           }
         }
