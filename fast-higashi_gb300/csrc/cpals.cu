@@ -61,7 +61,24 @@ enum CpRowMode { kRowsNorm = 0, kRowsAB = 1, kRowsD = 2, kRowsScale = 3, kRowsGr
 enum CpSmallMode { kSmallInit = 0, kSmallB = 1, kSmallD = 2, kSmallCore = 3 };
 
 __host__ __device__ inline size_t cp_pstride(int ld) { return (size_t)2 * ld * ld + 2; }
-constexpr size_t kCpRowsSmem = 4 * (size_t)kCpMaxR * kCpLz * sizeof(float);
+constexpr int kCpLy = kCpMaxR + 4;  // row stride of the Y tiles (16-byte rows for cp.async)
+constexpr size_t kCpRowsSmem =
+    (2 * (size_t)kCpMaxR * kCpLy + 4 * (size_t)kCpMaxR * kCpLz) * sizeof(float);
+
+// sum over k < nk of p[k * stride], in increasing k (the loads go out eight at a time)
+__device__ __forceinline__ float chunk_sum(const float* p, size_t stride, int nk) {
+  float s = 0.f;
+  int k = 0;
+  for (; k + 8 <= nk; k += 8) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = p[(size_t)(k + u) * stride];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s += v[u];
+  }
+  for (; k < nk; ++k) s += p[(size_t)k * stride];
+  return s;
+}
 
 // acc[u][v] = sum_k fa(w + 8u, k) fb(k, lane + 32v) over k < K for 256 threads (rows w + 8u,
 // u < 8; columns lane + 32 v, v < 2), rows / columns clamped to M-1 / N-1.
@@ -90,12 +107,14 @@ __device__ __forceinline__ void cp_mm(int M, int N, int K, FA fa, FB fb, float (
 
 __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode) {
   extern __shared__ __align__(16) float cps[];
-  float* Ys = cps;                        // Y_g (r x R)
-  float* Fs = Ys + kCpMaxR * kCpLz;       // D (R x r) or B (r x r)
+  float* Yb = cps;                        // two Y_g tiles (r x RP, stride kCpLy): row i, row i+1
+  float* Fs = Yb + 2 * kCpMaxR * kCpLy;   // D (R x r) or B (r x r)
   float* Bs = Fs + kCpMaxR * kCpLz;       // B (mode AB)
   float* Zs = Bs + kCpMaxR * kCpLz;       // Y_g D (r x r)
+  float* Ls = Zs + kCpMaxR * kCpLz;       // the A-row system's inverse (mode AB)
   __shared__ float rhs[kCpMaxR];
   __shared__ float ysol[kCpMaxR];
+  __shared__ float red4[4][kCpMaxR];
   __shared__ double dred[32];
   const int k = blockIdx.x;
   const int ci = a.k_chrom[k];
@@ -121,24 +140,38 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
           for (int i = 0; i < nrow; ++i) s = fmaf(a.A[(row0 + i) * ld + p], a.A[(row0 + i) * ld + q], s);
         out[p * ld + q] = s;
       }
-    float ys = 0.f;
-    for (int i = 0; i < nrow; ++i) {
-      const float* Yg = a.Y + (row0 + i) * (int64_t)a.ldy * a.RP;
-      for (int j = ty; j < r; j += 8)
-        for (int m = tx; m < R; m += 32) ys = fmaf(Yg[(int64_t)j * a.RP + m], Yg[(int64_t)j * a.RP + m], ys);
+    // ||Y||^2 of the chunk's rows as one contiguous run, four floats per load
+    float ys[4] = {0.f, 0.f, 0.f, 0.f};
+    const int64_t per = (int64_t)a.ldy * a.RP;
+    const float* Y0 = a.Y + row0 * per;
+#pragma unroll 4
+    for (int64_t e = (int64_t)tid * 4; e < nrow * per; e += kCpThreads * 4) {
+      const float4 v = *reinterpret_cast<const float4*>(Y0 + e);
+      const int64_t wv = e % per;
+      const int j = (int)(wv / a.RP), m = (int)(wv % a.RP);
+      if (j < r) {
+        const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (m + u < R) ys[u] = fmaf(vv[u], vv[u], ys[u]);
+      }
     }
-    const double ysd = block_sum<double>((double)ys, dred);
+    const double ysd = block_sum<double>((double)((ys[0] + ys[1]) + (ys[2] + ys[3])), dred);
     if (tid == 0) reinterpret_cast<double*>(out + 2 * ld * ld)[0] = ysd;
     return;
   }
   // ---- mode AB (solve the A rows, then the partials of A^T A and MTTKRP_B) or D
   const float* Dc = a.D + (size_t)ci * a.RP * ld;
   const float* Bc = a.B + (size_t)ci * ld * ld;
+  const float* Lc = a.L + (size_t)ci * ld * ld;
   if (mode == kRowsAB) {
     for (int m = ty; m < R; m += 8)
       for (int q = tx; q < r; q += 32) Fs[m * lz + q] = Dc[m * ld + q];
     for (int j = ty; j < r; j += 8)
-      for (int q = tx; q < r; q += 32) Bs[j * lz + q] = Bc[j * ld + q];
+      for (int q = tx; q < r; q += 32) {
+        Bs[j * lz + q] = Bc[j * ld + q];
+        Ls[j * lz + q] = Lc[j * ld + q];
+      }
   } else {
     for (int j = ty; j < r; j += 8)
       for (int q = tx; q < r; q += 32) Fs[j * lz + q] = Bc[j * ld + q];
@@ -148,19 +181,30 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
   for (int v = 0; v < 2; ++v)
 #pragma unroll
     for (int u = 0; u < 8; ++u) pA[v][u] = pB[v][u] = 0.f;
-  const float* Lc = a.L + (size_t)ci * ld * ld;
-  __syncthreads();
+  // Y_g tiles through a two-deep cp.async ring: row i + 1 loads while row i is used
+  const int q4 = a.RP / 4;
+  auto load_y = [&](int i) {
+    const float* Yg = a.Y + (row0 + i) * (int64_t)a.ldy * a.RP;
+    float* dst = Yb + (i & 1) * kCpMaxR * kCpLy;
+    for (int idx = tid; idx < r * q4; idx += kCpThreads) {
+      const int j = idx / q4, c = idx - j * q4;
+      cp_async16(dst + j * kCpLy + 4 * c, Yg + (int64_t)j * a.RP + 4 * c, true);
+    }
+    cp_async_commit();
+  };
+  if (nrow > 0) load_y(0);
   for (int i = 0; i < nrow; ++i) {
     const int64_t g = row0 + i;
-    const float* Yg = a.Y + g * (int64_t)a.ldy * a.RP;
-    for (int j = ty; j < r; j += 8)
-      for (int m = tx; m < R; m += 32) Ys[j * lz + m] = Yg[(int64_t)j * a.RP + m];
+    if (i + 1 < nrow) { load_y(i + 1); cp_async_wait<1>(); }
+    else cp_async_wait<0>();
     __syncthreads();
+    const float* Ys = Yb + (i & 1) * kCpMaxR * kCpLy;
+    const int ly = kCpLy;
     if (mode == kRowsAB) {
       // Z[j][q] = sum_m Y[j][m] D[m][q]
       {
         float zc[8][2];
-        cp_mm(r, r, R, [&](int j, int m) { return Ys[j * lz + m]; },
+        cp_mm(r, r, R, [&](int j, int m) { return Ys[j * ly + m]; },
               [&](int m, int q) { return Fs[m * lz + q]; }, zc);
 #pragma unroll
         for (int u = 0; u < 8; ++u)
@@ -171,16 +215,28 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
           }
       }
       __syncthreads();
-      if (tid < r) {
+      // rhs[q] = sum_j B[j][q] Z[j][q]: four partial sums per column, then their sum
+      {
+        const int q = tid & 63, part = tid >> 6;
         float s = 0.f;
-        for (int j = 0; j < r; ++j) s = fmaf(Bs[j * lz + tid], Zs[j * lz + tid], s);
-        rhs[tid] = s;
+        if (q < r)
+          for (int j = part; j < r; j += 4) s = fmaf(Bs[j * lz + q], Zs[j * lz + q], s);
+        red4[part][q] = s;
       }
       __syncthreads();
+      if (tid < r) rhs[tid] = (red4[0][tid] + red4[1][tid]) + (red4[2][tid] + red4[3][tid]);
+      __syncthreads();
       // A_g = G_A^{-1} rhs with the inverse the per-chromosome kernel left in L
-      if (tid < r) {
+      {
+        const int p = tid & 63, part = tid >> 6;
         float s = 0.f;
-        for (int q = 0; q < r; ++q) s = fmaf(Lc[tid * ld + q], rhs[q], s);
+        if (p < r)
+          for (int q = part; q < r; q += 4) s = fmaf(Ls[p * lz + q], rhs[q], s);
+        red4[part][p] = s;
+      }
+      __syncthreads();
+      if (tid < r) {
+        const float s = (red4[0][tid] + red4[1][tid]) + (red4[2][tid] + red4[3][tid]);
         ysol[tid] = s;
         a.A[g * ld + tid] = s;
       }
@@ -203,8 +259,11 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
     } else {
       // MTTKRP_D[m][q] += A[q] * sum_j Y[j][m] B[j][q]
       const float* Ag = a.A + g * ld;
+      float ag[2];
+#pragma unroll
+      for (int v = 0; v < 2; ++v) ag[v] = tx + 32 * v < r ? Ag[tx + 32 * v] : 0.f;
       float yb[8][2];
-      cp_mm(R, r, r, [&](int m, int j) { return Ys[j * lz + m]; },
+      cp_mm(R, r, r, [&](int m, int j) { return Ys[j * ly + m]; },
             [&](int j, int q) { return Fs[j * lz + q]; }, yb);
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
@@ -213,7 +272,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
 #pragma unroll
           for (int v = 0; v < 2; ++v) {
             const int q = tx + 32 * v;
-            if (q < r) pA[v][u] = fmaf(Ag[q], yb[u][v], pA[v][u]);
+            if (q < r) pA[v][u] = fmaf(ag[v], yb[u][v], pA[v][u]);
           }
         }
       }
@@ -310,12 +369,16 @@ __device__ void cp_apply_inverse(const float* RHS, int ldr, int nrhs, const floa
 
 // Gram F^T F of an (nrows x r, stride ld) factor into G (stride ld), fp32.
 __device__ void cp_gram(const float* F, int nrows, int r, int ld, float* G) {
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int p = ty; p < r; p += 8)
-    for (int q = tx; q < r; q += 32) {
-      float s = 0.f;
-      for (int i = 0; i < nrows; ++i) s = fmaf(F[i * ld + p], F[i * ld + q], s);
-      G[p * ld + q] = s;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  float acc[8][2];
+  cp_mm(r, r, nrows, [&](int p, int i) { return F[i * ld + p]; },
+        [&](int i, int q) { return F[i * ld + q]; }, acc);
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int p = w + 8 * u, q = l + 32 * v;
+      if (p < r && q < r) G[p * ld + q] = acc[u][v];
     }
 }
 
@@ -344,9 +407,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
   if (mode == kSmallCore) {
     for (int p = ty; p < r; p += 8)
       for (int q = tx; q < r; q += 32) {
-        float s = 0.f;
-        for (int k = 0; k < nk; ++k) s += a.part[(k0 + k) * ps + p * ld + q];
-        gAA[p * ld + q] = s;
+        gAA[p * ld + q] = chunk_sum(a.part + k0 * ps + p * ld + q, ps, nk);
       }
     cp_gram(Bc, r, r, ld, gBB);
     cp_gram(Dc, R, r, ld, gDD);
@@ -361,11 +422,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
   }
   if (mode == kSmallInit) {
     // column norms of A, ||Y||^2, then balance (parafac_integrative.py:19-27, :65)
-    if (tid < r) {
-      float s = 0.f;
-      for (int k = 0; k < nk; ++k) s += a.part[(k0 + k) * ps + tid * ld + tid];
-      nA[tid] = sqrtf(s);
-    }
+    if (tid < r) nA[tid] = sqrtf(chunk_sum(a.part + k0 * ps + tid * ld + tid, ps, nk));
     if (tid == 0) {
       double s = 0.0;
       for (int k = 0; k < nk; ++k)
@@ -386,11 +443,8 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
     // A^T A, MTTKRP_B; G_B = A^T A * D^T D + 1e-10 I; B <- MTTKRP_B G_B^{-1}
     for (int p = ty; p < r; p += 8)
       for (int q = tx; q < r; q += 32) {
-        float s = 0.f, t = 0.f;
-        for (int k = 0; k < nk; ++k) {
-          s += a.part[(k0 + k) * ps + p * ld + q];
-          t += a.part[(k0 + k) * ps + ld * ld + p * ld + q];
-        }
+        const float s = chunk_sum(a.part + k0 * ps + p * ld + q, ps, nk);
+        const float t = chunk_sum(a.part + k0 * ps + ld * ld + p * ld + q, ps, nk);
         gAA[p * ld + q] = s;
         work[p * ld + q] = t;
         G[p * lg + q] = s * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
@@ -408,9 +462,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
     // MTTKRP_D; G_D = A^T A * B^T B + 1e-10 I; D <- MTTKRP_D G_D^{-1}; loss; balance
     for (int m = ty; m < R; m += 8)
       for (int q = tx; q < r; q += 32) {
-        float s = 0.f;
-        for (int k = 0; k < nk; ++k) s += a.part[(k0 + k) * ps + m * ld + q];
-        work[m * ld + q] = s;
+        work[m * ld + q] = chunk_sum(a.part + k0 * ps + m * ld + q, ps, nk);
       }
     for (int p = ty; p < r; p += 8)
       for (int q = tx; q < r; q += 32)
