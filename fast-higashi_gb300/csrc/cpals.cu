@@ -8,11 +8,11 @@
 //     A <- MTTKRP_A (B^T B * D^T D + 1e-10 I)^{-1}   (and likewise for B, D)
 //     MTTKRP_A[i] = sum_j B[j] * (Y_i D)[j],   MTTKRP_B = sum_i A_i (x) (Y_i D),
 //     MTTKRP_D   = sum_i A_i (x) (Y_i^T B)      ((x): column-wise product).
-// The r x r systems are factored by Cholesky in fp32, the reference's own precision
-// (parafac_integrative.py:12-15 solves in fp32), and applied through the inverse
-// (L L^T)^{-1} = L^{-T} L^{-1} formed once per chromosome, so every right-hand side is a
-// register-tiled product instead of a serial substitution: this GB300 runs fp64 at
-// ~0.33 TFLOP/s, so fp64 is kept to the scalar sums (loss, core norm).  The reconstruction loss needs no Xhat:
+// The r x r systems (symmetric positive definite) are inverted in fp32, the reference's own
+// precision (parafac_integrative.py:12-15 solves in fp32), by Gauss-Jordan without pivoting
+// once per chromosome, so every right-hand side is a register-tiled product instead of a
+// serial substitution: this GB300 runs fp64 at ~0.33 TFLOP/s, so fp64 is kept to the scalar
+// sums (loss, core norm).  The reconstruction loss needs no Xhat:
 // ||Xhat||^2 = sum(A^TA * B^TB * D^TD) and <Xhat, Y> = sum(D * MTTKRP_D) with the final
 // A, B.  balance_norm (unit columns, the product of the column norms folded into D) follows
 // each sweep unless the relative loss change fell below 1e-5, as the reference breaks before
@@ -297,58 +297,44 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
   }
 }
 
-// Cholesky of G (r x r, stride lg, odd) in place into its lower triangle (fp32).
-__device__ bool cp_cholesky(float* G, int r, int lg) {
+// Gi = G^{-1} for an SPD G (r x r, stride lg) by in-place Gauss-Jordan without pivoting (the
+// sweep operator; the pivots of an SPD matrix are positive).  Two barriers per pivot, against
+// three per column for the Cholesky factor plus a serial triangular inverse.  scratch:
+// 2 * kCpMaxR floats.  Returns false on a pivot that is not positive (in every thread).
+__device__ bool cp_spd_inverse(const float* G, int r, int lg, float* scratch, float* Gi) {
   __shared__ int bad;
-  if (threadIdx.x == 0) bad = 0;
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  float* prow = scratch;
+  float* pcol = scratch + kCpMaxR;
+  if (tid == 0) bad = 0;
+  for (int p = ty; p < r; p += 8)
+    for (int q = tx; q < r; q += 32) Gi[p * lg + q] = G[p * lg + q];
   __syncthreads();
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int k = 0; k < r; ++k) {
-    if (threadIdx.x == 0) {
-      float d = G[k * lg + k];
-      if (!(d > 0.f)) { bad = 1; d = 1e-30f; }
-      G[k * lg + k] = sqrtf(d);
+    if (tid < r) {
+      prow[tid] = Gi[k * lg + tid];
+      pcol[tid] = Gi[tid * lg + k];
     }
     __syncthreads();
-    const float dk = G[k * lg + k];
-    for (int p = k + 1 + threadIdx.x; p < r; p += blockDim.x) G[p * lg + k] /= dk;
-    __syncthreads();
-    for (int p = k + 1 + ty; p < r; p += 8) {
-      const float gp = G[p * lg + k];
-      for (int q = k + 1 + tx; q <= p; q += 32) G[p * lg + q] = fmaf(-gp, G[q * lg + k], G[p * lg + q]);
+    float d = prow[k];
+    if (!(d > 0.f)) {
+      d = 1e-30f;
+      if (tid == 0) bad = 1;
+    }
+    const float inv = 1.f / d;
+    for (int p = ty; p < r; p += 8) {
+      const float cp = pcol[p] * inv;
+      for (int q = tx; q < r; q += 32) {
+        float v;
+        if (p == k) v = (q == k) ? inv : prow[q] * inv;
+        else if (q == k) v = -cp;
+        else v = fmaf(-cp, prow[q], Gi[p * lg + q]);
+        Gi[p * lg + q] = v;
+      }
     }
     __syncthreads();
   }
   return bad == 0;
-}
-
-// Gi = (L L^T)^{-1} from the Cholesky factor L (lower, stride lg): Li = L^{-1} by forward
-// substitution (one warp per column), then Gi = Li^T Li.  Li, Gi: r x lg scratch.
-__device__ void cp_chol_inverse(const float* L, int r, int lg, float* Li, float* Gi) {
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  for (int j = w; j < r; j += 8) {
-    for (int i = l; i < r; i += 32) Li[i * lg + j] = 0.f;
-    __syncwarp();
-    for (int i = j; i < r; ++i) {
-      float d = 0.f;
-      for (int q = j + l; q < i; q += 32) d = fmaf(L[i * lg + q], Li[q * lg + j], d);
-      d = warp_sum(d);
-      if (l == 0) Li[i * lg + j] = ((i == j ? 1.f : 0.f) - d) / L[i * lg + i];
-      __syncwarp();
-    }
-  }
-  __syncthreads();
-  float acc[8][2];
-  cp_mm(r, r, r, [&](int p, int i) { return Li[i * lg + p]; },
-        [&](int i, int q) { return Li[i * lg + q]; }, acc);
-#pragma unroll
-  for (int u = 0; u < 8; ++u)
-#pragma unroll
-    for (int v = 0; v < 2; ++v) {
-      const int p = w + 8 * u, q = l + 32 * v;
-      if (p < r && q < r) Gi[p * lg + q] = acc[u][v];
-    }
-  __syncthreads();
 }
 
 // out rows = RHS rows G^{-1} (RHS: nrhs x r, stride ldr, nrhs <= 64; Gi symmetric, stride lg).
@@ -388,8 +374,8 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
   const int r = a.c_rank[ci], R = a.R, ld = a.ld;
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   const int lg = ld + 1;                  // odd stride: column walks hit distinct banks
-  float* G = sf;                          // ld x lg: the system, then its Cholesky factor
-  float* Li = G + ld * lg;                // ld x lg: L^{-1}
+  float* G = sf;                          // ld x lg: the system
+  float* Li = G + ld * lg;                // ld x lg: scratch of the inverse (two rows used)
   float* Gi = Li + ld * lg;               // ld x lg: the system's inverse
   float* work = Gi + ld * lg;             // RP*ld
   __shared__ double dred[32];
@@ -450,9 +436,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
         G[p * lg + q] = s * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
       }
     __syncthreads();
-    if (!cp_cholesky(G, r, lg) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
-    __syncthreads();
-    cp_chol_inverse(G, r, lg, Li, Gi);
+    if (!cp_spd_inverse(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
     cp_apply_inverse(work, ld, r, Gi, r, lg, Bc, ld);
     __syncthreads();
     cp_gram(Bc, r, r, ld, gBB);
@@ -468,9 +452,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
       for (int q = tx; q < r; q += 32)
         G[p * lg + q] = gAA[p * ld + q] * gBB[p * ld + q] + (p == q ? 1e-10f : 0.f);
     __syncthreads();
-    if (!cp_cholesky(G, r, lg) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
-    __syncthreads();
-    cp_chol_inverse(G, r, lg, Li, Gi);
+    if (!cp_spd_inverse(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
     cp_apply_inverse(work, ld, R, Gi, r, lg, Dc, ld);
     __syncthreads();
     cp_gram(Dc, R, r, ld, gDD);
@@ -524,9 +506,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
     for (int q = tx; q < r; q += 32)
       G[p * lg + q] = gBB[p * ld + q] * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
   __syncthreads();
-  if (!cp_cholesky(G, r, lg) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
-  __syncthreads();
-  cp_chol_inverse(G, r, lg, Li, Gi);
+  if (!cp_spd_inverse(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
   for (int p = ty; p < r; p += 8)
     for (int q = tx; q < r; q += 32) Lc[p * ld + q] = Gi[p * lg + q];
 }
