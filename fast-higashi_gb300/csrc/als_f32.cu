@@ -189,13 +189,14 @@ __global__ void __launch_bounds__(256) project_y_kernel(const fh_tile* __restric
                                                         const float* __restrict__ U,
                                                         const float* __restrict__ W,
                                                         float* __restrict__ Y, int ldy_l) {
-  constexpr int JC = 32;
-  __shared__ __align__(16) float Us[JC][kMaxRank + 1];
-  __shared__ __align__(16) float Ws[JC][RP];
+  constexpr int JC = RP >= 128 ? 32 : 64;   // band columns per staged chunk
+  __shared__ __align__(16) float Uf[JC * RP];  // U_g rows j0.. (r <= RP floats each, packed)
+  __shared__ __align__(16) float Ws[JC * RP];
   const int g = blockIdx.x;
   const fh_tile T = tiles[row_tile[g]];
   const int i = (int)(g - T.brow0);
   const int n = T.width, r = T.rank;
+  if (r > RP) return;                        // the staged U rows hold at most RP values
   const float* Ug = U + T.uoff + (int64_t)i * n * r;
   const float* Wg = W + (T.xoff + (int64_t)i * n) * RP;
   const int tid = threadIdx.x;
@@ -210,24 +211,24 @@ __global__ void __launch_bounds__(256) project_y_kernel(const fh_tile* __restric
     for (int b = 0; b < MPT; ++b) acc[a][b] = 0.f;
   for (int j0 = 0; j0 < n; j0 += JC) {
     const int jn = min(JC, n - j0);
-    for (int idx = tid; idx < JC * r; idx += 256) {
-      const int jj = idx / r, l = idx % r;
-      Us[jj][l] = jj < jn ? Ug[(int64_t)(j0 + jj) * r + l] : 0.f;
-    }
-    for (int idx = tid; idx < JC * RP; idx += 256) {
-      const int jj = idx / RP, m = idx % RP;
-      Ws[jj][m] = jj < jn ? Wg[(int64_t)(j0 + jj) * RP + m] : 0.f;
-    }
+    // both chunks are contiguous runs in global memory: U_g rows of r floats, W rows of RP
+    const float* us = Ug + (int64_t)j0 * r;
+#pragma unroll 4
+    for (int idx = tid; idx < jn * r; idx += 256) Uf[idx] = us[idx];
+    const float4* ws = reinterpret_cast<const float4*>(Wg + (int64_t)j0 * RP);
+#pragma unroll 4
+    for (int idx = tid; idx < jn * (RP / 4); idx += 256)
+      reinterpret_cast<float4*>(Ws)[idx] = ws[idx];
     __syncthreads();
     for (int jj = 0; jj < jn; ++jj) {
       float wv[MPT];
 #pragma unroll
-      for (int b = 0; b < MPT; ++b) wv[b] = Ws[jj][mg * MPT + b];
+      for (int b = 0; b < MPT; ++b) wv[b] = Ws[jj * RP + mg * MPT + b];
 #pragma unroll
       for (int a = 0; a < 8; ++a) {
         if (a < LA) {
           const int l = lg + 16 * a;
-          const float uv = l < r ? Us[jj][l] : 0.f;
+          const float uv = l < r ? Uf[jj * r + l] : 0.f;
 #pragma unroll
           for (int b = 0; b < MPT; ++b) acc[a][b] = fmaf(uv, wv[b], acc[a][b]);
         }

@@ -58,7 +58,9 @@ struct CpArgs {
 };
 
 enum CpRowMode { kRowsNorm = 0, kRowsAB = 1, kRowsD = 2, kRowsScale = 3, kRowsGram = 4 };
-enum CpSmallMode { kSmallInit = 0, kSmallB = 1, kSmallD = 2, kSmallCore = 3 };
+// kSmallDLast: the D update of a call's last sweep, whose balanced Grams and A-row inverse
+// nobody reads (the next call starts from kSmallInit).
+enum CpSmallMode { kSmallInit = 0, kSmallB = 1, kSmallD = 2, kSmallCore = 3, kSmallDLast = 4 };
 
 __host__ __device__ inline size_t cp_pstride(int ld) { return (size_t)2 * ld * ld + 2; }
 constexpr int kCpLy = kCpMaxR + 4;  // row stride of the Y tiles (16-byte rows for cp.async)
@@ -442,7 +444,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
     cp_gram(Bc, r, r, ld, gBB);
     return;
   }
-  if (mode == kSmallD) {
+  if (mode == kSmallD || mode == kSmallDLast) {
     // MTTKRP_D; G_D = A^T A * B^T B + 1e-10 I; D <- MTTKRP_D G_D^{-1}; loss; balance
     for (int m = ty; m < R; m += 8)
       for (int q = tx; q < r; q += 32) {
@@ -498,7 +500,8 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
     for (int q = tx; q < r; q += 32)
       Dc[m * ld + q] = Dc[m * ld + q] / (nD[q] + 1e-15f) * (nA[q] * nB[q] * nD[q] + 1e-15f);
   __syncthreads();
-  // Grams of the balanced factors; L_A = chol(B^T B * D^T D + 1e-10 I) for the next A rows
+  if (mode == kSmallDLast) return;
+  // Grams of the balanced factors; the inverse of B^T B * D^T D + 1e-10 I for the next A rows
   cp_gram(Bc, r, r, ld, gBB);
   cp_gram(Dc, R, r, ld, gDD);
   __syncthreads();
@@ -580,7 +583,7 @@ extern "C" int fh_cp_als(int32_t nchrom, int32_t nchunks, const int32_t* meta, f
     cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsAB);
     cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, kSmallB);
     cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsD);
-    cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, kSmallD);
+    cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, it + 1 < n_iter ? kSmallD : kSmallDLast);
   }
   cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsScale);
   FH_CHECK_LAUNCH();

@@ -209,7 +209,8 @@ int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t 
                float* partial, float* out, int* status, void* stream);
 
 /* Y[g][l][m] = sum_j U_g[j][l] W[xoff + i*width + j][m] for every bin row g (K16 tail,
- * parafac2_intergrative.py:522-529); Y: float[n_rows][ldy_l][rp]; row_tile: int32[n_rows]. */
+ * parafac2_intergrative.py:522-529); Y: float[n_rows][ldy_l][rp]; row_tile: int32[n_rows];
+ * every tile rank r <= rp (a bin row with r > rp is left untouched). */
 int fh_project_y_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n_rows,
                      const float* U, const float* W, int32_t rp, float* Y, int32_t ldy_l,
                      void* stream);
