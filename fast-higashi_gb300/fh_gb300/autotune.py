@@ -14,6 +14,10 @@ Knobs in use (fh_gb300.engine):
               more splits fill more SMs, fewer splits cut the partial-sum traffic and the
               reduction; candidates: the heuristic (fh_xg_splits / fh_xg_bf16_splits), half,
               twice and four times it.
+  cp_chunk_rows  bin rows per CTA of the CP-ALS row kernels (fh_cp_als chunk table): more
+              rows per chunk mean fewer partial sums for the per-chromosome kernel and fewer
+              CTAs; candidates 8 (the default), 4 and 16, timed as one sweep on the live
+              factors, which are restored after every run.
 """
 from __future__ import annotations
 

@@ -132,23 +132,13 @@ class FitEngine:
         self.core = torch.zeros(nchrom, dtype=f64, device=dev)
         mw = _lib.value("fh_meta_polar_workspace", self.Ct, self.R)
         self.meta_ws = torch.empty(mw, dtype=torch.uint8, device=dev)
-        # CP-ALS chunk tables (<= 8 rows, inside one chromosome)
-        c_row0, c_nbin, c_rank, c_chunk0, c_nchunk = [], [], [], [], []
-        k_chrom, k_row0, k_nrow = [], [], []
-        for ci, name in enumerate(self.names):
-            k = self.chrom_index.index(ci)
-            rs = self.ds_rows[k]
-            c_row0.append(rs.start); c_nbin.append(rs.stop - rs.start); c_rank.append(self.ranks[k])
-            c_chunk0.append(len(k_chrom))
-            for r0 in range(rs.start, rs.stop, 8):
-                k_chrom.append(ci); k_row0.append(r0); k_nrow.append(min(8, rs.stop - r0))
-            c_nchunk.append(len(k_chrom) - c_chunk0[-1])
-        self.nchunks = len(k_chrom)
-        meta = np.array(c_row0 + c_nbin + c_rank + c_chunk0 + c_nchunk + k_chrom + k_row0 + k_nrow,
-                        dtype=np.int32)
-        self.cp_meta = torch.from_numpy(meta).to(dev)
-        cw = _lib.value("fh_cp_workspace", nchrom, self.nchunks, self.ld, self.rp)
+        # CP-ALS chunk tables (<= 8 rows of one chromosome; the autotuner may pick 4 or 16)
+        self._cp_tables = {}
+        self.cp_meta, self.nchunks = self.cp_table(8)
+        n_most = self.cp_table(4)[1]
+        cw = _lib.value("fh_cp_workspace", nchrom, n_most, self.ld, self.rp)
         self.cp_ws = torch.empty(cw, dtype=torch.uint8, device=dev)
+        self._cp_tuned = False
         self.history = []
 
     # ------------------------------------------------------------------ helpers
@@ -332,6 +322,8 @@ class FitEngine:
         """Split count of the X G^T pass over n_cells: the autotuner's pick among the
         heuristic, half, twice and four times it (autotune.py), timed on this engine's own
         buffers at the first call (an eager one: graph capture comes after the first pass)."""
+        if n_cells not in self._tuned and self.torch.cuda.is_current_stream_capturing():
+            return self.xg_splits(n_cells, self.rows)
         if n_cells not in self._tuned:
             from . import autotune
             h = self.xg_splits(n_cells, self.rows)
@@ -362,8 +354,56 @@ class FitEngine:
             "fh_project_y_f32", P(self.tiles_dev), P(self.row_tile), self.nb, P(self.U),
             P(self.W), self.rp, P(self.Y), self.ld, self.sp()))
 
+    def cp_table(self, rows):
+        """CP-ALS chunk table: chunks of <= rows bin rows inside one chromosome, as the int32
+        meta block of fh_cp_als (cached per size).  Returns (device tensor, number of chunks)."""
+        if rows not in self._cp_tables:
+            c_row0, c_nbin, c_rank, c_chunk0, c_nchunk = [], [], [], [], []
+            k_chrom, k_row0, k_nrow = [], [], []
+            for ci, name in enumerate(self.names):
+                k = self.chrom_index.index(ci)
+                rs = self.ds_rows[k]
+                c_row0.append(rs.start); c_nbin.append(rs.stop - rs.start)
+                c_rank.append(self.ranks[k]); c_chunk0.append(len(k_chrom))
+                for r0 in range(rs.start, rs.stop, rows):
+                    k_chrom.append(ci); k_row0.append(r0); k_nrow.append(min(rows, rs.stop - r0))
+                c_nchunk.append(len(k_chrom) - c_chunk0[-1])
+            meta = np.array(c_row0 + c_nbin + c_rank + c_chunk0 + c_nchunk + k_chrom + k_row0 +
+                            k_nrow, dtype=np.int32)
+            self._cp_tables[rows] = (self.torch.from_numpy(meta).to(self.device), len(k_chrom))
+        return self._cp_tables[rows]
+
+    def tune_cp(self):
+        """Chunk size of the CP-ALS row kernels (bin rows per CTA): the autotuner times one
+        sweep for 8 (the default), 4 and 16 rows on the current factors, restoring them after
+        each run, and keeps the fastest.  Runs at the first CP-ALS call (an eager one)."""
+        self._cp_tuned = True
+        if self.torch.cuda.is_current_stream_capturing():
+            return
+        from . import autotune
+        P = _lib.ptr
+        state = (self.A, self.B, self.D, self.core)
+        snap = [t.clone() for t in state]
+
+        def run(rows):
+            for t, v in zip(state, snap):
+                t.copy_(v)
+            meta, nch = self.cp_table(rows)
+            _lib.call("fh_cp_als", len(self.names), nch, P(meta), P(self.A), P(self.B), P(self.D),
+                      P(self.Y), self.ld, self.rp, self.R, self.ld, 1, P(self.core), None,
+                      P(self.cp_ws), self.cp_ws.numel(), P(self.status), self.sp())
+
+        sig = (self.nb, len(self.names), self.max_rank, self.R, self.ld)
+        dev = self.torch.cuda.get_device_name(self.device)
+        rows = autotune.default_tuner().choose(dev, "cp_chunk_rows", sig, [8, 4, 16], run)
+        for t, v in zip(state, snap):
+            t.copy_(v)
+        self.cp_meta, self.nchunks = self.cp_table(rows)
+
     def cp_als(self, n_iter):
         P = _lib.ptr
+        if not self._cp_tuned:
+            self.tune_cp()
         self._timed("cp_als", lambda: _lib.call(
             "fh_cp_als", len(self.names), self.nchunks, P(self.cp_meta), P(self.A), P(self.B),
             P(self.D), P(self.Y), self.ld, self.rp, self.R, self.ld, n_iter, P(self.core), None,
