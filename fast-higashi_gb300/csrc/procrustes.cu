@@ -43,7 +43,9 @@ struct ProcArgs {
 //            scratch (rows r .. 2r), then U = Q [polar(R); 0]
 __host__ __device__ inline int proc_r0_rows(int n, int r, int rp) { return n > rp + r ? n : rp + r; }
 __host__ __device__ inline int proc_r1_rows(int n, int r, int rp) {
-  int m = n > 2 * r ? n : 2 * r;
+  // also >= 2 r ldv / ldt + 4 floats: the polar iterate and its scratch at row stride
+  // ldv = ((r + 3) & ~3) + 4 <= r + 7, 16-byte aligned
+  int m = n > 2 * r + 12 ? n : 2 * r + 12;
   return m > rp ? m : rp;
 }
 __host__ __device__ inline size_t proc_smem_floats(int n, int r, int rp) {
@@ -144,11 +146,30 @@ __global__ void __launch_bounds__(kProcThreads, 2) procrustes_qr_kernel(ProcArgs
   }
   // ---- QR, polar factor of R, sum(S)
   householder_qr(R0, n, r, ldt, s);
-  float* X = R1;
+  // polar(R) on 16-byte aligned rows of stride ldv (4 x 4 register-tiled products), then
+  // back to stride ldt in region 1 for the Q apply
+  const int ldv = ((r + 3) & ~3) + 4;
+  float* Xv = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(R1) + 15) & ~uintptr_t(15));
   for (int p = ty; p < r; p += nw)
-    for (int q = tx; q < r; q += 32) X[p * ldt + q] = q >= p ? R0[p * ldt + q] : 0.f;
+    for (int q = tx; q < r; q += 32) Xv[p * ldv + q] = q >= p ? R0[p * ldt + q] : 0.f;
   __syncthreads();
-  newton_polar_r64(X, ldt, R1 + (size_t)r * ldt, r, true, s);
+  newton_polar_r64v(Xv, ldv, Xv + (size_t)r * ldv, r, s);
+  float* X = R1;
+  {
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int idx = tid + kProcThreads * e;
+      v[e] = idx < r * r ? Xv[(idx / r) * ldv + idx % r] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int idx = tid + kProcThreads * e;
+      if (idx < r * r) X[(idx / r) * ldt + idx % r] = v[e];
+    }
+    __syncthreads();
+  }
   {
     double acc = 0.0;
     for (int p = ty; p < r; p += nw)
