@@ -111,11 +111,22 @@ __device__ inline void householder_panel(float* T, int n, int k0, int k1, int ld
     }
     __syncthreads();
     const float beta = s.beta[k], vh = s.vh[k];
-    for (int j = k + 1 + ty; j < k1; j += nw) {       // w_j = v^T T[k:, j], one warp per column
-      float d = 0.f;
-      for (int i = k + 1 + tx; i < n; i += 32) d = fmaf(T[i * ldt + k], T[i * ldt + j], d);
-      d = warp_sum(d);
-      if (tx == 0) s.wv[j] = fmaf(vh, T[k * ldt + j], d);
+    // w_j = v^T T[k:, j]: four columns per warp (independent chains, one pass over v)
+    for (int jb = k + 1 + 4 * ty; jb < k1; jb += 4 * nw) {
+      float d[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int i = k + 1 + tx; i < n; i += 32) {
+        const float vi = T[i * ldt + k];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          if (jb + c < k1) d[c] = fmaf(vi, T[i * ldt + jb + c], d[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) d[c] = warp_sum(d[c]);
+      if (tx == 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          if (jb + c < k1) s.wv[jb + c] = fmaf(vh, T[k * ldt + jb + c], d[c]);
+      }
     }
     __syncthreads();
     if (beta != 0.f) {
