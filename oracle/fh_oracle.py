@@ -79,7 +79,7 @@ def densify(rows, cols, cells, vals, b, n, ncell, dtype=np.float64):
 
 
 # ----------------------------------------------------------------------------------------
-# Partial RWR: restates partial_rwr.py:75-175 (do_conv=False).
+# Partial RWR: restates partial_rwr.py:75-175.
 # ----------------------------------------------------------------------------------------
 def rwr_transition(A, s0, s1):
     """P of partial_rwr.py:84-111 for a (C, b, n) tile."""
@@ -96,10 +96,29 @@ def rwr_transition(A, s0, s1):
     return L / (L.sum(1, keepdims=True) + dt(1e-15))              # :111
 
 
+def conv3x3_mean(x):
+    """partial_rwr.py:79-83: F.avg_pool2d(x, 3, stride 1, padding 1, ceil_mode=True) on each
+    (b, n) tile (zero padding counted, so every output is a sum of nine over 9), then the
+    1e-8 floor.  Applied only when b > 1 (:80)."""
+    dt = x.dtype.type
+    C, b, n = x.shape
+    if b <= 1:
+        return x
+    p = np.zeros((C, b + 2, n + 2), dtype=x.dtype)
+    p[:, 1:-1, 1:-1] = x
+    s = np.zeros_like(x)
+    for di in range(3):
+        for dj in range(3):
+            s = s + p[:, di:di + b, dj:dj + n]
+    return np.maximum(s / dt(9), dt(1e-8))
+
+
 def partial_rwr(x, slice_start, slice_end, do_rwr=True, do_col=False, bin_cov=None,
-                force_rwr_epochs=-1, final_transpose=True, return_rwr_iter=False):
+                force_rwr_epochs=-1, final_transpose=True, return_rwr_iter=False, do_conv=False):
     """x: (C, b, n).  Returns ((b, n, C) if final_transpose else (C, b, n), n_iter)."""
     n_iter = 0
+    if do_conv:
+        x = conv3x3_mean(x)
     if do_rwr:
         dt = x.dtype.type
         A = x
@@ -225,7 +244,9 @@ class ALSOracle:
     """Holds the factor state (A per chromosome dataset, B and D per chromosome, E) and runs
     ALS iterations exactly as Fast_Higashi_core.fit does after init_params."""
 
-    def __init__(self, datas, rank, A_list, B_dict, D_dict, E, n_i, dtype=np.float64, cache_rwr=True):
+    def __init__(self, datas, rank, A_list, B_dict, D_dict, E, n_i, dtype=np.float64, cache_rwr=True,
+                 do_conv=False):
+        self.do_conv = do_conv
         self.datas = datas
         self.rank = rank
         self.dt = dtype
@@ -250,7 +271,8 @@ class ALSOracle:
         cs = d.cells()[cj]
         x = d.tile(bb, cs, self.dt)
         out, _ = partial_rwr(x, bb.local.start, bb.local.stop, do_rwr=True,
-                             force_rwr_epochs=self.n_i[ci], final_transpose=True)
+                             force_rwr_epochs=self.n_i[ci], final_transpose=True,
+                             do_conv=self.do_conv)
         out = np.ascontiguousarray(out)
         if self._cache is not None:
             self._cache[key] = out
