@@ -22,7 +22,10 @@
 namespace fh {
 
 
-enum RwrSource { kSparse = 0, kDense = 1 };
+// kSparse: densified from the (tile, cell) segments; kDense: one dense tile shape for every
+// cell (the partial_rwr drop-in); kDenseTiles: dense tiles in the X layout (row stride of a
+// cell cell_stride, a tile at tile.xoff), e.g. the 3 x 3 mean of conv_tiles_kernel.
+enum RwrSource { kSparse = 0, kDense = 1, kDenseTiles = 2 };
 enum RwrMode { kOutput = 0, kDeltas = 1, kOutput16 = 2 };
 
 struct RwrArgs {
@@ -84,7 +87,7 @@ __global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
 
   int b, n, s0, epochs;
   int64_t xoff = 0;
-  if (SRC == kSparse) {
+  if (SRC == kSparse || SRC == kDenseTiles) {
     const fh_tile T = a.tiles[t];
     b = T.rows; n = T.width; s0 = T.s0; epochs = T.n_rwr; xoff = T.xoff;
     if (b <= 0 || b > a.max_rows || n < b || n > a.max_width || s0 < 0 || s0 + b > n ||
@@ -121,7 +124,7 @@ __global__ void __launch_bounds__(kRwrThreads, 1) rwr_f32_kernel(RwrArgs a) {
       *z = fmaxf(*z, kFloor);
     }
   } else {
-    xin = a.dense + (int64_t)c * b * n;
+    xin = SRC == kDense ? a.dense + (int64_t)c * b * n : a.dense + (int64_t)c * a.cell_stride + xoff;
     for (int i = tid; i < b * n; i += kRwrThreads) Z[(i / n) * ldz + (i % n)] = xin[i];
   }
   __syncthreads();
@@ -240,6 +243,84 @@ static int launch_rwr(const RwrArgs& a, int n_tiles, int max_rows, int max_width
   return launch_rwr_u<20, SRC, MODE>(a, grid, smem, s);
 }
 
+// ---------------------------------------------------------------------------------------
+// 3 x 3 mean of each tile before the walk (partial_rwr.py:79-83, do_conv=True):
+// F.avg_pool2d(x, 3, stride 1, padding 1) counts the zero padding, so every output is the sum
+// of its 3 x 3 window (zeros outside the tile) over 9, then floored at 1e-8; a tile of one row
+// is left as it is (:80).  The input is the floored densified tile (sparse_for_schic.py:320):
+// from the (tile, cell) segment (sparse) or a dense [cell][rows][width] array.  One CTA per
+// (tile, cell); the output goes to the X layout (or the dense layout).
+// ---------------------------------------------------------------------------------------
+struct ConvArgs {
+  const fh_tile* tiles;
+  int n_cells;
+  const uint2* entries;
+  const int64_t* offsets;
+  const float* dense;      // dense source [cell][rows][width] (tiles == nullptr)
+  int d_rows, d_width;
+  int max_rows, max_width;
+  float* out;
+  int64_t cell_stride;
+  int* status;
+};
+
+__host__ __device__ inline size_t conv_smem_bytes(int b, int n) {
+  return (size_t)(b + 2) * (n + 2) * sizeof(float);
+}
+
+__global__ void __launch_bounds__(kRwrThreads) conv_tiles_kernel(ConvArgs a) {
+  extern __shared__ float cz[];
+  const int c = blockIdx.x, t = blockIdx.y, tid = threadIdx.x;
+  int b, n;
+  int64_t xoff = 0;
+  if (a.tiles) {
+    const fh_tile T = a.tiles[t];
+    b = T.rows; n = T.width; xoff = T.xoff;
+    if (b <= 0 || b > a.max_rows || n <= 0 || n > a.max_width) {
+      if (tid == 0) set_status(a.status, FH_ERR_ARG);
+      return;
+    }
+  } else {
+    b = a.d_rows; n = a.d_width;
+  }
+  const int ld = n + 2;
+  for (int i = tid; i < (b + 2) * ld; i += kRwrThreads) {
+    const int p = i / ld, q = i % ld;
+    cz[i] = (p >= 1 && p <= b && q >= 1 && q <= n && a.tiles) ? kFloor : 0.f;
+  }
+  __syncthreads();
+  if (a.tiles) {
+    const int64_t e0 = a.offsets[(int64_t)t * a.n_cells + c];
+    const int64_t e1 = a.offsets[(int64_t)t * a.n_cells + c + 1];
+    for (int64_t e = e0 + tid; e < e1; e += kRwrThreads) {
+      const uint2 en = a.entries[e];
+      const int r = (int)(en.x & 0xffffu), j = (int)(en.x >> 16);
+      if (r < b && j < n) cz[(r + 1) * ld + j + 1] = fmaxf(__uint_as_float(en.y), kFloor);
+      else set_status(a.status, FH_ERR_INDEX);
+    }
+  } else {
+    const float* x = a.dense + (int64_t)c * b * n;
+    for (int i = tid; i < b * n; i += kRwrThreads) cz[(i / n + 1) * ld + i % n + 1] = x[i];
+  }
+  __syncthreads();
+  float* o = a.tiles ? a.out + (int64_t)c * a.cell_stride + xoff : a.out + (int64_t)c * b * n;
+  for (int i = tid; i < b * n; i += kRwrThreads) {
+    const int p = i / n, q = i % n;
+    float v;
+    if (b > 1) {
+      float s = 0.f;
+#pragma unroll
+      for (int di = 0; di < 3; ++di)
+#pragma unroll
+        for (int dj = 0; dj < 3; ++dj) s += cz[(p + di) * ld + q + dj];
+      v = fmaxf(s / 9.f, kFloor);
+    } else {
+      v = cz[(p + 1) * ld + q + 1];
+    }
+    o[i] = v;
+  }
+}
+
 }  // namespace fh
 
 using namespace fh;
@@ -336,4 +417,82 @@ extern "C" int fh_rwr_tiles_deltas(const fh_tile* tiles, int32_t n_tiles, int32_
   a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
   a.offsets = offsets; a.deltas = deltas; a.cap = cap; a.status = status;
   return launch_rwr<kSparse, kDeltas>(a, n_tiles, mr, mw, s);
+}
+
+// ---- 3 x 3 mean (do_conv) and the walk from dense tiles -----------------------------------
+extern "C" int fh_conv_tiles_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                                 int32_t mr, int32_t mw, const fh_entry* entries,
+                                 const int64_t* offsets, float* out, int64_t cell_stride,
+                                 int* status, void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !offsets || !out || mr <= 0 || mw <= 0)
+    return FH_ERR_ARG;
+  if (mr > kMaxBinRows || mw > kMaxWidth) return FH_ERR_UNSUPPORTED;
+  const size_t smem = conv_smem_bytes(mr, mw);
+  if (ensure_smem((const void*)conv_tiles_kernel, smem)) return FH_ERR_LAUNCH;
+  ConvArgs a{};
+  a.tiles = tiles; a.n_cells = n_cells; a.entries = reinterpret_cast<const uint2*>(entries);
+  a.offsets = offsets; a.max_rows = mr; a.max_width = mw; a.out = out;
+  a.cell_stride = cell_stride; a.status = status;
+  conv_tiles_kernel<<<dim3((unsigned)n_cells, (unsigned)n_tiles), kRwrThreads, smem,
+                      (cudaStream_t)stream>>>(a);
+  FH_CHECK_LAUNCH();
+  return FH_OK;
+}
+
+extern "C" int fh_conv_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width,
+                                 float* out, void* stream) {
+  if (!x || !out || n_cells <= 0 || rows <= 0 || width <= 0) return FH_ERR_ARG;
+  if (rows > kMaxBinRows || width > kMaxWidth) return FH_ERR_UNSUPPORTED;
+  const size_t smem = conv_smem_bytes(rows, width);
+  if (ensure_smem((const void*)conv_tiles_kernel, smem)) return FH_ERR_LAUNCH;
+  ConvArgs a{};
+  a.dense = x; a.d_rows = rows; a.d_width = width; a.n_cells = n_cells; a.out = out;
+  conv_tiles_kernel<<<dim3((unsigned)n_cells, 1u), kRwrThreads, smem, (cudaStream_t)stream>>>(a);
+  FH_CHECK_LAUNCH();
+  return FH_OK;
+}
+
+extern "C" int fh_rwr_tiles_dense_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                                      int32_t mr, int32_t mw, const float* src, float* out,
+                                      int64_t cell_stride, double* sumsq, int* status,
+                                      void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !src || !out || mr <= 0 || mw < mr)
+    return FH_ERR_ARG;
+  RwrArgs a{};
+  a.rp = 0.5f;   // partial_rwr.py:109
+  a.max_rows = mr; a.max_width = mw;
+  a.tiles = tiles; a.n_cells = n_cells; a.dense = src; a.out = out;
+  a.cell_stride = cell_stride; a.sumsq = sumsq; a.status = status;
+  return launch_rwr<kDenseTiles, kOutput>(a, n_tiles, mr, mw, (cudaStream_t)stream);
+}
+
+extern "C" int fh_rwr_tiles_dense_bf16(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                                       int32_t mr, int32_t mw, const float* src, uint16_t* out16,
+                                       int64_t cell_stride, int64_t plane_stride, double* sumsq,
+                                       int* status, void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !src || !out16 || mr <= 0 || mw < mr ||
+      plane_stride < 0)
+    return FH_ERR_ARG;
+  RwrArgs a{};
+  a.rp = 0.5f;   // partial_rwr.py:109
+  a.max_rows = mr; a.max_width = mw;
+  a.tiles = tiles; a.n_cells = n_cells; a.dense = src;
+  a.out16 = reinterpret_cast<__nv_bfloat16*>(out16);
+  a.cell_stride = cell_stride; a.plane_stride = plane_stride; a.sumsq = sumsq; a.status = status;
+  return launch_rwr<kDenseTiles, kOutput16>(a, n_tiles, mr, mw, (cudaStream_t)stream);
+}
+
+extern "C" int fh_rwr_tiles_dense_deltas(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                                         int32_t mr, int32_t mw, const float* src,
+                                         int64_t cell_stride, int32_t cap, float* deltas,
+                                         int* status, void* stream) {
+  if (!tiles || n_tiles <= 0 || n_cells <= 0 || !src || !deltas || cap <= 0 || mr <= 0 ||
+      mw < mr)
+    return FH_ERR_ARG;
+  RwrArgs a{};
+  a.rp = 0.5f;   // partial_rwr.py:109
+  a.max_rows = mr; a.max_width = mw;
+  a.tiles = tiles; a.n_cells = n_cells; a.dense = src; a.cell_stride = cell_stride;
+  a.deltas = deltas; a.cap = cap; a.status = status;
+  return launch_rwr<kDenseTiles, kDeltas>(a, n_tiles, mr, mw, (cudaStream_t)stream);
 }

@@ -60,6 +60,11 @@ SIGNATURES = {
     "fh_factor_grad_workspace": (SZ, [I32, I32, I32]),
     "fh_factor_grad_f32": (C.c_int, [I32, I32, P, P, I32, P, P, P, I32, I32, I32, P, P, P, P,
                                      SZ, P]),
+    "fh_conv_tiles_f32": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, P, P]),
+    "fh_conv_dense_f32": (C.c_int, [P, I32, I32, I32, P, P]),
+    "fh_rwr_tiles_dense_f32": (C.c_int, [P, I32, I32, I32, I32, P, P, I64, P, P, P]),
+    "fh_rwr_tiles_dense_bf16": (C.c_int, [P, I32, I32, I32, I32, P, P, I64, I64, P, P, P]),
+    "fh_rwr_tiles_dense_deltas": (C.c_int, [P, I32, I32, I32, I32, P, I64, I32, P, P, P]),
     "fh_rwr_dense_f32": (C.c_int, [P, I32, I32, I32, I32, I32, P, P, P]),
     "fh_rwr_dense_deltas": (C.c_int, [P, I32, I32, I32, I32, I32, P, P, P]),
     "fh_rwr_tiles_deltas": (C.c_int, [P, I32, I32, I32, I32, P, P, I32, P, P, P]),
@@ -94,6 +99,8 @@ _KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_exclusive_scan_n
             "fh_rwr_dense_deltas": 1, "fh_rwr_tiles_deltas": 1, "fh_xe_f32": 1, "fh_xg_f32": 2,
             "fh_project_y_f32": 1, "fh_procrustes_f32": 1, "fh_projection_g_f32": 1,
             "fh_rwr_tiles_bf16": 1, "fh_rwr_tiles_tc": 1, "fh_split_bf16": 1, "fh_xe_bf16": 1, "fh_xg_bf16": 2,
+            "fh_conv_tiles_f32": 1, "fh_conv_dense_f32": 1, "fh_rwr_tiles_dense_f32": 1,
+            "fh_rwr_tiles_dense_bf16": 1, "fh_rwr_tiles_dense_deltas": 1,
             "fh_rwr_tiles_rp_f32": 1, "fh_rwr_grad_f32": 1, "fh_recon_loss_f32": 2,
             "fh_recon_loss_bwd_f32": 4, "fh_factor_grad_f32": 2,
             "fh_polar_f32": 1, "fh_polar_svals_f32": 1, "fh_meta_polar": 5, "fh_core_norm": 2}

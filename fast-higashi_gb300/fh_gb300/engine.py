@@ -37,7 +37,7 @@ def _pad_rank(R):
 
 class FitEngine:
     def __init__(self, schic, rank, chrom2size, n_i, device, do_rwr=True, stream=None,
-                 precision="fp32"):
+                 precision="fp32", do_conv=False):
         import torch
         self.torch = torch
         if precision not in ("fp32", "bf16", "bf16x2"):
@@ -72,6 +72,8 @@ class FitEngine:
         if max(self.ranks) > 64 or self.R > 64:
             raise _lib.FHError("FitEngine", 2, "ranks above 64 are not supported yet")
         self.do_rwr = do_rwr
+        self.do_conv = bool(do_conv)
+        self._xc = None     # fp32 3 x 3-mean tiles for the bf16 forms (do_conv)
         self.n_rwr = [int(v) if do_rwr else 0 for v in (n_i if n_i is not None else [0] * len(schic))]
         order = sorted(range(len(schic)), key=lambda k: self.chrom_index[k])
         self.tiles, self.tile_base = tile_table(schic, self.chrom_index, self.ranks, self.n_rwr, order)
@@ -189,16 +191,52 @@ class FitEngine:
         P = _lib.ptr
         out = self.torch.zeros((self.n_tiles, self.Ct, cap), dtype=self.torch.float32,
                                device=self.device)
-        _lib.call("fh_rwr_tiles_deltas", P(self.tiles_dev), self.n_tiles, self.Ct, self.max_rows,
-                  self.max_width, P(self.store.entries), P(self.store.offsets), cap, P(out),
-                  P(self.status), self.sp())
+        if self.do_conv:
+            src = self.conv_source()
+            _lib.call("fh_rwr_tiles_dense_deltas", P(self.tiles_dev), self.n_tiles, self.Ct,
+                      self.max_rows, self.max_width, P(src), self.ldx, cap, P(out),
+                      P(self.status), self.sp())
+        else:
+            _lib.call("fh_rwr_tiles_deltas", P(self.tiles_dev), self.n_tiles, self.Ct,
+                      self.max_rows, self.max_width, P(self.store.entries),
+                      P(self.store.offsets), cap, P(out), P(self.status), self.sp())
         return out[:, :self.C]
+
+    def conv_source(self):
+        """The 3 x 3 mean of every floored tile (do_conv, partial_rwr.py:79-83) in the X layout:
+        into X itself in the fp32 form (the walk then runs in place), into a scratch fp32
+        array in the bf16 forms."""
+        if self.bf16:
+            if self._xc is None:
+                self._xc = self.torch.empty((self.Ct, self.ldx), dtype=self.torch.float32,
+                                            device=self.device)
+            buf = self._xc
+        else:
+            buf = self.X
+        P = _lib.ptr
+        _lib.call("fh_conv_tiles_f32", P(self.tiles_dev), self.n_tiles, self.Ct, self.max_rows,
+                  self.max_width, P(self.store.entries), P(self.store.offsets), P(buf), self.ldx,
+                  P(self.status), self.sp())
+        return buf
 
     def run_rwr(self):
         self._timed("rwr", self._run_rwr)
 
     def _run_rwr(self):
         P = _lib.ptr
+        if self.do_conv:
+            # the walk from the smoothed tiles (fp32 CUDA cores in every form)
+            src = self.conv_source()
+            if self.bf16:
+                _lib.call("fh_rwr_tiles_dense_bf16", P(self.tiles_dev), self.n_tiles, self.Ct,
+                          self.max_rows, self.max_width, P(src), P(self.X16), self.ldx,
+                          self.Ct * self.ldx if self.planes == 2 else 0, P(self.sumsq),
+                          P(self.status), self.sp())
+            else:
+                _lib.call("fh_rwr_tiles_dense_f32", P(self.tiles_dev), self.n_tiles, self.Ct,
+                          self.max_rows, self.max_width, P(src), P(self.X), self.ldx,
+                          P(self.sumsq), P(self.status), self.sp())
+            return
         if self.bf16 and self.max_rows <= 128 and self.max_width <= 256:
             _lib.call("fh_rwr_tiles_tc", P(self.tiles_dev), self.n_tiles, self.Ct,
                       self.max_rows, self.max_width, P(self.store.entries),

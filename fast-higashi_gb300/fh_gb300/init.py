@@ -119,8 +119,8 @@ def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
 
 def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
     import torch
-    if do_conv or do_col:
-        raise NotImplementedError("do_conv / do_col are not supported")
+    if do_col:
+        raise NotImplementedError("do_col is not supported")
     rank = model.rank
     device = model.device
     sizes = model.chrom2size
@@ -129,7 +129,7 @@ def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
     B_dict = {c: torch.eye(s, device=device).add_(torch.randn(s, device=device), alpha=1e-2)
               for c, s in sizes.items()}
     eng = FitEngine(schic, rank, sizes, None, device, do_rwr=do_rwr,
-                    precision=getattr(model, "precision", "fp32"))
+                    precision=getattr(model, "precision", "fp32"), do_conv=do_conv)
     model.engine = eng
     if do_rwr:
         n_i, feat_epochs = auto_epochs(eng, schic)

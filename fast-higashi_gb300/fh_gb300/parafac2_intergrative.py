@@ -6,8 +6,9 @@ projected_tensor_list, n_i, bin_cov_list, chrom2size), computed by the CUDA kern
 libfhgb300.so.  Factor tensors live on the GPU (the reference keeps A_list and the
 projections in pinned host memory); they are torch tensors, so ``.cpu()`` works as before.
 
-Supported options: do_rwr True/False, do_conv=False, do_col=False, one resolution, ranks
-r <= R <= 64.  Anything else raises NotImplementedError.
+Supported options: do_rwr True/False, do_conv True/False (the 3 x 3 mean of
+partial_rwr.py:79-83 runs on the fp32 CUDA-core walk in every precision form), do_col=False,
+one resolution, ranks r <= R <= 64.  Anything else raises NotImplementedError.
 """
 from __future__ import annotations
 
@@ -73,8 +74,6 @@ class Fast_Higashi_core:
 
     @staticmethod
     def _check_options(do_conv, do_col):
-        if do_conv:
-            raise NotImplementedError("do_conv=True is not supported")
         if do_col:
             raise NotImplementedError("do_col=True is not supported")
 
@@ -88,10 +87,11 @@ class Fast_Higashi_core:
         init_params(self, schic, do_conv, do_rwr, do_col, seed=seed)
 
     # ------------------------------------------------------------------ fit
-    def _engine(self, schic, do_rwr):
-        if self.engine is None or self.engine.schic is not schic:
+    def _engine(self, schic, do_rwr, do_conv=False):
+        if (self.engine is None or self.engine.schic is not schic or
+                self.engine.do_conv != bool(do_conv)):
             self.engine = FitEngine(schic, self.rank, self.chrom2size, self.n_i, self.device,
-                                    do_rwr=do_rwr, precision=self.precision)
+                                    do_rwr=do_rwr, precision=self.precision, do_conv=do_conv)
         return self.engine
 
     def fit(self, schic, size_ratio=0.3, n_iter_max=2000, n_iter_parafac=5, do_conv=True,
@@ -104,7 +104,7 @@ class Fast_Higashi_core:
             print("empty params initialized")
         if run_init:
             self.init_params(schic, do_conv, do_rwr, do_col)
-        eng = self._engine(schic, do_rwr)
+        eng = self._engine(schic, do_rwr, do_conv)
         eng.set_state(self.A_list, self.B_dict, self.D_dict, self.meta_embedding)
         self.tensor_norm = eng.tensor_norms()
         eng.core_norm()
@@ -170,7 +170,7 @@ class Fast_Higashi_core:
         (projection_list, projected_tensor_list, rec_error_x_U, rec_error_x_V
         [, rec_error_tensor_norm])."""
         self._check_options(do_conv, do_col)
-        eng = self._engine(schic, do_rwr)
+        eng = self._engine(schic, do_rwr, do_conv)
         eng.set_state(self.A_list, self.B_dict, self.D_dict, self.meta_embedding)
         eng.update(first=True)
         eng.check_status("update_meta_embedding_interactions")
@@ -186,7 +186,7 @@ class Fast_Higashi_core:
     # ------------------------------------------------------------------ transform
     def transform(self, schic, do_conv, do_rwr, do_col):
         self._check_options(do_conv, do_col)
-        eng = self._engine(schic, do_rwr)
+        eng = self._engine(schic, do_rwr, do_conv)
         E = eng.transform()
         eng.check_status("transform")
         return (None, (self.A_list, self.B_dict.values(), self.D_dict.values(), E),

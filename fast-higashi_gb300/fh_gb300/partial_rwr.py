@@ -5,6 +5,8 @@ library's kernel builds P from the tile (partial_rwr.py:84-111) and returns Q_e 
 Q_{t+1} = 0.5 Q_t P + 0.5 I (:112-138).  With force_rwr_epochs < 0 the epoch count follows
 the auto-stop rule (:99-126): the first epoch e where max over cells of ||Q_e - Q_{e+1}||_F
 < 0.01 stops the walk after Q_{e+1}; n_iter = e (60 and Q_60 when it never stops).
+do_conv=True smooths the tile first with the 3 x 3 mean of :79-83 (fh_conv_dense_f32).  As in
+the reference, the output is transposed only when do_conv or do_rwr is set.
 """
 from __future__ import annotations
 
@@ -29,15 +31,20 @@ def partial_rwr(x, slice_start, slice_end, do_conv, do_rwr, do_col, bin_cov=None
                 return_rwr_iter=False, force_rwr_epochs=-1, final_transpose=True,
                 slice_arrange=False, slice_arrange_size=100, **kw):
     import torch
-    if do_conv:
-        raise NotImplementedError("do_conv=True is not supported")
     if do_col:
         raise NotImplementedError("do_col=True is not supported")
     n_iter = 0
+    if not (do_conv or do_rwr):
+        return (x, n_iter) if return_rwr_iter else (x, 0)
+    if not (x.is_cuda and x.dtype == torch.float32 and x.dim() == 3):
+        raise _lib.FHError("partial_rwr", 1, "x must be a (cells, b, n) float32 CUDA tensor")
+    x = x.contiguous()
+    if do_conv and x.shape[1] > 1:
+        out = torch.empty_like(x)
+        _lib.call("fh_conv_dense_f32", _lib.ptr(x), x.shape[0], x.shape[1], x.shape[2],
+                  _lib.ptr(out), _lib.stream_ptr())
+        x = out
     if do_rwr:
-        if not (x.is_cuda and x.dtype == torch.float32 and x.dim() == 3):
-            raise _lib.FHError("partial_rwr", 1, "x must be a (cells, b, n) float32 CUDA tensor")
-        x = x.contiguous()
         C, rows, width = x.shape
         if slice_end - slice_start != rows:
             raise _lib.FHError("partial_rwr", 1, "slice must span the tile's rows")

@@ -149,6 +149,32 @@ int fh_rwr_grad_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells, int3
                     float rp, float* x, float* dx, int64_t cell_stride, int* status,
                     void* stream);
 
+/* ---- do_conv: the 3 x 3 mean before the walk (partial_rwr.py:79-83) ----------------------
+ * fh_conv_tiles_f32: for every (tile, cell), the floored densified tile (segments as in
+ * fh_rwr_tiles_f32) smoothed by F.avg_pool2d(x, 3, 1, padding=1) (zero padding counted: the
+ * window sum over 9) and floored at 1e-8 again, written to out in the X layout
+ * (out[c * cell_stride + xoff + i*width + j]); tiles of one row are copied unsmoothed.
+ * fh_conv_dense_f32: the same on a dense x[n_cells][rows][width] -> out (same shape).
+ * fh_rwr_tiles_dense_f32 / _bf16 / _deltas: fh_rwr_tiles_f32 / _bf16 / _deltas with the tiles
+ * read from a dense fp32 array in the X layout (src; out may be src: each tile is read by the
+ * CTA that writes it, before it writes). */
+int fh_conv_tiles_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells, int32_t max_rows,
+                      int32_t max_width, const fh_entry* entries, const int64_t* offsets,
+                      float* out, int64_t cell_stride, int* status, void* stream);
+int fh_conv_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width, float* out,
+                      void* stream);
+int fh_rwr_tiles_dense_f32(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                           int32_t max_rows, int32_t max_width, const float* src, float* out,
+                           int64_t cell_stride, double* sumsq, int* status, void* stream);
+int fh_rwr_tiles_dense_bf16(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                            int32_t max_rows, int32_t max_width, const float* src,
+                            uint16_t* out16, int64_t cell_stride, int64_t plane_stride,
+                            double* sumsq, int* status, void* stream);
+int fh_rwr_tiles_dense_deltas(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
+                              int32_t max_rows, int32_t max_width, const float* src,
+                              int64_t cell_stride, int32_t cap, float* deltas, int* status,
+                              void* stream);
+
 /* Same arithmetic on a dense tile x[n_cells][rows][width] (the partial_rwr drop-in: no
  * floor is applied to x); out[n_cells][rows][width]. */
 int fh_rwr_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width, int32_t s0,

@@ -147,7 +147,7 @@ def partial_rwr(x, slice_start, slice_end, do_rwr=True, do_col=False, bin_cov=No
             Q = Q / (Q.sum(2, keepdims=True) + dt(1e-15))
             A = A / bin_cov[:, None, :]
         x = np.matmul(Q, A)                                       # :138
-    if final_transpose:
+    if final_transpose and (do_conv or do_rwr):                   # :168-169
         x = x.transpose(1, 2, 0)
     return (x, n_iter) if return_rwr_iter else (x, 0)
 

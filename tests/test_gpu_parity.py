@@ -59,6 +59,49 @@ def test_partial_rwr_dropin_matches_reference():
         assert rel(ya, z["t%d_yauto" % k]) < 1e-5
 
 
+def test_partial_rwr_dropin_with_conv_matches_reference():
+    """do_conv=True: the 3 x 3 mean before the walk, with 3 epochs, the auto-stop rule and
+    the smoothing alone (do_rwr=False), against the reference's own outputs."""
+    from fh_gb300 import partial_rwr
+    z = G.load("rwr_conv_tiles.npz")
+    for k in range(int(z["n_tiles"])):
+        _, _, _, s0, s1, n_auto = z["t%d_meta" % k]
+        x = torch.from_numpy(z["t%d_x" % k]).to(CUDA)
+        y3, _ = partial_rwr(x, int(s0), int(s1), True, True, False, force_rwr_epochs=3)
+        assert rel(y3, z["t%d_y3" % k]) < 1e-5
+        ya, na = partial_rwr(x, int(s0), int(s1), True, True, False, force_rwr_epochs=-1,
+                             return_rwr_iter=True, final_transpose=False)
+        assert na == n_auto
+        assert rel(ya, z["t%d_yauto" % k]) < 1e-5
+        y0, _ = partial_rwr(x, int(s0), int(s1), True, False, False)
+        assert rel(y0, z["t%d_y0" % k]) < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16x2"])
+def test_fused_conv_rwr_tiles_match_oracle(precision):
+    """The engine's do_conv path (3 x 3 mean into the X layout, then the walk from the dense
+    tiles) against the oracle's partial_rwr(do_conv=True) of every tile."""
+    from fh_gb300.engine import FitEngine
+    z = G.load("rwr_conv_tiles.npz")
+    ds = datasets_from(z, resolution=1000000)
+    eng = FitEngine(ds, 4, {d.chrom: 2 for d in ds}, [3] * len(ds), CUDA, precision=precision,
+                    do_conv=True)
+    torch.cuda.synchronize()
+    eng.check_status("conv rwr")
+    X = eng.X if eng.X is not None else eng.X16.double().sum(0)
+    datas = G.chrom_datas(z, O)
+    tol = 1e-5 if precision == "fp32" else 2e-5
+    for k, d in enumerate(datas):
+        for bi, bb in enumerate(d.layout()):
+            t = eng.tile_base[k] + bi
+            x0 = int(eng.tiles["xoff"][t])
+            x = d.tile(bb, slice(0, d.num_cell), np.float64)
+            ref, _ = O.partial_rwr(x, bb.local.start, bb.local.stop, force_rwr_epochs=3,
+                                   do_conv=True, final_transpose=False)
+            got = X[:d.num_cell, x0:x0 + bb.rows * bb.width].double().cpu().numpy()
+            assert O.rel_err(got, ref.reshape(d.num_cell, -1)) < tol
+
+
 def test_fused_rwr_tiles_match_reference():
     """Contact build + fused densify/RWR over every tile at once (force_rwr_epochs=3)."""
     from fh_gb300.engine import FitEngine
@@ -179,21 +222,24 @@ def test_one_update_matches_reference_and_oracle():
         assert rel(ptl[d.chrom], Y_o[ci]) < 1e-4
 
 
-@pytest.mark.parametrize("fixture,n_iter,ref_tol", [("als_small.npz", 4, 1e-4), ("c1_fit.npz", 10, 2e-3)])
-def test_fit_trajectory(fixture, n_iter, ref_tol):
+@pytest.mark.parametrize("fixture,n_iter,ref_tol,conv", [("als_small.npz", 4, 1e-4, False),
+                                                         ("c1_fit.npz", 10, 2e-3, False),
+                                                         ("als_conv_small.npz", 4, 1e-4, True)])
+def test_fit_trajectory(fixture, n_iter, ref_tol, conv):
     z = G.load(fixture)
     n = int(z["n_chrom"])
     m, ds = _model_from(z, n)
-    m.fit(ds, size_ratio=float(z["dim1"]), n_iter_max=n_iter, n_iter_parafac=1, do_conv=False,
+    m.fit(ds, size_ratio=float(z["dim1"]), n_iter_max=n_iter, n_iter_parafac=1, do_conv=conv,
           do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
     traj = np.asarray(m.rec_errors_total)
-    orc = O.ALSOracle(G.chrom_datas(z, O), int(z["rank"]), *G.state(z, "init", n)).fit(n_iter)
+    orc = O.ALSOracle(G.chrom_datas(z, O), int(z["rank"]), *G.state(z, "init", n),
+                      do_conv=conv).fit(n_iter)
     np.testing.assert_allclose(traj, orc.rec_errors_total, rtol=1e-5)
     np.testing.assert_allclose(traj, z["fit_rec_total"], rtol=ref_tol)
     E = m.meta_embedding.cpu().numpy()
     assert O.rel_err(O.procrustes_align(E, orc.E), orc.E) < 1e-4
     # transform: embedding over all cells, aligned with the reference's
-    res = m.transform(ds, False, True, False)
+    res = m.transform(ds, conv, True, False)
     Et = res[1][3].cpu().numpy()
     Et_ref = z["fit_E_transform"]
     assert O.rel_err(O.procrustes_align(Et, Et_ref), Et_ref) < 1e-2
