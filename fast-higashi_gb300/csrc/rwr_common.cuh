@@ -99,4 +99,28 @@ __device__ inline void rwr_transition(const float* Z, int ldz, float* Pt, int ld
   __syncthreads();
 }
 
+// acc[u][v] += sum_k Z[k][ty + 16u] * Pt[k][tx + 16v]  ==  (P Z)[tx+16v][ty+16u]
+template <int MAXU>
+__device__ __forceinline__ void pz_product(const float* __restrict__ Z, int ldz,
+                                           const float* __restrict__ Pt, int ldp, int b,
+                                           int ty, int tx, float (&acc)[MAXU][8]) {
+#pragma unroll
+  for (int u = 0; u < MAXU; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+  for (int k = 0; k < b; ++k) {
+    float zk[MAXU], pk[8];
+    const float* zr = Z + k * ldz + ty;
+    const float* pr = Pt + k * ldp + tx;
+#pragma unroll
+    for (int u = 0; u < MAXU; ++u) zk[u] = zr[16 * u];
+#pragma unroll
+    for (int v = 0; v < 8; ++v) pk[v] = pr[16 * v];
+#pragma unroll
+    for (int u = 0; u < MAXU; ++u)
+#pragma unroll
+      for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(zk[u], pk[v], acc[u][v]);
+  }
+}
+
 }  // namespace fh

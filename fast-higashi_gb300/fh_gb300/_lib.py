@@ -66,6 +66,11 @@ SIGNATURES = {
     "fh_rwr_tiles_dense_bf16": (C.c_int, [P, I32, I32, I32, I32, P, P, I64, I64, P, P, P]),
     "fh_rwr_tiles_dense_deltas": (C.c_int, [P, I32, I32, I32, I32, P, I64, I32, P, P, P]),
     "fh_rwr_dense_f32": (C.c_int, [P, I32, I32, I32, I32, I32, P, P, P]),
+    "fh_rwr_col_tiles": (C.c_int, [P, I32, I32, I32, I32, P, P, P, P, I64, P, P, P, I64, I64,
+                                   P, P, P, P]),
+    "fh_rwr_col_dense": (C.c_int, [P, I32, I32, I32, I32, I32, P, P, P, P]),
+    "fh_col_coverage": (C.c_int, [P, I32, I32, P, I32, P, I64, I64, P, P]),
+    "fh_col_coverage_finalize": (C.c_int, [P, I64, P]),
     "fh_rwr_dense_deltas": (C.c_int, [P, I32, I32, I32, I32, I32, P, P, P]),
     "fh_rwr_tiles_deltas": (C.c_int, [P, I32, I32, I32, I32, P, P, I32, P, P, P]),
     "fh_xe_f32": (C.c_int, [P, I64, I32, I64, P, I32, P, P]),
@@ -102,7 +107,8 @@ _KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_exclusive_scan_n
             "fh_conv_tiles_f32": 1, "fh_conv_dense_f32": 1, "fh_rwr_tiles_dense_f32": 1,
             "fh_rwr_tiles_dense_bf16": 1, "fh_rwr_tiles_dense_deltas": 1,
             "fh_rwr_tiles_rp_f32": 1, "fh_rwr_grad_f32": 1, "fh_recon_loss_f32": 2,
-            "fh_recon_loss_bwd_f32": 4, "fh_factor_grad_f32": 2,
+            "fh_recon_loss_bwd_f32": 4, "fh_factor_grad_f32": 2, "fh_rwr_col_tiles": 1,
+            "fh_rwr_col_dense": 1, "fh_col_coverage": 1, "fh_col_coverage_finalize": 1,
             "fh_polar_f32": 1, "fh_polar_svals_f32": 1, "fh_meta_polar": 5, "fh_core_norm": 2}
 launches = 0
 

@@ -41,6 +41,9 @@ class ReconstructionLoss:
             raise _lib.FHError("ReconstructionLoss", 1, "the model has not been fitted")
         if eng.max_rank > 64 or eng.rp > 64:
             raise _lib.FHError("ReconstructionLoss", 2, "ranks above 64 are not supported")
+        if eng.do_conv or eng.do_col:
+            raise _lib.FHError("ReconstructionLoss", 2,
+                               "the differentiable walk covers do_conv=False, do_col=False")
         self.eng = eng
         self.torch = torch
         self._ws = {}

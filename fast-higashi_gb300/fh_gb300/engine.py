@@ -37,7 +37,9 @@ def _pad_rank(R):
 
 class FitEngine:
     def __init__(self, schic, rank, chrom2size, n_i, device, do_rwr=True, stream=None,
-                 precision="fp32", do_conv=False):
+                 precision="fp32", do_conv=False, do_col=False, bin_cov=None):
+        """bin_cov: (bin_cov_list, bad_bin_cov_list) of the model, required with do_col when
+        n_i is given (the walk runs at construction); init_params computes it otherwise."""
         import torch
         self.torch = torch
         if precision not in ("fp32", "bf16", "bf16x2"):
@@ -73,7 +75,10 @@ class FitEngine:
             raise _lib.FHError("FitEngine", 2, "ranks above 64 are not supported yet")
         self.do_rwr = do_rwr
         self.do_conv = bool(do_conv)
+        self.do_col = bool(do_col) and bool(do_rwr)   # do_col acts inside the walk only
         self._xc = None     # fp32 3 x 3-mean tiles for the bf16 forms (do_conv)
+        self.cov = None     # do_col coverage rows [Ct][nb] (bin_cov, then bad_bin_cov rows)
+        self.cov_lists = None
         self.n_rwr = [int(v) if do_rwr else 0 for v in (n_i if n_i is not None else [0] * len(schic))]
         order = sorted(range(len(schic)), key=lambda k: self.chrom_index[k])
         self.tiles, self.tile_base = tile_table(schic, self.chrom_index, self.ranks, self.n_rwr, order)
@@ -109,6 +114,8 @@ class FitEngine:
             self.X = torch.zeros((self.Ct, self.ldx), dtype=f32, device=dev)
             self.X16 = None
         self.sumsq = torch.zeros(self.n_tiles * self.Ct, dtype=f64, device=dev)
+        if self.do_col and bin_cov is not None:
+            self.set_coverage(*bin_cov)
         if n_i is not None:
             self.run_rwr()
         # ---- factor state and work buffers
@@ -186,8 +193,9 @@ class FitEngine:
             per_tile[self.tile_base[k]:self.tile_base[k] + d.num_bin_batch] = self.n_rwr[k]
         self.set_epochs(per_tile)
 
-    def auto_deltas(self, cap):
-        """||Q_e - Q_{e+1}||_F for e < cap for every (tile, good cell) (partial_rwr.py:99-123)."""
+    def auto_deltas(self, cap, all_cells=False):
+        """||Q_e - Q_{e+1}||_F for e < cap for every (tile, good cell), or every cell with
+        all_cells (partial_rwr.py:99-123)."""
         P = _lib.ptr
         out = self.torch.zeros((self.n_tiles, self.Ct, cap), dtype=self.torch.float32,
                                device=self.device)
@@ -200,7 +208,7 @@ class FitEngine:
             _lib.call("fh_rwr_tiles_deltas", P(self.tiles_dev), self.n_tiles, self.Ct,
                       self.max_rows, self.max_width, P(self.store.entries),
                       P(self.store.offsets), cap, P(out), P(self.status), self.sp())
-        return out[:, :self.C]
+        return out if all_cells else out[:, :self.C]
 
     def conv_source(self):
         """The 3 x 3 mean of every floored tile (do_conv, partial_rwr.py:79-83) in the X layout:
@@ -219,11 +227,76 @@ class FitEngine:
                   P(self.status), self.sp())
         return buf
 
+    # ------------------------------------------------------------------ do_col
+    def set_coverage(self, good, bad):
+        """Coverage rows from the model's bin_cov_list (per dataset [num_cell][num_bin]) and
+        bad_bin_cov_list (per dataset [bad cells][num_bin], or 0 without bad cells)."""
+        torch = self.torch
+        if self.cov is None:
+            self.cov = torch.ones((self.Ct, self.nb), dtype=torch.float32, device=self.device)
+        for k in range(len(self.schic)):
+            cols = self.ds_rows[k]
+            self.cov[:self.C, cols] = torch.as_tensor(good[k]).to(self.device, torch.float32)
+            if self.Ct > self.C and not np.isscalar(bad[k]):
+                self.cov[self.C:, cols] = torch.as_tensor(bad[k]).to(self.device, torch.float32)
+        self.cov_lists = (good, bad)
+
+    def coverage_views(self):
+        """(bin_cov_list, bad_bin_cov_list) as views of the coverage rows."""
+        good = [self.cov[:self.C, self.ds_rows[k]] for k in range(len(self.schic))]
+        bad = [self.cov[self.C:, self.ds_rows[k]] if self.Ct > self.C else 0
+               for k in range(len(self.schic))]
+        return good, bad
+
+    def _col_walk(self, cov, cell_epochs=None, to_x=True, colsum=None):
+        P = _lib.ptr
+        dense = self.conv_source() if self.do_conv else None
+        _lib.call("fh_rwr_col_tiles", P(self.tiles_dev), self.n_tiles, self.Ct, self.max_rows,
+                  self.max_width, P(self.store.entries), P(self.store.offsets),
+                  P(dense) if dense is not None else None,
+                  P(cov) if cov is not None else None, self.nb,
+                  P(cell_epochs) if cell_epochs is not None else None,
+                  P(self.X) if to_x and not self.bf16 else None,
+                  P(self.X16) if to_x and self.bf16 else None, self.ldx,
+                  self.Ct * self.ldx if self.planes == 2 else 0,
+                  P(self.sumsq) if to_x else None, P(colsum) if colsum is not None else None,
+                  P(self.status), self.sp())
+
+    def compute_coverage(self, cell_epochs):
+        """init_params' coverage rows (parafac2_intergrative.py:96-142, 186-200) for all cells:
+        1e-4 plus the column sums of the auto-stopped plain walk (cell_epochs: int32 [tile]
+        [Ct] per cell batch), added in bin-batch order.  Not yet marked inf."""
+        torch, P = self.torch, _lib.ptr
+        ep = torch.as_tensor(np.ascontiguousarray(cell_epochs, dtype=np.int32)).to(self.device)
+        colsum = torch.empty((self.n_tiles, self.Ct, self.max_width), dtype=torch.float32,
+                             device=self.device)
+        self._col_walk(None, ep, to_x=False, colsum=colsum)
+        if self.cov is None:
+            self.cov = torch.empty((self.Ct, self.nb), dtype=torch.float32, device=self.device)
+        _lib.call("fh_col_coverage", P(self.tiles_dev), self.n_tiles, self.Ct, P(colsum),
+                  self.max_width, P(self.cov), self.nb, self.nb, P(self.status), self.sp())
+        del colsum
+        self.cov_lists = None
+
+    def col_features(self, cell_epochs):
+        """The do_col walk with per-cell-batch epochs (the init feature pass, :203-240)."""
+        ep = self.torch.as_tensor(np.ascontiguousarray(cell_epochs, dtype=np.int32)).to(self.device)
+        self._timed("rwr", lambda: self._col_walk(self.cov, ep))
+
+    def finalize_coverage(self):
+        """bin_cov[bin_cov <= 1e-4] = inf (parafac2_intergrative.py:266-270)."""
+        _lib.call("fh_col_coverage_finalize", _lib.ptr(self.cov), self.cov.numel(), self.sp())
+
     def run_rwr(self):
         self._timed("rwr", self._run_rwr)
 
     def _run_rwr(self):
         P = _lib.ptr
+        if self.do_col:
+            if self.cov is None:
+                raise _lib.FHError("FitEngine", 1, "do_col needs the coverage rows (bin_cov_list)")
+            self._col_walk(self.cov)
+            return
         if self.do_conv:
             # the walk from the smoothed tiles (fp32 CUDA cores in every form)
             src = self.conv_source()

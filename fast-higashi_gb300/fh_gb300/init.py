@@ -15,6 +15,10 @@
    taken from the eigen-decomposition of their Gram matrix.
 At resolutions finer than 1 Mb the reference pools the features to 1 Mb first; this
 restatement sketches the unpooled band features.
+With do_col (and do_rwr) the coverage rows bin_cov come first (:96-200): 1e-4 plus the
+column sums of the auto-stopped plain walk, every cell batch (good and bad) stopping on its
+own; the features are then the do_col walk's output with the same per-batch epochs
+(:203-240), and entries <= 1e-4 of the rows become inf (:266-270).
 """
 from __future__ import annotations
 
@@ -33,18 +37,22 @@ def _stop_epochs(deltas, cap, tol=0.01):
     return int(below[0]) if below.size else None
 
 
-def auto_epochs(eng, schic):
-    """Per-tile stopping epochs and per-dataset n_i (partial_rwr.py:99-126, :265)."""
+def auto_epochs(eng, schic, per_cell=False):
+    """Per-tile stopping epochs and per-dataset n_i (partial_rwr.py:99-126, :265).  With
+    per_cell, also the epoch count of every (tile, cell) as the reference's batched loops
+    see it: each cell batch, good (:118-142) and bad (:178-200), stops on its own."""
     n_i = np.zeros(len(schic), dtype=np.int64)
     feat_epochs = np.zeros(eng.n_tiles, dtype=np.int32)
+    cell_ep = np.zeros((eng.n_tiles, eng.Ct), dtype=np.int32) if per_cell else None
     for cap in (12, 60):
-        deltas = eng.auto_deltas(cap).cpu().numpy()       # (tiles, cells, cap)
+        deltas = eng.auto_deltas(cap, all_cells=per_cell).cpu().numpy()   # (tiles, cells, cap)
         ok = True
         for k, d in enumerate(schic):
+            batches = d.cell_slice_list if per_cell else d.cell_slice_list[:d.num_cell_batch]
             for bi in range(d.num_bin_batch):
                 t = eng.tile_base[k] + bi
                 fe = 0
-                for cs in d.cell_slice_list[:d.num_cell_batch]:
+                for j, cs in enumerate(batches):
                     e = _stop_epochs(deltas[t, cs], cap)
                     if e is None:
                         if cap < 60:
@@ -53,17 +61,20 @@ def auto_epochs(eng, schic):
                         e, out = 60, 60                   # ran all 60 epochs without stopping
                     else:
                         out = e + 1                       # Q was advanced once more before break
-                    n_i[k] = max(n_i[k], e)
-                    fe = max(fe, out)
+                    if per_cell:
+                        cell_ep[t, cs] = out
+                    if j < d.num_cell_batch:
+                        n_i[k] = max(n_i[k], e)
+                        fe = max(fe, out)
                 feat_epochs[t] = fe
                 if not ok:
                     break
             if not ok:
                 break
         if ok:
-            return n_i, feat_epochs
+            return (n_i, feat_epochs, cell_ep) if per_cell else (n_i, feat_epochs)
         n_i[:] = 0
-    return n_i, feat_epochs
+    return (n_i, feat_epochs, cell_ep) if per_cell else (n_i, feat_epochs)
 
 
 def _chrom_band_rows(eng, k):
@@ -119,8 +130,6 @@ def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
 
 def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
     import torch
-    if do_col:
-        raise NotImplementedError("do_col is not supported")
     rank = model.rank
     device = model.device
     sizes = model.chrom2size
@@ -129,15 +138,22 @@ def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
     B_dict = {c: torch.eye(s, device=device).add_(torch.randn(s, device=device), alpha=1e-2)
               for c, s in sizes.items()}
     eng = FitEngine(schic, rank, sizes, None, device, do_rwr=do_rwr,
-                    precision=getattr(model, "precision", "fp32"), do_conv=do_conv)
+                    precision=getattr(model, "precision", "fp32"), do_conv=do_conv,
+                    do_col=do_col)
     model.engine = eng
-    if do_rwr:
+    if eng.do_col:
+        # coverage from the plain walk, then the features from the do_col walk (:96-240)
+        n_i, feat_epochs, cell_ep = auto_epochs(eng, schic, per_cell=True)
+        eng.compute_coverage(cell_ep)
+        eng.col_features(cell_ep)
+    elif do_rwr:
         n_i, feat_epochs = auto_epochs(eng, schic)
         eng.set_epochs(feat_epochs)
+        eng.run_rwr()
     else:
         n_i = np.zeros(len(schic), dtype=np.int64)
         eng.set_n_i(n_i)
-    eng.run_rwr()
+        eng.run_rwr()
     rng = np.random.default_rng(seed)
     feats, cols = [], []
     start = 0
@@ -162,7 +178,12 @@ def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
     model.A_list = A_list
     model.B_dict = B_dict
     model.n_i = np.asarray(n_i)
-    model.bin_cov_list = [None] * len(schic)
-    model.bad_bin_cov_list = [0] * len(schic)
+    if eng.do_col:
+        eng.finalize_coverage()
+        model.bin_cov_list, model.bad_bin_cov_list = eng.coverage_views()
+        eng.cov_lists = (model.bin_cov_list, model.bad_bin_cov_list)
+    else:
+        model.bin_cov_list = [None] * len(schic)
+        model.bad_bin_cov_list = [0] * len(schic)
     eng.set_n_i(model.n_i)
     eng.run_rwr()

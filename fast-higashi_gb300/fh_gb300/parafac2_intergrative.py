@@ -7,8 +7,10 @@ libfhgb300.so.  Factor tensors live on the GPU (the reference keeps A_list and t
 projections in pinned host memory); they are torch tensors, so ``.cpu()`` works as before.
 
 Supported options: do_rwr True/False, do_conv True/False (the 3 x 3 mean of
-partial_rwr.py:79-83 runs on the fp32 CUDA-core walk in every precision form), do_col=False,
-one resolution, ranks r <= R <= 64.  Anything else raises NotImplementedError.
+partial_rwr.py:79-83 runs on the fp32 CUDA-core walk in every precision form), do_col
+True/False (the column-normalised walk of partial_rwr.py:131-138 on fp32 CUDA cores, with the
+coverage rows bin_cov_list / bad_bin_cov_list that init_params computes or the caller
+assigns), one resolution, ranks r <= R <= 64.  Anything else raises NotImplementedError.
 """
 from __future__ import annotations
 
@@ -74,8 +76,7 @@ class Fast_Higashi_core:
 
     @staticmethod
     def _check_options(do_conv, do_col):
-        if do_col:
-            raise NotImplementedError("do_col=True is not supported")
+        """Every combination of do_conv / do_rwr / do_col is supported."""
 
     # ------------------------------------------------------------------ init
     def init_params(self, schic, do_conv, do_rwr, do_col, seed=None):
@@ -87,11 +88,23 @@ class Fast_Higashi_core:
         init_params(self, schic, do_conv, do_rwr, do_col, seed=seed)
 
     # ------------------------------------------------------------------ fit
-    def _engine(self, schic, do_rwr, do_conv=False):
+    def _coverage(self):
+        return (getattr(self, "bin_cov_list", None), getattr(self, "bad_bin_cov_list", None))
+
+    def _engine(self, schic, do_rwr, do_conv=False, do_col=False):
+        col = bool(do_col) and bool(do_rwr)
         if (self.engine is None or self.engine.schic is not schic or
-                self.engine.do_conv != bool(do_conv)):
+                self.engine.do_conv != bool(do_conv) or self.engine.do_col != col):
             self.engine = FitEngine(schic, self.rank, self.chrom2size, self.n_i, self.device,
-                                    do_rwr=do_rwr, precision=self.precision, do_conv=do_conv)
+                                    do_rwr=do_rwr, precision=self.precision, do_conv=do_conv,
+                                    do_col=col, bin_cov=self._coverage() if col else None)
+        elif col:
+            good, bad = self._coverage()
+            held = self.engine.cov_lists
+            if held is None or held[0] is not good or held[1] is not bad:
+                # coverage rows replaced since the walk ran (bin_cov_list was assigned)
+                self.engine.set_coverage(good, bad)
+                self.engine.run_rwr()
         return self.engine
 
     def fit(self, schic, size_ratio=0.3, n_iter_max=2000, n_iter_parafac=5, do_conv=True,
@@ -104,7 +117,7 @@ class Fast_Higashi_core:
             print("empty params initialized")
         if run_init:
             self.init_params(schic, do_conv, do_rwr, do_col)
-        eng = self._engine(schic, do_rwr, do_conv)
+        eng = self._engine(schic, do_rwr, do_conv, do_col)
         eng.set_state(self.A_list, self.B_dict, self.D_dict, self.meta_embedding)
         self.tensor_norm = eng.tensor_norms()
         eng.core_norm()
@@ -170,7 +183,7 @@ class Fast_Higashi_core:
         (projection_list, projected_tensor_list, rec_error_x_U, rec_error_x_V
         [, rec_error_tensor_norm])."""
         self._check_options(do_conv, do_col)
-        eng = self._engine(schic, do_rwr, do_conv)
+        eng = self._engine(schic, do_rwr, do_conv, do_col)
         eng.set_state(self.A_list, self.B_dict, self.D_dict, self.meta_embedding)
         eng.update(first=True)
         eng.check_status("update_meta_embedding_interactions")
@@ -186,7 +199,7 @@ class Fast_Higashi_core:
     # ------------------------------------------------------------------ transform
     def transform(self, schic, do_conv, do_rwr, do_col):
         self._check_options(do_conv, do_col)
-        eng = self._engine(schic, do_rwr, do_conv)
+        eng = self._engine(schic, do_rwr, do_conv, do_col)
         E = eng.transform()
         eng.check_status("transform")
         return (None, (self.A_list, self.B_dict.values(), self.D_dict.values(), E),

@@ -5,8 +5,11 @@ library's kernel builds P from the tile (partial_rwr.py:84-111) and returns Q_e 
 Q_{t+1} = 0.5 Q_t P + 0.5 I (:112-138).  With force_rwr_epochs < 0 the epoch count follows
 the auto-stop rule (:99-126): the first epoch e where max over cells of ||Q_e - Q_{e+1}||_F
 < 0.01 stops the walk after Q_{e+1}; n_iter = e (60 and Q_60 when it never stops).
-do_conv=True smooths the tile first with the 3 x 3 mean of :79-83 (fh_conv_dense_f32).  As in
-the reference, the output is transposed only when do_conv or do_rwr is set.
+do_conv=True smooths the tile first with the 3 x 3 mean of :79-83 (fh_conv_dense_f32).
+do_col=True (with do_rwr) returns Q' (x / bin_cov) instead, Q' the symmetrised, clipped,
+row-normalised Q (:131-138, fh_rwr_col_dense); bin_cov is the (cells, n) coverage slice the
+reference passes (anything that broadcasts to it).  As in the reference, the output is
+transposed only when do_conv or do_rwr is set.
 """
 from __future__ import annotations
 
@@ -31,8 +34,6 @@ def partial_rwr(x, slice_start, slice_end, do_conv, do_rwr, do_col, bin_cov=None
                 return_rwr_iter=False, force_rwr_epochs=-1, final_transpose=True,
                 slice_arrange=False, slice_arrange_size=100, **kw):
     import torch
-    if do_col:
-        raise NotImplementedError("do_col=True is not supported")
     n_iter = 0
     if not (do_conv or do_rwr):
         return (x, n_iter) if return_rwr_iter else (x, 0)
@@ -53,8 +54,16 @@ def partial_rwr(x, slice_start, slice_end, do_conv, do_rwr, do_col, bin_cov=None
         else:
             n_iter = epochs = int(force_rwr_epochs)
         out = torch.empty_like(x)
-        _lib.call("fh_rwr_dense_f32", _lib.ptr(x), C, rows, width, slice_start, epochs,
-                  _lib.ptr(out), None, _lib.stream_ptr())
+        if do_col:
+            if bin_cov is None:
+                raise _lib.FHError("partial_rwr", 1, "do_col needs bin_cov")
+            cov = torch.as_tensor(bin_cov).to(x.device, torch.float32)
+            cov = cov.expand(C, width).contiguous()
+            _lib.call("fh_rwr_col_dense", _lib.ptr(x), C, rows, width, slice_start, epochs,
+                      _lib.ptr(cov), _lib.ptr(out), None, _lib.stream_ptr())
+        else:
+            _lib.call("fh_rwr_dense_f32", _lib.ptr(x), C, rows, width, slice_start, epochs,
+                      _lib.ptr(out), None, _lib.stream_ptr())
         x = out
     if final_transpose:
         x = x.permute(1, 2, 0)

@@ -175,6 +175,38 @@ int fh_rwr_tiles_dense_deltas(const fh_tile* tiles, int32_t n_tiles, int32_t n_c
                               int64_t cell_stride, int32_t cap, float* deltas, int* status,
                               void* stream);
 
+/* ---- do_col: the column-normalised walk (partial_rwr.py:112-138, parafac2_intergrative.py
+ * :96-276) -------------------------------------------------------------------------------
+ * fh_rwr_col_tiles: for every (tile, cell), Q_T (Q_0 = I, Q_{t+1} = 0.5 Q_t P + 0.5 I), then
+ *   with cov: X = Q' (A / cov_row), Q' = rownorm(max((Q + Q^T) / 2, 0)) (row sums + 1e-15),
+ *             cov_row[j] = cov[c * cov_ld + (brow0 - row0) + shift + j] (the cell's coverage
+ *             of the tile's global column j, bins numbered across chromosomes);
+ *   cov null: X = Q A (the plain walk in the reference's association).
+ * A is the floored tile of the (tile, cell) segment (entries/offsets as fh_rwr_tiles_f32), or
+ * the dense fp32 tile in the X layout when dense is given (the 3 x 3 mean of do_conv; out may
+ * be dense).  cell_epochs[t * n_cells + c] overrides the tile's n_rwr when given.  X goes to
+ * out (fp32, X layout), else to out16 (bf16 planes as fh_rwr_tiles_bf16), else nowhere;
+ * sumsq[t * n_cells + c] = ||X||^2 when sumsq is given (and X is written); colsum, when given,
+ * receives the column sums of X at colsum[(t * n_cells + c) * max_width + j].  Shared memory
+ * 4 * (2 b ((b+3)&~3) + b (((n+31)/32)*32 + 1) + 384) bytes must fit in 227 KB.
+ * fh_rwr_col_dense: the with-cov form on a dense x[n_cells][rows][width] with cov[n_cells]
+ *   [width] (partial_rwr's bin_cov argument) -> out[n_cells][rows][width].
+ * fh_col_coverage: cov[c][g] = 1e-4 + the colsum entries of every tile holding global column
+ *   g, added in tile order (bin_cov of init_params, :96-99, 141-142, 199-200), for g < n_cols.
+ * fh_col_coverage_finalize: cov[i] <= 1e-4 -> +inf for i < n (:266-270). */
+int fh_rwr_col_tiles(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells, int32_t max_rows,
+                     int32_t max_width, const fh_entry* entries, const int64_t* offsets,
+                     const float* dense, const float* cov, int64_t cov_ld,
+                     const int32_t* cell_epochs, float* out, uint16_t* out16,
+                     int64_t cell_stride, int64_t plane_stride, double* sumsq, float* colsum,
+                     int* status, void* stream);
+int fh_rwr_col_dense(const float* x, int32_t n_cells, int32_t rows, int32_t width, int32_t s0,
+                     int32_t n_epochs, const float* cov, float* out, int* status, void* stream);
+int fh_col_coverage(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells, const float* colsum,
+                    int32_t max_width, float* cov, int64_t cov_ld, int64_t n_cols, int* status,
+                    void* stream);
+int fh_col_coverage_finalize(float* cov, int64_t n, void* stream);
+
 /* Same arithmetic on a dense tile x[n_cells][rows][width] (the partial_rwr drop-in: no
  * floor is applied to x); out[n_cells][rows][width]. */
 int fh_rwr_dense_f32(const float* x, int32_t n_cells, int32_t rows, int32_t width, int32_t s0,

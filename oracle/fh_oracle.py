@@ -245,8 +245,13 @@ class ALSOracle:
     ALS iterations exactly as Fast_Higashi_core.fit does after init_params."""
 
     def __init__(self, datas, rank, A_list, B_dict, D_dict, E, n_i, dtype=np.float64, cache_rwr=True,
-                 do_conv=False):
+                 do_conv=False, do_col=False, bin_cov_list=None):
         self.do_conv = do_conv
+        self.do_col = do_col
+        if do_col:
+            if bin_cov_list is None:
+                raise ValueError("do_col needs the coverage rows (bin_cov_list)")
+            self.bin_cov = [np.asarray(c, dtype=dtype) for c in bin_cov_list]
         self.datas = datas
         self.rank = rank
         self.dt = dtype
@@ -270,9 +275,10 @@ class ALSOracle:
         bb = d.layout()[bi]
         cs = d.cells()[cj]
         x = d.tile(bb, cs, self.dt)
+        cov = self.bin_cov[ci][cs, bb.col] if self.do_col else None   # :363
         out, _ = partial_rwr(x, bb.local.start, bb.local.stop, do_rwr=True,
                              force_rwr_epochs=self.n_i[ci], final_transpose=True,
-                             do_conv=self.do_conv)
+                             do_conv=self.do_conv, do_col=self.do_col, bin_cov=cov)
         out = np.ascontiguousarray(out)
         if self._cache is not None:
             self._cache[key] = out
@@ -391,6 +397,28 @@ class ALSOracle:
                     SVD_term[:, cs] += lhs @ proj.reshape(-1, proj.shape[-1])
         E, _ = project2orthogonal(SVD_term.T, self.rank)
         return E
+
+
+def col_coverage(datas, dtype=np.float64, do_conv=False, mark_inf=True):
+    """bin_cov of init_params (parafac2_intergrative.py:96-99, 118-142, 266-267), good cells:
+    per chromosome, 1e-4 plus, for every (bin batch, cell batch) in loop order, the column
+    sums (over the tile's rows) of the auto-stopped do_col=False walk, added at the tile's
+    global columns; entries still <= 1e-4 become inf when mark_inf (the do_col feature pass
+    of :203-240 runs before that replacement)."""
+    dt = dtype
+    out = []
+    for d in datas:
+        cov = np.full((d.num_cell, d.num_bin), dt(1e-4), dtype=dt)
+        for bb in d.layout():
+            for cs in d.cells():
+                x = d.tile(bb, cs, dt)
+                y, _ = partial_rwr(x, bb.local.start, bb.local.stop, do_rwr=True,
+                                   force_rwr_epochs=-1, final_transpose=False, do_conv=do_conv)
+                cov[cs, bb.col] += y.sum(1)                               # :141-142
+        if mark_inf:
+            cov[cov <= dt(1e-4)] = np.inf                                 # :266-267
+        out.append(cov)
+    return out
 
 
 def procrustes_align(X, Y):

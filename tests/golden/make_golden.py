@@ -22,8 +22,13 @@ Every output is produced by the reference's own functions on seeded synthetic in
                    3 x 3 mean before the walk): force_rwr_epochs=3, the auto-stop rule, and
                    do_rwr=False (the smoothed tile alone).
   als_conv_small.npz  als_small.npz's workload fitted with do_conv=True.
+  rwr_col_tiles.npz  the tiles of rwr_tiles.npz through partial_rwr with do_col=True and a
+                   seeded coverage argument (positive, a few entries inf): force_rwr_epochs=3,
+                   the auto-stop rule, and do_conv=True with force_rwr_epochs=3.
+  als_col_small.npz  als_small.npz's workload fitted with do_col=True, with the coverage
+                   rows (bin_cov_list) init_params computed.
 
-    python tests/golden/make_golden.py rwr_conv als_conv    (only the named fixtures)
+    python tests/golden/make_golden.py rwr_conv als_conv rwr_col als_col   (only the named ones)
 """
 import copy
 import os
@@ -112,6 +117,43 @@ def make_rwr_conv_tiles():
     print("rwr_conv_tiles", k, "tiles")
 
 
+def make_rwr_col_tiles():
+    w = synth.workload("tiny")
+    coo, _ = synth.generate(w, seed=11)
+    ds = build_chrom_datasets(ref, coo, w.chrom_names, [12] * 2, [10] * 2, w.band, w.resolution)
+    rng = np.random.default_rng(17)
+    out = coo_arrays("in", coo)
+    out.update(bs_bin=12, bs_cell=10, flank=w.band, n_chrom=len(coo))
+    k = 0
+    for ci, d in enumerate(ds):
+        for bi in range(d.num_bin_batch):
+            loc = d.local_bin_slice_list[bi]
+            for cj in range(d.num_cell_batch):
+                (x, _), kind = d.fetch(bi, cj, save_context=dict(device=CPU), transpose=True)
+                cov = rng.uniform(0.5, 4.0, size=(x.shape[0], x.shape[2])).astype(np.float32)
+                cov[rng.random(cov.shape) < 0.05] = np.inf
+                tc = torch.from_numpy(cov)
+                y3, _ = ref["rwr"].partial_rwr(x.clone(), loc.start, loc.stop, False, True, True,
+                                               bin_cov=tc.clone(), force_rwr_epochs=3,
+                                               return_rwr_iter=True)
+                ya, na = ref["rwr"].partial_rwr(x.clone(), loc.start, loc.stop, False, True, True,
+                                                bin_cov=tc.clone(), force_rwr_epochs=-1,
+                                                return_rwr_iter=True, final_transpose=False)
+                yc, _ = ref["rwr"].partial_rwr(x.clone(), loc.start, loc.stop, True, True, True,
+                                               bin_cov=tc.clone(), force_rwr_epochs=3,
+                                               return_rwr_iter=True)
+                out["t%d_meta" % k] = np.array([ci, bi, cj, loc.start, loc.stop, na], dtype=np.int64)
+                out["t%d_x" % k] = x.numpy()
+                out["t%d_cov" % k] = cov
+                out["t%d_y3" % k] = y3.contiguous().numpy()
+                out["t%d_yauto" % k] = ya.contiguous().numpy()
+                out["t%d_yconv3" % k] = yc.contiguous().numpy()
+                k += 1
+    out["n_tiles"] = k
+    np.savez_compressed(os.path.join(HERE, "rwr_col_tiles.npz"), **out)
+    print("rwr_col_tiles", k, "tiles")
+
+
 def make_parafac():
     rng = np.random.default_rng(5)
     X = rng.standard_normal((40, 6, 9)).astype(np.float32)
@@ -174,18 +216,18 @@ def state_arrays(prefix, st, names):
     return out
 
 
-def run_fit(w, ds, n_iter, init_state, dim1, do_conv=False):
+def run_fit(w, ds, n_iter, init_state, dim1, do_conv=False, do_col=False):
     m = core.Fast_Higashi_core(rank=w.rank, off_diag=w.band, res_list=[w.resolution]).to(CPU)
     inject(m, init_state)
     with FitLocals() as fl:
         m.fit(ds, size_ratio=dim1, n_iter_max=n_iter, n_iter_parafac=1, do_conv=do_conv,
-              do_rwr=True, do_col=False, tol=0, run_init=False)
-    res = m.transform(ds, do_conv, True, False)
+              do_rwr=True, do_col=do_col, tol=0, run_init=False)
+    res = m.transform(ds, do_conv, True, do_col)
     return m, fl.locals, res
 
 
 def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U=True,
-             do_conv=False):
+             do_conv=False, do_col=False):
     w = synth.workload(wname)
     coo, _ = synth.generate(w, seed=seed)
     bsb = [bs_bin or synth.recommend_batches(w, nb, w.n_cells)[0] for nb in w.chrom_bins]
@@ -195,10 +237,13 @@ def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U
     torch.manual_seed(seed)
     m = core.Fast_Higashi_core(rank=w.rank, off_diag=w.band, res_list=[w.resolution]).to(CPU)
     m.fit(ds, size_ratio=w.dim1, n_iter_max=0, n_iter_parafac=1, do_conv=do_conv, do_rwr=True,
-          do_col=False, tol=0, run_init=True)
+          do_col=do_col, tol=0, run_init=True)
     st0 = snapshot(m)
     out = coo_arrays("in", coo) if save_input else {}
     out.update(state_arrays("init", st0, w.chrom_names))
+    if do_col:
+        for k, c in enumerate(st0["bin_cov"]):
+            out["init_bincov%d" % k] = c.numpy()
     out.update(bs_bin=np.asarray(bsb), bs_cell=np.asarray(bsc), flank=w.band, rank=w.rank,
                resolution=w.resolution, dim1=w.dim1, n_iter=n_iter, seed=seed,
                n_chrom=len(coo), sizes=np.asarray([m.chrom2size[n] for n in w.chrom_names]))
@@ -206,7 +251,7 @@ def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U
     proj_list = [[torch.empty(0)] * d.num_bin_batch for d in ds]
     ptl = {d.chrom: torch.empty([d.num_bin, m.chrom2size[d.chrom], w.rank]) for d in ds}
     r = m.update_meta_embedding_interactions(ds, proj_list, ptl, do_conv=do_conv, do_rwr=True,
-                                             do_col=False, first_iter=True)
+                                             do_col=do_col, first_iter=True)
     pl, ptl, exU, exV, tn = r
     for ci, d in enumerate(ds):
         for bi in range(d.num_bin_batch if save_U else 0):
@@ -215,12 +260,12 @@ def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U
     out.update(it1_exU=np.asarray(exU).ravel(), it1_exV=float(exV), it1_tnorm=np.asarray(tn).ravel(),
                it1_E=m.meta_embedding.numpy())
     # the fit loop from the same state
-    m2, loc, res = run_fit(w, ds, n_iter, st0, w.dim1, do_conv)
+    m2, loc, res = run_fit(w, ds, n_iter, st0, w.dim1, do_conv, do_col)
     out["fit_rec_total"] = np.asarray(loc["rec_errors_total"], dtype=np.float64)
     out["fit_rec_block"] = np.stack([np.asarray(x).ravel() for x in loc["rec_errors"]])
     out.update(state_arrays("fit", snapshot(m2), w.chrom_names))
     out["fit_E_transform"] = res[1][3].numpy()
-    m3, loc1, _ = run_fit(w, ds, 1, st0, w.dim1, do_conv)
+    m3, loc1, _ = run_fit(w, ds, 1, st0, w.dim1, do_conv, do_col)
     out.update(state_arrays("one", snapshot(m3), w.chrom_names))
     out["one_rec_total"] = np.asarray(loc1["rec_errors_total"], dtype=np.float64)
     np.savez_compressed(os.path.join(HERE, name), **out)
@@ -234,6 +279,10 @@ if __name__ == "__main__":
             make_rwr_conv_tiles()
         if "als_conv" in only:
             make_als("als_conv_small.npz", "small", 25, 40, 4, seed=3, do_conv=True)
+        if "rwr_col" in only:
+            make_rwr_col_tiles()
+        if "als_col" in only:
+            make_als("als_col_small.npz", "small", 25, 40, 4, seed=3, do_col=True)
         sys.exit(0)
     make_rwr_tiles()
     make_rwr_conv_tiles()
@@ -241,3 +290,5 @@ if __name__ == "__main__":
     make_als("als_small.npz", "small", 25, 40, 4, seed=3)
     make_als("c1_fit.npz", "c1", None, None, 10, seed=1, save_U=False)
     make_als("als_conv_small.npz", "small", 25, 40, 4, seed=3, do_conv=True)
+    make_rwr_col_tiles()
+    make_als("als_col_small.npz", "small", 25, 40, 4, seed=3, do_col=True)

@@ -102,6 +102,96 @@ def test_fused_conv_rwr_tiles_match_oracle(precision):
             assert O.rel_err(got, ref.reshape(d.num_cell, -1)) < tol
 
 
+def test_partial_rwr_dropin_with_col_matches_reference():
+    """do_col=True: Q' (x / bin_cov) with 3 epochs, the auto-stop rule, and after the 3 x 3
+    mean, against the reference's own outputs (bin_cov has inf entries)."""
+    from fh_gb300 import partial_rwr
+    z = G.load("rwr_col_tiles.npz")
+    for k in range(int(z["n_tiles"])):
+        _, _, _, s0, s1, n_auto = z["t%d_meta" % k]
+        x = torch.from_numpy(z["t%d_x" % k]).to(CUDA)
+        cov = torch.from_numpy(z["t%d_cov" % k]).to(CUDA)
+        y3, _ = partial_rwr(x, int(s0), int(s1), False, True, True, bin_cov=cov,
+                            force_rwr_epochs=3)
+        assert rel(y3, z["t%d_y3" % k]) < 1e-5
+        ya, na = partial_rwr(x, int(s0), int(s1), False, True, True, bin_cov=cov,
+                             force_rwr_epochs=-1, return_rwr_iter=True, final_transpose=False)
+        assert na == n_auto
+        assert rel(ya, z["t%d_yauto" % k]) < 1e-5
+        yc, _ = partial_rwr(x, int(s0), int(s1), True, True, True, bin_cov=cov,
+                            force_rwr_epochs=3)
+        assert rel(yc, z["t%d_yconv3" % k]) < 1e-5
+
+
+@pytest.mark.parametrize("precision,conv", [("fp32", False), ("fp32", True), ("bf16x2", False),
+                                            ("bf16x2", True)])
+def test_fused_col_rwr_tiles_match_oracle(precision, conv):
+    """The engine's do_col walk over every tile (coverage rows with inf entries, bins
+    numbered across chromosomes) against the oracle's partial_rwr(do_col=True)."""
+    from fh_gb300.engine import FitEngine
+    z = G.load("rwr_col_tiles.npz")
+    ds = datasets_from(z, resolution=1000000)
+    datas = G.chrom_datas(z, O)
+    rng = np.random.default_rng(5)
+    covs = []
+    for d in datas:
+        c = rng.uniform(0.5, 4.0, size=(d.num_cell, d.num_bin))
+        c[rng.random(c.shape) < 0.05] = np.inf
+        covs.append(c.astype(np.float32))
+    eng = FitEngine(ds, 4, {d.chrom: 2 for d in ds}, [3] * len(ds), CUDA, precision=precision,
+                    do_conv=conv, do_col=True, bin_cov=([torch.from_numpy(c) for c in covs],
+                                                       [0] * len(ds)))
+    torch.cuda.synchronize()
+    eng.check_status("col rwr")
+    X = eng.X if eng.X is not None else eng.X16.double().sum(0)
+    tol = 1e-5 if precision == "fp32" else 2e-5
+    for k, d in enumerate(datas):
+        for bi, bb in enumerate(d.layout()):
+            t = eng.tile_base[k] + bi
+            x0 = int(eng.tiles["xoff"][t])
+            x = d.tile(bb, slice(0, d.num_cell), np.float64)
+            ref, _ = O.partial_rwr(x, bb.local.start, bb.local.stop, force_rwr_epochs=3,
+                                   do_conv=conv, do_col=True,
+                                   bin_cov=covs[k][:, bb.col].astype(np.float64),
+                                   final_transpose=False)
+            got = X[:d.num_cell, x0:x0 + bb.rows * bb.width].double().cpu().numpy()
+            assert O.rel_err(got, ref.reshape(d.num_cell, -1)) < tol
+    ss = eng.sumsq.view(eng.n_tiles, eng.Ct)[0].cpu().numpy()
+    t0 = eng.tiles[0]
+    x = X[:, int(t0["xoff"]):int(t0["xoff"]) + int(t0["rows"]) * int(t0["width"])]
+    np.testing.assert_allclose(ss, (x.double() ** 2).sum(1).cpu().numpy(), rtol=1e-6)
+
+
+def test_col_coverage_matches_reference_init():
+    """init_params with do_col: n_i and the coverage rows bin_cov_list against the values the
+    reference's init_params computed on the same input."""
+    from fh_gb300 import Fast_Higashi_core
+    z = G.load("als_col_small.npz")
+    n = int(z["n_chrom"])
+    ds = datasets_from(z)
+    m = Fast_Higashi_core(int(z["rank"]), int(z["flank"]), [int(z["resolution"])]).to(CUDA)
+    m._sizes(ds, float(z["dim1"]), None)
+    m.init_params(ds, False, True, True)
+    np.testing.assert_array_equal(np.asarray(m.n_i), z["init_n_i"])
+    for k in range(n):
+        got = m.bin_cov_list[k].cpu().numpy()
+        ref = z["init_bincov%d" % k]
+        np.testing.assert_array_equal(np.isinf(got), np.isinf(ref))
+        fin = np.isfinite(ref)
+        assert O.rel_err(got[fin], ref[fin]) < 1e-5
+    # the fit's walk afterwards used these rows: one tile against the oracle
+    eng = m.engine
+    datas = G.chrom_datas(z, O)
+    d, bb = datas[0], datas[0].layout()[1]
+    x0 = int(eng.tiles["xoff"][eng.tile_base[0] + 1])
+    x = d.tile(bb, slice(0, d.num_cell), np.float64)
+    ref, _ = O.partial_rwr(x, bb.local.start, bb.local.stop, force_rwr_epochs=int(m.n_i[0]),
+                           do_col=True, bin_cov=z["init_bincov0"][:, bb.col].astype(np.float64),
+                           final_transpose=False)
+    got = eng.X[:d.num_cell, x0:x0 + bb.rows * bb.width].double().cpu().numpy()
+    assert O.rel_err(got, ref.reshape(d.num_cell, -1)) < 1e-5
+
+
 def test_fused_rwr_tiles_match_reference():
     """Contact build + fused densify/RWR over every tile at once (force_rwr_epochs=3)."""
     from fh_gb300.engine import FitEngine
@@ -194,7 +284,11 @@ def _model_from(z, n_chrom):
     m.D_dict = {k: torch.from_numpy(v) for k, v in D.items()}
     m.meta_embedding = torch.from_numpy(E)
     m.n_i = np.asarray(n_i)
-    m.bin_cov_list = [None] * n_chrom
+    if "init_bincov0" in z:
+        m.bin_cov_list = [torch.from_numpy(z["init_bincov%d" % k]) for k in range(n_chrom)]
+    else:
+        m.bin_cov_list = [None] * n_chrom
+    m.bad_bin_cov_list = [0] * n_chrom
     return m, ds
 
 
@@ -222,24 +316,27 @@ def test_one_update_matches_reference_and_oracle():
         assert rel(ptl[d.chrom], Y_o[ci]) < 1e-4
 
 
-@pytest.mark.parametrize("fixture,n_iter,ref_tol,conv", [("als_small.npz", 4, 1e-4, False),
-                                                         ("c1_fit.npz", 10, 2e-3, False),
-                                                         ("als_conv_small.npz", 4, 1e-4, True)])
-def test_fit_trajectory(fixture, n_iter, ref_tol, conv):
+@pytest.mark.parametrize("fixture,n_iter,ref_tol,conv,col", [
+    ("als_small.npz", 4, 1e-4, False, False),
+    ("c1_fit.npz", 10, 2e-3, False, False),
+    ("als_conv_small.npz", 4, 1e-4, True, False),
+    ("als_col_small.npz", 4, 1e-4, False, True)])
+def test_fit_trajectory(fixture, n_iter, ref_tol, conv, col):
     z = G.load(fixture)
     n = int(z["n_chrom"])
     m, ds = _model_from(z, n)
     m.fit(ds, size_ratio=float(z["dim1"]), n_iter_max=n_iter, n_iter_parafac=1, do_conv=conv,
-          do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
+          do_rwr=True, do_col=col, tol=0, run_init=False, verbose=False)
     traj = np.asarray(m.rec_errors_total)
+    cov = [z["init_bincov%d" % k] for k in range(n)] if col else None
     orc = O.ALSOracle(G.chrom_datas(z, O), int(z["rank"]), *G.state(z, "init", n),
-                      do_conv=conv).fit(n_iter)
+                      do_conv=conv, do_col=col, bin_cov_list=cov).fit(n_iter)
     np.testing.assert_allclose(traj, orc.rec_errors_total, rtol=1e-5)
     np.testing.assert_allclose(traj, z["fit_rec_total"], rtol=ref_tol)
     E = m.meta_embedding.cpu().numpy()
     assert O.rel_err(O.procrustes_align(E, orc.E), orc.E) < 1e-4
     # transform: embedding over all cells, aligned with the reference's
-    res = m.transform(ds, conv, True, False)
+    res = m.transform(ds, conv, True, col)
     Et = res[1][3].cpu().numpy()
     Et_ref = z["fit_E_transform"]
     assert O.rel_err(O.procrustes_align(Et, Et_ref), Et_ref) < 1e-2

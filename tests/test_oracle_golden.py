@@ -49,6 +49,38 @@ def test_partial_rwr_with_conv_matches_reference(dtype, tol):
         assert O.rel_err(y0, z["t%d_y0" % k]) < tol
 
 
+@pytest.mark.parametrize("dtype,tol", [(np.float32, 2e-6), (np.float64, 1e-5)])
+def test_partial_rwr_with_col_matches_reference(dtype, tol):
+    """do_col=True (partial_rwr.py:131-138): the symmetrised, row-normalised Q applied to the
+    tile divided by the coverage argument (inf entries zero their columns)."""
+    z = G.load("rwr_col_tiles.npz")
+    for k in range(int(z["n_tiles"])):
+        _, _, _, s0, s1, n_auto = z["t%d_meta" % k]
+        x = z["t%d_x" % k].astype(dtype)
+        cov = z["t%d_cov" % k].astype(dtype)
+        y3, _ = O.partial_rwr(x.copy(), s0, s1, force_rwr_epochs=3, do_col=True, bin_cov=cov)
+        assert O.rel_err(y3, z["t%d_y3" % k]) < tol
+        ya, na = O.partial_rwr(x.copy(), s0, s1, force_rwr_epochs=-1, final_transpose=False,
+                               return_rwr_iter=True, do_col=True, bin_cov=cov)
+        assert na == n_auto
+        assert O.rel_err(ya, z["t%d_yauto" % k]) < tol
+        yc, _ = O.partial_rwr(x.copy(), s0, s1, force_rwr_epochs=3, do_col=True, bin_cov=cov,
+                              do_conv=True)
+        assert O.rel_err(yc, z["t%d_yconv3" % k]) < tol
+
+
+def test_col_coverage_matches_reference_init():
+    """bin_cov of init_params (parafac2_intergrative.py:96-142, 266-267) on the small workload."""
+    z = G.load("als_col_small.npz")
+    datas = G.chrom_datas(z, O)
+    cov = O.col_coverage(datas, np.float32)
+    for k, c in enumerate(cov):
+        ref = z["init_bincov%d" % k]
+        np.testing.assert_array_equal(np.isinf(c), np.isinf(ref))
+        fin = np.isfinite(ref)
+        assert O.rel_err(c[fin], ref[fin]) < 2e-6
+
+
 @pytest.mark.parametrize("n", [1, 3])
 def test_parafac_matches_reference(n):
     z = G.load("parafac.npz")
@@ -59,10 +91,12 @@ def test_parafac_matches_reference(n):
     assert abs(lx - float(z["lx%d" % n])) / abs(float(z["lx%d" % n])) < 1e-5
 
 
-def _oracle_from(z, prefix="init", dtype=np.float64, do_conv=False):
+def _oracle_from(z, prefix="init", dtype=np.float64, do_conv=False, do_col=False):
     datas = G.chrom_datas(z, O)
     A, B, D, E, n_i = G.state(z, prefix, len(datas))
-    return O.ALSOracle(datas, int(z["rank"]), A, B, D, E, n_i, dtype=dtype, do_conv=do_conv)
+    cov = [z["init_bincov%d" % k] for k in range(len(datas))] if do_col else None
+    return O.ALSOracle(datas, int(z["rank"]), A, B, D, E, n_i, dtype=dtype, do_conv=do_conv,
+                       do_col=do_col, bin_cov_list=cov)
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
@@ -88,12 +122,14 @@ def test_one_update_matches_reference(dtype):
 # rec ~ 0.2, and the reference forms |core|^2 in fp32 with a 1.5e-5 relative error on c1
 # (its chr1 value 1102.7616 against 1102.7785 exactly), so its own trajectory is off by
 # ~1e-3 there.  The fp32 and fp64 restatements agree with each other to 2e-6.
-@pytest.mark.parametrize("fixture,n_iter,rtol,conv", [("als_small.npz", 4, 1e-4, False),
-                                                     ("c1_fit.npz", 10, 2e-3, False),
-                                                     ("als_conv_small.npz", 4, 1e-4, True)])
-def test_fit_trajectory_matches_reference(fixture, n_iter, rtol, conv):
+@pytest.mark.parametrize("fixture,n_iter,rtol,conv,col", [
+    ("als_small.npz", 4, 1e-4, False, False),
+    ("c1_fit.npz", 10, 2e-3, False, False),
+    ("als_conv_small.npz", 4, 1e-4, True, False),
+    ("als_col_small.npz", 4, 1e-4, False, True)])
+def test_fit_trajectory_matches_reference(fixture, n_iter, rtol, conv, col):
     z = G.load(fixture)
-    orc = _oracle_from(z, do_conv=conv)
+    orc = _oracle_from(z, do_conv=conv, do_col=col)
     orc.fit(n_iter)
     traj = np.asarray(orc.rec_errors_total)
     np.testing.assert_allclose(traj, z["fit_rec_total"], rtol=rtol)
