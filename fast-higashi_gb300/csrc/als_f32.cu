@@ -19,15 +19,16 @@
 namespace fh {
 
 // ---------------------------------------------------------------------------------------
-// W[row][m] = sum_c X[c][row] * E[c][m]; CTA = 128 band rows x RP, K = cells in steps of 32.
+// W[row][m] = sum_c X[c][row] * E[c][m]; CTA = 128 band rows x RP, K = cells in steps of 32
+// (16 at RP = 128, which keeps the two staged tiles within 48 KB).
 // ---------------------------------------------------------------------------------------
 constexpr int kXeRows = 128;
-constexpr int kXeK = 32;
 
 template <int RP>
 __global__ void __launch_bounds__(256) xe_f32_kernel(const float* __restrict__ X, int64_t ldx,
                                                      int C, const float* __restrict__ E,
                                                      float* __restrict__ W, int64_t rows) {
+  constexpr int kXeK = RP >= 128 ? 16 : 32;
   constexpr int MG = RP / 4;          // m-groups of 4
   constexpr int RG = 256 / MG;        // row groups
   constexpr int RPT = kXeRows / RG;   // rows per thread
@@ -103,17 +104,19 @@ __global__ void __launch_bounds__(256) xe_f32_kernel(const float* __restrict__ X
 
 // ---------------------------------------------------------------------------------------
 // Partial[s][c][m] = sum_{row in split s} X[c][row] * Gt[row][m]; CTA = 128 cells x RP.
-// Thread (cg, mg) owns cells cg + 16*i (i < 8) and m = mg*MPT + j.
+// Thread (cg, mg) owns cells cg + 16*i (i < 8) and m = mg*MPT + j.  Band rows are staged 32
+// at a time (16 at RP = 128); splits span multiples of 32 rows.
 // ---------------------------------------------------------------------------------------
 constexpr int kXgCells = 128;
-constexpr int kXgK = 32;
-constexpr int kXgLd = kXgK + 4;
+constexpr int kXgSplitK = 32;
 
 template <int RP>
 __global__ void __launch_bounds__(256) xg_f32_kernel(const float* __restrict__ X, int64_t ldx,
                                                      int C, const float* __restrict__ Gt,
                                                      int64_t rows, int64_t rows_per_split,
                                                      float* __restrict__ partial) {
+  constexpr int kXgK = RP >= 128 ? 16 : 32;
+  constexpr int kXgLd = kXgK + 4;
   constexpr int MPT = RP / 16;
   __shared__ __align__(16) float Xs[2][kXgCells][kXgLd];
   __shared__ __align__(16) float Gs[2][kXgK][RP];
@@ -272,7 +275,7 @@ extern "C" int fh_xe_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t r
 extern "C" int fh_xg_splits(int32_t n_cells, int64_t rows) {
   const int64_t ct = ceil_div(n_cells, kXgCells);
   int64_t s = ceil_div(3 * 152, ct);
-  const int64_t max_s = ceil_div(rows, 4 * kXgK);
+  const int64_t max_s = ceil_div(rows, 4 * kXgSplitK);
   if (s > max_s) s = max_s;
   if (s < 1) s = 1;
   return (int)s;
@@ -285,7 +288,7 @@ extern "C" int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t r
       !rp_ok(rp) || splits <= 0)
     return FH_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
-  int64_t per = ceil_div(ceil_div(rows, splits), kXgK) * kXgK;
+  int64_t per = ceil_div(ceil_div(rows, splits), kXgSplitK) * kXgSplitK;
   dim3 grid((unsigned)ceil_div(n_cells, kXgCells), (unsigned)splits);
   switch (rp) {
     case 16: xg_f32_kernel<16><<<grid, 256, 0, s>>>(X, ldx, n_cells, Gt, rows, per, partial); break;

@@ -20,13 +20,24 @@
 //
 // Bin rows are processed in chunks of <= 8 rows of one chromosome; per-chunk partial sums
 // are reduced in a fixed order by the per-chromosome kernel (deterministic).
+//
+// The kernels are instantiated for ranks up to MR = 64 (256 threads) and up to MR = 128
+// (512 threads): 4 MR threads, outputs on 8 x (MR / 32) register tiles.  At MR = 128 the
+// row kernel keeps two Y tiles and one factor in shared memory and holds Y_g D in registers;
+// B and the A-row inverse are read from global memory (L2).
 #include "fh_common.cuh"
 
 namespace fh {
 
-constexpr int kCpThreads = 256;
-constexpr int kCpMaxR = 64;  // r and R handled by these kernels
-constexpr int kCpLz = kCpMaxR + 1;
+constexpr int kCpMaxR = 128;  // r and R handled by these kernels
+
+// Launch shape of the MR instantiation: 4 MR threads, NW warps, output tiles 8 x TN.
+template <int MR>
+struct CpShape {
+  static constexpr int NT = 4 * MR, NW = NT / 32, TN = MR / 32;
+  static constexpr int LY = MR + 4;   // row stride of the Y tiles (16-byte rows for cp.async)
+  static constexpr int LZ = MR + 1;   // odd stride of the staged factors
+};
 
 struct CpArgs {
   int nchrom;
@@ -63,9 +74,15 @@ enum CpRowMode { kRowsNorm = 0, kRowsAB = 1, kRowsD = 2, kRowsScale = 3, kRowsGr
 enum CpSmallMode { kSmallInit = 0, kSmallB = 1, kSmallD = 2, kSmallCore = 3, kSmallDLast = 4 };
 
 __host__ __device__ inline size_t cp_pstride(int ld) { return (size_t)2 * ld * ld + 2; }
-constexpr int kCpLy = kCpMaxR + 4;  // row stride of the Y tiles (16-byte rows for cp.async)
-constexpr size_t kCpRowsSmem =
-    (2 * (size_t)kCpMaxR * kCpLy + 4 * (size_t)kCpMaxR * kCpLz) * sizeof(float);
+// Dynamic shared memory of cp_rows_kernel<MR>: two Y tiles and four factor tiles (MR = 64),
+// or two Y tiles, one factor tile and the warps' column partials (MR = 128).
+template <int MR>
+constexpr size_t cp_rows_smem() {
+  using S = CpShape<MR>;
+  return MR <= 64 ? (2 * (size_t)MR * S::LY + 4 * (size_t)MR * S::LZ) * sizeof(float)
+                  : (2 * (size_t)MR * S::LY + (size_t)MR * S::LZ + (size_t)S::NW * MR) *
+                        sizeof(float);
+}
 
 // sum over k < nk of p[k * stride], in increasing k (the loads go out eight at a time)
 __device__ __forceinline__ float chunk_sum(const float* p, size_t stride, int nk) {
@@ -82,60 +99,69 @@ __device__ __forceinline__ float chunk_sum(const float* p, size_t stride, int nk
   return s;
 }
 
-// acc[u][v] = sum_k fa(w + 8u, k) fb(k, lane + 32v) over k < K for 256 threads (rows w + 8u,
-// u < 8; columns lane + 32 v, v < 2), rows / columns clamped to M-1 / N-1.
-template <class FA, class FB>
-__device__ __forceinline__ void cp_mm(int M, int N, int K, FA fa, FB fb, float (&acc)[8][2]) {
+// acc[u][v] = sum_k fa(w + NW u, k) fb(k, lane + 32v) over k < K for the 4 MR threads (rows
+// w + NW u, u < 8; columns lane + 32 v, v < TN), rows / columns clamped to M-1 / N-1.
+template <int MR, class FA, class FB>
+__device__ __forceinline__ void cp_mm(int M, int N, int K, FA fa, FB fb,
+                                      float (&acc)[8][CpShape<MR>::TN]) {
+  constexpr int NW = CpShape<MR>::NW, TN = CpShape<MR>::TN;
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  int ri[8], cj[2];
+  int ri[8], cj[TN];
 #pragma unroll
-  for (int u = 0; u < 8; ++u) ri[u] = min(w + 8 * u, M - 1);
+  for (int u = 0; u < 8; ++u) ri[u] = min(w + NW * u, M - 1);
 #pragma unroll
-  for (int v = 0; v < 2; ++v) cj[v] = min(l + 32 * v, N - 1);
+  for (int v = 0; v < TN; ++v) cj[v] = min(l + 32 * v, N - 1);
 #pragma unroll
-  for (int u = 0; u < 8; ++u) acc[u][0] = acc[u][1] = 0.f;
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < TN; ++v) acc[u][v] = 0.f;
   for (int k = 0; k < K; ++k) {
-    float av[8], bv[2];
+    float av[8], bv[TN];
 #pragma unroll
     for (int u = 0; u < 8; ++u) av[u] = fa(ri[u], k);
 #pragma unroll
-    for (int v = 0; v < 2; ++v) bv[v] = fb(k, cj[v]);
+    for (int v = 0; v < TN; ++v) bv[v] = fb(k, cj[v]);
 #pragma unroll
     for (int u = 0; u < 8; ++u)
 #pragma unroll
-      for (int v = 0; v < 2; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+      for (int v = 0; v < TN; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
   }
 }
 
-__global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode) {
+template <int MR>
+__global__ void __launch_bounds__(4 * MR) cp_rows_kernel(CpArgs a, int mode) {
+  using S = CpShape<MR>;
+  constexpr int NT = S::NT, NW = S::NW, TN = S::TN, LY = S::LY, LZ = S::LZ;
   extern __shared__ __align__(16) float cps[];
-  float* Yb = cps;                        // two Y_g tiles (r x RP, stride kCpLy): row i, row i+1
-  float* Fs = Yb + 2 * kCpMaxR * kCpLy;   // D (R x r) or B (r x r)
-  float* Bs = Fs + kCpMaxR * kCpLz;       // B (mode AB)
-  float* Zs = Bs + kCpMaxR * kCpLz;       // Y_g D (r x r)
-  float* Ls = Zs + kCpMaxR * kCpLz;       // the A-row system's inverse (mode AB)
-  __shared__ float rhs[kCpMaxR];
-  __shared__ float ysol[kCpMaxR];
-  __shared__ float red4[4][kCpMaxR];
+  float* Yb = cps;                        // two Y_g tiles (r x RP, stride LY): row i, row i+1
+  float* Fs = Yb + 2 * MR * LY;           // D (R x r) or B (r x r)
+  // MR <= 64: B, Y_g D and the A-row inverse staged too; MR = 128: the warps' partials
+  float* Bs = Fs + MR * LZ;               // B (mode AB)
+  float* Zs = Bs + MR * LZ;               // Y_g D (r x r)
+  float* Ls = Zs + MR * LZ;               // the A-row system's inverse (mode AB)
+  float* red = Fs + MR * LZ;              // [NW][MR] (MR = 128)
+  __shared__ float rhs[MR];
+  __shared__ float ysol[MR];
+  __shared__ float red4[4][MR];
   __shared__ double dred[32];
   const int k = blockIdx.x;
   const int ci = a.k_chrom[k];
   if (mode != kRowsNorm && mode != kRowsGram && (a.state[ci] & 1)) return;
-  const int r = a.c_rank[ci], R = a.R, ld = a.ld, lz = kCpLz;
+  const int r = a.c_rank[ci], R = a.R, ld = a.ld, lz = LZ;
   const int64_t row0 = a.k_row0[k];
   const int nrow = a.k_nrow[k];
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
 
   if (mode == kRowsScale) {
     const float* sc = a.scaleA + (size_t)ci * ld;
-    for (int i = ty; i < nrow; i += 8)
+    for (int i = ty; i < nrow; i += NW)
       for (int p = tx; p < r; p += 32) a.A[(row0 + i) * ld + p] *= sc[p];
     return;
   }
   float* out = a.part + (size_t)k * cp_pstride(ld);
   if (mode == kRowsNorm || mode == kRowsGram) {
     // partial A^T A (diagonal only for kRowsNorm) and ||Y||^2 of the chunk
-    for (int p = ty; p < r; p += 8)
+    for (int p = ty; p < r; p += NW)
       for (int q = tx; q < r; q += 32) {
         float s = 0.f;
         if (mode == kRowsGram || p == q)
@@ -147,7 +173,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
     const int64_t per = (int64_t)a.ldy * a.RP;
     const float* Y0 = a.Y + row0 * per;
 #pragma unroll 4
-    for (int64_t e = (int64_t)tid * 4; e < nrow * per; e += kCpThreads * 4) {
+    for (int64_t e = (int64_t)tid * 4; e < nrow * per; e += NT * 4) {
       const float4 v = *reinterpret_cast<const float4*>(Y0 + e);
       const int64_t wv = e % per;
       const int j = (int)(wv / a.RP), m = (int)(wv % a.RP);
@@ -167,30 +193,32 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
   const float* Bc = a.B + (size_t)ci * ld * ld;
   const float* Lc = a.L + (size_t)ci * ld * ld;
   if (mode == kRowsAB) {
-    for (int m = ty; m < R; m += 8)
+    for (int m = ty; m < R; m += NW)
       for (int q = tx; q < r; q += 32) Fs[m * lz + q] = Dc[m * ld + q];
-    for (int j = ty; j < r; j += 8)
-      for (int q = tx; q < r; q += 32) {
-        Bs[j * lz + q] = Bc[j * ld + q];
-        Ls[j * lz + q] = Lc[j * ld + q];
-      }
+    if constexpr (MR <= 64) {
+      for (int j = ty; j < r; j += NW)
+        for (int q = tx; q < r; q += 32) {
+          Bs[j * lz + q] = Bc[j * ld + q];
+          Ls[j * lz + q] = Lc[j * ld + q];
+        }
+    }
   } else {
-    for (int j = ty; j < r; j += 8)
+    for (int j = ty; j < r; j += NW)
       for (int q = tx; q < r; q += 32) Fs[j * lz + q] = Bc[j * ld + q];
   }
-  float pA[2][8], pB[2][8];   // partials at (row p = ty + 8u, column q = tx + 32v)
+  float pA[TN][8], pB[TN][8];   // partials at (row p = ty + NW u, column q = tx + 32v)
 #pragma unroll
-  for (int v = 0; v < 2; ++v)
+  for (int v = 0; v < TN; ++v)
 #pragma unroll
     for (int u = 0; u < 8; ++u) pA[v][u] = pB[v][u] = 0.f;
   // Y_g tiles through a two-deep cp.async ring: row i + 1 loads while row i is used
   const int q4 = a.RP / 4;
   auto load_y = [&](int i) {
     const float* Yg = a.Y + (row0 + i) * (int64_t)a.ldy * a.RP;
-    float* dst = Yb + (i & 1) * kCpMaxR * kCpLy;
-    for (int idx = tid; idx < r * q4; idx += kCpThreads) {
+    float* dst = Yb + (i & 1) * MR * LY;
+    for (int idx = tid; idx < r * q4; idx += NT) {
       const int j = idx / q4, c = idx - j * q4;
-      cp_async16(dst + j * kCpLy + 4 * c, Yg + (int64_t)j * a.RP + 4 * c, true);
+      cp_async16(dst + j * LY + 4 * c, Yg + (int64_t)j * a.RP + 4 * c, true);
     }
     cp_async_commit();
   };
@@ -200,59 +228,105 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
     if (i + 1 < nrow) { load_y(i + 1); cp_async_wait<1>(); }
     else cp_async_wait<0>();
     __syncthreads();
-    const float* Ys = Yb + (i & 1) * kCpMaxR * kCpLy;
-    const int ly = kCpLy;
+    const float* Ys = Yb + (i & 1) * MR * LY;
+    const int ly = LY;
     if (mode == kRowsAB) {
       // Z[j][q] = sum_m Y[j][m] D[m][q]
-      {
-        float zc[8][2];
-        cp_mm(r, r, R, [&](int j, int m) { return Ys[j * ly + m]; },
-              [&](int m, int q) { return Fs[m * lz + q]; }, zc);
+      float zc[8][TN];
+      cp_mm<MR>(r, r, R, [&](int j, int m) { return Ys[j * ly + m]; },
+                [&](int m, int q) { return Fs[m * lz + q]; }, zc);
+      if constexpr (MR <= 64) {
 #pragma unroll
         for (int u = 0; u < 8; ++u)
 #pragma unroll
-          for (int v = 0; v < 2; ++v) {
-            const int j = ty + 8 * u, q = tx + 32 * v;
+          for (int v = 0; v < TN; ++v) {
+            const int j = ty + NW * u, q = tx + 32 * v;
             if (j < r && q < r) Zs[j * lz + q] = zc[u][v];
           }
-      }
-      __syncthreads();
-      // rhs[q] = sum_j B[j][q] Z[j][q]: four partial sums per column, then their sum
-      {
-        const int q = tid & 63, part = tid >> 6;
-        float s = 0.f;
-        if (q < r)
-          for (int j = part; j < r; j += 4) s = fmaf(Bs[j * lz + q], Zs[j * lz + q], s);
-        red4[part][q] = s;
-      }
-      __syncthreads();
-      if (tid < r) rhs[tid] = (red4[0][tid] + red4[1][tid]) + (red4[2][tid] + red4[3][tid]);
-      __syncthreads();
-      // A_g = G_A^{-1} rhs with the inverse the per-chromosome kernel left in L
-      {
-        const int p = tid & 63, part = tid >> 6;
-        float s = 0.f;
-        if (p < r)
-          for (int q = part; q < r; q += 4) s = fmaf(Ls[p * lz + q], rhs[q], s);
-        red4[part][p] = s;
-      }
-      __syncthreads();
-      if (tid < r) {
-        const float s = (red4[0][tid] + red4[1][tid]) + (red4[2][tid] + red4[3][tid]);
-        ysol[tid] = s;
-        a.A[g * ld + tid] = s;
-      }
-      __syncthreads();
+        __syncthreads();
+        // rhs[q] = sum_j B[j][q] Z[j][q]: four partial sums per column, then their sum
+        {
+          const int q = tid & (MR - 1), part = tid / MR;
+          float s = 0.f;
+          if (q < r)
+            for (int j = part; j < r; j += 4) s = fmaf(Bs[j * lz + q], Zs[j * lz + q], s);
+          red4[part][q] = s;
+        }
+        __syncthreads();
+        if (tid < r) rhs[tid] = (red4[0][tid] + red4[1][tid]) + (red4[2][tid] + red4[3][tid]);
+        __syncthreads();
+        // A_g = G_A^{-1} rhs with the inverse the per-chromosome kernel left in L
+        {
+          const int p = tid & (MR - 1), part = tid / MR;
+          float s = 0.f;
+          if (p < r)
+            for (int q = part; q < r; q += 4) s = fmaf(Ls[p * lz + q], rhs[q], s);
+          red4[part][p] = s;
+        }
+        __syncthreads();
+        if (tid < r) {
+          const float s = (red4[0][tid] + red4[1][tid]) + (red4[2][tid] + red4[3][tid]);
+          ysol[tid] = s;
+          a.A[g * ld + tid] = s;
+        }
+        __syncthreads();
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int p = ty + 8 * u;
-        if (p < r) {
+        for (int u = 0; u < 8; ++u) {
+          const int p = ty + NW * u;
+          if (p < r) {
 #pragma unroll
-          for (int v = 0; v < 2; ++v) {
-            const int q = tx + 32 * v;
-            if (q < r) {
-              pA[v][u] = fmaf(ysol[p], ysol[q], pA[v][u]);           // A^T A
-              pB[v][u] = fmaf(ysol[q], Zs[p * lz + q], pB[v][u]);    // MTTKRP_B[p][q]
+            for (int v = 0; v < TN; ++v) {
+              const int q = tx + 32 * v;
+              if (q < r) {
+                pA[v][u] = fmaf(ysol[p], ysol[q], pA[v][u]);           // A^T A
+                pB[v][u] = fmaf(ysol[q], Zs[p * lz + q], pB[v][u]);    // MTTKRP_B[p][q]
+              }
+            }
+          }
+        }
+      } else {
+        // Z stays in registers: rhs[q] = sum_j B[j][q] Z[j][q] as per-warp partials, summed
+        // over the warps in order
+#pragma unroll
+        for (int v = 0; v < TN; ++v) {
+          const int q = tx + 32 * v;
+          float s = 0.f;
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int j = ty + NW * u;
+            if (j < r && q < r) s = fmaf(__ldg(Bc + j * ld + q), zc[u][v], s);
+          }
+          red[ty * MR + q] = s;
+        }
+        __syncthreads();
+        if (tid < r) {
+          float s = 0.f;
+          for (int w = 0; w < NW; ++w) s += red[w * MR + tid];
+          rhs[tid] = s;
+        }
+        __syncthreads();
+        // A_g = G_A^{-1} rhs: one warp per row of the inverse, lanes along its columns
+        for (int p = ty; p < r; p += NW) {
+          float s = 0.f;
+          for (int q = tx; q < r; q += 32) s = fmaf(__ldg(Lc + p * ld + q), rhs[q], s);
+          s = warp_sum(s);
+          if (tx == 0) {
+            ysol[p] = s;
+            a.A[g * ld + p] = s;
+          }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int p = ty + NW * u;
+          if (p < r) {
+#pragma unroll
+            for (int v = 0; v < TN; ++v) {
+              const int q = tx + 32 * v;
+              if (q < r) {
+                pA[v][u] = fmaf(ysol[p], ysol[q], pA[v][u]);           // A^T A
+                pB[v][u] = fmaf(ysol[q], zc[u][v], pB[v][u]);          // MTTKRP_B[p][q]
+              }
             }
           }
         }
@@ -261,18 +335,18 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
     } else {
       // MTTKRP_D[m][q] += A[q] * sum_j Y[j][m] B[j][q]
       const float* Ag = a.A + g * ld;
-      float ag[2];
+      float ag[TN];
 #pragma unroll
-      for (int v = 0; v < 2; ++v) ag[v] = tx + 32 * v < r ? Ag[tx + 32 * v] : 0.f;
-      float yb[8][2];
-      cp_mm(R, r, r, [&](int m, int j) { return Ys[j * ly + m]; },
-            [&](int j, int q) { return Fs[j * lz + q]; }, yb);
+      for (int v = 0; v < TN; ++v) ag[v] = tx + 32 * v < r ? Ag[tx + 32 * v] : 0.f;
+      float yb[8][TN];
+      cp_mm<MR>(R, r, r, [&](int m, int j) { return Ys[j * ly + m]; },
+                [&](int j, int q) { return Fs[j * lz + q]; }, yb);
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const int m = ty + 8 * u;
+        const int m = ty + NW * u;
         if (m < R) {
 #pragma unroll
-          for (int v = 0; v < 2; ++v) {
+          for (int v = 0; v < TN; ++v) {
             const int q = tx + 32 * v;
             if (q < r) pA[v][u] = fmaf(ag[v], yb[u][v], pA[v][u]);
           }
@@ -283,9 +357,9 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
   }
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
-    const int p = ty + 8 * u;
+    const int p = ty + NW * u;
 #pragma unroll
-    for (int v = 0; v < 2; ++v) {
+    for (int v = 0; v < TN; ++v) {
       const int q = tx + 32 * v;
       if (mode == kRowsAB) {
         if (p < r && q < r) {
@@ -302,14 +376,16 @@ __global__ void __launch_bounds__(kCpThreads) cp_rows_kernel(CpArgs a, int mode)
 // Gi = G^{-1} for an SPD G (r x r, stride lg) by in-place Gauss-Jordan without pivoting (the
 // sweep operator; the pivots of an SPD matrix are positive).  Two barriers per pivot, against
 // three per column for the Cholesky factor plus a serial triangular inverse.  scratch:
-// 2 * kCpMaxR floats.  Returns false on a pivot that is not positive (in every thread).
+// 2 * MR floats.  Returns false on a pivot that is not positive (in every thread).
+template <int MR>
 __device__ bool cp_spd_inverse(const float* G, int r, int lg, float* scratch, float* Gi) {
+  constexpr int NW = CpShape<MR>::NW;
   __shared__ int bad;
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   float* prow = scratch;
-  float* pcol = scratch + kCpMaxR;
+  float* pcol = scratch + MR;
   if (tid == 0) bad = 0;
-  for (int p = ty; p < r; p += 8)
+  for (int p = ty; p < r; p += NW)
     for (int q = tx; q < r; q += 32) Gi[p * lg + q] = G[p * lg + q];
   __syncthreads();
   for (int k = 0; k < r; ++k) {
@@ -324,7 +400,7 @@ __device__ bool cp_spd_inverse(const float* G, int r, int lg, float* scratch, fl
       if (tid == 0) bad = 1;
     }
     const float inv = 1.f / d;
-    for (int p = ty; p < r; p += 8) {
+    for (int p = ty; p < r; p += NW) {
       const float cp = pcol[p] * inv;
       for (int q = tx; q < r; q += 32) {
         float v;
@@ -339,49 +415,61 @@ __device__ bool cp_spd_inverse(const float* G, int r, int lg, float* scratch, fl
   return bad == 0;
 }
 
-// out rows = RHS rows G^{-1} (RHS: nrhs x r, stride ldr, nrhs <= 64; Gi symmetric, stride lg).
+// out rows = RHS rows G^{-1} (RHS: nrhs x r, stride ldr, nrhs <= MR; Gi symmetric, stride lg).
+template <int MR>
 __device__ void cp_apply_inverse(const float* RHS, int ldr, int nrhs, const float* Gi, int r,
                                  int lg, float* out, int ldo) {
+  constexpr int NW = CpShape<MR>::NW, TN = CpShape<MR>::TN;
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  float acc[8][2];
-  cp_mm(nrhs, r, r, [&](int row, int p) { return RHS[(size_t)row * ldr + p]; },
-        [&](int p, int q) { return Gi[p * lg + q]; }, acc);
+  float acc[8][TN];
+  cp_mm<MR>(nrhs, r, r, [&](int row, int p) { return RHS[(size_t)row * ldr + p]; },
+            [&](int p, int q) { return Gi[p * lg + q]; }, acc);
 #pragma unroll
   for (int u = 0; u < 8; ++u)
 #pragma unroll
-    for (int v = 0; v < 2; ++v) {
-      const int row = w + 8 * u, q = l + 32 * v;
+    for (int v = 0; v < TN; ++v) {
+      const int row = w + NW * u, q = l + 32 * v;
       if (row < nrhs && q < r) out[(size_t)row * ldo + q] = acc[u][v];
     }
 }
 
 // Gram F^T F of an (nrows x r, stride ld) factor into G (stride ld), fp32.
+template <int MR>
 __device__ void cp_gram(const float* F, int nrows, int r, int ld, float* G) {
+  constexpr int NW = CpShape<MR>::NW, TN = CpShape<MR>::TN;
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  float acc[8][2];
-  cp_mm(r, r, nrows, [&](int p, int i) { return F[i * ld + p]; },
-        [&](int i, int q) { return F[i * ld + q]; }, acc);
+  float acc[8][TN];
+  cp_mm<MR>(r, r, nrows, [&](int p, int i) { return F[i * ld + p]; },
+            [&](int i, int q) { return F[i * ld + q]; }, acc);
 #pragma unroll
   for (int u = 0; u < 8; ++u)
 #pragma unroll
-    for (int v = 0; v < 2; ++v) {
-      const int p = w + 8 * u, q = l + 32 * v;
+    for (int v = 0; v < TN; ++v) {
+      const int p = w + NW * u, q = l + 32 * v;
       if (p < r && q < r) G[p * ld + q] = acc[u][v];
     }
 }
 
-__global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode) {
+// Dynamic shared memory of cp_small_kernel: the system and its inverse (ld x (ld + 1) each),
+// the inverse's two scratch rows and an RP x ld work tile.
+__host__ __device__ inline size_t cp_small_smem(int ld, int rp, int mr) {
+  return (2 * (size_t)ld * (ld + 1) + 2 * (size_t)mr + (size_t)rp * ld) * sizeof(float);
+}
+
+template <int MR>
+__global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
+  constexpr int NW = CpShape<MR>::NW;
   extern __shared__ __align__(16) float sf[];
   const int ci = blockIdx.x;
   const int r = a.c_rank[ci], R = a.R, ld = a.ld;
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   const int lg = ld + 1;                  // odd stride: column walks hit distinct banks
   float* G = sf;                          // ld x lg: the system
-  float* Li = G + ld * lg;                // ld x lg: scratch of the inverse (two rows used)
-  float* Gi = Li + ld * lg;               // ld x lg: the system's inverse
-  float* work = Gi + ld * lg;             // RP*ld
+  float* Gi = G + ld * lg;                // ld x lg: the system's inverse
+  float* Li = Gi + ld * lg;               // 2 MR: scratch rows of the inverse
+  float* work = Li + 2 * MR;              // RP*ld
   __shared__ double dred[32];
-  __shared__ float nA[kCpMaxR], nB[kCpMaxR], nD[kCpMaxR];
+  __shared__ float nA[MR], nB[MR], nD[MR];
   __shared__ int stop;
   float* gAA = a.gAA + (size_t)ci * ld * ld;
   float* gBB = a.gBB + (size_t)ci * ld * ld;
@@ -393,15 +481,15 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
   const size_t ps = cp_pstride(ld);
 
   if (mode == kSmallCore) {
-    for (int p = ty; p < r; p += 8)
+    for (int p = ty; p < r; p += NW)
       for (int q = tx; q < r; q += 32) {
         gAA[p * ld + q] = chunk_sum(a.part + k0 * ps + p * ld + q, ps, nk);
       }
-    cp_gram(Bc, r, r, ld, gBB);
-    cp_gram(Dc, R, r, ld, gDD);
+    cp_gram<MR>(Bc, r, r, ld, gBB);
+    cp_gram<MR>(Dc, R, r, ld, gDD);
     __syncthreads();
     double c = 0.0;
-    for (int p = ty; p < r; p += 8)
+    for (int p = ty; p < r; p += NW)
       for (int q = tx; q < r; q += 32)
         c += (double)gAA[p * ld + q] * (double)gBB[p * ld + q] * (double)gDD[p * ld + q];
     c = block_sum<double>(c, dred);
@@ -420,8 +508,8 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
       a.loss[2 * ci] = 0.0;
       a.loss[2 * ci + 1] = 0.0;
     }
-    cp_gram(Bc, r, r, ld, gBB);
-    cp_gram(Dc, R, r, ld, gDD);
+    cp_gram<MR>(Bc, r, r, ld, gBB);
+    cp_gram<MR>(Dc, R, r, ld, gDD);
     __syncthreads();
   } else if (a.state[ci] & 1) {
     return;
@@ -429,7 +517,7 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
 
   if (mode == kSmallB) {
     // A^T A, MTTKRP_B; G_B = A^T A * D^T D + 1e-10 I; B <- MTTKRP_B G_B^{-1}
-    for (int p = ty; p < r; p += 8)
+    for (int p = ty; p < r; p += NW)
       for (int q = tx; q < r; q += 32) {
         const float s = chunk_sum(a.part + k0 * ps + p * ld + q, ps, nk);
         const float t = chunk_sum(a.part + k0 * ps + ld * ld + p * ld + q, ps, nk);
@@ -438,32 +526,32 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
         G[p * lg + q] = s * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
       }
     __syncthreads();
-    if (!cp_spd_inverse(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
-    cp_apply_inverse(work, ld, r, Gi, r, lg, Bc, ld);
+    if (!cp_spd_inverse<MR>(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+    cp_apply_inverse<MR>(work, ld, r, Gi, r, lg, Bc, ld);
     __syncthreads();
-    cp_gram(Bc, r, r, ld, gBB);
+    cp_gram<MR>(Bc, r, r, ld, gBB);
     return;
   }
   if (mode == kSmallD || mode == kSmallDLast) {
     // MTTKRP_D; G_D = A^T A * B^T B + 1e-10 I; D <- MTTKRP_D G_D^{-1}; loss; balance
-    for (int m = ty; m < R; m += 8)
+    for (int m = ty; m < R; m += NW)
       for (int q = tx; q < r; q += 32) {
         work[m * ld + q] = chunk_sum(a.part + k0 * ps + m * ld + q, ps, nk);
       }
-    for (int p = ty; p < r; p += 8)
+    for (int p = ty; p < r; p += NW)
       for (int q = tx; q < r; q += 32)
         G[p * lg + q] = gAA[p * ld + q] * gBB[p * ld + q] + (p == q ? 1e-10f : 0.f);
     __syncthreads();
-    if (!cp_spd_inverse(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
-    cp_apply_inverse(work, ld, R, Gi, r, lg, Dc, ld);
+    if (!cp_spd_inverse<MR>(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+    cp_apply_inverse<MR>(work, ld, R, Gi, r, lg, Dc, ld);
     __syncthreads();
-    cp_gram(Dc, R, r, ld, gDD);
+    cp_gram<MR>(Dc, R, r, ld, gDD);
     __syncthreads();
     double xh = 0.0, xy = 0.0;
-    for (int p = ty; p < r; p += 8)
+    for (int p = ty; p < r; p += NW)
       for (int q = tx; q < r; q += 32)
         xh += (double)gAA[p * ld + q] * (double)gBB[p * ld + q] * (double)gDD[p * ld + q];
-    for (int m = ty; m < R; m += 8)
+    for (int m = ty; m < R; m += NW)
       for (int q = tx; q < r; q += 32) xy += (double)Dc[m * ld + q] * (double)work[m * ld + q];
     xh = block_sum<double>(xh, dred);
     xy = block_sum<double>(xy, dred);
@@ -494,23 +582,23 @@ __global__ void __launch_bounds__(kCpThreads) cp_small_kernel(CpArgs a, int mode
   }
   __syncthreads();
   if (tid < r) a.scaleA[(size_t)ci * ld + tid] = 1.f / (nA[tid] + 1e-15f);
-  for (int j = ty; j < r; j += 8)
+  for (int j = ty; j < r; j += NW)
     for (int q = tx; q < r; q += 32) Bc[j * ld + q] = Bc[j * ld + q] / (nB[q] + 1e-15f);
-  for (int m = ty; m < R; m += 8)
+  for (int m = ty; m < R; m += NW)
     for (int q = tx; q < r; q += 32)
       Dc[m * ld + q] = Dc[m * ld + q] / (nD[q] + 1e-15f) * (nA[q] * nB[q] * nD[q] + 1e-15f);
   __syncthreads();
   if (mode == kSmallDLast) return;
   // Grams of the balanced factors; the inverse of B^T B * D^T D + 1e-10 I for the next A rows
-  cp_gram(Bc, r, r, ld, gBB);
-  cp_gram(Dc, R, r, ld, gDD);
+  cp_gram<MR>(Bc, r, r, ld, gBB);
+  cp_gram<MR>(Dc, R, r, ld, gDD);
   __syncthreads();
-  for (int p = ty; p < r; p += 8)
+  for (int p = ty; p < r; p += NW)
     for (int q = tx; q < r; q += 32)
       G[p * lg + q] = gBB[p * ld + q] * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
   __syncthreads();
-  if (!cp_spd_inverse(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
-  for (int p = ty; p < r; p += 8)
+  if (!cp_spd_inverse<MR>(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+  for (int p = ty; p < r; p += NW)
     for (int q = tx; q < r; q += 32) Lc[p * ld + q] = Gi[p * lg + q];
 }
 
@@ -526,19 +614,12 @@ extern "C" size_t fh_cp_workspace(int32_t nchrom, int32_t nchunks, int32_t ld, i
          sizeof(int) * (size_t)nchrom + 256;
 }
 
-// Runs n_iter CP-ALS sweeps on every chromosome (parafac with n_iter_max = n_iter) and leaves
-// core[chrom] = ||[[A,B,D]]||^2 of the result.  meta: int32 tables
-//   [c_row0, c_nbin, c_rank, c_chunk0, c_nchunk] (nchrom each) then
-//   [k_chrom, k_row0, k_nrow] (nchunks each).
-extern "C" int fh_cp_als(int32_t nchrom, int32_t nchunks, const int32_t* meta, float* A,
-                         float* B, float* D, const float* Y, int32_t ld, int32_t rp, int32_t R,
-                         int32_t ldy, int32_t n_iter, double* core, double* cross,
-                         void* workspace, size_t workspace_bytes, int* status, void* stream) {
-  if (nchrom <= 0 || nchunks <= 0 || !meta || !A || !B || !D || !Y || !core || !workspace ||
-      n_iter < 0 || R > rp || ld < R || rp > ld)
-    return FH_ERR_ARG;
-  if (ld > kCpMaxR || R > kCpMaxR) return FH_ERR_UNSUPPORTED;
-  if (workspace_bytes < fh_cp_workspace(nchrom, nchunks, ld, rp)) return FH_ERR_ARG;
+template <int MR>
+static int cp_launch(int32_t nchrom, int32_t nchunks, const int32_t* meta, float* A, float* B,
+                     float* D, const float* Y, int32_t ld, int32_t rp, int32_t R, int32_t ldy,
+                     int32_t n_iter, double* core, double* cross, void* workspace, int* status,
+                     void* stream) {
+  constexpr int NT = CpShape<MR>::NT;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t l = (size_t)ld * ld;
   CpArgs a{};
@@ -563,31 +644,51 @@ extern "C" int fh_cp_als(int32_t nchrom, int32_t nchunks, const int32_t* meta, f
   a.core = core;
   a.cross = cross;
   a.status = status;
-  const size_t small_smem = (3 * (size_t)ld * (ld + 1) + (size_t)rp * ld) * sizeof(float);
-  if (ensure_smem((const void*)cp_small_kernel, small_smem) ||
-      ensure_smem((const void*)cp_rows_kernel, kCpRowsSmem))
+  const size_t small_smem = cp_small_smem(ld, rp, MR);
+  const size_t rs = cp_rows_smem<MR>();
+  if (small_smem > 227 * 1024) return FH_ERR_UNSUPPORTED;
+  if (ensure_smem((const void*)cp_small_kernel<MR>, small_smem) ||
+      ensure_smem((const void*)cp_rows_kernel<MR>, rs))
     return FH_ERR_LAUNCH;
-  const size_t rs = kCpRowsSmem;
   if (n_iter == 0) {  // core norm only, factors untouched
-    cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsGram);
-    cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, kSmallCore);
+    cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsGram);
+    cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, kSmallCore);
     FH_CHECK_LAUNCH();
     return FH_OK;
   }
   // Each sweep recomputes every A row from Y, B and D, so the A scaling of a balance only
   // matters after the last sweep: the initial balance and the intermediate ones rescale B
   // and D (in place) and leave A to the next sweep.
-  cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsNorm);
-  cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, kSmallInit);
+  cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsNorm);
+  cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, kSmallInit);
   for (int it = 0; it < n_iter; ++it) {
-    cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsAB);
-    cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, kSmallB);
-    cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsD);
-    cp_small_kernel<<<nchrom, kCpThreads, small_smem, s>>>(a, it + 1 < n_iter ? kSmallD : kSmallDLast);
+    cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsAB);
+    cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, kSmallB);
+    cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsD);
+    cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, it + 1 < n_iter ? kSmallD : kSmallDLast);
   }
-  cp_rows_kernel<<<nchunks, kCpThreads, rs, s>>>(a, kRowsScale);
+  cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsScale);
   FH_CHECK_LAUNCH();
   return FH_OK;
+}
+
+// Runs n_iter CP-ALS sweeps on every chromosome (parafac with n_iter_max = n_iter) and leaves
+// core[chrom] = ||[[A,B,D]]||^2 of the result.  meta: int32 tables
+//   [c_row0, c_nbin, c_rank, c_chunk0, c_nchunk] (nchrom each) then
+//   [k_chrom, k_row0, k_nrow] (nchunks each).
+extern "C" int fh_cp_als(int32_t nchrom, int32_t nchunks, const int32_t* meta, float* A,
+                         float* B, float* D, const float* Y, int32_t ld, int32_t rp, int32_t R,
+                         int32_t ldy, int32_t n_iter, double* core, double* cross,
+                         void* workspace, size_t workspace_bytes, int* status, void* stream) {
+  if (nchrom <= 0 || nchunks <= 0 || !meta || !A || !B || !D || !Y || !core || !workspace ||
+      n_iter < 0 || R > rp || ld < R || rp > ld)
+    return FH_ERR_ARG;
+  if (ld > kCpMaxR || R > kCpMaxR) return FH_ERR_UNSUPPORTED;
+  if (workspace_bytes < fh_cp_workspace(nchrom, nchunks, ld, rp)) return FH_ERR_ARG;
+  if (ld > 64) return cp_launch<128>(nchrom, nchunks, meta, A, B, D, Y, ld, rp, R, ldy, n_iter,
+                                     core, cross, workspace, status, stream);
+  return cp_launch<64>(nchrom, nchunks, meta, A, B, D, Y, ld, rp, R, ldy, n_iter, core, cross,
+                       workspace, status, stream);
 }
 
 // core[chrom] = ||[[A, B, D]]||^2 without changing the factors (parafac2_intergrative.py:621-632).

@@ -55,6 +55,15 @@ __global__ void meta_gram_reduce_kernel(const double* __restrict__ partial, int 
   }
 }
 
+// Bytes before the misc floats of meta_small_kernel for R > 64: G (fp64), later reused by the
+// iterate and its scratch ((R + 4) rows each at stride ldv).
+__host__ __device__ inline size_t meta_big_body_bytes(int R) {
+  const int ldv = ((R + 3) & ~3) + 4;
+  const size_t g = (size_t)R * R * sizeof(double);
+  const size_t it = 2 * (size_t)(R + 4) * ldv * sizeof(float);
+  return g > it ? g : it;
+}
+
 // One CTA: Cholesky (fp64), Newton polar of Rc (fp32), sum(S), K = Rc^{-1} P (fp64).
 __global__ void __launch_bounds__(kPolThreads) meta_small_kernel(const double* __restrict__ Gg,
                                                                  int R, double* __restrict__ K,
@@ -71,6 +80,7 @@ __global__ void __launch_bounds__(kPolThreads) meta_small_kernel(const double* _
   float* X = fbase;
   float* Aug = X + (size_t)R * ldt;
   float* misc = Aug + newton_scratch_floats(R);
+  if (R > 64) misc = reinterpret_cast<float*>(smraw + meta_big_body_bytes(R));
   PolarScratch s = polar_scratch(misc, red, dred, ival);
   if (tid == 0) ival[0] = 0;
   for (int idx = tid; idx < R * R; idx += kPolThreads) G[idx] = Gg[idx];
@@ -96,13 +106,42 @@ __global__ void __launch_bounds__(kPolThreads) meta_small_kernel(const double* _
     }
     __syncthreads();
   }
+  if (R > 64) {
+    // R <= 128: Rc goes out to K first, then the iterate and its scratch (stride ldv) take
+    // the shared memory G used; P = polar(Rc) by the 4 x 8-tiled iteration
+    for (int idx = tid; idx < R * R; idx += kPolThreads) {
+      const int p = idx / R, q = idx % R;
+      K[R * R + idx] = q >= p ? G[idx] : 0.0;
+    }
+    __syncthreads();
+    const int ldv = ((R + 3) & ~3) + 4;
+    float* Xv = reinterpret_cast<float*>(smraw);
+    float* Sv = Xv + (size_t)(R + 4) * ldv;
+    const double* Rg = K + (size_t)R * R;
+    for (int idx = tid; idx < R * R; idx += kPolThreads) {
+      const int p = idx / R, q = idx % R;
+      Xv[p * ldv + q] = (float)Rg[idx];
+    }
+    __syncthreads();
+    newton_polar_tiled<8>(Xv, ldv, Sv, R, s);
+    double acc = 0.0;
+    for (int idx = tid; idx < R * R; idx += kPolThreads) {
+      const int p = idx / R, q = idx % R;
+      if (q >= p) acc += (double)Xv[p * ldv + q] * Rg[idx];
+    }
+    acc = block_sum<double>(acc, dred);
+    if (tid == 0) *ssum_out = acc;
+    for (int idx = tid; idx < R * R; idx += kPolThreads)
+      K[idx] = (double)Xv[(idx / R) * ldv + idx % R];   // P, overwritten by K column by column
+    if (tid == 0 && ival[0]) set_status(status, FH_ERR_ILLCOND);
+    return;
+  }
   for (int idx = tid; idx < R * R; idx += kPolThreads) {
     const int p = idx / R, q = idx % R;
     X[p * ldt + q] = q >= p ? (float)G[p * R + q] : 0.f;
   }
   __syncthreads();
-  if (R <= 64) newton_polar_r64(X, ldt, Aug, R, true, s);
-  else newton_polar(X, ldt, Aug, R, true, s);
+  newton_polar_r64(X, ldt, Aug, R, true, s);
   double acc = 0.0;
   for (int idx = tid; idx < R * R; idx += kPolThreads) {
     const int p = idx / R, q = idx % R;
@@ -138,7 +177,7 @@ __global__ void __launch_bounds__(32) meta_ksolve_kernel(double* __restrict__ KR
 __global__ void __launch_bounds__(256) meta_apply_kernel(const float* __restrict__ S, int C, int R,
                                                          int RP, const double* __restrict__ K,
                                                          float* __restrict__ E) {
-  __shared__ double Ks[64 * 64];  // R <= 64 here
+  extern __shared__ double Ks[];  // R x R
   for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) Ks[idx] = K[idx];
   __syncthreads();
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)C * RP;
@@ -167,7 +206,7 @@ extern "C" int fh_meta_polar(const float* S, int32_t n_cells, int32_t R, int32_t
                              double* ssum, void* workspace, size_t workspace_bytes, int* status,
                              void* stream) {
   if (!S || !E || !ssum || !workspace || n_cells <= 0 || R <= 0 || R > rp) return FH_ERR_ARG;
-  if (R > 64) return FH_ERR_UNSUPPORTED;
+  if (R > kMaxRank) return FH_ERR_UNSUPPORTED;
   if (workspace_bytes < fh_meta_polar_workspace(n_cells, R)) return FH_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream;
   const int blocks = (int)ceil_div(n_cells, kGramCells);
@@ -177,9 +216,11 @@ extern "C" int fh_meta_polar(const float* S, int32_t n_cells, int32_t R, int32_t
   meta_gram_kernel<<<blocks, 256, 0, s>>>(S, n_cells, R, rp, partial);
   meta_gram_reduce_kernel<<<(R * R + 255) / 256, 256, 0, s>>>(partial, blocks, R, G);
   const int ldt = R + 1;
-  const size_t smem = (size_t)R * R * sizeof(double) +
-                      ((size_t)R * ldt + newton_scratch_floats(R) + kPolarMiscFloats) *
-                          sizeof(float);
+  size_t smem = (size_t)R * R * sizeof(double) +
+                ((size_t)R * ldt + newton_scratch_floats(R) + kPolarMiscFloats) * sizeof(float);
+  if (R > 64)   // G, then the iterate and scratch in the same bytes, then the misc floats
+    smem = meta_big_body_bytes(R) + (size_t)kPolarMiscFloats * sizeof(float);
+  if (smem > 227 * 1024) return FH_ERR_UNSUPPORTED;
   if (ensure_smem((const void*)meta_small_kernel, smem))
     return FH_ERR_LAUNCH;
   meta_small_kernel<<<1, kPolThreads, smem, s>>>(G, R, K, ssum, status);
@@ -187,7 +228,9 @@ extern "C" int fh_meta_polar(const float* S, int32_t n_cells, int32_t R, int32_t
   const int64_t total = (int64_t)n_cells * rp;
   int grid = (int)ceil_div(total, 256);
   if (grid > 152 * 8) grid = 152 * 8;
-  meta_apply_kernel<<<grid, 256, 0, s>>>(S, n_cells, R, rp, K, E);
+  const size_t ksmem = (size_t)R * R * sizeof(double);
+  if (ensure_smem((const void*)meta_apply_kernel, ksmem)) return FH_ERR_LAUNCH;
+  meta_apply_kernel<<<grid, 256, ksmem, s>>>(S, n_cells, R, rp, K, E);
   FH_CHECK_LAUNCH();
   return FH_OK;
 }

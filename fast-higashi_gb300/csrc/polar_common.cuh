@@ -707,50 +707,63 @@ __device__ inline void newton_polar_r64(float* X, int ldx, float* Sc, int r, boo
 }
 
 
-// ---- 64 x 64 products with 4 x 4 register tiles (threads 0..255; r <= 64) -----------------
-// acc[u][v] = sum_{k < r} A[i0 + u][k] B[k][j0 + v] with i0 = 4 (t >> 4), j0 = 4 (t & 15);
-// fa4(k, i0) returns A[i0 .. i0+3][k], B is read as float4 rows (ldb a multiple of 4, the
-// base 16-byte aligned).  Threads from 256 on, and blocks past r, leave acc zero.
-template <class FA>
-__device__ __forceinline__ void mm44(int r, FA fa4, const float* B, int ldb, float (&acc)[4][4]) {
-  const int t = threadIdx.x, i0 = 4 * (t >> 4), j0 = 4 * (t & 15);
+// ---- r x r products on 4 x TJ register tiles (r <= 16 TJ; threads 0 .. 64 TJ - 1) -------
+// acc[u][v] = sum_{k < r} A[i0 + u][k] B[k][j0 + v] with i0 = 4 (t >> 4), j0 = TJ (t & 15):
+// TJ = 4 covers r <= 64 on 256 threads, TJ = 8 covers r <= 128 on 512.  fa4(k, i0) returns
+// A[i0 .. i0+3][k], B is read as float4 rows (ldb a multiple of 4, the base 16-byte aligned,
+// ldb >= 4 ceil(r / 4) + 4 so a tile's columns stay inside its row).  Threads past 64 TJ,
+// and tiles past r, leave acc zero.
+template <int TJ, class FA>
+__device__ __forceinline__ void mm4t(int r, FA fa4, const float* B, int ldb, float (&acc)[4][TJ]) {
+  const int t = threadIdx.x, i0 = 4 * (t >> 4), j0 = TJ * (t & 15);
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
-  if (t >= 256 || i0 >= r || j0 >= r) return;
+    for (int v = 0; v < TJ; ++v) acc[u][v] = 0.f;
+  if (t >= 64 * TJ || i0 >= r || j0 >= r) return;
 #pragma unroll 4
   for (int k = 0; k < r; ++k) {
     const float4 a = fa4(k, i0);
-    const float4 b = *reinterpret_cast<const float4*>(B + k * ldb + j0);
-    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+    const float av[4] = {a.x, a.y, a.z, a.w};
+    float bv[TJ];
+#pragma unroll
+    for (int h = 0; h < TJ / 4; ++h) {
+      const float4 b = *reinterpret_cast<const float4*>(B + k * ldb + j0 + 4 * h);
+      bv[4 * h] = b.x; bv[4 * h + 1] = b.y; bv[4 * h + 2] = b.z; bv[4 * h + 3] = b.w;
+    }
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+      for (int v = 0; v < TJ; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
   }
 }
 
-// Writes a 4 x 4 tile (rows i0.., columns j0..) of C (ldc a multiple of 4) from mm44's thread.
-__device__ __forceinline__ void st44(float* C, int ldc, int r, const float (&v)[4][4]) {
-  const int t = threadIdx.x, i0 = 4 * (t >> 4), j0 = 4 * (t & 15);
-  if (t >= 256 || i0 >= r || j0 >= r) return;
+// Writes a 4 x TJ tile (rows i0.., columns j0..) of C (ldc a multiple of 4) from mm4t's thread.
+template <int TJ>
+__device__ __forceinline__ void st4t(float* C, int ldc, int r, const float (&v)[4][TJ]) {
+  const int t = threadIdx.x, i0 = 4 * (t >> 4), j0 = TJ * (t & 15);
+  if (t >= 64 * TJ || i0 >= r || j0 >= r) return;
 #pragma unroll
   for (int u = 0; u < 4; ++u)
-    if (i0 + u < r)   // rows past r belong to the next buffer; columns up to j0 + 3 < ldc
-      *reinterpret_cast<float4*>(C + (i0 + u) * ldc + j0) =
-          make_float4(v[u][0], v[u][1], v[u][2], v[u][3]);
+    if (i0 + u < r)   // rows past r belong to the next buffer; columns up to j0 + TJ - 1 < ldc
+#pragma unroll
+      for (int h = 0; h < TJ / 4; ++h)
+        *reinterpret_cast<float4*>(C + (i0 + u) * ldc + j0 + 4 * h) =
+            make_float4(v[u][4 * h], v[u][4 * h + 1], v[u][4 * h + 2], v[u][4 * h + 3]);
 }
 
-// newton_polar_r64 for an upper-triangular R with its products on 4 x 4 register tiles:
-// X and Sc use the row stride ldv (a multiple of 4, 16-byte aligned rows), the steps and
-// their arithmetic are those of newton_polar_r64 (scaled Newton step with the blocked
+// newton_polar_r64 for an upper-triangular R with its products on 4 x TJ register tiles:
+// X and Sc use the row stride ldv (a multiple of 4, 16-byte aligned rows, >= 4 ceil(r/4) + 4),
+// the steps and their arithmetic are those of newton_polar_r64 (scaled Newton step with the
 // triangular inverse, scaling by sqrt of the largest row sum of X^T X, quintic boosts, cubic
-// Newton-Schulz to 3e-5 plus one step).  512 threads; products on threads 0..255.
-__device__ inline void newton_polar_r64v(float* X, int ldv, float* Sc, int r, PolarScratch& s) {
+// Newton-Schulz to 3e-5 plus one step).  512 threads; TJ = 4 for r <= 64 (products on threads
+// 0..255, the blocked triangular inverse), TJ = 8 for r <= 128 (products on all 512 threads,
+// the column-by-column triangular inverse).
+template <int TJ>
+__device__ inline void newton_polar_tiled(float* X, int ldv, float* Sc, int r, PolarScratch& s) {
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, t = threadIdx.x;
-  const int i0 = 4 * (t >> 4), j0 = 4 * (t & 15);
-  const bool mine = t < 256 && i0 < r && j0 < r;
+  const int i0 = 4 * (t >> 4), j0 = TJ * (t & 15);
+  const bool mine = t < 64 * TJ && i0 < r && j0 < r;
   auto at = [&](const float* M, int k, int i) {            // M[i..i+3][k] (rows)
     return make_float4(M[i * ldv + k], M[(i + 1) * ldv + k], M[(i + 2) * ldv + k],
                        M[(i + 3) * ldv + k]);
@@ -759,7 +772,8 @@ __device__ inline void newton_polar_r64v(float* X, int ldv, float* Sc, int r, Po
     return *reinterpret_cast<const float4*>(M + k * ldv + i);
   };
   // ---- 1. scaled Newton step
-  tri_inverse_blocked(X, ldv, Sc, ldv, r, true, s);
+  if (TJ == 4) tri_inverse_blocked(X, ldv, Sc, ldv, r, true, s);
+  else tri_inverse(X, ldv, Sc, ldv, r, s);
   {
     float a = 0.f, b = 0.f;
     for (int i = w; i < r; i += 16)
@@ -777,15 +791,15 @@ __device__ inline void newton_polar_r64v(float* X, int ldv, float* Sc, int r, Po
     __syncthreads();
   }
   // ---- 2. scale into [1/U, 1]: U = sqrt of the largest row sum of |X^T X|
-  float acc[4][4];
-  mm44(r, [&](int k, int i) { return col(X, k, i); }, X, ldv, acc);
+  float acc[4][TJ];
+  mm4t<TJ>(r, [&](int k, int i) { return col(X, k, i); }, X, ldv, acc);
   {
     float rmax = 0.f;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       float rs = 0.f;
 #pragma unroll
-      for (int v = 0; v < 4; ++v)
+      for (int v = 0; v < TJ; ++v)
         if (j0 + v < r) rs += fabsf(acc[u][v]);
       for (int o = 8; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);  // 16 lanes
       if (mine && i0 + u < r) rmax = fmaxf(rmax, rs);
@@ -808,43 +822,47 @@ __device__ inline void newton_polar_r64v(float* X, int ldv, float* Sc, int r, Po
   int kq = (Ub > 0.f) ? (int)ceilf(logf(0.6f * Ub) / logf(3.2f)) : 0;
   kq = kq < 0 ? 0 : (kq > 16 ? 16 : kq);
   for (int q = 0; q < kq; ++q) {
-    mm44(r, [&](int k, int i) { return col(X, k, i); }, X, ldv, acc);     // A = X^T X
-    st44(Sc, ldv, r, acc);
+    mm4t<TJ>(r, [&](int k, int i) { return col(X, k, i); }, X, ldv, acc);     // A = X^T X
+    st4t<TJ>(Sc, ldv, r, acc);
     __syncthreads();
-    float a2[4][4];
-    mm44(r, [&](int k, int i) { return col(Sc, k, i); }, Sc, ldv, a2);   // A^2 (A symmetric)
+    float a2[4][TJ];
+    mm4t<TJ>(r, [&](int k, int i) { return col(Sc, k, i); }, Sc, ldv, a2);   // A^2 (A symmetric)
     __syncthreads();
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v)
+      for (int v = 0; v < TJ; ++v)
         a2[u][v] = (i0 + u == j0 + v ? 3.4445f : 0.f) - 4.7750f * acc[u][v] + 2.0315f * a2[u][v];
-    st44(Sc, ldv, r, a2);
+    st4t<TJ>(Sc, ldv, r, a2);
     __syncthreads();
-    mm44(r, [&](int k, int i) { return at(X, k, i); }, Sc, ldv, acc);     // X P
+    mm4t<TJ>(r, [&](int k, int i) { return at(X, k, i); }, Sc, ldv, acc);     // X P
     __syncthreads();
-    st44(X, ldv, r, acc);
+    st4t<TJ>(X, ldv, r, acc);
     __syncthreads();
   }
   // ---- 4. cubic Newton-Schulz to convergence
   bool last = false;
   for (int it = 0; it < 16; ++it) {
     float dn = 0.f, nn = 0.f;
-    mm44(r, [&](int k, int i) { return col(X, k, i); }, X, ldv, acc);
+    mm4t<TJ>(r, [&](int k, int i) { return col(X, k, i); }, X, ldv, acc);
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) acc[u][v] = (i0 + u == j0 + v ? 1.5f : 0.f) - 0.5f * acc[u][v];
-    st44(Sc, ldv, r, acc);
+      for (int v = 0; v < TJ; ++v) acc[u][v] = (i0 + u == j0 + v ? 1.5f : 0.f) - 0.5f * acc[u][v];
+    st4t<TJ>(Sc, ldv, r, acc);
     __syncthreads();
-    mm44(r, [&](int k, int i) { return at(X, k, i); }, Sc, ldv, acc);
-    float old[4][4] = {};
+    mm4t<TJ>(r, [&](int k, int i) { return at(X, k, i); }, Sc, ldv, acc);
+    float old[4][TJ] = {};
     if (mine) {
 #pragma unroll
       for (int u = 0; u < 4; ++u)
         if (i0 + u < r) {
-          const float4 o = *reinterpret_cast<const float4*>(X + (i0 + u) * ldv + j0);
-          old[u][0] = o.x; old[u][1] = o.y; old[u][2] = o.z; old[u][3] = o.w;
+#pragma unroll
+          for (int h = 0; h < TJ / 4; ++h) {
+            const float4 o = *reinterpret_cast<const float4*>(X + (i0 + u) * ldv + j0 + 4 * h);
+            old[u][4 * h] = o.x; old[u][4 * h + 1] = o.y;
+            old[u][4 * h + 2] = o.z; old[u][4 * h + 3] = o.w;
+          }
         }
     }
     __syncthreads();
@@ -852,20 +870,24 @@ __device__ inline void newton_polar_r64v(float* X, int ldv, float* Sc, int r, Po
 #pragma unroll
       for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int v = 0; v < 4; ++v)
+        for (int v = 0; v < TJ; ++v)
           if (i0 + u < r && j0 + v < r) {
             const float d = acc[u][v] - old[u][v];
             dn = fmaf(d, d, dn);
             nn = fmaf(acc[u][v], acc[u][v], nn);
           }
     }
-    st44(X, ldv, r, acc);
+    st4t<TJ>(X, ldv, r, acc);
     dn = block_sum<float>(dn, s.red);
     nn = block_sum<float>(nn, s.red);
     __syncthreads();
     if (last) break;
     if (sqrtf(dn / nn) < 3e-5f) last = true;
   }
+}
+
+__device__ inline void newton_polar_r64v(float* X, int ldv, float* Sc, int r, PolarScratch& s) {
+  newton_polar_tiled<4>(X, ldv, Sc, r, s);
 }
 
 }  // namespace fh

@@ -53,7 +53,8 @@ __host__ __device__ inline size_t proc_smem_floats(int n, int r, int rp) {
 }
 
 // M[m][l] = sum_rho D[m][rho] A_g[rho] B[l][rho] (m < RP, rows m >= R zero) into dst (stride
-// ldt); stage: (RP + r) x ldt floats, may overlap dst.  Called by the whole CTA.
+// ldt); stage: (RP + r) x ldt floats, may overlap dst (the product is held in registers).
+// Called by the whole CTA.
 template <int RP>
 __device__ inline void form_m(const ProcArgs& a, int64_t g, int ci, int r, int ldt, float* stage,
                               float* dst) {
@@ -69,14 +70,15 @@ __device__ inline void form_m(const ProcArgs& a, int64_t g, int ci, int r, int l
   for (int l = ty; l < r; l += 16)
     for (int rho = tx; rho < r; rho += 32) Bs[l * ldt + rho] = Bc[l * a.ldb + rho];
   __syncthreads();
-  float acc[4][2];
-  cta_mm<4, 2>(RP, r, r, 0, [&](int m, int rho) { return DA[m * ldt + rho]; },
-               [&](int rho, int l) { return Bs[l * ldt + rho]; }, acc);
+  constexpr int TM = RP > 64 ? 8 : 4, TN = RP > 64 ? 4 : 2;   // the whole RP x r in registers
+  float acc[TM][TN];
+  cta_mm<TM, TN>(RP, r, r, 0, [&](int m, int rho) { return DA[m * ldt + rho]; },
+                 [&](int rho, int l) { return Bs[l * ldt + rho]; }, acc);
   __syncthreads();
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < TM; ++u)
 #pragma unroll
-    for (int v = 0; v < 2; ++v) {
+    for (int v = 0; v < TN; ++v) {
       const int m = ty + 16 * u, l = tx + 32 * v;
       if (m < RP && l < r) dst[m * ldt + l] = acc[u][v];
     }
@@ -86,7 +88,7 @@ __device__ inline void form_m(const ProcArgs& a, int64_t g, int ci, int r, int l
 // Gg[i][m] = sum_l U[i][l] M[m][l] for i < n, m < RP (U read through fu(i, l)).
 template <int RP, class FU>
 __device__ inline void gt_rows(int n, int r, int ldt, FU fu, const float* M, float* Gg) {
-  constexpr int TN = RP >= 64 ? 2 : 1;
+  constexpr int TN = RP >= 128 ? 4 : (RP >= 64 ? 2 : 1);
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int row0 = 0; row0 < n; row0 += 96) {
     float acc[6][TN];
@@ -195,6 +197,120 @@ __global__ void __launch_bounds__(kProcThreads, 2) procrustes_qr_kernel(ProcArgs
   if (tid == 0 && ival[0]) set_status(a.status, FH_ERR_ILLCOND);
 }
 
+// ---- ranks up to 128 (RP = 128) ------------------------------------------------------------
+// The same step with two regions of max(n, RP) rows at stride ldt = r + 1 (219.5 KB at
+// n = 205, r = 128; one CTA per SM).  The regions cannot hold the reflectors, the Newton
+// iterate and its scratch at once, so the CTA parks what it needs later in the bin row's own
+// output slots, which it overwrites at the end: M (RP x r) in its G^T rows (n x RP floats) and
+// the factored temp (R and the reflectors, n x r) in its U rows.  Reads of those parked values
+// come after a barrier and use ordinary loads (the CTA's own global writes are visible to it).
+//   RA: stage of M / temp -> QR / Newton scratch / reflectors again / M again
+//   RB: M / the Newton iterate (stride ldv) / U = Q [polar(R); 0]
+__host__ __device__ inline size_t procb_region_floats(int n, int r, int rp) {
+  const int ldt = r + 1, ldv = ((r + 3) & ~3) + 4;
+  size_t a = (size_t)(n > rp ? n : rp) * ldt;
+  const size_t v = (size_t)(r + 4) * ldv + 4;   // aligned iterate / scratch plus the rows mm4t
+  if (v > a) a = v;                             // reads past r
+  return (a + 3) & ~(size_t)3;
+}
+__host__ __device__ inline size_t procb_smem_floats(int n, int r, int rp) {
+  return 2 * procb_region_floats(n, r, rp) + kPolarMiscFloats;
+}
+
+__global__ void __launch_bounds__(kProcThreads, 1) procrustes_qr_big_kernel(ProcArgs a,
+                                                                           int region) {
+  constexpr int RP = 128;
+  extern __shared__ __align__(16) float sm[];
+  __shared__ float red[32];
+  __shared__ double dred[32];
+  __shared__ int ival[4];
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5, nw = kProcThreads / 32;
+  const int64_t g = blockIdx.x;
+  const fh_tile T = a.tiles[a.row_tile[g]];
+  const int i0 = (int)(g - T.brow0);
+  const int n = T.width, r = T.rank, ci = T.chrom;
+  const int ldt = r + 1, ldv = ((r + 3) & ~3) + 4;
+  float* RA = sm;
+  float* RB = sm + region;
+  PolarScratch s = polar_scratch(RB + region, red, dred, ival);
+  if (tid == 0) ival[0] = 0;
+  const int64_t brow = T.xoff + (int64_t)i0 * n;
+  float* Gg = a.Gt + brow * RP;
+  float* Ug = a.U + T.uoff + (int64_t)i0 * n * r;
+  form_m<RP>(a, g, ci, r, ldt, RA, RB);   // M in RB (the stage spans RA and RB)
+  if (a.mode == 1) {
+    // transform: Gt_g = U_g M^T with the stored projection (parafac2_intergrative.py:772-801)
+    const float* Us = Ug;
+    gt_rows<RP>(n, r, ldt, [&](int i, int l) { return __ldg(Us + (int64_t)i * r + l); }, RB, Gg);
+    return;
+  }
+  for (int m = ty; m < RP; m += nw)
+    for (int l = tx; l < r; l += 32) Gg[m * r + l] = RB[m * ldt + l];   // park M
+  // ---- temp[i][l] = sum_m W_g[i][m] M[m][l] into RA
+  {
+    const float* Wg = a.W + brow * RP;
+    for (int row0 = 0; row0 < n; row0 += 96) {
+      float acc[6][4];
+      cta_mm<6, 4>(n, r, RP, row0, [&](int i, int m) { return __ldg(Wg + (int64_t)i * RP + m); },
+                   [&](int m, int l) { return RB[m * ldt + l]; }, acc);
+#pragma unroll
+      for (int u = 0; u < 6; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const int i = row0 + ty + 16 * u, l = tx + 32 * v;
+          if (i < n && l < r) RA[i * ldt + l] = acc[u][v];
+        }
+    }
+    __syncthreads();
+  }
+  householder_qr(RA, n, r, ldt, s);
+  // park R and the reflectors; the iterate X = R (upper) at stride ldv in RB, scratch in RA
+  for (int i = ty; i < n; i += nw)
+    for (int l = tx; l < r; l += 32) Ug[(int64_t)i * r + l] = RA[i * ldt + l];
+  for (int p = ty; p < r; p += nw)
+    for (int q = tx; q < r; q += 32) RB[p * ldv + q] = q >= p ? RA[p * ldt + q] : 0.f;
+  __syncthreads();
+  newton_polar_tiled<8>(RB, ldv, RA, r, s);
+  // X to stride ldt in place (through registers), the parked factorization back into RA
+  {
+    float v[32];
+#pragma unroll
+    for (int e = 0; e < 32; ++e) {
+      const int idx = tid + kProcThreads * e;
+      v[e] = idx < r * r ? RB[(idx / r) * ldv + idx % r] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < 32; ++e) {
+      const int idx = tid + kProcThreads * e;
+      if (idx < r * r) RB[(idx / r) * ldt + idx % r] = v[e];
+    }
+    for (int i = ty; i < n; i += nw)
+      for (int l = tx; l < r; l += 32) RA[i * ldt + l] = Ug[(int64_t)i * r + l];
+    __syncthreads();
+  }
+  {
+    double acc = 0.0;
+    for (int p = ty; p < r; p += nw)
+      for (int q = p + tx; q < r; q += 32) acc += (double)RB[p * ldt + q] * (double)RA[p * ldt + q];
+    acc = block_sum<double>(acc, dred);
+    if (tid == 0) a.ssum[g] = acc;
+  }
+  // ---- U = Q [P; 0]
+  for (int j = r + ty; j < n; j += nw)
+    for (int l = tx; l < r; l += 32) RB[j * ldt + l] = 0.f;
+  __syncthreads();
+  apply_q(RA, ldt, RB, ldt, n, r, s);
+  for (int j = ty; j < n; j += nw)
+    for (int l = tx; l < r; l += 32) Ug[(int64_t)j * r + l] = RB[j * ldt + l];
+  // ---- Gt = U M^T with the parked M
+  for (int m = ty; m < RP; m += nw)
+    for (int l = tx; l < r; l += 32) RA[m * ldt + l] = Gg[m * r + l];
+  __syncthreads();
+  gt_rows<RP>(n, r, ldt, [&](int i, int l) { return RB[i * ldt + l]; }, RA, Gg);
+  if (tid == 0 && ival[0]) set_status(a.status, FH_ERR_ILLCOND);
+}
+
 // project2orthogonal drop-in: polar factor of each M[b] (n x r, n >= r).
 __global__ void __launch_bounds__(kProcThreads) polar_qr_kernel(const float* __restrict__ M, int n,
                                                                 int r, float* __restrict__ U,
@@ -247,7 +363,17 @@ using namespace fh;
 
 static int proc_launch(const ProcArgs& a, int64_t n_rows, int max_width, int max_rank, int rp,
                        cudaStream_t s) {
-  if (max_rank > 64 || max_width > kMaxWidth) return FH_ERR_UNSUPPORTED;
+  if (max_width > kMaxWidth || max_rank > rp) return FH_ERR_UNSUPPORTED;
+  if (rp == 128) {
+    const size_t region = procb_region_floats(max_width, max_rank, rp);
+    const size_t smem = procb_smem_floats(max_width, max_rank, rp) * sizeof(float);
+    if (smem > 227 * 1024) return FH_ERR_UNSUPPORTED;
+    if (ensure_smem((const void*)procrustes_qr_big_kernel, smem)) return FH_ERR_LAUNCH;
+    procrustes_qr_big_kernel<<<(unsigned)n_rows, kProcThreads, smem, s>>>(a, (int)region);
+    FH_CHECK_LAUNCH();
+    return FH_OK;
+  }
+  if (max_rank > 64) return FH_ERR_UNSUPPORTED;
   const size_t smem = proc_smem_floats(max_width, max_rank, rp) * sizeof(float);
   if (smem > 227 * 1024) return FH_ERR_UNSUPPORTED;
 #define FH_PROC(RPV)                                                                        \

@@ -71,8 +71,8 @@ class FitEngine:
             raise _lib.FHError("FitEngine", 2, "one dataset per chromosome (single resolution)")
         self.chrom_index = [self.names.index(d.chrom) for d in schic]
         self.ranks = [int(chrom2size[d.chrom]) for d in schic]
-        if max(self.ranks) > 64 or self.R > 64:
-            raise _lib.FHError("FitEngine", 2, "ranks above 64 are not supported yet")
+        if max(self.ranks) > 128 or self.R > 128:
+            raise _lib.FHError("FitEngine", 2, "ranks above 128 are not supported")
         self.do_rwr = do_rwr
         self.do_conv = bool(do_conv)
         self.do_col = bool(do_col) and bool(do_rwr)   # do_col acts inside the walk only
@@ -83,6 +83,10 @@ class FitEngine:
         order = sorted(range(len(schic)), key=lambda k: self.chrom_index[k])
         self.tiles, self.tile_base = tile_table(schic, self.chrom_index, self.ranks, self.n_rwr, order)
         t = self.tiles
+        if (t["width"] < t["rank"]).any():
+            # the per-bin polar factors are taken through a QR of the n x r matrix (n >= r)
+            raise _lib.FHError("FitEngine", 2,
+                               "a bin batch has fewer compact columns than its chromosome's rank")
         self.n_tiles = len(t)
         self.rows = int((t["rows"] * t["width"]).sum())
         self.ldx = int(math.ceil(self.rows / 128) * 128)

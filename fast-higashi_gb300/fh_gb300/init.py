@@ -88,34 +88,49 @@ def _chrom_band_rows(eng, k):
 
 
 def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
-    """U_k S_k (cells x n_comp) of chromosome k's band features F (cells x band rows)."""
+    """U_k S_k (cells x n_comp) of chromosome k's band features F (cells x band rows).
+    The sketch's n_comp + n_oversamples columns go through the X passes in blocks of at most
+    128 (the passes' widest operand)."""
     torch = eng.torch
-    P = _lib.ptr
     C = eng.C
     x0, x1 = _chrom_band_rows(eng, k)
     a0 = (x0 // 128) * 128
     a1 = min(eng.ldx, int(math.ceil(x1 / 128) * 128))
     rows = a1 - a0
     n = n_comp + n_oversamples
-    rp = 128 if n > 64 else (64 if n > 32 else (32 if n > 16 or eng.bf16 else 16))
     dev, f32 = eng.device, torch.float32
-    W = torch.zeros((rows, rp), dtype=f32, device=dev)
-    S = torch.zeros((C, rp), dtype=f32, device=dev)
-    splits = eng.xg_splits(C, rows)
-    part = torch.empty((splits, C, rp), dtype=f32, device=dev)
     lo, hi = x0 - a0, x1 - a0
+    blocks = [(c0, min(c0 + 128, n)) for c0 in range(0, n, 128)]
+    bufs = {}
+
+    def buffers(w):
+        rp = 128 if w > 64 else (64 if w > 32 else (32 if w > 16 or eng.bf16 else 16))
+        if rp not in bufs:
+            splits = eng.xg_splits(C, rows)
+            bufs[rp] = (torch.zeros((rows, rp), dtype=f32, device=dev),
+                        torch.zeros((C, rp), dtype=f32, device=dev),
+                        splits, torch.empty((splits, C, rp), dtype=f32, device=dev))
+        return rp, bufs[rp]
 
     def ft_times(Ecells):                     # F^T E: (band rows of k) x n
-        E = torch.zeros((C, rp), dtype=f32, device=dev)
-        E[:, :n] = Ecells
-        eng.x_times_e(a0, rows, C, E, rp, W)
-        return W[lo:hi, :n].clone()
+        out = []
+        for c0, c1 in blocks:
+            rp, (W, _, _, _) = buffers(c1 - c0)
+            E = torch.zeros((C, rp), dtype=f32, device=dev)
+            E[:, :c1 - c0] = Ecells[:, c0:c1]
+            eng.x_times_e(a0, rows, C, E, rp, W)
+            out.append(W[lo:hi, :c1 - c0].clone())
+        return torch.cat(out, dim=1)
 
     def f_times(Qrows):                       # F Q: cells x n
-        G = torch.zeros((rows, rp), dtype=f32, device=dev)
-        G[lo:hi, :n] = Qrows
-        eng.x_times_g(a0, rows, C, G, rp, splits, part, S)
-        return S[:, :n].clone()
+        out = []
+        for c0, c1 in blocks:
+            rp, (_, S, splits, part) = buffers(c1 - c0)
+            G = torch.zeros((rows, rp), dtype=f32, device=dev)
+            G[lo:hi, :c1 - c0] = Qrows[:, c0:c1]
+            eng.x_times_g(a0, rows, C, G, rp, splits, part, S)
+            out.append(S[:, :c1 - c0].clone())
+        return torch.cat(out, dim=1)
 
     omega = torch.from_numpy(rng.standard_normal((C, n)).astype(np.float32)).to(dev)
     Q = ft_times(omega)                       # range of F^T (band rows x n)

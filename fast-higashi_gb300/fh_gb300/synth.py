@@ -71,6 +71,8 @@ def workload(name: str) -> Workload:
     ``c3``  10,000 cells, 22 autosomes at 500 kb (5,774 bins), band 30, R=64, 30 iterations.
     ``c4``  2,000 cells at 500 kb, band 20, R=32 (differentiation workload).
     ``c5``  50,000 cells at 500 kb, band 40, R=128, 5 % ultra-sparse cells.
+    ``r128``  240 cells, 2 chromosomes of 440/300 bins at 500 kb, band 20, R=128 (ranks 128
+              and 90: the rank-128 kernels at test size).
     ``tiny`` / ``small``  reduced cases for tests.
     """
     if name == "c1":
@@ -87,6 +89,8 @@ def workload(name: str) -> Workload:
     if name == "c5":
         return Workload("c5", 50_000, genome_bins(500_000), 500_000, 40, (0.9, 1.3),
                         150_000, 1.0, 12, 128, 30, ultra_sparse_frac=0.05)
+    if name == "r128":
+        return Workload("r128", 240, [440, 300], 500_000, 20, (0.9, 1.3), 30_000, 0.6, 4, 128, 3)
     if name == "small":
         return Workload("small", 96, [70, 45, 33], 1_000_000, 6, (0.9, 1.3), 6_000, 0.6, 3, 8, 4)
     if name == "tiny":

@@ -129,6 +129,20 @@ def precision_report(name, iters=None, seed=0):
 
 
 @pytest.mark.gpu
+def test_rank128_against_fp64():
+    """R = 128 (chromosome ranks 128 and 90): init, the fit in every precision form and the
+    FP64 restatement from the same state; the rank-128 kernels (per-bin polar with parked
+    reflectors, 4 x 8-tiled Newton iteration, 512-thread CP-ALS, meta polar) at test size."""
+    r = precision_report("r128", iters=3)
+    print(json.dumps(r))
+    assert r["fp32_aligned_embedding_error"] < 5e-4
+    assert r["bf16x2_aligned_embedding_error"] < 1e-3
+    assert r["bf16_aligned_embedding_error"] < 1e-2
+    assert r["fp32_loss_max_rel_diff"] < 1e-4
+    assert r["bf16x2_loss_max_rel_diff"] < 1e-3
+
+
+@pytest.mark.gpu
 def test_aligned_embedding_error_c1():
     r = precision_report("c1")
     print(json.dumps(r))
