@@ -49,6 +49,9 @@ def parse():
                     help="time the differentiable reconstruction loss (forward + backward) "
                          "instead of the fit; prints its own JSON line")
     ap.add_argument("--iters", type=int, default=None, help="ALS iterations (default: the workload's 30)")
+    ap.add_argument("--cells", type=int, default=None,
+                    help="run the workload's shapes with this many cells instead (a reduced "
+                         "case, named as such in config.workload; never the headline)")
     ap.add_argument("--sample-cells", type=int, default=96,
                     help="cells of the CPU-baseline sample (at least the rank R)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -74,10 +77,13 @@ def dist_setup():
     return rank, local, ws
 
 
-def make_workload(name, seed=0):
+def make_workload(name, seed=0, cells=None):
+    import dataclasses
     from fh_gb300 import synth
     from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
     w = synth.workload(name)
+    if cells:
+        w = dataclasses.replace(w, n_cells=int(cells), name="%s at %d cells" % (name, cells))
     coo, _ = synth.generate(w, seed=seed)
     ds = []
     for (idx, val, shape), cname, nb in zip(coo, w.chrom_names, w.chrom_bins):
@@ -216,7 +222,7 @@ def cpu_sample_rate(coo, w, n_cells, iters, threads=None):
 def reference_arm(args, rank, ws):
     if rank != 0:
         return
-    w, coo, _ = make_workload(args.config)
+    w, coo, _ = make_workload(args.config, cells=args.cells)
     iters = args.iters or w.n_iter
     threads = os.cpu_count()
     rates, desc = [], ""
@@ -230,7 +236,7 @@ def reference_arm(args, rank, ws):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator, %s)" % args.config, "impl": "reference",
             "config": {"workload": "%s: %d cells, %d bins, R=%d, band %d, %d ALS iterations" %
-                       (args.config, w.n_cells, sum(w.chrom_bins), w.rank, w.band, iters),
+                       (w.name, w.n_cells, sum(w.chrom_bins), w.rank, w.band, iters),
                        "l2": "inputs larger than L2"},
             "cpu_baseline": {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
                              "sample": desc},
@@ -244,7 +250,7 @@ def gb300_arm(args, rank, local, ws):
     from fh_gb300 import Fast_Higashi_core, _lib
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    w, coo, ds = make_workload(args.config)
+    w, coo, ds = make_workload(args.config, cells=args.cells)
     iters = args.iters or w.n_iter
     C = w.n_cells
     # ---- init (untimed): the GPU init_params, then the state every step starts from
@@ -379,7 +385,7 @@ def gb300_arm(args, rank, local, ws):
             "vs_baseline": None, "dtype": "bf16" if eng.bf16 else "f32", "data": "synthetic (seeded generator, %s)" % args.config,
             "config": {"workload": "%s: %d cells, %d bins (%d bin batches), R=%d, band %d, %d ALS "
                                    "iterations, RWR epochs %s" %
-                                   (args.config, C, sum(w.chrom_bins), eng.n_tiles, w.rank, w.band,
+                                   (w.name, C, sum(w.chrom_bins), eng.n_tiles, w.rank, w.band,
                                     iters, sorted(set(int(v) for v in n_i))),
                        "precision": ({"bf16": "X in one bf16 plane, tensor-core X passes",
                                       "bf16x2": "X in two bf16 planes (hi+lo), tensor-core X passes"}
@@ -402,7 +408,7 @@ def grad_arm(args, rank, local, ws):
     from fh_gb300.differentiable import ReconstructionLoss
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    w, coo, ds = make_workload(args.config)
+    w, coo, ds = make_workload(args.config, cells=args.cells)
     torch.manual_seed(0)
     m = Fast_Higashi_core(w.rank, w.band, [w.resolution]).to(dev)
     m.fit(ds, size_ratio=w.dim1, n_iter_max=args.iters or 3, n_iter_parafac=1, do_conv=False,
@@ -464,7 +470,7 @@ def grad_arm(args, rank, local, ws):
             "data": "synthetic (seeded generator, %s)" % args.config,
             "config": {"workload": "%s: %d cells, %d bins (%d bin batches), R=%d, band %d, fitted "
                                    "state after %d ALS iterations" %
-                                   (args.config, C, sum(w.chrom_bins), eng.n_tiles, R, w.band,
+                                   (w.name, C, sum(w.chrom_bins), eng.n_tiles, R, w.band,
                                     args.iters or 3),
                        "l2": "inputs larger than L2 (X %.2f GB fp32)" % (Ct * eng.ldx * 4 / 1e9)},
             "roofline": {"kernel": fam, "bound": "fp32", "achieved": ach, "peak": fp32_peak,

@@ -22,9 +22,9 @@ struct PolarScratch {
   float* grow;   // [2][128] scaled pivot row
   float* grp;    // [2]      1 / pivot
   int* gi;       // [0, 64) row used as a pivot, [64, 128) step that pivoted the row, [128, 130) pivot
-  float* tri;    // [3][16][16] off-diagonal block products of the blocked triangular inverse
+  float* tri;    // [7][16][16] off-diagonal block products of the blocked triangular inverse
 };
-constexpr int kPolarMiscFloats = 5 * kMaxRank + 64 + 128 + 256 + 4 + 132 + 768;
+constexpr int kPolarMiscFloats = 5 * kMaxRank + 64 + 128 + 256 + 4 + 132 + 7 * 256;
 
 // Carves the scratch out of kPolarMiscFloats floats of shared memory.
 __device__ inline PolarScratch polar_scratch(float* misc, float* red, double* dred, int* ival) {
@@ -87,30 +87,40 @@ __device__ __forceinline__ int pc_nwarps() { return blockDim.x >> 5; }
 // householder_panel factors columns [k0, k1) and applies each reflector to the columns
 // below k1 only; householder_qr is the whole matrix as one panel.  (A blocked variant with
 // UT-form trailing updates measured 9 % slower here: the panel steps keep their barriers.)
+// The squared norm of the next column below its diagonal is gathered while the update writes
+// that column (per-warp partials, summed in warp order), so every thread forms the next
+// reflector itself: two barriers per column.
 __device__ inline void householder_panel(float* T, int n, int k0, int k1, int ldt,
                                          PolarScratch& s) {
   const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
-  for (int k = k0; k < k1; ++k) {
+  float* np = s.fcol;   // [nw] partial sums of squares of column k below row k
+  if (k0 < k1) {
     if (ty == 0) {
       float ss = 0.f;
-      for (int i = k + 1 + tx; i < n; i += 32) ss = fmaf(T[i * ldt + k], T[i * ldt + k], ss);
+      for (int i = k0 + 1 + tx; i < n; i += 32) ss = fmaf(T[i * ldt + k0], T[i * ldt + k0], ss);
       ss = warp_sum(ss);
-      if (tx == 0) {
-        const float x0 = T[k * ldt + k];
-        const float s2 = fmaf(x0, x0, ss);
-        if (s2 == 0.f) {
-          s.beta[k] = 0.f; s.vh[k] = 0.f; s.wv[2 * kMaxRank - 1] = 0.f;
-        } else {
-          const float nrm = sqrtf(s2);
-          const float alpha = x0 >= 0.f ? -nrm : nrm;
-          s.vh[k] = x0 - alpha;
-          s.beta[k] = 1.f / (s2 - x0 * alpha);
-          s.wv[2 * kMaxRank - 1] = alpha;
-        }
-      }
+      if (tx == 0) np[0] = ss;
+    } else if (tx == 0) {
+      np[ty] = 0.f;
     }
     __syncthreads();
-    const float beta = s.beta[k], vh = s.vh[k];
+  }
+  for (int k = k0; k < k1; ++k) {
+    float ss = 0.f;
+    for (int q = 0; q < nw; ++q) ss += np[q];
+    const float x0 = T[k * ldt + k];
+    const float s2 = fmaf(x0, x0, ss);
+    float beta = 0.f, vh = 0.f, alpha = 0.f;
+    if (s2 != 0.f) {
+      const float nrm = sqrtf(s2);
+      alpha = x0 >= 0.f ? -nrm : nrm;
+      vh = x0 - alpha;
+      beta = 1.f / (s2 - x0 * alpha);
+    }
+    if (threadIdx.x == 0) {
+      s.beta[k] = beta;
+      s.vh[k] = vh;
+    }
     // w_j = v^T T[k:, j]: four columns per warp (independent chains, one pass over v)
     for (int jb = k + 1 + 4 * ty; jb < k1; jb += 4 * nw) {
       float d[4] = {0.f, 0.f, 0.f, 0.f};
@@ -129,13 +139,22 @@ __device__ inline void householder_panel(float* T, int n, int k0, int k1, int ld
       }
     }
     __syncthreads();
+    float part = 0.f;   // this warp's rows of column k + 1 (lane 0 holds that column)
     if (beta != 0.f) {
       for (int i = k + ty; i < n; i += nw) {
         const float bv = -beta * ((i == k) ? vh : T[i * ldt + k]);
-        for (int j = k + 1 + tx; j < k1; j += 32) T[i * ldt + j] = fmaf(bv, s.wv[j], T[i * ldt + j]);
+        for (int j = k + 1 + tx; j < k1; j += 32) {
+          const float v = fmaf(bv, s.wv[j], T[i * ldt + j]);
+          T[i * ldt + j] = v;
+          if (j == k + 1 && i > k + 1) part = fmaf(v, v, part);
+        }
       }
+    } else if (tx == 0 && k + 1 < k1) {
+      for (int i = k + ty; i < n; i += nw)
+        if (i > k + 1) part = fmaf(T[i * ldt + k + 1], T[i * ldt + k + 1], part);
     }
-    if (threadIdx.x == 0) T[k * ldt + k] = s.wv[2 * kMaxRank - 1];
+    if (tx == 0) np[ty] = part;
+    if (threadIdx.x == 0) T[k * ldt + k] = alpha;
     __syncthreads();
   }
 }
@@ -145,17 +164,29 @@ __device__ inline void householder_qr(float* T, int n, int r, int ldt, PolarScra
 }
 
 // ---- U = Q U: apply the stored reflectors in reverse to U (n x r, stride ldu) ----------
+// The dot products v^T U[:, j] go four columns per warp (independent chains, one pass over v);
+// each column's sum runs in the same order as one column at a time.
 __device__ inline void apply_q(const float* T, int ldt, float* U, int ldu, int n, int r,
                                PolarScratch& s) {
   const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
   for (int k = r - 1; k >= 0; --k) {
     const float beta = s.beta[k], vh = s.vh[k];
     if (beta == 0.f) continue;  // uniform across the block
-    for (int j = ty; j < r; j += nw) {
-      float d = 0.f;
-      for (int i = k + 1 + tx; i < n; i += 32) d = fmaf(T[i * ldt + k], U[i * ldu + j], d);
-      d = warp_sum(d);
-      if (tx == 0) s.wv[j] = fmaf(vh, U[k * ldu + j], d);
+    for (int jb = 4 * ty; jb < r; jb += 4 * nw) {
+      float d[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int i = k + 1 + tx; i < n; i += 32) {
+        const float vi = T[i * ldt + k];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          if (jb + c < r) d[c] = fmaf(vi, U[i * ldu + jb + c], d[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) d[c] = warp_sum(d[c]);
+      if (tx == 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          if (jb + c < r) s.wv[jb + c] = fmaf(vh, U[k * ldu + jb + c], d[c]);
+      }
     }
     __syncthreads();
     for (int i = k + ty; i < n; i += nw) {
@@ -189,11 +220,11 @@ __device__ inline void tri_inverse(const float* R, int ldr, float* Xi, int ldo, 
   __syncthreads();
 }
 
-// ---- inverse of an upper-triangular R (r <= 64, stride ldr) into Xi (stride ldo), 512 threads
+// ---- inverse of an upper-triangular R (r <= 128, stride ldr) into Xi (stride ldo), 512 threads
 // Blocked: the 16 x 16 diagonal blocks are inverted by one warp each (a lane per column, the
 // column in registers, no synchronisation), then the off-diagonal blocks by block diagonals,
-// X_ij = -X_ii sum_{k=i+1..j} R_ik X_kj, as small products over all threads: six barriers in
-// all instead of a serial chain of r dependent steps.  Writes the upper triangle of Xi (and
+// X_ij = -X_ii sum_{k=i+1..j} R_ik X_kj, as small products over all threads: 2 (r/16 - 1) + 1
+// barriers in all instead of a serial chain of r dependent steps.  Writes the upper triangle of Xi (and
 // zeroes the strictly lower part when zero_lower is set).
 __device__ inline void tri_inverse_blocked(const float* R, int ldr, float* Xi, int ldo, int r,
                                            bool zero_lower, PolarScratch& s) {
@@ -757,8 +788,7 @@ __device__ __forceinline__ void st4t(float* C, int ldc, int r, const float (&v)[
 // the steps and their arithmetic are those of newton_polar_r64 (scaled Newton step with the
 // triangular inverse, scaling by sqrt of the largest row sum of X^T X, quintic boosts, cubic
 // Newton-Schulz to 3e-5 plus one step).  512 threads; TJ = 4 for r <= 64 (products on threads
-// 0..255, the blocked triangular inverse), TJ = 8 for r <= 128 (products on all 512 threads,
-// the column-by-column triangular inverse).
+// 0..255), TJ = 8 for r <= 128 (products on all 512 threads).
 template <int TJ>
 __device__ inline void newton_polar_tiled(float* X, int ldv, float* Sc, int r, PolarScratch& s) {
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, t = threadIdx.x;
@@ -772,8 +802,7 @@ __device__ inline void newton_polar_tiled(float* X, int ldv, float* Sc, int r, P
     return *reinterpret_cast<const float4*>(M + k * ldv + i);
   };
   // ---- 1. scaled Newton step
-  if (TJ == 4) tri_inverse_blocked(X, ldv, Sc, ldv, r, true, s);
-  else tri_inverse(X, ldv, Sc, ldv, r, s);
+  tri_inverse_blocked(X, ldv, Sc, ldv, r, true, s);
   {
     float a = 0.f, b = 0.f;
     for (int i = w; i < r; i += 16)
