@@ -87,40 +87,30 @@ __device__ __forceinline__ int pc_nwarps() { return blockDim.x >> 5; }
 // householder_panel factors columns [k0, k1) and applies each reflector to the columns
 // below k1 only; householder_qr is the whole matrix as one panel.  (A blocked variant with
 // UT-form trailing updates measured 9 % slower here: the panel steps keep their barriers.)
-// The squared norm of the next column below its diagonal is gathered while the update writes
-// that column (per-warp partials, summed in warp order), so every thread forms the next
-// reflector itself: two barriers per column.
 __device__ inline void householder_panel(float* T, int n, int k0, int k1, int ldt,
                                          PolarScratch& s) {
   const int tx = pc_lane(), ty = pc_warp(), nw = pc_nwarps();
-  float* np = s.fcol;   // [nw] partial sums of squares of column k below row k
-  if (k0 < k1) {
+  for (int k = k0; k < k1; ++k) {
     if (ty == 0) {
       float ss = 0.f;
-      for (int i = k0 + 1 + tx; i < n; i += 32) ss = fmaf(T[i * ldt + k0], T[i * ldt + k0], ss);
+      for (int i = k + 1 + tx; i < n; i += 32) ss = fmaf(T[i * ldt + k], T[i * ldt + k], ss);
       ss = warp_sum(ss);
-      if (tx == 0) np[0] = ss;
-    } else if (tx == 0) {
-      np[ty] = 0.f;
+      if (tx == 0) {
+        const float x0 = T[k * ldt + k];
+        const float s2 = fmaf(x0, x0, ss);
+        if (s2 == 0.f) {
+          s.beta[k] = 0.f; s.vh[k] = 0.f; s.wv[2 * kMaxRank - 1] = 0.f;
+        } else {
+          const float nrm = sqrtf(s2);
+          const float alpha = x0 >= 0.f ? -nrm : nrm;
+          s.vh[k] = x0 - alpha;
+          s.beta[k] = 1.f / (s2 - x0 * alpha);
+          s.wv[2 * kMaxRank - 1] = alpha;
+        }
+      }
     }
     __syncthreads();
-  }
-  for (int k = k0; k < k1; ++k) {
-    float ss = 0.f;
-    for (int q = 0; q < nw; ++q) ss += np[q];
-    const float x0 = T[k * ldt + k];
-    const float s2 = fmaf(x0, x0, ss);
-    float beta = 0.f, vh = 0.f, alpha = 0.f;
-    if (s2 != 0.f) {
-      const float nrm = sqrtf(s2);
-      alpha = x0 >= 0.f ? -nrm : nrm;
-      vh = x0 - alpha;
-      beta = 1.f / (s2 - x0 * alpha);
-    }
-    if (threadIdx.x == 0) {
-      s.beta[k] = beta;
-      s.vh[k] = vh;
-    }
+    const float beta = s.beta[k], vh = s.vh[k];
     // w_j = v^T T[k:, j]: four columns per warp (independent chains, one pass over v)
     for (int jb = k + 1 + 4 * ty; jb < k1; jb += 4 * nw) {
       float d[4] = {0.f, 0.f, 0.f, 0.f};
@@ -139,22 +129,13 @@ __device__ inline void householder_panel(float* T, int n, int k0, int k1, int ld
       }
     }
     __syncthreads();
-    float part = 0.f;   // this warp's rows of column k + 1 (lane 0 holds that column)
     if (beta != 0.f) {
       for (int i = k + ty; i < n; i += nw) {
         const float bv = -beta * ((i == k) ? vh : T[i * ldt + k]);
-        for (int j = k + 1 + tx; j < k1; j += 32) {
-          const float v = fmaf(bv, s.wv[j], T[i * ldt + j]);
-          T[i * ldt + j] = v;
-          if (j == k + 1 && i > k + 1) part = fmaf(v, v, part);
-        }
+        for (int j = k + 1 + tx; j < k1; j += 32) T[i * ldt + j] = fmaf(bv, s.wv[j], T[i * ldt + j]);
       }
-    } else if (tx == 0 && k + 1 < k1) {
-      for (int i = k + ty; i < n; i += nw)
-        if (i > k + 1) part = fmaf(T[i * ldt + k + 1], T[i * ldt + k + 1], part);
     }
-    if (tx == 0) np[ty] = part;
-    if (threadIdx.x == 0) T[k * ldt + k] = alpha;
+    if (threadIdx.x == 0) T[k * ldt + k] = s.wv[2 * kMaxRank - 1];
     __syncthreads();
   }
 }
@@ -739,19 +720,24 @@ __device__ inline void newton_polar_r64(float* X, int ldx, float* Sc, int r, boo
 
 
 // ---- r x r products on 4 x TJ register tiles (r <= 16 TJ; threads 0 .. 64 TJ - 1) -------
-// acc[u][v] = sum_{k < r} A[i0 + u][k] B[k][j0 + v] with i0 = 4 (t >> 4), j0 = TJ (t & 15):
-// TJ = 4 covers r <= 64 on 256 threads, TJ = 8 covers r <= 128 on 512.  fa4(k, i0) returns
+// Thread t owns rows i0 .. i0+3, i0 = 4 (t >> 4), and TJ / 4 column chunks of four: chunk h
+// starts at 4 (t & 15) + 64 h, so each float4 access of a half-warp covers 64 consecutive
+// floats (conflict-free).  TJ = 4 covers r <= 64 on 256 threads, TJ = 8 covers r <= 128 on
+// 512.  acc[u][4 h + e] = sum_{k < r} A[i0 + u][k] B[k][chunk h + e]; fa4(k, i0) returns
 // A[i0 .. i0+3][k], B is read as float4 rows (ldb a multiple of 4, the base 16-byte aligned,
-// ldb >= 4 ceil(r / 4) + 4 so a tile's columns stay inside its row).  Threads past 64 TJ,
-// and tiles past r, leave acc zero.
+// ldb >= 4 ceil(r / 4) + 4 so a chunk starting below r stays inside its row).  Threads past
+// 64 TJ, rows past r and chunks starting at or past r leave acc zero.
+__device__ __forceinline__ int tile_chunk(int h) { return 4 * (threadIdx.x & 15) + 64 * h; }
+
 template <int TJ, class FA>
 __device__ __forceinline__ void mm4t(int r, FA fa4, const float* B, int ldb, float (&acc)[4][TJ]) {
-  const int t = threadIdx.x, i0 = 4 * (t >> 4), j0 = TJ * (t & 15);
+  const int t = threadIdx.x, i0 = 4 * (t >> 4);
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
     for (int v = 0; v < TJ; ++v) acc[u][v] = 0.f;
-  if (t >= 64 * TJ || i0 >= r || j0 >= r) return;
+  if (t >= 64 * TJ || i0 >= r || tile_chunk(0) >= r) return;
+  const bool hi = TJ > 4 && tile_chunk(1) < r;
 #pragma unroll 4
   for (int k = 0; k < r; ++k) {
     const float4 a = fa4(k, i0);
@@ -759,7 +745,8 @@ __device__ __forceinline__ void mm4t(int r, FA fa4, const float* B, int ldb, flo
     float bv[TJ];
 #pragma unroll
     for (int h = 0; h < TJ / 4; ++h) {
-      const float4 b = *reinterpret_cast<const float4*>(B + k * ldb + j0 + 4 * h);
+      float4 b = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (h == 0 || hi) b = *reinterpret_cast<const float4*>(B + k * ldb + tile_chunk(h));
       bv[4 * h] = b.x; bv[4 * h + 1] = b.y; bv[4 * h + 2] = b.z; bv[4 * h + 3] = b.w;
     }
 #pragma unroll
@@ -769,18 +756,20 @@ __device__ __forceinline__ void mm4t(int r, FA fa4, const float* B, int ldb, flo
   }
 }
 
-// Writes a 4 x TJ tile (rows i0.., columns j0..) of C (ldc a multiple of 4) from mm4t's thread.
+// Writes mm4t's tile of C (ldc a multiple of 4): rows i0.. below r, the chunks starting below
+// r (their last columns stay inside the row padding).
 template <int TJ>
 __device__ __forceinline__ void st4t(float* C, int ldc, int r, const float (&v)[4][TJ]) {
-  const int t = threadIdx.x, i0 = 4 * (t >> 4), j0 = TJ * (t & 15);
-  if (t >= 64 * TJ || i0 >= r || j0 >= r) return;
+  const int t = threadIdx.x, i0 = 4 * (t >> 4);
+  if (t >= 64 * TJ || i0 >= r) return;
 #pragma unroll
   for (int u = 0; u < 4; ++u)
-    if (i0 + u < r)   // rows past r belong to the next buffer; columns up to j0 + TJ - 1 < ldc
+    if (i0 + u < r)   // rows past r belong to the next buffer
 #pragma unroll
       for (int h = 0; h < TJ / 4; ++h)
-        *reinterpret_cast<float4*>(C + (i0 + u) * ldc + j0 + 4 * h) =
-            make_float4(v[u][4 * h], v[u][4 * h + 1], v[u][4 * h + 2], v[u][4 * h + 3]);
+        if (tile_chunk(h) < r)
+          *reinterpret_cast<float4*>(C + (i0 + u) * ldc + tile_chunk(h)) =
+              make_float4(v[u][4 * h], v[u][4 * h + 1], v[u][4 * h + 2], v[u][4 * h + 3]);
 }
 
 // newton_polar_r64 for an upper-triangular R with its products on 4 x TJ register tiles:
@@ -792,8 +781,9 @@ __device__ __forceinline__ void st4t(float* C, int ldc, int r, const float (&v)[
 template <int TJ>
 __device__ inline void newton_polar_tiled(float* X, int ldv, float* Sc, int r, PolarScratch& s) {
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31, t = threadIdx.x;
-  const int i0 = 4 * (t >> 4), j0 = TJ * (t & 15);
-  const bool mine = t < 64 * TJ && i0 < r && j0 < r;
+  const int i0 = 4 * (t >> 4);
+  const bool mine = t < 64 * TJ && i0 < r && tile_chunk(0) < r;
+  auto jcol = [&](int v) { return tile_chunk(v >> 2) + (v & 3); };   // column of acc[.][v]
   auto at = [&](const float* M, int k, int i) {            // M[i..i+3][k] (rows)
     return make_float4(M[i * ldv + k], M[(i + 1) * ldv + k], M[(i + 2) * ldv + k],
                        M[(i + 3) * ldv + k]);
@@ -829,7 +819,7 @@ __device__ inline void newton_polar_tiled(float* X, int ldv, float* Sc, int r, P
       float rs = 0.f;
 #pragma unroll
       for (int v = 0; v < TJ; ++v)
-        if (j0 + v < r) rs += fabsf(acc[u][v]);
+        if (jcol(v) < r) rs += fabsf(acc[u][v]);
       for (int o = 8; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);  // 16 lanes
       if (mine && i0 + u < r) rmax = fmaxf(rmax, rs);
     }
@@ -861,7 +851,7 @@ __device__ inline void newton_polar_tiled(float* X, int ldv, float* Sc, int r, P
     for (int u = 0; u < 4; ++u)
 #pragma unroll
       for (int v = 0; v < TJ; ++v)
-        a2[u][v] = (i0 + u == j0 + v ? 3.4445f : 0.f) - 4.7750f * acc[u][v] + 2.0315f * a2[u][v];
+        a2[u][v] = (i0 + u == jcol(v) ? 3.4445f : 0.f) - 4.7750f * acc[u][v] + 2.0315f * a2[u][v];
     st4t<TJ>(Sc, ldv, r, a2);
     __syncthreads();
     mm4t<TJ>(r, [&](int k, int i) { return at(X, k, i); }, Sc, ldv, acc);     // X P
@@ -877,7 +867,7 @@ __device__ inline void newton_polar_tiled(float* X, int ldv, float* Sc, int r, P
 #pragma unroll
     for (int u = 0; u < 4; ++u)
 #pragma unroll
-      for (int v = 0; v < TJ; ++v) acc[u][v] = (i0 + u == j0 + v ? 1.5f : 0.f) - 0.5f * acc[u][v];
+      for (int v = 0; v < TJ; ++v) acc[u][v] = (i0 + u == jcol(v) ? 1.5f : 0.f) - 0.5f * acc[u][v];
     st4t<TJ>(Sc, ldv, r, acc);
     __syncthreads();
     mm4t<TJ>(r, [&](int k, int i) { return at(X, k, i); }, Sc, ldv, acc);
@@ -887,11 +877,12 @@ __device__ inline void newton_polar_tiled(float* X, int ldv, float* Sc, int r, P
       for (int u = 0; u < 4; ++u)
         if (i0 + u < r) {
 #pragma unroll
-          for (int h = 0; h < TJ / 4; ++h) {
-            const float4 o = *reinterpret_cast<const float4*>(X + (i0 + u) * ldv + j0 + 4 * h);
-            old[u][4 * h] = o.x; old[u][4 * h + 1] = o.y;
-            old[u][4 * h + 2] = o.z; old[u][4 * h + 3] = o.w;
-          }
+          for (int h = 0; h < TJ / 4; ++h)
+            if (tile_chunk(h) < r) {
+              const float4 o = *reinterpret_cast<const float4*>(X + (i0 + u) * ldv + tile_chunk(h));
+              old[u][4 * h] = o.x; old[u][4 * h + 1] = o.y;
+              old[u][4 * h + 2] = o.z; old[u][4 * h + 3] = o.w;
+            }
         }
     }
     __syncthreads();
@@ -900,7 +891,7 @@ __device__ inline void newton_polar_tiled(float* X, int ldv, float* Sc, int r, P
       for (int u = 0; u < 4; ++u)
 #pragma unroll
         for (int v = 0; v < TJ; ++v)
-          if (i0 + u < r && j0 + v < r) {
+          if (i0 + u < r && jcol(v) < r) {
             const float d = acc[u][v] - old[u][v];
             dn = fmaf(d, d, dn);
             nn = fmaf(acc[u][v], acc[u][v], nn);
