@@ -118,3 +118,54 @@ def test_autotuner_disabled_keeps_heuristic():
 
     t = Tuner(path="", enabled=False, timer=lambda fn, reps: fn())
     assert t.choose("dev", "xg_splits", (1,), [7, 3, 14], run) == 7
+
+
+class _FakeDeltas:
+    """Stands in for FitEngine.auto_deltas: planted ||Q_e - Q_{e+1}||_F per (tile, cell)."""
+
+    def __init__(self, deltas, n_good):
+        self.d, self.C, self.Ct = deltas, n_good, deltas.shape[1]
+        self.n_tiles = deltas.shape[0]
+        self.tile_base = [0, 2]
+
+    def auto_deltas(self, cap, all_cells=False):
+        import torch
+        out = torch.from_numpy(np.ascontiguousarray(self.d[:, :, :cap]))
+        return out if all_cells else out[:, :self.C]
+
+
+def test_auto_epochs_per_cell_batch():
+    """partial_rwr.py:99-126 per cell batch: a batch stops at the first epoch whose largest
+    delta over its cells is below 0.01 and keeps Q_{e+1}; 60 epochs without stopping keep Q_60;
+    n_i is the largest stopping epoch over the good batches only (parafac2_intergrative.py:265)."""
+    pytest.importorskip("torch")
+    from fh_gb300.init import auto_epochs
+
+    class D:   # two datasets of 2 bin batches, cells [0, 4) good in batches of 2, [4, 6) bad
+        def __init__(self):
+            self.num_bin_batch = 2
+            self.num_cell_batch = 2
+            self.cell_slice_list = [slice(0, 2), slice(2, 4), slice(4, 6)]
+
+    rng = np.random.default_rng(0)
+    d = rng.uniform(0.02, 1.0, size=(4, 6, 60)).astype(np.float32)
+    stops = {(0, 0): 3, (0, 1): 5, (0, 2): 20, (1, 0): 0, (1, 1): None, (1, 2): 2,
+             (2, 0): 14, (2, 1): 7, (2, 2): 1, (3, 0): 59, (3, 1): 4, (3, 2): None}
+    for (t, b), e in stops.items():
+        cs = D().cell_slice_list[b]
+        if e is not None:
+            d[t, cs, e] = 0.005          # every cell of the batch below 0.01 at epoch e
+    eng = _FakeDeltas(d, 4)
+    schic = [D(), D()]
+    n_i, feat, cell_ep = auto_epochs(eng, schic, per_cell=True)
+    want = np.zeros((4, 6), dtype=np.int32)
+    for (t, b), e in stops.items():
+        want[t, D().cell_slice_list[b]] = 60 if e is None else e + 1
+    np.testing.assert_array_equal(cell_ep, want)
+    stop = lambda t, b: 60 if stops[(t, b)] is None else stops[(t, b)]
+    assert list(n_i) == [max(stop(t, b) for t in (0, 1) for b in (0, 1)),
+                         max(stop(t, b) for t in (2, 3) for b in (0, 1))]
+    np.testing.assert_array_equal(feat, [max(want[t, :4]) for t in range(4)])
+    n_i2, feat2 = auto_epochs(eng, schic)       # the good batches alone give the same n_i
+    np.testing.assert_array_equal(n_i2, n_i)
+    np.testing.assert_array_equal(feat2, feat)
