@@ -12,8 +12,8 @@ the user sees them; and the largest relative difference of the loss trajectory.
 Bounds at 200 cells (c1): fp32 form 5e-4, bf16x2 form (X as two bf16 planes) 1e-3 (the target),
 bf16 form (one plane) 1e-2, losses 1e-3.
 
-FH_PRECISION_WORKLOAD=c2|c3 adds a full-size report (written to
-gpurun_out/precision_<workload>.json when that folder exists) to the GPU run.
+FH_PRECISION_WORKLOAD=c2|c3 adds a full-size report to the GPU run (also written to
+$FH_PRECISION_OUT/precision_<workload>.json when FH_PRECISION_OUT names a folder).
 """
 import json
 import math
@@ -160,8 +160,8 @@ def test_precision_report_full_size():
     name = os.environ["FH_PRECISION_WORKLOAD"]
     r = precision_report(name)
     print(json.dumps(r))
-    d = os.path.join(ROOT, "gpurun_out")
-    if os.path.isdir(d):
+    d = os.environ.get("FH_PRECISION_OUT", "")
+    if d and os.path.isdir(d):
         with open(os.path.join(d, "precision_%s.json" % name), "w") as f:
             json.dump(r, f, indent=1)
     assert math.isfinite(r["bf16x2_aligned_embedding_error"])
