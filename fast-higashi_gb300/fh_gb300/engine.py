@@ -78,7 +78,7 @@ class FitEngine:
         self.do_col = bool(do_col) and bool(do_rwr)   # do_col acts inside the walk only
         self._xc = None     # fp32 3 x 3-mean tiles for the bf16 forms (do_conv)
         self.cov = None     # do_col coverage rows [Ct][nb] (bin_cov, then bad_bin_cov rows)
-        self.cov_lists = None
+        self.cov_src = None  # the caller's (bin_cov_list, bad_bin_cov_list) the rows came from
         self.n_rwr = [int(v) if do_rwr else 0 for v in (n_i if n_i is not None else [0] * len(schic))]
         order = sorted(range(len(schic)), key=lambda k: self.chrom_index[k])
         self.tiles, self.tile_base = tile_table(schic, self.chrom_index, self.ranks, self.n_rwr, order)
@@ -243,7 +243,6 @@ class FitEngine:
             self.cov[:self.C, cols] = torch.as_tensor(good[k]).to(self.device, torch.float32)
             if self.Ct > self.C and not np.isscalar(bad[k]):
                 self.cov[self.C:, cols] = torch.as_tensor(bad[k]).to(self.device, torch.float32)
-        self.cov_lists = (good, bad)
 
     def coverage_views(self):
         """(bin_cov_list, bad_bin_cov_list) as views of the coverage rows."""
@@ -280,7 +279,7 @@ class FitEngine:
         _lib.call("fh_col_coverage", P(self.tiles_dev), self.n_tiles, self.Ct, P(colsum),
                   self.max_width, P(self.cov), self.nb, self.nb, P(self.status), self.sp())
         del colsum
-        self.cov_lists = None
+        self.cov_src = None
 
     def col_features(self, cell_epochs):
         """The do_col walk with per-cell-batch epochs (the init feature pass, :203-240)."""

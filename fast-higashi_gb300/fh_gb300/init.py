@@ -196,7 +196,7 @@ def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
     if eng.do_col:
         eng.finalize_coverage()
         model.bin_cov_list, model.bad_bin_cov_list = eng.coverage_views()
-        eng.cov_lists = (model.bin_cov_list, model.bad_bin_cov_list)
+        eng.cov_src = (model.bin_cov_list, model.bad_bin_cov_list)
     else:
         model.bin_cov_list = [None] * len(schic)
         model.bad_bin_cov_list = [0] * len(schic)

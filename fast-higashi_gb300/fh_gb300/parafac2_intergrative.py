@@ -88,22 +88,38 @@ class Fast_Higashi_core:
         init_params(self, schic, do_conv, do_rwr, do_col, seed=seed)
 
     # ------------------------------------------------------------------ fit
-    def _coverage(self):
+    def _coverage_src(self):
         return (getattr(self, "bin_cov_list", None), getattr(self, "bad_bin_cov_list", None))
+
+    def _coverage(self):
+        """(bin_cov_list, bad_bin_cov_list), or None while no coverage rows are set."""
+        good, bad = self._coverage_src()
+        if good is None or any(c is None for c in good):
+            return None
+        return good, (bad if bad is not None else [0] * len(good))
 
     def _engine(self, schic, do_rwr, do_conv=False, do_col=False):
         col = bool(do_col) and bool(do_rwr)
         if (self.engine is None or self.engine.schic is not schic or
                 self.engine.do_conv != bool(do_conv) or self.engine.do_col != col):
+            cov = self._coverage() if col else None
+            if col and cov is None:
+                raise _lib.FHError("fit", 1, "do_col needs bin_cov_list (init_params sets it)")
             self.engine = FitEngine(schic, self.rank, self.chrom2size, self.n_i, self.device,
                                     do_rwr=do_rwr, precision=self.precision, do_conv=do_conv,
-                                    do_col=col, bin_cov=self._coverage() if col else None)
+                                    do_col=col, bin_cov=cov)
+            if col:
+                self.engine.cov_src = self._coverage_src()
         elif col:
-            good, bad = self._coverage()
-            held = self.engine.cov_lists
-            if held is None or held[0] is not good or held[1] is not bad:
-                # coverage rows replaced since the walk ran (bin_cov_list was assigned)
-                self.engine.set_coverage(good, bad)
+            src = self._coverage_src()
+            held = self.engine.cov_src
+            if held is None or held[0] is not src[0] or held[1] is not src[1]:
+                # coverage rows assigned since the walk ran: take them and walk again
+                cov = self._coverage()
+                if cov is None:
+                    raise _lib.FHError("fit", 1, "do_col needs bin_cov_list (init_params sets it)")
+                self.engine.set_coverage(*cov)
+                self.engine.cov_src = src
                 self.engine.run_rwr()
         return self.engine
 

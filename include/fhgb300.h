@@ -280,7 +280,11 @@ int fh_project_y_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n_ro
  *   ssum[g] = sum of the singular values of temp,
  *   Gt[xoff + i*n + j][m] = sum_l U_g[j][l] M[m][l]  (the rows of lhs2 U^T).
  * A: float[n_rows][lda]; B: float[nchrom][ldb][ldb]; D: float[nchrom][rp][ldb] (rows >= R
- * zero); U: tile-major (rows x width x rank at tile.uoff).  r <= 64, rp <= 64, width <= 320. */
+ * zero); U: tile-major (rows x width x rank at tile.uoff).  r <= rp, width <= 320, width >= r.
+ * rp <= 64: two CTAs per SM.  rp = 128 (r <= 128): one CTA per SM with two regions of
+ * max(width, 128) rows of r + 1 floats (2 x max(width, 128) x (r + 1) x 4 + 12 KB <= 227 KB,
+ * so width <= 217 at r = 128); the CTA parks M in the bin row's own Gt rows and the factored
+ * temp in its own U rows while it iterates, then overwrites both (FH_ERR_UNSUPPORTED beyond). */
 int fh_procrustes_f32(const fh_tile* tiles, const int32_t* row_tile, int64_t n_rows,
                       int32_t max_width, int32_t max_rank, const float* W, const float* A,
                       int32_t lda, const float* B, const float* D, int32_t ldb, int32_t R,
@@ -340,7 +344,7 @@ int fh_polar_svals_f32(const float* M, const float* U, int64_t batch, int32_t n,
                        float* S, void* stream);
 
 /* ---- meta polar (parafac2_intergrative.py:483-486): E = polar(S), S = SVD_term^T
- * (float[n_cells][rp], R columns used, R <= 64); *ssum = sum of singular values = <E, S>.
+ * (float[n_cells][rp], R columns used, R <= 128); *ssum = sum of singular values = <E, S>.
  * fp64 Gram, fp64 Cholesky, Newton polar of the factor, fp64 apply. */
 size_t fh_meta_polar_workspace(int32_t n_cells, int32_t R);
 int fh_meta_polar(const float* S, int32_t n_cells, int32_t R, int32_t rp, float* E,
@@ -354,7 +358,8 @@ int fh_meta_polar(const float* S, int32_t n_cells, int32_t R, int32_t rp, float*
  * c_nchunk (nchrom each) then k_chrom, k_row0, k_nrow (nchunks each): bin-row chunks of at
  * most 8 rows, each inside one chromosome.  core: double[nchrom] = ||[[A,B,D]]||^2 after
  * the sweeps; cross (optional): double[nchrom] = <[[A,B,D]], Y> of the last sweep
- * (parafac's loss_norm and loss_x).  Requires r <= ld <= 64, R <= rp <= ld. */
+ * (parafac's loss_norm and loss_x).  Requires r <= ld <= 128, R <= rp <= ld (ld > 64 runs
+ * the 512-thread instantiation). */
 size_t fh_cp_workspace(int32_t nchrom, int32_t nchunks, int32_t ld, int32_t rp);
 int fh_cp_als(int32_t nchrom, int32_t nchunks, const int32_t* meta, float* A, float* B,
               float* D, const float* Y, int32_t ld, int32_t rp, int32_t R, int32_t ldy,
