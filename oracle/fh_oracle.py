@@ -215,16 +215,22 @@ class ChromData:
     indices: np.ndarray       # int32[3, nnz] (row, col, cell)
     values: np.ndarray        # float32[nnz]
     num_bin: int
-    num_cell: int
+    num_cell: int             # good-QC cells: [0, num_cell)
     bs_bin: int
     bs_cell: int
     flank: int
+    total_cell: int = 0       # all cells (0: num_cell); cells past num_cell are bad-QC
 
     def layout(self):
         return tile_layout(self.num_bin, self.bs_bin, self.flank)
 
     def cells(self):
         return cell_batches(self.num_cell, self.bs_cell)
+
+    def bad_cells(self):
+        """Bad-QC cell batches in global cell numbers (sparse_for_schic.py:422-427)."""
+        total = max(self.total_cell, self.num_cell)
+        return [slice(c, min(c + self.bs_cell, total)) for c in range(self.num_cell, total, self.bs_cell)]
 
     def tile(self, bb, cs, dtype):
         r, c, k, v = tile_coo(self.indices, self.values, bb, cs)
@@ -245,13 +251,15 @@ class ALSOracle:
     ALS iterations exactly as Fast_Higashi_core.fit does after init_params."""
 
     def __init__(self, datas, rank, A_list, B_dict, D_dict, E, n_i, dtype=np.float64, cache_rwr=True,
-                 do_conv=False, do_col=False, bin_cov_list=None):
+                 do_conv=False, do_col=False, bin_cov_list=None, bad_bin_cov_list=None):
         self.do_conv = do_conv
         self.do_col = do_col
         if do_col:
             if bin_cov_list is None:
                 raise ValueError("do_col needs the coverage rows (bin_cov_list)")
             self.bin_cov = [np.asarray(c, dtype=dtype) for c in bin_cov_list]
+            self.bad_bin_cov = [None if c is None or np.isscalar(c) else np.asarray(c, dtype=dtype)
+                                for c in (bad_bin_cov_list or [None] * len(datas))]
         self.datas = datas
         self.rank = rank
         self.dt = dtype
@@ -266,16 +274,20 @@ class ALSOracle:
         self.norm_tensor = None
         self.core_norm = self._core_norm()
 
-    def rwr_tile(self, ci, bi, cj):
-        """X of one tile after partial RWR with force_rwr_epochs = n_i, as (b, n, C)."""
-        key = (ci, bi, cj)
+    def rwr_tile(self, ci, bi, cj, bad=False):
+        """X of one tile after partial RWR with force_rwr_epochs = n_i, as (b, n, C); bad
+        selects the bad-QC cell batches (transform, parafac2_intergrative.py:803-827)."""
+        key = (ci, bi, cj, bad)
         if self._cache is not None and key in self._cache:
             return self._cache[key]
         d = self.datas[ci]
         bb = d.layout()[bi]
-        cs = d.cells()[cj]
+        cs = (d.bad_cells() if bad else d.cells())[cj]
         x = d.tile(bb, cs, self.dt)
-        cov = self.bin_cov[ci][cs, bb.col] if self.do_col else None   # :363
+        cov = None
+        if self.do_col:                                                   # :363, :819
+            cov = (self.bad_bin_cov[ci][cs.start - d.num_cell:cs.stop - d.num_cell, bb.col] if bad
+                   else self.bin_cov[ci][cs, bb.col])
         out, _ = partial_rwr(x, bb.local.start, bb.local.stop, do_rwr=True,
                              force_rwr_epochs=self.n_i[ci], final_transpose=True,
                              do_conv=self.do_conv, do_col=self.do_col, bin_cov=cov)
@@ -351,6 +363,7 @@ class ALSOracle:
         per chromosome (single resolution), so the per-chromosome Y is the dataset's Y."""
         first = self.norm_tensor is None
         U_all, Y, err_x_U, err_x_V, tnorm = self.update(first_iter=first)
+        self.U_last = U_all                      # the projections transform reuses (:750)
         if first:
             self.tensor_norm = tnorm
             self.norm_tensor = np.sqrt(tnorm)
@@ -382,10 +395,12 @@ class ALSOracle:
         return self
 
     def transform(self, U_all):
-        """transform (parafac2_intergrative.py:742-834), good-QC cells only: final SVD_term with
-        the stored projections and the current factors, then its polar factor."""
+        """transform (parafac2_intergrative.py:742-834): final SVD_term over the good and then
+        the bad-QC cells with the stored projections and the current factors, then its polar
+        factor (total cells x R)."""
         dt = self.dt
-        SVD_term = np.zeros((self.E.shape[1], self.E.shape[0]), dtype=dt)
+        total = max(max(d.total_cell, d.num_cell) for d in self.datas)
+        SVD_term = np.zeros((self.E.shape[1], total), dtype=dt)
         for ci, d in enumerate(self.datas):
             A, B, D = self.A_list[ci], self.B[d.name], self.D[d.name]
             for bi, bb in enumerate(d.layout()):
@@ -395,26 +410,34 @@ class ALSOracle:
                     X = self.rwr_tile(ci, bi, cj)
                     proj = np.matmul(U_all[ci][bi].transpose(0, 2, 1), X)
                     SVD_term[:, cs] += lhs @ proj.reshape(-1, proj.shape[-1])
+                for cj, cs in enumerate(d.bad_cells()):                      # :803-827
+                    X = self.rwr_tile(ci, bi, cj, bad=True)
+                    proj = np.matmul(U_all[ci][bi].transpose(0, 2, 1), X)
+                    SVD_term[:, cs] += lhs @ proj.reshape(-1, proj.shape[-1])
         E, _ = project2orthogonal(SVD_term.T, self.rank)
         return E
 
 
-def col_coverage(datas, dtype=np.float64, do_conv=False, mark_inf=True):
+def col_coverage(datas, dtype=np.float64, do_conv=False, mark_inf=True, bad=False):
     """bin_cov of init_params (parafac2_intergrative.py:96-99, 118-142, 266-267), good cells:
     per chromosome, 1e-4 plus, for every (bin batch, cell batch) in loop order, the column
     sums (over the tile's rows) of the auto-stopped do_col=False walk, added at the tile's
     global columns; entries still <= 1e-4 become inf when mark_inf (the do_col feature pass
-    of :203-240 runs before that replacement)."""
+    of :203-240 runs before that replacement).  bad: bad_bin_cov over the bad-QC cell
+    batches instead (:176-200, :268-271)."""
     dt = dtype
     out = []
     for d in datas:
-        cov = np.full((d.num_cell, d.num_bin), dt(1e-4), dtype=dt)
+        batches = d.bad_cells() if bad else d.cells()
+        c0 = d.num_cell if bad else 0
+        n = (max(d.total_cell, d.num_cell) - d.num_cell) if bad else d.num_cell
+        cov = np.full((n, d.num_bin), dt(1e-4), dtype=dt)
         for bb in d.layout():
-            for cs in d.cells():
+            for cs in batches:
                 x = d.tile(bb, cs, dt)
                 y, _ = partial_rwr(x, bb.local.start, bb.local.stop, do_rwr=True,
                                    force_rwr_epochs=-1, final_transpose=False, do_conv=do_conv)
-                cov[cs, bb.col] += y.sum(1)                               # :141-142
+                cov[cs.start - c0:cs.stop - c0, bb.col] += y.sum(1)       # :141-142, :199-200
         if mark_inf:
             cov[cov <= dt(1e-4)] = np.inf                                 # :266-267
         out.append(cov)

@@ -27,8 +27,11 @@ Every output is produced by the reference's own functions on seeded synthetic in
                    the auto-stop rule, and do_conv=True with force_rwr_epochs=3.
   als_col_small.npz  als_small.npz's workload fitted with do_col=True, with the coverage
                    rows (bin_cov_list) init_params computed.
+  als_bad_small.npz / als_badcol_small.npz  the same workload with its last 16 cells bad-QC
+                   (good_qc_num=80): init, fit and transform (which embeds the bad cells too),
+                   with do_col=False / True (the latter with bin_cov and bad_bin_cov).
 
-    python tests/golden/make_golden.py rwr_conv als_conv rwr_col als_col   (only the named ones)
+    python tests/golden/make_golden.py rwr_conv als_conv rwr_col als_col als_bad   (only those)
 """
 import copy
 import os
@@ -227,12 +230,13 @@ def run_fit(w, ds, n_iter, init_state, dim1, do_conv=False, do_col=False):
 
 
 def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U=True,
-             do_conv=False, do_col=False):
+             do_conv=False, do_col=False, good_qc_num=-1):
     w = synth.workload(wname)
     coo, _ = synth.generate(w, seed=seed)
     bsb = [bs_bin or synth.recommend_batches(w, nb, w.n_cells)[0] for nb in w.chrom_bins]
     bsc = [bs_cell or w.n_cells for _ in w.chrom_bins]
-    ds = build_chrom_datasets(ref, coo, w.chrom_names, bsb, bsc, w.band, w.resolution)
+    ds = build_chrom_datasets(ref, coo, w.chrom_names, bsb, bsc, w.band, w.resolution,
+                              good_qc_num=good_qc_num)
     np.random.seed(seed)
     torch.manual_seed(seed)
     m = core.Fast_Higashi_core(rank=w.rank, off_diag=w.band, res_list=[w.resolution]).to(CPU)
@@ -244,6 +248,11 @@ def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U
     if do_col:
         for k, c in enumerate(st0["bin_cov"]):
             out["init_bincov%d" % k] = c.numpy()
+        for k, c in enumerate(st0["bad_bin_cov"]):
+            if torch.is_tensor(c):
+                out["init_badbincov%d" % k] = c.numpy()
+    if good_qc_num >= 0:
+        out["good_qc_num"] = good_qc_num
     out.update(bs_bin=np.asarray(bsb), bs_cell=np.asarray(bsc), flank=w.band, rank=w.rank,
                resolution=w.resolution, dim1=w.dim1, n_iter=n_iter, seed=seed,
                n_chrom=len(coo), sizes=np.asarray([m.chrom2size[n] for n in w.chrom_names]))
@@ -283,6 +292,10 @@ if __name__ == "__main__":
             make_rwr_col_tiles()
         if "als_col" in only:
             make_als("als_col_small.npz", "small", 25, 40, 4, seed=3, do_col=True)
+        if "als_bad" in only:
+            make_als("als_bad_small.npz", "small", 25, 40, 4, seed=3, good_qc_num=80)
+            make_als("als_badcol_small.npz", "small", 25, 40, 4, seed=3, do_col=True,
+                     good_qc_num=80)
         sys.exit(0)
     make_rwr_tiles()
     make_rwr_conv_tiles()
@@ -292,3 +305,5 @@ if __name__ == "__main__":
     make_als("als_conv_small.npz", "small", 25, 40, 4, seed=3, do_conv=True)
     make_rwr_col_tiles()
     make_als("als_col_small.npz", "small", 25, 40, 4, seed=3, do_col=True)
+    make_als("als_bad_small.npz", "small", 25, 40, 4, seed=3, good_qc_num=80)
+    make_als("als_badcol_small.npz", "small", 25, 40, 4, seed=3, do_col=True, good_qc_num=80)

@@ -26,9 +26,11 @@ def chrom_datas(z, oracle_mod, names=None):
     bs_cell = np.broadcast_to(np.asarray(z["bs_cell"]), (len(coo),))
     names = names or ["chr%d" % (k + 1) for k in range(len(coo))]
     out = []
+    good = int(z["good_qc_num"]) if "good_qc_num" in z else -1
     for k, (idx, val, shape) in enumerate(coo):
-        out.append(oracle_mod.ChromData(names[k], idx, val, shape[0], shape[2], int(bs_bin[k]),
-                                        int(bs_cell[k]), int(z["flank"])))
+        n_good = shape[2] if good < 0 else good
+        out.append(oracle_mod.ChromData(names[k], idx, val, shape[0], n_good, int(bs_bin[k]),
+                                        int(bs_cell[k]), int(z["flank"]), shape[2]))
     return out
 
 

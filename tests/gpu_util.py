@@ -12,9 +12,10 @@ def datasets_from(z, names=None, resolution=None):
     bs_cell = np.broadcast_to(np.asarray(z["bs_cell"]), (n,))
     names = names or ["chr%d" % (k + 1) for k in range(n)]
     res = int(z["resolution"]) if resolution is None and "resolution" in z else (resolution or 1000000)
+    good = int(z["good_qc_num"]) if "good_qc_num" in z else -1
     out = []
     for k, (idx, val, shape) in enumerate(coo):
         out.append(Chrom_Dataset(Sparse(idx, val, shape), int(bs_bin[k]), int(bs_cell[k]),
-                                 compact=True, flank=int(z["flank"]), chrom=names[k],
-                                 resolution=res))
+                                 good_qc_num=good, compact=True, flank=int(z["flank"]),
+                                 chrom=names[k], resolution=res))
     return out

@@ -162,11 +162,13 @@ def test_fused_col_rwr_tiles_match_oracle(precision, conv):
     np.testing.assert_allclose(ss, (x.double() ** 2).sum(1).cpu().numpy(), rtol=1e-6)
 
 
-def test_col_coverage_matches_reference_init():
-    """init_params with do_col: n_i and the coverage rows bin_cov_list against the values the
-    reference's init_params computed on the same input."""
+@pytest.mark.parametrize("fixture", ["als_col_small.npz", "als_badcol_small.npz"])
+def test_col_coverage_matches_reference_init(fixture):
+    """init_params with do_col: n_i and the coverage rows bin_cov_list (and bad_bin_cov_list
+    for the bad-QC cells) against the values the reference's init_params computed on the same
+    input."""
     from fh_gb300 import Fast_Higashi_core
-    z = G.load("als_col_small.npz")
+    z = G.load(fixture)
     n = int(z["n_chrom"])
     ds = datasets_from(z)
     m = Fast_Higashi_core(int(z["rank"]), int(z["flank"]), [int(z["resolution"])]).to(CUDA)
@@ -179,6 +181,12 @@ def test_col_coverage_matches_reference_init():
         np.testing.assert_array_equal(np.isinf(got), np.isinf(ref))
         fin = np.isfinite(ref)
         assert O.rel_err(got[fin], ref[fin]) < 1e-5
+        if "init_badbincov%d" % k in z:
+            got = m.bad_bin_cov_list[k].cpu().numpy()
+            ref = z["init_badbincov%d" % k]
+            np.testing.assert_array_equal(np.isinf(got), np.isinf(ref))
+            fin = np.isfinite(ref)
+            assert O.rel_err(got[fin], ref[fin]) < 1e-5
     # the fit's walk afterwards used these rows: one tile against the oracle
     eng = m.engine
     datas = G.chrom_datas(z, O)
@@ -288,7 +296,8 @@ def _model_from(z, n_chrom):
         m.bin_cov_list = [torch.from_numpy(z["init_bincov%d" % k]) for k in range(n_chrom)]
     else:
         m.bin_cov_list = [None] * n_chrom
-    m.bad_bin_cov_list = [0] * n_chrom
+    m.bad_bin_cov_list = [torch.from_numpy(z["init_badbincov%d" % k])
+                          if "init_badbincov%d" % k in z else 0 for k in range(n_chrom)]
     return m, ds
 
 
@@ -320,7 +329,9 @@ def test_one_update_matches_reference_and_oracle():
     ("als_small.npz", 4, 1e-4, False, False),
     ("c1_fit.npz", 10, 2e-3, False, False),
     ("als_conv_small.npz", 4, 1e-4, True, False),
-    ("als_col_small.npz", 4, 1e-4, False, True)])
+    ("als_col_small.npz", 4, 1e-4, False, True),
+    ("als_bad_small.npz", 4, 1e-4, False, False),
+    ("als_badcol_small.npz", 4, 1e-4, False, True)])
 def test_fit_trajectory(fixture, n_iter, ref_tol, conv, col):
     z = G.load(fixture)
     n = int(z["n_chrom"])
@@ -329,8 +340,11 @@ def test_fit_trajectory(fixture, n_iter, ref_tol, conv, col):
           do_rwr=True, do_col=col, tol=0, run_init=False, verbose=False)
     traj = np.asarray(m.rec_errors_total)
     cov = [z["init_bincov%d" % k] for k in range(n)] if col else None
+    bad = [z["init_badbincov%d" % k] if "init_badbincov%d" % k in z else None
+           for k in range(n)] if col else None
     orc = O.ALSOracle(G.chrom_datas(z, O), int(z["rank"]), *G.state(z, "init", n),
-                      do_conv=conv, do_col=col, bin_cov_list=cov).fit(n_iter)
+                      do_conv=conv, do_col=col, bin_cov_list=cov,
+                      bad_bin_cov_list=bad).fit(n_iter)
     np.testing.assert_allclose(traj, orc.rec_errors_total, rtol=1e-5)
     np.testing.assert_allclose(traj, z["fit_rec_total"], rtol=ref_tol)
     E = m.meta_embedding.cpu().numpy()
@@ -339,4 +353,7 @@ def test_fit_trajectory(fixture, n_iter, ref_tol, conv, col):
     res = m.transform(ds, conv, True, col)
     Et = res[1][3].cpu().numpy()
     Et_ref = z["fit_E_transform"]
+    assert Et.shape == Et_ref.shape     # good and bad-QC cells
     assert O.rel_err(O.procrustes_align(Et, Et_ref), Et_ref) < 1e-2
+    Et_o = orc.transform(orc.U_last)
+    assert O.rel_err(O.procrustes_align(Et, Et_o), Et_o) < 1e-4

@@ -95,8 +95,10 @@ def _oracle_from(z, prefix="init", dtype=np.float64, do_conv=False, do_col=False
     datas = G.chrom_datas(z, O)
     A, B, D, E, n_i = G.state(z, prefix, len(datas))
     cov = [z["init_bincov%d" % k] for k in range(len(datas))] if do_col else None
+    bad = [z["init_badbincov%d" % k] if "init_badbincov%d" % k in z else None
+           for k in range(len(datas))] if do_col else None
     return O.ALSOracle(datas, int(z["rank"]), A, B, D, E, n_i, dtype=dtype, do_conv=do_conv,
-                       do_col=do_col, bin_cov_list=cov)
+                       do_col=do_col, bin_cov_list=cov, bad_bin_cov_list=bad)
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
@@ -126,7 +128,9 @@ def test_one_update_matches_reference(dtype):
     ("als_small.npz", 4, 1e-4, False, False),
     ("c1_fit.npz", 10, 2e-3, False, False),
     ("als_conv_small.npz", 4, 1e-4, True, False),
-    ("als_col_small.npz", 4, 1e-4, False, True)])
+    ("als_col_small.npz", 4, 1e-4, False, True),
+    ("als_bad_small.npz", 4, 1e-4, False, False),
+    ("als_badcol_small.npz", 4, 1e-4, False, True)])
 def test_fit_trajectory_matches_reference(fixture, n_iter, rtol, conv, col):
     z = G.load(fixture)
     orc = _oracle_from(z, do_conv=conv, do_col=col)
@@ -137,3 +141,30 @@ def test_fit_trajectory_matches_reference(fixture, n_iter, rtol, conv, col):
     A, B, D, E, _ = G.state(z, "fit", n)
     # the final embedding agrees after orthogonal Procrustes alignment
     assert O.rel_err(O.procrustes_align(orc.E, E), E) < 1e-3
+
+
+@pytest.mark.parametrize("fixture,col", [("als_bad_small.npz", False), ("als_badcol_small.npz", True)])
+def test_transform_with_bad_cells_matches_reference(fixture, col):
+    """transform over good and bad-QC cells (parafac2_intergrative.py:742-834; 80 good and 16
+    bad cells), after the 4-iteration fit: the embedding of all 96 cells against the
+    reference's after orthogonal Procrustes alignment."""
+    z = G.load(fixture)
+    orc = _oracle_from(z, do_col=col)
+    orc.fit(4)
+    E = orc.transform(orc.U_last)
+    ref = z["fit_E_transform"]
+    assert E.shape == ref.shape == (96, int(z["rank"]))
+    assert O.rel_err(O.procrustes_align(E, ref), ref) < 1e-3
+
+
+def test_bad_cell_coverage_matches_reference_init():
+    """bad_bin_cov of init_params (parafac2_intergrative.py:176-200, 268-271)."""
+    z = G.load("als_badcol_small.npz")
+    datas = G.chrom_datas(z, O)
+    good = O.col_coverage(datas, np.float32)
+    bad = O.col_coverage(datas, np.float32, bad=True)
+    for k in range(len(datas)):
+        for got, ref in ((good[k], z["init_bincov%d" % k]), (bad[k], z["init_badbincov%d" % k])):
+            np.testing.assert_array_equal(np.isinf(got), np.isinf(ref))
+            fin = np.isfinite(ref)
+            assert O.rel_err(got[fin], ref[fin]) < 2e-6
