@@ -23,10 +23,10 @@ def parafac(X, rank, n_iter_max=100, init=None, verbose=False, common_factor=Non
     nbin, r, R = X.shape
     if r != rank:
         raise _lib.FHError("parafac", 1, "X.shape[1] must equal rank")
-    rp = 16 if R <= 16 else (32 if R <= 32 else 64)
+    rp = 16 if R <= 16 else (32 if R <= 32 else (64 if R <= 64 else 128))
     ld = max(rp, rank)
-    if ld > 64:
-        raise _lib.FHError("parafac", 2, "ranks above 64 are not supported")
+    if ld > 128 or R > 128:
+        raise _lib.FHError("parafac", 2, "ranks above 128 are not supported")
     A = torch.zeros((nbin, ld), dtype=torch.float32, device=dev)
     B = torch.zeros((1, ld, ld), dtype=torch.float32, device=dev)
     D = torch.zeros((1, rp, ld), dtype=torch.float32, device=dev)

@@ -3,7 +3,7 @@
 Returns (U Vh, S) of matrix (..., d1, d2) as the reference's thin SVD would
 (project2orthogonal.py:6-34): the orthonormal polar factor and the singular values in
 descending order.  Matrices that fit in shared memory take the Householder-QR + Newton
-kernel; taller ones with d2 <= 64 (the meta-embedding case) take the fp64-Gram route.  S
+kernel; taller ones with d2 <= 128 (the meta-embedding case) take the fp64-Gram route.  S
 comes from a one-sided Jacobi of the symmetric U^T M.  Wide matrices are transposed.
 """
 from __future__ import annotations
@@ -20,8 +20,8 @@ def _polar_tall(M):
     if r <= 128 and _lib.value("fh_polar_smem", n, r) <= 227 * 1024:
         _lib.call("fh_polar_f32", _lib.ptr(M), batch, n, r, _lib.ptr(U), None, _lib.ptr(st),
                   _lib.stream_ptr())
-    elif r <= 64:
-        rp = 16 if r <= 16 else (32 if r <= 32 else 64)
+    elif r <= 128:
+        rp = 16 if r <= 16 else (32 if r <= 32 else (64 if r <= 64 else 128))
         ws = torch.empty(_lib.value("fh_meta_polar_workspace", n, r), dtype=torch.uint8,
                          device=M.device)
         ssum = torch.zeros(1, dtype=torch.float64, device=M.device)
@@ -33,7 +33,7 @@ def _polar_tall(M):
                       _lib.ptr(ws), ws.numel(), _lib.ptr(st), _lib.stream_ptr())
             U[b] = Ep[:, :r]
     else:
-        raise _lib.FHError("project2orthogonal", 2, "more than 64 columns")
+        raise _lib.FHError("project2orthogonal", 2, "more than 128 columns")
     _lib.call("fh_polar_svals_f32", _lib.ptr(M), _lib.ptr(U), batch, n, r, _lib.ptr(S),
               _lib.stream_ptr())
     return U, S
