@@ -169,3 +169,41 @@ def test_auto_epochs_per_cell_batch():
     n_i2, feat2 = auto_epochs(eng, schic)       # the good batches alone give the same n_i
     np.testing.assert_array_equal(n_i2, n_i)
     np.testing.assert_array_equal(feat2, feat)
+
+
+def _header_prototypes():
+    """name -> list of parameter type strings, from the declarations in include/fhgb300.h."""
+    txt = open(os.path.join(ROOT, "include", "fhgb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(fh_\w+)\s*\(([^;{]*?)\)\s*;", txt):
+        params = " ".join(m.group(2).split())
+        out[m.group(1)] = [] if params in ("", "void") else [p.strip() for p in params.split(",")]
+    return out
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every ctypes binding has the header's parameter count, and each parameter's kind
+    (pointer, 32-bit or 64-bit integer, size_t, float) matches its declared C type."""
+    import ctypes as C
+    protos = _header_prototypes()
+    assert sorted(protos) == sorted(_lib.SIGNATURES)
+
+    def kind(ctype):
+        t = ctype.replace("const ", "").strip()
+        if "*" in t:
+            return C.c_void_p
+        t = t.rsplit(" ", 1)[0] if " " in t else t
+        return {"int32_t": C.c_int32, "int": C.c_int, "int64_t": C.c_int64, "size_t": C.c_size_t,
+                "float": C.c_float, "double": C.c_double}[t]
+
+    for name, (res, args) in _lib.SIGNATURES.items():
+        params = protos[name]
+        assert len(args) == len(params), (name, len(args), len(params))
+        for i, (a, p) in enumerate(zip(args, params)):
+            want = kind(p)
+            same = a is want or (C.sizeof(a) == C.sizeof(want) and
+                                 a not in (C.c_float, C.c_double) and
+                                 want not in (C.c_float, C.c_double) and
+                                 (a is C.c_void_p) == (want is C.c_void_p))
+            assert same, (name, i, p, a)
