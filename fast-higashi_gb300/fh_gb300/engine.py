@@ -14,9 +14,13 @@ Layout in HBM (all on one GPU):
   U         projections, tile-major (rows, width, r) as the reference's projection_list
   Y         [bin row][ld][rp] projected tensors
   A         [bin row][ld];  B [chrom][ld][ld];  D [chrom][rp][ld];  E [cell][rp]
+  cov       do_col coverage rows [cell][bin across chromosomes] (good cells, then bad)
 Per ALS iteration (parafac2_intergrative.py:635-737): procrustes (per bin row polar) ->
 X G^T (SVD_term) -> meta polar (E) -> X^T E (W) -> Y -> CP-ALS sweeps.  Loss scalars go
 into a device history and are turned into the reference's rec_error values on the host.
+Ranks: R and every chromosome's r up to 128 (rp in {16, 32, 64, 128}; the bf16 forms use
+rp >= 32).  The walk's options: do_conv (3 x 3 mean first), do_col (column-normalised walk
+over the coverage rows); both run on fp32 CUDA cores and write X in the engine's precision.
 """
 from __future__ import annotations
 
