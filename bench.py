@@ -85,6 +85,9 @@ def make_workload(name, seed=0, cells=None):
     if cells:
         w = dataclasses.replace(w, n_cells=int(cells), name="%s at %d cells" % (name, cells))
     coo, _ = synth.generate(w, seed=seed)
+    # The generator fills each chromosome's arrays in its own worker thread; copy them once in
+    # this thread, as arrays read from a file by the caller would be allocated.  Untimed.
+    coo = [(np.array(idx, copy=True), np.array(val, copy=True), shape) for idx, val, shape in coo]
     ds = []
     for (idx, val, shape), cname, nb in zip(coo, w.chrom_names, w.chrom_bins):
         bsb, bsc = synth.recommend_batches(w, nb, w.n_cells)
