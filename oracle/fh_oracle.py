@@ -251,8 +251,10 @@ class ALSOracle:
     ALS iterations exactly as Fast_Higashi_core.fit does after init_params."""
 
     def __init__(self, datas, rank, A_list, B_dict, D_dict, E, n_i, dtype=np.float64, cache_rwr=True,
-                 do_conv=False, do_col=False, bin_cov_list=None, bad_bin_cov_list=None):
+                 do_conv=False, do_col=False, bin_cov_list=None, bad_bin_cov_list=None,
+                 do_rwr=True):
         self.do_conv = do_conv
+        self.do_rwr = do_rwr
         self.do_col = do_col
         if do_col:
             if bin_cov_list is None:
@@ -288,9 +290,12 @@ class ALSOracle:
         if self.do_col:                                                   # :363, :819
             cov = (self.bad_bin_cov[ci][cs.start - d.num_cell:cs.stop - d.num_cell, bb.col] if bad
                    else self.bin_cov[ci][cs, bb.col])
-        out, _ = partial_rwr(x, bb.local.start, bb.local.stop, do_rwr=True,
+        out, _ = partial_rwr(x, bb.local.start, bb.local.stop, do_rwr=self.do_rwr,
                              force_rwr_epochs=self.n_i[ci], final_transpose=True,
                              do_conv=self.do_conv, do_col=self.do_col, bin_cov=cov)
+        if not (self.do_rwr or self.do_conv):
+            # nothing to do: the reference fetches the tile untransposed, (b, n, C) (:345-348)
+            out = out.transpose(1, 2, 0)
         out = np.ascontiguousarray(out)
         if self._cache is not None:
             self._cache[key] = out

@@ -27,11 +27,13 @@ Every output is produced by the reference's own functions on seeded synthetic in
                    the auto-stop rule, and do_conv=True with force_rwr_epochs=3.
   als_col_small.npz  als_small.npz's workload fitted with do_col=True, with the coverage
                    rows (bin_cov_list) init_params computed.
+  als_defaults_small.npz  the same workload with the reference's fit defaults (do_conv=True,
+                   do_rwr=False: the 3 x 3 mean and no walk).
   als_bad_small.npz / als_badcol_small.npz  the same workload with its last 16 cells bad-QC
                    (good_qc_num=80): init, fit and transform (which embeds the bad cells too),
                    with do_col=False / True (the latter with bin_cov and bad_bin_cov).
 
-    python tests/golden/make_golden.py rwr_conv als_conv rwr_col als_col als_bad   (only those)
+    python tests/golden/make_golden.py rwr_conv als_conv rwr_col als_col als_bad als_defaults
 """
 import copy
 import os
@@ -219,18 +221,18 @@ def state_arrays(prefix, st, names):
     return out
 
 
-def run_fit(w, ds, n_iter, init_state, dim1, do_conv=False, do_col=False):
+def run_fit(w, ds, n_iter, init_state, dim1, do_conv=False, do_col=False, do_rwr=True):
     m = core.Fast_Higashi_core(rank=w.rank, off_diag=w.band, res_list=[w.resolution]).to(CPU)
     inject(m, init_state)
     with FitLocals() as fl:
         m.fit(ds, size_ratio=dim1, n_iter_max=n_iter, n_iter_parafac=1, do_conv=do_conv,
-              do_rwr=True, do_col=do_col, tol=0, run_init=False)
-    res = m.transform(ds, do_conv, True, do_col)
+              do_rwr=do_rwr, do_col=do_col, tol=0, run_init=False)
+    res = m.transform(ds, do_conv, do_rwr, do_col)
     return m, fl.locals, res
 
 
 def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U=True,
-             do_conv=False, do_col=False, good_qc_num=-1):
+             do_conv=False, do_col=False, good_qc_num=-1, do_rwr=True):
     w = synth.workload(wname)
     coo, _ = synth.generate(w, seed=seed)
     bsb = [bs_bin or synth.recommend_batches(w, nb, w.n_cells)[0] for nb in w.chrom_bins]
@@ -240,7 +242,7 @@ def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U
     np.random.seed(seed)
     torch.manual_seed(seed)
     m = core.Fast_Higashi_core(rank=w.rank, off_diag=w.band, res_list=[w.resolution]).to(CPU)
-    m.fit(ds, size_ratio=w.dim1, n_iter_max=0, n_iter_parafac=1, do_conv=do_conv, do_rwr=True,
+    m.fit(ds, size_ratio=w.dim1, n_iter_max=0, n_iter_parafac=1, do_conv=do_conv, do_rwr=do_rwr,
           do_col=do_col, tol=0, run_init=True)
     st0 = snapshot(m)
     out = coo_arrays("in", coo) if save_input else {}
@@ -253,13 +255,14 @@ def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U
                 out["init_badbincov%d" % k] = c.numpy()
     if good_qc_num >= 0:
         out["good_qc_num"] = good_qc_num
+    out["do_rwr"] = int(do_rwr)
     out.update(bs_bin=np.asarray(bsb), bs_cell=np.asarray(bsc), flank=w.band, rank=w.rank,
                resolution=w.resolution, dim1=w.dim1, n_iter=n_iter, seed=seed,
                n_chrom=len(coo), sizes=np.asarray([m.chrom2size[n] for n in w.chrom_names]))
     # one update_meta_embedding_interactions call from the initial state
     proj_list = [[torch.empty(0)] * d.num_bin_batch for d in ds]
     ptl = {d.chrom: torch.empty([d.num_bin, m.chrom2size[d.chrom], w.rank]) for d in ds}
-    r = m.update_meta_embedding_interactions(ds, proj_list, ptl, do_conv=do_conv, do_rwr=True,
+    r = m.update_meta_embedding_interactions(ds, proj_list, ptl, do_conv=do_conv, do_rwr=do_rwr,
                                              do_col=do_col, first_iter=True)
     pl, ptl, exU, exV, tn = r
     for ci, d in enumerate(ds):
@@ -269,12 +272,12 @@ def make_als(name, wname, bs_bin, bs_cell, n_iter, seed, save_input=True, save_U
     out.update(it1_exU=np.asarray(exU).ravel(), it1_exV=float(exV), it1_tnorm=np.asarray(tn).ravel(),
                it1_E=m.meta_embedding.numpy())
     # the fit loop from the same state
-    m2, loc, res = run_fit(w, ds, n_iter, st0, w.dim1, do_conv, do_col)
+    m2, loc, res = run_fit(w, ds, n_iter, st0, w.dim1, do_conv, do_col, do_rwr)
     out["fit_rec_total"] = np.asarray(loc["rec_errors_total"], dtype=np.float64)
     out["fit_rec_block"] = np.stack([np.asarray(x).ravel() for x in loc["rec_errors"]])
     out.update(state_arrays("fit", snapshot(m2), w.chrom_names))
     out["fit_E_transform"] = res[1][3].numpy()
-    m3, loc1, _ = run_fit(w, ds, 1, st0, w.dim1, do_conv, do_col)
+    m3, loc1, _ = run_fit(w, ds, 1, st0, w.dim1, do_conv, do_col, do_rwr)
     out.update(state_arrays("one", snapshot(m3), w.chrom_names))
     out["one_rec_total"] = np.asarray(loc1["rec_errors_total"], dtype=np.float64)
     np.savez_compressed(os.path.join(HERE, name), **out)
@@ -292,6 +295,9 @@ if __name__ == "__main__":
             make_rwr_col_tiles()
         if "als_col" in only:
             make_als("als_col_small.npz", "small", 25, 40, 4, seed=3, do_col=True)
+        if "als_defaults" in only:
+            make_als("als_defaults_small.npz", "small", 25, 40, 4, seed=3, do_conv=True,
+                     do_rwr=False)
         if "als_bad" in only:
             make_als("als_bad_small.npz", "small", 25, 40, 4, seed=3, good_qc_num=80)
             make_als("als_badcol_small.npz", "small", 25, 40, 4, seed=3, do_col=True,
@@ -307,3 +313,4 @@ if __name__ == "__main__":
     make_als("als_col_small.npz", "small", 25, 40, 4, seed=3, do_col=True)
     make_als("als_bad_small.npz", "small", 25, 40, 4, seed=3, good_qc_num=80)
     make_als("als_badcol_small.npz", "small", 25, 40, 4, seed=3, do_col=True, good_qc_num=80)
+    make_als("als_defaults_small.npz", "small", 25, 40, 4, seed=3, do_conv=True, do_rwr=False)

@@ -97,8 +97,9 @@ def _oracle_from(z, prefix="init", dtype=np.float64, do_conv=False, do_col=False
     cov = [z["init_bincov%d" % k] for k in range(len(datas))] if do_col else None
     bad = [z["init_badbincov%d" % k] if "init_badbincov%d" % k in z else None
            for k in range(len(datas))] if do_col else None
+    do_rwr = bool(int(z["do_rwr"])) if "do_rwr" in z else True
     return O.ALSOracle(datas, int(z["rank"]), A, B, D, E, n_i, dtype=dtype, do_conv=do_conv,
-                       do_col=do_col, bin_cov_list=cov, bad_bin_cov_list=bad)
+                       do_col=do_col, bin_cov_list=cov, bad_bin_cov_list=bad, do_rwr=do_rwr)
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
@@ -130,7 +131,8 @@ def test_one_update_matches_reference(dtype):
     ("als_conv_small.npz", 4, 1e-4, True, False),
     ("als_col_small.npz", 4, 1e-4, False, True),
     ("als_bad_small.npz", 4, 1e-4, False, False),
-    ("als_badcol_small.npz", 4, 1e-4, False, True)])
+    ("als_badcol_small.npz", 4, 1e-4, False, True),
+    ("als_defaults_small.npz", 4, 1e-4, True, False)])
 def test_fit_trajectory_matches_reference(fixture, n_iter, rtol, conv, col):
     z = G.load(fixture)
     orc = _oracle_from(z, do_conv=conv, do_col=col)
