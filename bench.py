@@ -66,15 +66,29 @@ def parse():
 
 
 def dist_setup():
+    """One process per GPU under torchrun (NCCL); gloo where no GPU is visible (the host-side
+    logic of the N > 1 runs, exercised by the CPU tests)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 0, 1
     import torch
     import torch.distributed as dist
     rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist.init_process_group("gloo")
     return rank, local, ws
+
+
+def max_over_ranks(x, ws):
+    """The largest of every rank's x (a one-element tensor): whole-job time is the slowest
+    replica's."""
+    if ws > 1:
+        import torch.distributed as dist
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+    return x
 
 
 def make_workload(name, seed=0, cells=None):
@@ -294,9 +308,7 @@ def gb300_arm(args, rank, local, ws):
             s1.record()
             torch.cuda.synchronize()
         n_launch = (_lib.launches - n0) // args.steps
-        t = torch.tensor([s0.elapsed_time(s1) / args.steps], device=dev)
-        if ws > 1:
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t = max_over_ranks(torch.tensor([s0.elapsed_time(s1) / args.steps], device=dev), ws)
         e.check_status("bench")
         return float(t.item()), n_launch, clk
 
@@ -371,6 +383,7 @@ def gb300_arm(args, rank, local, ws):
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = float(np.median(e2e_times))     # each step is a whole fit through the public API
+    e2e_s = float(max_over_ranks(torch.tensor([e2e_s], device=dev), ws).item())
     h2d = store_h2d[0] + sum(a.numel() * 4 for a in A0) + E0.numel() * 4 + \
         sum(v.numel() * 4 for v in B0.values()) + sum(v.numel() * 4 for v in D0.values())
     d2h = emb.numel() * 4 + iters * (eng.nb + 1 + len(eng.names)) * 8
