@@ -228,3 +228,45 @@ def test_bench_reference_arm_prints_the_contract_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_c_abi_rejects_bad_arguments_before_any_launch():
+    """The entry points check their arguments before touching a device, and say why:
+    FH_ERR_ARG (1) for malformed calls, FH_ERR_UNSUPPORTED for sizes past the kernels' range.
+    Non-null dummy addresses are never dereferenced on these paths."""
+    import ctypes as C
+    if not os.path.exists(_lib.LIB_PATH):
+        from fh_gb300 import build
+        build.build()
+    lib = _lib.load()
+    p = C.c_void_p(16)                    # a dummy device address
+    # malformed: null pointers, empty sizes, inconsistent shapes
+    assert lib.fh_rwr_dense_f32(None, 4, 8, 12, 2, 3, p, None, None) == 1
+    assert lib.fh_rwr_dense_f32(p, 4, 8, 12, 6, 3, p, None, None) == 1          # s0 + rows > width
+    assert lib.fh_conv_dense_f32(p, 0, 8, 12, p, None) == 1
+    assert lib.fh_polar_f32(p, 2, 8, 16, p, None, None, None) == 1              # n < r
+    assert lib.fh_xe_f32(p, 100, 10, 100, p, 64, p, None) == 1                  # ldx % 128
+    assert lib.fh_xe_f32(p, 128, 10, 100, p, 48, p, None) == 1                  # rp not 16/32/64/128
+    assert lib.fh_cp_als(1, 1, p, p, p, p, p, 64, 64, 64, 64, -1, p, None, p, 1 << 20,
+                         None, None) == 1                                       # n_iter < 0
+    assert lib.fh_meta_polar(p, 100, 65, 64, p, p, p, 1 << 20, None, None) == 1  # R > rp
+    assert lib.fh_rwr_col_dense(p, 4, 8, 12, 2, 3, None, p, None, None) == 1     # no coverage
+    assert lib.fh_rwr_col_tiles(p, 1, 4, 8, 12, None, None, None, None, 12, None, p, None,
+                                100, 0, None, None, None, None) == 1           # no segments
+    # past the kernels' range
+    unsup = lib.fh_polar_f32(p, 2, 300, 200, p, None, None, None)               # r > 128
+    assert unsup not in (0, 1)
+    assert lib.fh_status_string(unsup).decode() == lib.fh_status_string(
+        lib.fh_meta_polar(p, 1000, 200, 256, p, p, p, 1 << 30, None, None)).decode()
+    assert lib.fh_conv_dense_f32(p, 4, 200, 12, p, None) == unsup               # rows > 128
+
+
+def test_product_path_raises_without_cuda():
+    """No CPU fallback: the drop-ins refuse host tensors and the engine refuses a CPU device."""
+    torch = pytest.importorskip("torch")
+    from fh_gb300 import partial_rwr
+    from fh_gb300.engine import FitEngine
+    with pytest.raises(_lib.FHError):
+        partial_rwr(torch.rand(2, 5, 9), 2, 7, False, True, False)
+    with pytest.raises(_lib.FHError):
+        FitEngine([], 4, {}, None, "cpu")
