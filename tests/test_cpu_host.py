@@ -270,3 +270,13 @@ def test_product_path_raises_without_cuda():
         partial_rwr(torch.rand(2, 5, 9), 2, 7, False, True, False)
     with pytest.raises(_lib.FHError):
         FitEngine([], 4, {}, None, "cpu")
+
+
+def test_parafac_sweep_schedule():
+    """CP-ALS sweeps per fit iteration (parafac2_intergrative.py:636-637): one more every 10
+    iterations after the first ten, capped at 10; the oracle's fit loop follows the same rule."""
+    from fh_gb300.engine import FitEngine
+    s = FitEngine.parafac_schedule(35, 1)
+    assert s[:10] == [1] * 10 and s[10:20] == [2] * 10 and s[20:30] == [3] * 10 and s[30:] == [4] * 5
+    assert FitEngine.parafac_schedule(200, 5)[-1] == 10
+    assert FitEngine.parafac_schedule(3, 12) == [12, 12, 12]     # above the cap: left alone
