@@ -79,6 +79,51 @@ def densify(rows, cols, cells, vals, b, n, ncell, dtype=np.float64):
 
 
 # ----------------------------------------------------------------------------------------
+# Input packing: restates FastHigashi.pack_training_data_one_process
+# (FastHigashi_Wrapper.py:221-366) for one chromosome without a blacklist or batch ids,
+# fac_size 1 and a symmetric map, with preprocessing.py:114-193, 474-489.
+# ----------------------------------------------------------------------------------------
+def pack_chromosome(cells, nbin, reorder, off_diag, merge=1):
+    """cells[c] = (row, col, value) of cell c's raw contact matrix (nbin x nbin, canonical CSR
+    order).  Returns (indices int32[3, nnz] = (row, col, cell), values float32[nnz], shape)
+    as the packed Sparse input of the fit: cells taken in `reorder`, bins merged by `merge`
+    (:255-261), contacts beyond `off_diag` dropped (:264-268), bins with no contact in any
+    cell removed and renumbered (filter_bin), each cell scaled to total `bins` (normalize_by_
+    coverage), then log1p and a clip at mean + 15 std over the chromosome (:358-364)."""
+    nb = int(math.ceil(nbin / merge))
+    mats = []
+    for c in reorder:
+        row, col, val = cells[c]
+        if merge > 1:
+            # the reference divides the coordinates of a canonical COO in place, so its
+            # sum_duplicates() call is a no-op: merged duplicates stay separate entries
+            row, col = row // merge, col // merge
+        keep = np.abs(col - row) <= off_diag
+        mats.append((row[keep], col[keep], val[keep].astype(np.float32)))
+    # valid bins: any contact in any cell (the bulk's row sums, filter_bin; the reference's
+    # buffered x[row, col] += data counts a duplicated coordinate once, which cannot change
+    # which rows are positive)
+    bulk = np.zeros((nb, nb))
+    for row, col, val in mats:
+        bulk[row, col] += val
+    valid = (bulk / len(mats)).sum(1) > 0
+    new_id = np.cumsum(valid) - 1
+    new_id[~valid] = -1
+    idx, vals = [], []
+    for k, (row, col, val) in enumerate(mats):
+        n = val.sum()
+        val = val * (nb / (n + 1e-15))                    # normalize_by_coverage, scale = bins
+        r, c = new_id[row], new_id[col]
+        ok = (r != -1) & (c != -1)
+        idx.append(np.stack([r[ok], c[ok], np.full(int(ok.sum()), k)]))
+        vals.append(val[ok])
+    indices = np.concatenate(idx, axis=1).astype(np.int32)
+    values = np.log1p(np.concatenate(vals).astype(np.float32))
+    values = np.clip(values, None, np.mean(values) + 15 * np.std(values))
+    return indices, values, (int(valid.sum()), int(valid.sum()), len(mats))
+
+
+# ----------------------------------------------------------------------------------------
 # Partial RWR: restates partial_rwr.py:75-175.
 # ----------------------------------------------------------------------------------------
 def rwr_transition(A, s0, s1):

@@ -27,13 +27,17 @@ Every output is produced by the reference's own functions on seeded synthetic in
                    the auto-stop rule, and do_conv=True with force_rwr_epochs=3.
   als_col_small.npz  als_small.npz's workload fitted with do_col=True, with the coverage
                    rows (bin_cov_list) init_params computed.
+  pack.npz         FastHigashi.pack_training_data_one_process (FastHigashi_Wrapper.py:221-366)
+                   on seeded raw per-cell contact matrices of two chromosomes (some bins empty in
+                   every cell, contacts past the band, a cell order to apply), with merge
+                   factors 1 and 2: the packed (row, col, cell) indices, values and shape.
   als_defaults_small.npz  the same workload with the reference's fit defaults (do_conv=True,
                    do_rwr=False: the 3 x 3 mean and no walk).
   als_bad_small.npz / als_badcol_small.npz  the same workload with its last 16 cells bad-QC
                    (good_qc_num=80): init, fit and transform (which embeds the bad cells too),
                    with do_col=False / True (the latter with bin_cov and bad_bin_cov).
 
-    python tests/golden/make_golden.py rwr_conv als_conv rwr_col als_col als_bad als_defaults
+    python tests/golden/make_golden.py rwr_conv als_conv rwr_col als_col als_bad als_defaults pack
 """
 import copy
 import os
@@ -46,7 +50,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.join(HERE, "..", "..", "fast-higashi_gb300"))
 
-from ref_import import import_reference, build_chrom_datasets  # noqa: E402
+from ref_import import import_reference, import_wrapper, build_chrom_datasets  # noqa: E402
 from fh_gb300 import synth  # noqa: E402
 
 torch.set_num_threads(4)
@@ -157,6 +161,64 @@ def make_rwr_col_tiles():
     out["n_tiles"] = k
     np.savez_compressed(os.path.join(HERE, "rwr_col_tiles.npz"), **out)
     print("rwr_col_tiles", k, "tiles")
+
+
+def pack_raw_cells(rng, nbin, n_cells, reach=12, empty=()):
+    """Seeded raw per-cell contact matrices (scipy csr, float32, both triangles)."""
+    from scipy.sparse import coo_matrix
+    out = []
+    for _ in range(n_cells):
+        i, j = np.triu_indices(nbin)
+        keep = (j - i) <= reach
+        i, j = i[keep], j[keep]
+        lam = 3.0 * (j - i + 1.0) ** -1.1 * rng.uniform(0.3, 1.5)
+        c = rng.poisson(lam).astype(np.float32)
+        for e in empty:
+            c[(i == e) | (j == e)] = 0
+        nz = c > 0
+        i, j, c = i[nz], j[nz], c[nz]
+        off = i != j
+        rows = np.concatenate([i, j[off]])
+        cols = np.concatenate([j, i[off]])
+        vals = np.concatenate([c, c[off]])
+        out.append(coo_matrix((vals, (rows, cols)), shape=(nbin, nbin)).tocsr())
+    return out
+
+
+def make_pack():
+    import tempfile
+    import types as T
+    wr = import_wrapper()
+    rng = np.random.default_rng(21)
+    chroms = [("chrA", 40, (5, 17)), ("chrB", 33, (0, 32))]
+    n_cells = 24
+    reorder = rng.permutation(n_cells)
+    out = dict(reorder=reorder, n_cells=n_cells, n_chrom=len(chroms))
+    with tempfile.TemporaryDirectory() as raw:
+        for k, (name, nbin, empty) in enumerate(chroms):
+            mats = pack_raw_cells(rng, nbin, n_cells, empty=empty)
+            arr = np.empty(n_cells, dtype=object)
+            for c, m in enumerate(mats):
+                arr[c] = m
+                cm = m.tocoo()
+                out["raw%d_cell%d" % (k, c)] = np.stack([cm.row, cm.col]).astype(np.int32)
+                out["raw%d_val%d" % (k, c)] = cm.data.astype(np.float32)
+            out["raw%d_nbin" % k] = nbin
+            np.save(os.path.join(raw, "%s_sparse_adj.npy" % name), arr, allow_pickle=True)
+            for case, (merge, off_diag) in enumerate(((1, 4), (2, 3))):
+                me = T.SimpleNamespace(config={}, temp_dir=os.path.join(raw, "none"),
+                                       sum_sparse_coo=wr.FastHigashi.sum_sparse_coo)
+                idx, val, shape = wr.FastHigashi.pack_training_data_one_process(
+                    me, raw, name, reorder, off_diag=off_diag, fac_size=1, merge_fac_row=merge,
+                    merge_fac_col=merge, is_sym=True, filename_pattern="%s_sparse_adj.npy",
+                    force_shift=False, batch_norm=True, bar=None)
+                key = "out%d_%d" % (k, case)
+                out[key + "_idx"] = idx
+                out[key + "_val"] = val
+                out[key + "_shape"] = np.asarray(shape, dtype=np.int64)
+                out[key + "_args"] = np.asarray([merge, off_diag], dtype=np.int64)
+    np.savez_compressed(os.path.join(HERE, "pack.npz"), **out)
+    print("pack", {k: v.shape for k, v in out.items() if k.startswith("out") and k.endswith("_idx")})
 
 
 def make_parafac():
@@ -295,6 +357,8 @@ if __name__ == "__main__":
             make_rwr_col_tiles()
         if "als_col" in only:
             make_als("als_col_small.npz", "small", 25, 40, 4, seed=3, do_col=True)
+        if "pack" in only:
+            make_pack()
         if "als_defaults" in only:
             make_als("als_defaults_small.npz", "small", 25, 40, 4, seed=3, do_conv=True,
                      do_rwr=False)
@@ -314,3 +378,4 @@ if __name__ == "__main__":
     make_als("als_bad_small.npz", "small", 25, 40, 4, seed=3, good_qc_num=80)
     make_als("als_badcol_small.npz", "small", 25, 40, 4, seed=3, do_col=True, good_qc_num=80)
     make_als("als_defaults_small.npz", "small", 25, 40, 4, seed=3, do_conv=True, do_rwr=False)
+    make_pack()

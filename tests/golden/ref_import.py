@@ -7,6 +7,8 @@ Two host-side shims, both outside the arithmetic:
   2. ``Sparse.__init__`` (``fasthigashi/sparse_for_schic.py:63-66``) calls
      ``np.array(shape, copy=False)``, which NumPy 2 rejects for tuples; the
      objects are built with ``copy=True`` (same values).
+``import_wrapper`` also stubs h5py (not installed; the packing path never calls it) while
+``fasthigashi/FastHigashi_Wrapper.py`` imports.
 Only ``tests/golden/make_golden.py`` uses this module; nothing that runs on a
 GPU host does.
 """
@@ -34,6 +36,21 @@ def import_reference():
             del sys.modules["pandas"]
     # quiet progress printing of the reference's tqdm bars
     return dict(core=p2, parafac=p1, rwr=prwr, p2o=p2o, sparse=sfs)
+
+
+def import_wrapper():
+    """fasthigashi.FastHigashi_Wrapper with pandas and h5py stubbed during its import."""
+    if REF_ROOT not in sys.path:
+        sys.path.insert(0, REF_ROOT)
+    stubs = [m for m in ("pandas", "h5py") if m not in sys.modules]
+    for m in stubs:
+        sys.modules[m] = types.ModuleType(m)
+    try:
+        import fasthigashi.FastHigashi_Wrapper as wr
+    finally:
+        for m in stubs:
+            del sys.modules[m]
+    return wr
 
 
 def build_chrom_datasets(ref, coo_list, names, bs_bins, bs_cells, flank, resolution,

@@ -170,3 +170,19 @@ def test_bad_cell_coverage_matches_reference_init():
             np.testing.assert_array_equal(np.isinf(got), np.isinf(ref))
             fin = np.isfinite(ref)
             assert O.rel_err(got[fin], ref[fin]) < 2e-6
+
+
+@pytest.mark.parametrize("k,case", [(0, 0), (0, 1), (1, 0), (1, 1)])
+def test_pack_matches_reference(k, case):
+    """Input packing of raw per-cell matrices (FastHigashi_Wrapper.py:221-366): bin merging,
+    the band, empty-bin removal and renumbering, coverage scaling, log1p and the clip."""
+    z = G.load("pack.npz")
+    n = int(z["n_cells"])
+    cells = [(z["raw%d_cell%d" % (k, c)][0].astype(np.int64), z["raw%d_cell%d" % (k, c)][1].astype(np.int64),
+              z["raw%d_val%d" % (k, c)]) for c in range(n)]
+    merge, off_diag = (int(v) for v in z["out%d_%d_args" % (k, case)])
+    idx, val, shape = O.pack_chromosome(cells, int(z["raw%d_nbin" % k]), z["reorder"], off_diag, merge)
+    ref = "out%d_%d" % (k, case)
+    assert tuple(shape) == tuple(z[ref + "_shape"])
+    np.testing.assert_array_equal(idx, z[ref + "_idx"])
+    np.testing.assert_array_equal(val, z[ref + "_val"])      # bit-exact: same fp32 operations
