@@ -12,8 +12,9 @@ initial state (init_params runs once, untimed, as the metric states).
               the speed-up of the headline form over it
   e2e         the public API (Fast_Higashi_core.fit on host Sparse data) with the COO H2D and
               the embedding / loss D2H inside the timed region
-  --impl reference   the CPU restatement of the reference (the oracle, fp32, all host threads)
-                     on a bounded cell sample, extrapolated to cells/s
+  --impl reference   the reference's own Fast_Higashi_core (installed under baseline/_ref) on
+                     the host CPU, all cores, one ALS iteration per step on a cell sample,
+                     extrapolated to the workload's cells and iterations (cpu_baseline says how)
 
 Multi-GPU runs (torchrun) are independent replicas: the fit does not shard (scaling weak).
 """
@@ -52,14 +53,16 @@ def parse():
     ap.add_argument("--cells", type=int, default=None,
                     help="run the workload's shapes with this many cells instead (a reduced "
                          "case, named as such in config.workload; never the headline)")
-    ap.add_argument("--sample-cells", type=int, default=96,
-                    help="cells of the CPU-baseline sample (at least the rank R)")
+    ap.add_argument("--sample-cells", type=int, default=128,
+                    help="cells of the reference's CPU sample (at least the rank R)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", default="bf16x2", choices=["fp32", "bf16x2", "bf16"],
                     help="form timed for the headline: bf16x2 (default) the tensor-core form, X "
                          "as two bf16 planes; bf16 one plane; fp32 the plain drop-in")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip timing the plain fp32 form beside the headline form")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the FP64 fit that states both forms' embedding error")
     args = ap.parse_args()
     args.config = args.config or ("c4" if args.grad else "c3")
     return args
@@ -190,6 +193,84 @@ def autotune_summary():
             for k, times, best in autotune.default_tuner().log}
 
 
+# DRAM bytes per launch of the per-bin polar kernel per bin row, from its ncu capture at 2,000
+# cells (79 MB read + 96 MB written over 2,887 bin rows: W rows in, U and G^T out); the bench
+# scales it by its own bin rows.
+PROCRUSTES_TRAFFIC_PER_ROW = (79e6 + 96e6) / 2887
+
+
+def family_work(eng, iters_sched=None):
+    """Algorithmic work per launch of each kernel family of the fit, as (amount, unit, bound):
+      rwr         sum over tiles of cells x 2 b^2 n (1 + epochs): the transition matrix's
+                  A A^T and one b x b by b x n product per walk epoch (the tensor-core form runs
+                  each product as three split-bf16 products; only one is counted)
+      xe, xg      the X bytes one pass reads: cells x band rows x bytes per element
+      procrustes  per bin row (n columns, rank r, meta rank R): temp 2nRr + Householder QR
+                  2nr^2 - 2r^3/3 + the polar factor of the r x r triangle counted as ten r x r
+                  products (20 r^3, the class of its Newton and Newton-Schulz steps) + forming U
+                  4nr^2 - 2r^3 + G^T 2nrR, fp32
+      meta_polar  cells x R^2 (fp64 Gram, one triangle) + 2 cells x R^2 (apply)
+      project_y   bytes of U, W read and Y written
+      cp_als      per sweep and bin row 6 r^2 R (three MTTKRPs), times the mean sweeps per call
+    """
+    t = eng.tiles
+    b = t["rows"].astype(np.float64)
+    n = t["width"].astype(np.float64)
+    r = t["rank"].astype(np.float64)
+    ep = t["n_rwr"].astype(np.float64)
+    R, rp, ld = float(eng.R), eng.rp, eng.ld
+    xel = 2 * eng.planes if eng.bf16 else 4
+    nr = np.repeat(n, t["rows"])
+    rr = np.repeat(r, t["rows"])
+    proc = float((2 * nr * R * rr + 2 * nr * rr ** 2 - 2 * rr ** 3 / 3 + 20 * rr ** 3 +
+                  4 * nr * rr ** 2 - 2 * rr ** 3 + 2 * nr * rr * R).sum())
+    sweeps = float(np.mean(iters_sched)) if iters_sched else 1.0
+    return {
+        "rwr": (eng.Ct * float((2 * b * b * n * (1 + ep)).sum()), "FLOP",
+                "tensor" if eng.bf16 else "fp32"),
+        "xe": (float(eng.C) * eng.rows * xel, "B", "hbm"),
+        "xg": (float(eng.C) * eng.rows * xel, "B", "hbm"),
+        "procrustes": (proc, "FLOP", "fp32"),
+        "meta_polar": (3.0 * eng.C * R * R, "FLOP", "fp64"),
+        "project_y": (4.0 * (eng.u_size + eng.rows * rp + eng.nb * ld * rp), "B", "hbm"),
+        "cp_als": (sweeps * float((6 * rr ** 2 * R).sum()), "FLOP", "fp32"),
+    }
+
+
+def family_rooflines(eng, kt, sm_max_mhz, sched):
+    """Per kernel family: algorithmic work per launch, its CUDA-event time (mean over the
+    launches of one instrumented fit), the rate, the bound and its fraction of that bound's
+    peak.  Peaks: HBM and bf16 tensor from MEASURED_PEAKS.json (the sustained bf16 figure: these
+    kernels run inside a long step); fp32 and fp64 CUDA-core rates are nominal at the sampled
+    maximum SM clock (128 fp32 and 2 fp64 FMA per SM per clock, 152 SMs)."""
+    hbm, _, peak_kind = peaks()
+    bf16s = sustained_bf16()
+    mhz = sm_max_mhz or 2070.0
+    fp32 = 2 * 128 * 152 * mhz * 1e6 / 1e12
+    peak = {"hbm": (hbm, "GB/s", peak_kind), "tensor": (bf16s, "TFLOP/s", peak_kind),
+            "fp32": (fp32, "TFLOP/s", "nominal"), "fp64": (fp32 / 64, "TFLOP/s", "nominal")}
+    out = []
+    for fam, (work, unit, bound) in family_work(eng, sched).items():
+        if fam not in kt:
+            continue
+        sec = kt[fam]["mean_ms"] / 1000.0
+        rate = work / sec / (1e9 if unit == "B" else 1e12)
+        pk, pu, pkind = peak[bound]
+        out.append({"kernel": fam, "bound": bound, "achieved": rate, "peak": pk, "unit": pu,
+                    "frac": rate / pk, "peak_kind": pkind, "work_per_launch": work,
+                    "work_unit": unit, "ms_per_launch": kt[fam]["mean_ms"],
+                    "launches_per_fit": kt[fam]["calls"]})
+    return out
+
+
+def sustained_bf16():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops_sustained"])
+    except (OSError, KeyError, ValueError):
+        return 1700.0
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -200,64 +281,261 @@ def peaks():
 
 
 # --------------------------------------------------------------------------------------
-def cpu_sample_rate(coo, w, n_cells, iters, threads=None):
-    """Cells/s of the CPU restatement (fp32, the reference's loop structure with its RWR
-    recomputation) on the first n_cells cells: RWR + one warm ALS iteration, extrapolated
-    to RWR + iters iterations.  Returns (cells/s, sample description, seconds spent)."""
-    from oracle import fh_oracle as O
+REF_DIR = os.path.join(ROOT, "baseline", "_ref")
+
+
+def import_reference(path=REF_DIR):
+    """The reference package (fasthigashi) from its pip --target install, unmodified.
+
+    Third-party modules its fit path imports are used where installed.  Where the host lacks
+    one, a stand-in is placed in sys.modules for the import only (the reference binds the
+    names it needs at import time) and named in the returned notes:
+      pandas      util.py:2, parafac_integrative.py:5; nothing on the fit path uses it: an
+                  empty module
+      sklearn     TruncatedSVD (init_params, parafac2_intergrative.py:257) and NearestNeighbors
+                  (util.py:7, unused): TruncatedSVD.fit_transform as numpy's SVD of the same
+                  matrix (init is not timed); NearestNeighbors raises if called
+      opt_einsum  contract (parafac2_intergrative.py:374,422,522,629; parafac_integrative.py:
+                  57,82): torch.einsum of the same subscripts
+    Returns (modules, notes)."""
+    import importlib.util
+    import types
+    notes = []
+    stubs = {}
+    if importlib.util.find_spec("pandas") is None:
+        stubs["pandas"] = types.ModuleType("pandas")
+        notes.append("pandas: empty module (no use on the fit path)")
+    if importlib.util.find_spec("sklearn") is None:
+        sk, dec, nei = (types.ModuleType(n) for n in ("sklearn", "sklearn.decomposition",
+                                                       "sklearn.neighbors"))
+
+        class TruncatedSVD:
+            def __init__(self, n_components=2, **kw):
+                self.k = int(n_components)
+
+            def fit_transform(self, X):
+                U, S, _ = np.linalg.svd(np.asarray(X, dtype=np.float64), full_matrices=False)
+                return U[:, :self.k] * S[:self.k]
+
+        class NearestNeighbors:
+            def __init__(self, *a, **kw):
+                raise RuntimeError("NearestNeighbors is not available on this host")
+
+        dec.TruncatedSVD = TruncatedSVD
+        nei.NearestNeighbors = NearestNeighbors
+        sk.decomposition, sk.neighbors = dec, nei
+        stubs.update({"sklearn": sk, "sklearn.decomposition": dec, "sklearn.neighbors": nei})
+        notes.append("sklearn: TruncatedSVD as numpy SVD (init only, untimed)")
+    if importlib.util.find_spec("opt_einsum") is None:
+        import torch
+        oe = types.ModuleType("opt_einsum")
+        oe.contract = lambda eq, *ops, **kw: torch.einsum(eq, *ops)
+        stubs["opt_einsum"] = oe
+        notes.append("opt_einsum: contract as torch.einsum")
+    if not os.path.isdir(os.path.join(path, "fasthigashi")):
+        raise FileNotFoundError("the reference is not installed under %s" % path)
+    if path not in sys.path:
+        sys.path.insert(0, path)
+    added = [k for k in stubs if k not in sys.modules]
+    for k in added:
+        sys.modules[k] = stubs[k]
+    try:
+        import fasthigashi.parafac2_intergrative as core
+        import fasthigashi.sparse_for_schic as sfs
+    finally:
+        for k in added:
+            del sys.modules[k]
+    return {"core": core, "sparse": sfs}, notes
+
+
+def reference_datasets(ref, w, coo):
+    """The reference's own Sparse / Chrom_Dataset objects for a workload's COO, with the
+    batching the GPU arm uses (one cell batch; bin batches per FastHigashi_Wrapper.py:501,
+    507-512).  Sparse is built with copy=True: its np.array(shape, copy=False) rejects the
+    shape tuple under NumPy 2 (same values)."""
     from fh_gb300 import synth
-    n_cells = max(n_cells, w.rank)
-    t0 = time.perf_counter()
-    datas = []
-    for k, ((idx, val, shape), nb) in enumerate(zip(coo, w.chrom_bins)):
-        m = idx[2] < n_cells
+    sfs = ref["sparse"]
+    out = []
+    for (idx, val, shape), name, nb in zip(coo, w.chrom_names, w.chrom_bins):
         bsb, _ = synth.recommend_batches(w, nb, w.n_cells)
-        datas.append(O.ChromData("chr%d" % (k + 1), idx[:, m], val[m], nb, n_cells, bsb, n_cells, w.band))
-    sizes = O.chrom2size(datas, w.rank, w.dim1, w.resolution)
-    rng = np.random.default_rng(0)
-    A = [1 + 0.01 * rng.standard_normal((d.num_bin, sizes[d.name])) for d in datas]
-    B = {d.name: np.eye(sizes[d.name]) + 0.01 * rng.standard_normal(sizes[d.name]) for d in datas}
-    D = {d.name: rng.standard_normal((w.rank, sizes[d.name])) for d in datas}
-    E, _ = np.linalg.qr(rng.standard_normal((n_cells, w.rank)))
-    orc = O.ALSOracle(datas, w.rank, A, B, D, E, [6] * len(datas), dtype=np.float32, cache_rwr=False)
-    t = time.perf_counter()
-    for ci, d in enumerate(datas):                       # the RWR pass of init / the first fetch
-        for bi in range(len(d.layout())):
-            orc.rwr_tile(ci, bi, 0)
-    t_rwr = time.perf_counter() - t
-    orc.iterate(0, 1)
-    t = time.perf_counter()
-    orc.iterate(1, 1)
-    t_iter = time.perf_counter() - t
-    rate = n_cells / (t_rwr + iters * t_iter)
-    desc = ("%d of %d cells, RWR pass %.2fs + 1 timed ALS iteration %.2fs (3 RWR recomputations "
-            "per bin batch, as the reference), extrapolated to %d iterations" %
-            (n_cells, w.n_cells, t_rwr, t_iter, iters))
-    return rate, desc, time.perf_counter() - t0
+        obj = sfs.Sparse(idx.copy(), val.copy(), shape, copy=True)
+        obj.sort_indices()
+        out.append(sfs.Chrom_Dataset(tensor=obj, bs_bin=bsb, bs_cell=w.n_cells, good_qc_num=-1,
+                                     kind="hic", upper_sim=False, compact=True, flank=w.band,
+                                     chrom=name, resolution=w.resolution))
+    return out
+
+
+class _Quiet:
+    """Silences the reference's progress printing and bars (stdout, stderr) while it runs."""
+
+    def __enter__(self):
+        self.saved = (sys.stdout, sys.stderr)
+        sys.stdout = sys.stderr = open(os.devnull, "w")
+
+    def __exit__(self, *a):
+        sys.stdout.close()
+        sys.stdout, sys.stderr = self.saved
+        return False
+
+
+def reference_fit_rate(config, n_cells, iters, steps, warmup):
+    """Times the reference's own Fast_Higashi_core.fit on the host CPU (all cores) on a cell
+    sample of the workload: the reference's init_params once (untimed), then warmup + steps
+    fits of one ALS iteration each from that state (every iteration recomputes the RWR of each
+    tile, as the reference does).  One more fit at half the sample separates the cost that
+    does not grow with cells (the per-bin polar factors, CP-ALS); the full fit of the
+    workload's cells is extrapolated as iters x (fixed + per-cell x cells).
+    Returns (cells/s, step seconds, description dict)."""
+    import dataclasses
+    import torch
+    from fh_gb300 import synth
+    ref, notes = import_reference()
+    core = ref["core"]
+    threads = os.cpu_count()
+    torch.set_num_threads(threads)
+    w_full = synth.workload(config)
+    cpu = torch.device("cpu")
+
+    def sample(c):
+        w = dataclasses.replace(w_full, n_cells=int(c))
+        coo, _ = synth.generate(w, seed=0)
+        return w, reference_datasets(ref, w, coo)
+
+    def one_fit(w, ds, state):
+        m = core.Fast_Higashi_core(rank=w.rank, off_diag=w.band, res_list=[w.resolution]).to(cpu)
+        if state is None:
+            np.random.seed(0)
+            torch.manual_seed(0)
+            with _Quiet():
+                m.fit(ds, size_ratio=w.dim1, n_iter_max=0, n_iter_parafac=1, do_conv=False,
+                      do_rwr=True, do_col=False, tol=0, run_init=True)
+            return m, None
+        m.A_list = [a.clone() for a in state[0]]
+        m.B_dict = {k: v.clone() for k, v in state[1].items()}
+        m.D_dict = {k: v.clone() for k, v in state[2].items()}
+        m.meta_embedding = state[3].clone()
+        m.n_i = state[4].copy()
+        m.bin_cov_list = [b.clone() if torch.is_tensor(b) else b for b in state[5]]
+        m.bad_bin_cov_list = list(state[6])
+        t0 = time.perf_counter()
+        with _Quiet():
+            m.fit(ds, size_ratio=w.dim1, n_iter_max=1, n_iter_parafac=1, do_conv=False,
+                  do_rwr=True, do_col=False, tol=0, run_init=False)
+        return m, time.perf_counter() - t0
+
+    def init_state(w, ds):
+        m, _ = one_fit(w, ds, None)
+        return ([a.clone() for a in m.A_list], {k: v.clone() for k, v in m.B_dict.items()},
+                {k: v.clone() for k, v in m.D_dict.items()}, m.meta_embedding.clone(),
+                np.array(m.n_i).copy(), list(m.bin_cov_list), list(m.bad_bin_cov_list))
+
+    w, ds = sample(n_cells)
+    state = init_state(w, ds)
+    times = []
+    for i in range(warmup + steps):
+        _, t = one_fit(w, ds, state)
+        if i >= warmup:
+            times.append(t)
+    t_full = float(np.median(times))
+    wh, dsh = sample(max(w.rank, n_cells // 2))
+    st_h = init_state(wh, dsh)
+    one_fit(wh, dsh, st_h)
+    _, t_half = one_fit(wh, dsh, st_h)
+    per_cell = max((t_full - t_half) / (w.n_cells - wh.n_cells), 0.0)
+    fixed = max(t_full - per_cell * w.n_cells, 0.0)
+    fit_s = iters * (fixed + per_cell * w_full.n_cells)
+    rate = w_full.n_cells / fit_s
+    desc = {"kind": "reference", "cores": threads, "extrapolated": True,
+            "sample_cells": w.n_cells, "sample_iters": 1, "measured_s": [round(t, 3) for t in times],
+            "half_sample_cells": wh.n_cells, "half_sample_s": round(t_half, 3),
+            "fixed_s_per_iter": round(fixed, 4), "per_cell_s_per_iter": round(per_cell, 6),
+            "rwr_epochs": sorted(set(int(v) for v in state[4])), "stand_ins": notes,
+            "sample": ("the reference's Fast_Higashi_core.fit on the host CPU (%d threads), one "
+                       "ALS iteration (with its RWR recomputations) per step on %d of %d cells, "
+                       "from the reference's own init; one more at %d cells separates the "
+                       "per-iteration cost that does not grow with cells; extrapolated to %d "
+                       "iterations x %d cells" % (threads, w.n_cells, w_full.n_cells,
+                                                 wh.n_cells, iters, w_full.n_cells))}
+    return rate, t_full, desc
+
+
+def fp64_check(w, coo, state, n_i, iters, dev, embeddings):
+    """Both forms' final meta embedding against an FP64 fit of the same workload from the same
+    initial state and RWR epochs (tests/fp64_reference.py: the reference's fit loop in torch
+    float64 on this GPU, pinned to the numpy oracle by the CPU tests), after an orthogonal
+    Procrustes rotation.  Untimed; runs after every timed region."""
+    import torch
+    from fh_gb300 import synth
+    tests = os.path.join(ROOT, "tests")
+    if tests not in sys.path:
+        sys.path.insert(0, tests)
+    import fp64_reference as F
+    bsb = [synth.recommend_batches(w, nb, w.n_cells)[0] for nb in w.chrom_bins]
+    datas = F.chrom_datas(coo, w.chrom_names, bsb, [w.n_cells] * len(bsb), w.band)
+    A0 = [a.detach().cpu().numpy() for a in state[0]]
+    B0 = {k: v.detach().cpu().numpy() for k, v in state[1].items()}
+    D0 = {k: v.detach().cpu().numpy() for k, v in state[2].items()}
+    E0 = state[3].detach().cpu().numpy()
+    t0 = time.perf_counter()
+    ref = F.FP64Fit(datas, w.rank, A0, B0, D0, E0, [int(v) for v in n_i], dev).fit(iters)
+    E64 = ref.E.cpu().numpy()
+    secs = time.perf_counter() - t0
+    del ref
+    torch.cuda.empty_cache()
+    out = {"aligned_embedding_error_vs_fp64": {k: F.aligned_error(v.detach().cpu().numpy(), E64)
+                                               for k, v in embeddings.items()},
+           "target": 1e-3, "fp64_fit_seconds": round(secs, 1), "iterations": iters,
+           "yardstick": "the reference's fit loop in torch float64 on this GPU, same initial "
+                        "state and RWR epochs (tests/fp64_reference.py)"}
+    out["meets_target"] = all(v <= 1e-3 for v in out["aligned_embedding_error_vs_fp64"].values())
+    return out
+
+
+def bench_config(w, rows, iters, ws):
+    """The config object both arms print (the same workload, so the same dict)."""
+    return {"workload": "%s: %d cells, %d bins, R=%d, band %d, %d ALS iterations" %
+                        (w.name, w.n_cells, sum(w.chrom_bins), w.rank, w.band, iters),
+            "l2": "inputs larger than L2 (X: %d cells x %d band rows, %.1f GB in fp32)" %
+                  (w.n_cells, rows, w.n_cells * rows * 4 / 1e9),
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
+
+
+def band_rows(w):
+    """Band rows (bin-batch rows x compact columns, summed) of a workload: the X row count."""
+    from fh_gb300 import synth
+    total = 0
+    for nb in w.chrom_bins:
+        bsb, _ = synth.recommend_batches(w, nb, w.n_cells)
+        for r0 in range(0, nb, bsb):
+            rows = min(bsb, nb - r0)
+            lo, hi = max(0, r0 - w.band), min(nb, r0 + rows + w.band)
+            total += rows * (hi - lo)
+    return total
 
 
 def reference_arm(args, rank, ws):
     if rank != 0:
         return
-    w, coo, _ = make_workload(args.config, cells=args.cells)
+    from fh_gb300 import synth
+    w = synth.workload(args.config)
     iters = args.iters or w.n_iter
-    threads = os.cpu_count()
-    rates, desc = [], ""
-    for i in range(args.warmup + args.steps):
-        r, desc, _ = cpu_sample_rate(coo, w, args.sample_cells, iters)
-        if i >= args.warmup:
-            rates.append(r)
-    v = float(np.mean(rates))
-    line = {"metric": METRIC, "value": v, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * w.n_cells / v,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded generator, %s)" % args.config, "impl": "reference",
-            "config": {"workload": "%s: %d cells, %d bins, R=%d, band %d, %d ALS iterations" %
-                       (w.name, w.n_cells, sum(w.chrom_bins), w.rank, w.band, iters),
-                       "l2": "inputs larger than L2"},
-            "cpu_baseline": {"value": v, "unit": "cells/s", "cores": threads, "kind": "port",
-                             "sample": desc},
-            "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line = {"metric": METRIC, "impl": "reference"}
+    try:
+        v, t_step, desc = reference_fit_rate(args.config, args.sample_cells, iters, args.steps,
+                                             args.warmup)
+    except (ImportError, FileNotFoundError, OSError) as e:
+        line["unavailable"] = "the reference could not be imported: %s" % e
+        print(json.dumps(line), flush=True)
+        return
+    line.update({"value": v, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
+                 "warmup": args.warmup, "ms_per_step": 1000.0 * t_step,
+                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                 "dtype": "f32", "data": "synthetic (seeded generator, %s)" % args.config,
+                 "config": bench_config(w, band_rows(w), iters, ws),
+                 "cpu_baseline": dict(desc, value=v, unit="cells/s"),
+                 "e2e": {"value": v, "unit": "cells/s", "h2d_bytes_per_step": 0,
+                         "d2h_bytes_per_step": 0}})
     print(json.dumps(line), flush=True)
 
 
@@ -325,6 +603,7 @@ def gb300_arm(args, rank, local, ws):
         device_step(peng, phist, graph=False)
         torch.cuda.synchronize()
         pkt = peng.timing_summary()
+        E_plain = peng.E[:, :w.rank].clone()
         plain = {"value": ws * C / (pms / 1000.0), "unit": "cells/s", "ms_per_step": pms,
                  "gpu_launches": int(plaunch),
                  "kernel_ms": {k: round(v["mean_ms"], 4) for k, v in pkt.items()},
@@ -339,21 +618,24 @@ def gb300_arm(args, rank, local, ws):
     torch.cuda.synchronize()
     kt = eng.timing_summary()
     eng.timing = None
-    hbm, bf16, peak_kind = peaks()
     xel = 2 * eng.planes if eng.bf16 else 4
-    xbytes = C * eng.rows * xel
-    fam = max(("xe", "xg"), key=lambda k: kt.get(k, {}).get("total_ms", 0))
-    dom = max(kt, key=lambda k: kt[k]["total_ms"])
-    ach = xbytes / (kt[fam]["mean_ms"] / 1000.0) / 1e9
-    traffic = (XPASS_TRAFFIC_RATIO[fam] * xbytes / 1e9) if eng.precision == "bf16x2" else None
-    roof = {"kernel": fam, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-            "frac": ach / hbm, "peak_kind": peak_kind, "traffic": traffic,
-            "traffic_unit": "GB per launch (ncu at 2,000 cells, scaled by cells x band rows)",
-            "algorithmic_bytes_per_launch": xbytes,
-            "note": ("X pass (%d cells x %d band rows %s); kernel share of the step: %s; "
-                     "largest family: %s" % (C, eng.rows, eng.precision,
-                                             {k: round(v["total_ms"] / ms, 3) for k, v in kt.items()},
-                                             dom))}
+    from fh_gb300.engine import FitEngine
+    fams = family_rooflines(eng, kt, clk.summary().get("sm_max_mhz"),
+                            FitEngine.parafac_schedule(iters, 1))
+    share = {k: round(v["total_ms"] / ms, 3) for k, v in kt.items()}
+    dom = max(fams, key=lambda f: kt[f["kernel"]]["total_ms"])
+    roof = dict(dom)
+    if dom["kernel"] in ("xe", "xg") and eng.precision == "bf16x2":
+        roof["traffic"] = XPASS_TRAFFIC_RATIO[dom["kernel"]] * dom["work_per_launch"] / 1e9
+        roof["traffic_unit"] = "GB per launch (ncu at 2,000 cells, scaled by cells x band rows)"
+    elif dom["kernel"] == "procrustes":
+        roof["traffic"] = PROCRUSTES_TRAFFIC_PER_ROW * eng.nb / 1e9
+        roof["traffic_unit"] = "GB per launch (ncu at 2,000 cells, scaled by bin rows)"
+    else:
+        roof["traffic"] = None
+    roof["note"] = ("the family with the largest share of the step; every family in families, "
+                    "shares of the step: %s" % share)
+    roof["families"] = fams
     # ---- end to end through the public API, host data in and out
     A0, B0, D0, E0 = [x.cpu() for x in state[0]], {k: v.cpu() for k, v in state[1].items()}, \
         {k: v.cpu() for k, v in state[2].items()}, state[3].cpu()
@@ -390,27 +672,35 @@ def gb300_arm(args, rank, local, ws):
     e2e = {"value": ws * C / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1000.0,
            "ms_steps": [round(t * 1000.0, 1) for t in e2e_times], "statistic": "median"}
+    # ---- both forms' error against an FP64 fit from the same state (untimed)
+    precision = None
+    if not args.no_fp64:
+        embs = {eng.precision: eng.E[:, :w.rank].clone()}
+        if plain is not None:
+            embs["fp32"] = E_plain
+        precision = fp64_check(w, coo, state, n_i, iters, dev, embs)
     if rank != 0:
         return
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        r, desc, _ = cpu_sample_rate(coo, w, args.sample_cells, iters)
-        cpu = {"value": r, "unit": "cells/s", "cores": os.cpu_count(), "kind": "port", "sample": desc}
+        try:
+            r, _, desc = reference_fit_rate(args.config, args.sample_cells, iters, 2, 1)
+            cpu = dict(desc, value=r, unit="cells/s")
+        except (ImportError, FileNotFoundError, OSError) as e:
+            cpu = {"unavailable": "the reference could not be imported: %s" % e}
     line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16" if eng.bf16 else "f32", "data": "synthetic (seeded generator, %s)" % args.config,
-            "config": {"workload": "%s: %d cells, %d bins (%d bin batches), R=%d, band %d, %d ALS "
-                                   "iterations, RWR epochs %s" %
-                                   (w.name, C, sum(w.chrom_bins), eng.n_tiles, w.rank, w.band,
-                                    iters, sorted(set(int(v) for v in n_i))),
-                       "precision": ({"bf16": "X in one bf16 plane, tensor-core X passes",
-                                      "bf16x2": "X in two bf16 planes (hi+lo), tensor-core X passes"}
-                                     .get(eng.precision, "fp32 (plain)")),
-                       "l2": "inputs larger than L2 (X %.2f GB)" % (eng.Ct * eng.ldx * xel / 1e9), "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "vs_baseline": None, "dtype": "bf16" if eng.bf16 else "f32",
+            "data": "synthetic (seeded generator, %s)" % args.config,
+            "config": bench_config(w, eng.rows, iters, ws),
+            "precision": ({"bf16": "X in one bf16 plane, tensor-core X passes",
+                           "bf16x2": "X in two bf16 planes (hi+lo), tensor-core X passes"}
+                          .get(eng.precision, "fp32 (plain)")),
+            "rwr_epochs": sorted(set(int(v) for v in n_i)), "bin_batches": eng.n_tiles,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
             "plain_fp32": plain,
             "clocks": clk.summary(), "kernel_ms": {k: round(v["mean_ms"], 4) for k, v in kt.items()},
-            "autotune": autotune_summary(),
+            "autotune": autotune_summary(), "precision_check": precision,
             "loss_final": float(m.engine.losses(hist[-1], eng.tensor_norms())[0])}
     print(json.dumps(line), flush=True)
 

@@ -14,9 +14,27 @@
 // W computed after the meta-embedding update serves this iteration's Y and the next
 // iteration's temp, so an iteration costs two passes over X instead of three passes plus
 // three RWR recomputations.
+//
+// Summation order.  Both passes sum long runs (10,000 cells in W, ~35,000 band rows per split
+// in SVD^T at 10,000 cells x 500 kb).  A single fp32 chain over such a run loses about
+// sqrt(n) ulps where the terms cancel, and the fitted embedding inherits it (the meta polar
+// amplifies the error of SVD^T by its condition number).  Each thread therefore sums one
+// staged tile of K (16 or 32 terms) in a fresh fp32 chain and folds that partial into a
+// running sum with Kahan compensation: the register that holds the tile's chain starts at
+// minus the running compensation, so the fold is three adds and no extra registers.  Split
+// partials are added in fp64.
 #include "fh_common.cuh"
 
 namespace fh {
+
+// Folds a tile's chain into the running sum (Kahan).  On entry acc = tile sum - c, where c is
+// the running compensation; on exit sum holds the new running sum and acc = -c' (the start of
+// the next tile's chain).  sum + acc is the compensated total.
+__device__ __forceinline__ void kahan_fold(float& sum, float& acc) {
+  const float t = sum + acc;
+  acc = acc - (t - sum);
+  sum = t;
+}
 
 // ---------------------------------------------------------------------------------------
 // W[row][m] = sum_c X[c][row] * E[c][m]; CTA = 128 band rows x RP, K = cells in steps of 32
@@ -56,11 +74,11 @@ __global__ void __launch_bounds__(256) xe_f32_kernel(const float* __restrict__ X
     cp_async_commit();
   };
 
-  float acc[RPT][4];
+  float acc[RPT][4], sum[RPT][4];   // tile chains (from -compensation) and running sums
 #pragma unroll
   for (int i = 0; i < RPT; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < 4; ++j) acc[i][j] = sum[i][j] = 0.f;
 
   load(0, 0);
   for (int kt = 0; kt < ntiles; ++kt) {
@@ -91,6 +109,10 @@ __global__ void __launch_bounds__(256) xe_f32_kernel(const float* __restrict__ X
         acc[i][3] = fmaf(xv[i], ev.w, acc[i][3]);
       }
     }
+#pragma unroll
+    for (int i = 0; i < RPT; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) kahan_fold(sum[i][j], acc[i][j]);
     __syncthreads();
   }
 #pragma unroll
@@ -98,7 +120,8 @@ __global__ void __launch_bounds__(256) xe_f32_kernel(const float* __restrict__ X
     const int64_t r = r0 + rg * RPT + i;
     if (r < rows)
       *reinterpret_cast<float4*>(W + r * RP + mg * 4) =
-          make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+          make_float4(sum[i][0] + acc[i][0], sum[i][1] + acc[i][1], sum[i][2] + acc[i][2],
+                      sum[i][3] + acc[i][3]);
   }
 }
 
@@ -146,11 +169,11 @@ __global__ void __launch_bounds__(256) xg_f32_kernel(const float* __restrict__ X
     cp_async_commit();
   };
 
-  float acc[8][MPT];
+  float acc[8][MPT], sum[8][MPT];   // tile chains (from -compensation) and running sums
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < MPT; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < MPT; ++j) acc[i][j] = sum[i][j] = 0.f;
 
   if (ntiles > 0) load(0, 0);
   for (int kt = 0; kt < ntiles; ++kt) {
@@ -170,6 +193,10 @@ __global__ void __launch_bounds__(256) xg_f32_kernel(const float* __restrict__ X
 #pragma unroll
         for (int j = 0; j < MPT; ++j) acc[i][j] = fmaf(xv[i], gv[j], acc[i][j]);
     }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < MPT; ++j) kahan_fold(sum[i][j], acc[i][j]);
     __syncthreads();
   }
   float* out = partial + (int64_t)s * C * RP;
@@ -178,7 +205,7 @@ __global__ void __launch_bounds__(256) xg_f32_kernel(const float* __restrict__ X
     const int c = c0 + cg + 16 * i;
     if (c < C) {
 #pragma unroll
-      for (int j = 0; j < MPT; ++j) out[(int64_t)c * RP + mg * MPT + j] = acc[i][j];
+      for (int j = 0; j < MPT; ++j) out[(int64_t)c * RP + mg * MPT + j] = sum[i][j] + acc[i][j];
     }
   }
 }

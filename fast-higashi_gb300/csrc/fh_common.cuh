@@ -46,15 +46,16 @@ __device__ inline T block_sum(T v, T* scratch /* >= 32 */) {
   return s;
 }
 
-// out[i] = sum over k of partial[k][i] in a fixed order (deterministic split-K reduction).
+// out[i] = sum over k of partial[k][i] in a fixed order (deterministic split-K reduction),
+// added in fp64 and rounded once.
 template <typename T>
 __global__ void reduce_splits_kernel(const T* __restrict__ partial, int splits, int64_t n,
                                      T* __restrict__ out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    T s = 0;
-    for (int k = 0; k < splits; ++k) s += partial[(int64_t)k * n + i];
-    out[i] = s;
+    double s = 0.0;
+    for (int k = 0; k < splits; ++k) s += (double)partial[(int64_t)k * n + i];
+    out[i] = (T)s;
   }
 }
 

@@ -13,15 +13,25 @@
 // The small operands E (cells x rp) and G^T (band rows x rp) are split the same way and
 // stacked along N, so one MMA per plane and K step produces X*hi and X*lo side by side in
 // TMEM; the epilogue adds them.  The products are exact in the fp32 accumulator, so the
-// error is that of X's planes: 2^-9 relative with one plane, 2^-17 with two.
+// representation error is that of the operands: X's planes (2^-9 relative with one plane,
+// 2^-17 with two) and the 16-significant-bit split of the small operand.
 //
-// CTA (192 threads, one per SM, persistent over work items):
+// Summation order.  A run of K chunks (fold, 8 by default: 512 cells or band rows) goes into
+// one TMEM accumulator, which the epilogue then folds into fp32 running sums with Kahan
+// compensation (plain running sums at rank 128) while the MMAs of the next run fill the other
+// accumulator.  Each output is
+// therefore a short tensor-core chain per run plus a compensated sum over runs, instead of
+// one chain over the whole K range (10,000 cells in W, ~35,000 band rows per split of S^T at
+// 10,000 cells x 500 kb), whose rounding the fitted embedding inherits.
+//
+// CTA (64 + 32 EW threads, one per SM, persistent over work items):
 //   warp 0  TMA producer: per K step one 128 x 64 tile of X (two 64 x 64 boxes) and the
 //           N x 64 slab of the hi|lo operand (N/64 boxes) into an NST-deep smem ring
-//   warp 1  TMEM owner and MMA issuer: 4 x tcgen05.mma (K = 16 each) per K step, commit to
-//           free the stage; two TMEM accumulators so the epilogue of one item overlaps the
-//           main loop of the next
-//   warps 2-5 epilogue: tcgen05.ld of their 32-lane quarter, hi + lo, fp32 stores
+//   warp 1  TMEM owner and MMA issuer: 4 x tcgen05.mma (K = 16 each) per K step and plane,
+//           commit to free the stage; a commit to the accumulator's barrier after each run
+//   warps 2..  EW epilogue warps (4 per 64 output columns): tcgen05.ld of their 32-lane
+//           quarter and column group, hi + lo, the compensated fold, fp32 stores at the end
+//           of an item
 #include "tc_common.cuh"
 
 namespace fh {
@@ -37,14 +47,20 @@ struct XPassArgs {
   int64_t chunks_per_split;  // xg
   int cell_tiles;       // xg
   int plane_rows;       // rows of the X map between planes (the cells of a plane)
+  int fold;             // K chunks per accumulator run (>= 1)
   float* out;           // xe: W[rows][rp]; xg: partial[splits][n_cells][rp]
   int* status;
 };
 
-constexpr int kXpThreads = 192;
+constexpr int kXpFold = 8;     // default run length in K chunks of 64
 
 template <int N, int PLANES>
 struct XpCfg {
+  static constexpr int kRP = N / 2;                     // output columns
+  static constexpr int kCW = kRP < 64 ? kRP : 64;       // output columns per epilogue warp
+  static constexpr int kEW = 4 * (kRP / kCW);           // epilogue warps
+  static constexpr int kThreads = 64 + 32 * kEW;
+  static constexpr bool kKahan = kEW == 4;              // compensated folds (ranks <= 64)
   static constexpr uint32_t kA = PLANES * 128 * 64 * 2; // 16 KB per plane: two 64 x 64 boxes
   static constexpr uint32_t kB = (uint32_t)N * 64 * 2;  // N/64 boxes of the hi|lo operand
   static constexpr uint32_t kStage = kA + kB;
@@ -57,6 +73,7 @@ struct XpItem {
   int x0;        // xe: first band row of the tile; xg: first cell of the tile
   int split;     // xg
   int64_t k0, k1;
+  int64_t runs;  // accumulator runs of the item (one, empty, when k1 == k0)
 };
 
 template <int PASS>
@@ -76,15 +93,17 @@ __device__ __forceinline__ XpItem xp_item(const XPassArgs& p, int64_t item) {
     if (it.k1 > p.k_chunks) it.k1 = p.k_chunks;
     if (it.k0 > it.k1) it.k0 = it.k1;
   }
+  it.runs = it.k1 > it.k0 ? (it.k1 - it.k0 + p.fold - 1) / p.fold : 1;
   return it;
 }
 
 template <int PASS, int N, int PLANES>
-__global__ void __launch_bounds__(kXpThreads, 1)
+__global__ void __launch_bounds__(XpCfg<N, PLANES>::kThreads, 1)
     xpass_bf16_kernel(const __grid_constant__ CUtensorMap amap,
                       const __grid_constant__ CUtensorMap bmap, XPassArgs p) {
   using Cfg = XpCfg<N, PLANES>;
   constexpr int NST = Cfg::kStages;
+  constexpr int CW = Cfg::kCW;
   constexpr uint32_t kIdesc = idesc_bf16(128, N, PASS == kPassXE, true);
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
@@ -110,7 +129,7 @@ __global__ void __launch_bounds__(kXpThreads, 1)
     }
     for (int a = 0; a < 2; ++a) {
       mbar_init(accf(a), 1);
-      mbar_init(acce(a), 4);
+      mbar_init(acce(a), Cfg::kEW);
     }
     mbar_init(drain, 1);
     misc[1] = 0;
@@ -168,34 +187,38 @@ __global__ void __launch_bounds__(kXpThreads, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------------- MMA issuer
     if (lane == 0) {
-      uint32_t it = 0, tc = 0;
+      uint32_t it = 0, tc = 0;   // stages consumed, accumulator runs issued
       bool ok = true;
-      for (int64_t item = blockIdx.x; ok && item < p.n_items; item += gridDim.x, ++tc) {
+      for (int64_t item = blockIdx.x; ok && item < p.n_items; item += gridDim.x) {
         const XpItem w = xp_item<PASS>(p, item);
-        const uint32_t a = tc & 1u, aph = (tc >> 1) & 1u;
-        if (!mbar_wait(acce(a), aph ^ 1u, abort)) { ok = false; break; }
-        tc_fence_after();
-        const uint32_t d = tmem + a * (uint32_t)N;
-        for (int64_t kc = w.k0; kc < w.k1; ++kc, ++it) {
-          const uint32_t s = it % NST, ph = (it / NST) & 1u;
-          if (!mbar_wait(full(s), ph, abort)) { ok = false; break; }
+        for (int64_t run = 0; ok && run < w.runs; ++run, ++tc) {
+          const uint32_t a = tc & 1u, aph = (tc >> 1) & 1u;
+          if (!mbar_wait(acce(a), aph ^ 1u, abort)) { ok = false; break; }
           tc_fence_after();
-          misc[3] = it + 1;
-          const uint32_t sa = base + s * Cfg::kStage, sb = sa + Cfg::kA;
+          const uint32_t d = tmem + a * (uint32_t)N;
+          const int64_t ks = w.k0 + run * p.fold;
+          const int64_t ke = ks + p.fold < w.k1 ? ks + p.fold : w.k1;
+          for (int64_t kc = ks; kc < ke; ++kc, ++it) {
+            const uint32_t s = it % NST, ph = (it / NST) & 1u;
+            if (!mbar_wait(full(s), ph, abort)) { ok = false; break; }
+            tc_fence_after();
+            misc[3] = it + 1;
+            const uint32_t sa = base + s * Cfg::kStage, sb = sa + Cfg::kA;
 #pragma unroll
-          for (int pl = 0; pl < PLANES; ++pl)
+            for (int pl = 0; pl < PLANES; ++pl)
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
-              const uint32_t ap = sa + 16384u * pl;
-              const uint64_t ad = PASS == kPassXE ? sdesc_sw128(ap + 2048u * kk, 8192, 1024)
-                                                  : sdesc_sw128(ap + 32u * kk, 16, 1024);
-              const uint64_t bd = sdesc_sw128(sb + 2048u * kk, 8192, 1024);
-              mma_bf16(d, ad, bd, kIdesc, (kc > w.k0 || kk > 0 || pl > 0) ? 1u : 0u);
-            }
-          mma_commit(empty(s));
+              for (int kk = 0; kk < 4; ++kk) {
+                const uint32_t ap = sa + 16384u * pl;
+                const uint64_t ad = PASS == kPassXE ? sdesc_sw128(ap + 2048u * kk, 8192, 1024)
+                                                    : sdesc_sw128(ap + 32u * kk, 16, 1024);
+                const uint64_t bd = sdesc_sw128(sb + 2048u * kk, 8192, 1024);
+                mma_bf16(d, ad, bd, kIdesc, (kc > ks || kk > 0 || pl > 0) ? 1u : 0u);
+              }
+            mma_commit(empty(s));
+          }
+          if (!ok) break;
+          mma_commit(accf(a));
         }
-        if (!ok) break;
-        mma_commit(accf(a));
       }
       if (!ok) {
         *abort = 1;
@@ -204,49 +227,80 @@ __global__ void __launch_bounds__(kXpThreads, 1)
     }
     __syncwarp();
   } else {
-    // ------------------------------------------------------------- epilogue (warps 2-5)
-    const int q = warp & 3;   // TMEM lane quarter this warp may access
+    // ------------------------------------------------------------- epilogue
+    const int q = warp & 3;                 // TMEM lane quarter this warp may access
+    const int cb = ((warp - 2) >> 2) * CW;  // first output column of this warp
     uint32_t tc = 0;
-    for (int64_t item = blockIdx.x; item < p.n_items; item += gridDim.x, ++tc) {
+    bool ok = true;
+    for (int64_t item = blockIdx.x; ok && item < p.n_items; item += gridDim.x) {
       const XpItem w = xp_item<PASS>(p, item);
-      const uint32_t a = tc & 1u, aph = (tc >> 1) & 1u;
-      const bool got = __all_sync(0xffffffffu, mbar_wait(accf(a), aph, abort));
-      if (!got) {
-        if (lane == 0) {
-          *abort = 1;
-          set_status(p.status, FH_ERR_TIMEOUT);
+      // running sums; acc = minus the Kahan compensation (ranks <= 64; at rank 128 the ten
+      // warps leave no registers for it, and the runs add into plain fp32 running sums)
+      float sum[CW], acc[Cfg::kKahan ? CW : 1];
+#pragma unroll
+      for (int c = 0; c < CW; ++c) sum[c] = 0.f;
+#pragma unroll
+      for (int c = 0; c < (Cfg::kKahan ? CW : 1); ++c) acc[c] = 0.f;
+      for (int64_t run = 0; run < w.runs; ++run, ++tc) {
+        const uint32_t a = tc & 1u, aph = (tc >> 1) & 1u;
+        const bool got = __all_sync(0xffffffffu, mbar_wait(accf(a), aph, abort));
+        if (!got) {
+          if (lane == 0) {
+            *abort = 1;
+            set_status(p.status, FH_ERR_TIMEOUT);
+          }
+          ok = false;
+          break;
         }
-        break;
+        tc_fence_after();
+        if (w.k1 > w.k0) {
+          const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + a * (uint32_t)N + cb;
+          // 8 columns per load at rank 128, where 320 threads leave fewer registers each
+          constexpr int STEP = Cfg::kEW > 4 ? 8 : 16;
+#pragma unroll
+          for (int c = 0; c < CW; c += STEP) {
+            float hi[STEP], lo[STEP];
+            if constexpr (STEP == 16) tmem_ld16x2(ta + c, ta + N / 2 + c, hi, lo);
+            else tmem_ld8x2(ta + c, ta + N / 2 + c, hi, lo);
+#pragma unroll
+            for (int v = 0; v < STEP; ++v) {
+              if constexpr (Cfg::kKahan) {
+                const float y = acc[c + v] + (hi[v] + lo[v]);
+                const float t = sum[c + v] + y;
+                acc[c + v] = y - (t - sum[c + v]);
+                sum[c + v] = t;
+              } else {
+                sum[c + v] += hi[v] + lo[v];
+              }
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acce(a));
       }
-      tc_fence_after();
+      if (!ok) break;
       const int64_t r = (int64_t)w.x0 + 32 * q + lane;
       float* o;
       bool valid;
       if (PASS == kPassXE) {
         valid = r < p.rows;
-        o = p.out + r * p.rp;
+        o = p.out + r * p.rp + cb;
       } else {
         valid = r < p.n_cells;
-        o = p.out + ((int64_t)w.split * p.n_cells + r) * p.rp;
+        o = p.out + ((int64_t)w.split * p.n_cells + r) * p.rp + cb;
       }
-      const bool has = w.k1 > w.k0;
-      const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + a * (uint32_t)N;
-#pragma unroll 1
-      for (int c = 0; c < N / 2; c += 16) {
-        float hi[16], lo[16];
-        tmem_ld16x2(ta + c, ta + N / 2 + c, hi, lo);
-        if (valid) {
-          float4* o4 = reinterpret_cast<float4*>(o + c);
+      if (valid) {
+        float4* o4 = reinterpret_cast<float4*>(o);
 #pragma unroll
-          for (int v = 0; v < 4; ++v)
-            o4[v] = has ? make_float4(hi[4 * v] + lo[4 * v], hi[4 * v + 1] + lo[4 * v + 1],
-                                      hi[4 * v + 2] + lo[4 * v + 2], hi[4 * v + 3] + lo[4 * v + 3])
-                        : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int v = 0; v < CW / 4; ++v) {
+          if constexpr (Cfg::kKahan)
+            o4[v] = make_float4(sum[4 * v] + acc[4 * v], sum[4 * v + 1] + acc[4 * v + 1],
+                                sum[4 * v + 2] + acc[4 * v + 2], sum[4 * v + 3] + acc[4 * v + 3]);
+          else
+            o4[v] = make_float4(sum[4 * v], sum[4 * v + 1], sum[4 * v + 2], sum[4 * v + 3]);
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(acce(a));
     }
   }
 
@@ -295,7 +349,7 @@ static int launch_xpass(const CUtensorMap& am, const CUtensorMap& bm, const XPas
   const int sms = sm_count();
   if (sms <= 0) return FH_ERR_LAUNCH;
   const int64_t grid = p.n_items < sms ? p.n_items : sms;
-  k<<<(unsigned)grid, kXpThreads, Cfg::kSmem, s>>>(am, bm, p);
+  k<<<(unsigned)grid, Cfg::kThreads, Cfg::kSmem, s>>>(am, bm, p);
   FH_CHECK_LAUNCH();
   return FH_OK;
 }
@@ -336,9 +390,9 @@ extern "C" int fh_split_bf16(const float* src, int64_t n_rows, int32_t rp, int64
 
 extern "C" int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total,
                           int32_t planes, int32_t n_cells, int64_t rows, const uint16_t* E2,
-                          int32_t rp, float* W, int* status, void* stream) {
+                          int32_t rp, int32_t fold, float* W, int* status, void* stream) {
   if (!X16 || !E2 || !W || n_cells <= 0 || n_cells > n_cells_total || rows <= 0 || ldx < rows ||
-      ldx % 128 || (planes != 1 && planes != 2))
+      ldx % 128 || (planes != 1 && planes != 2) || fold < 0)
     return FH_ERR_ARG;
   if (rp != 32 && rp != 64 && rp != 128) return FH_ERR_UNSUPPORTED;
   // the map ends at the last 128-row tile, so no box reads past the band rows asked for
@@ -354,6 +408,7 @@ extern "C" int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_tota
   p.rp = rp;
   p.n_items = ceil_div(rows, 128);
   p.k_chunks = ceil_div(n_cells, 64);
+  p.fold = fold > 0 ? fold : kXpFold;
   p.out = W;
   p.status = status;
   return dispatch_xpass<kPassXE>(am, bm, p, planes, (cudaStream_t)stream);
@@ -378,10 +433,10 @@ extern "C" int fh_xg_bf16_splits(int32_t n_cells, int64_t rows) {
 
 extern "C" int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total,
                           int32_t planes, int32_t n_cells, int64_t rows, const uint16_t* G2,
-                          int32_t rp, int32_t splits, float* partial, float* out, int* status,
-                          void* stream) {
+                          int32_t rp, int32_t splits, int32_t fold, float* partial, float* out,
+                          int* status, void* stream) {
   if (!X16 || !G2 || !partial || !out || n_cells <= 0 || n_cells > n_cells_total || rows <= 0 ||
-      ldx < rows || ldx % 128 || splits <= 0 || (planes != 1 && planes != 2))
+      ldx < rows || ldx % 128 || splits <= 0 || (planes != 1 && planes != 2) || fold < 0)
     return FH_ERR_ARG;
   if (rp != 32 && rp != 64 && rp != 128) return FH_ERR_UNSUPPORTED;
   const uint64_t inner = (uint64_t)ceil_div(rows, 128) * 128;
@@ -401,6 +456,7 @@ extern "C" int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_tota
   p.n_items = (int64_t)p.cell_tiles * used;
   p.k_chunks = chunks;
   p.chunks_per_split = per;
+  p.fold = fold > 0 ? fold : kXpFold;
   p.out = partial;
   p.status = status;
   cudaStream_t s = (cudaStream_t)stream;

@@ -80,9 +80,9 @@ SIGNATURES = {
     "fh_rwr_tiles_bf16": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, I64, P, P, P]),
     "fh_rwr_tiles_tc": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, I64, P, P, P]),
     "fh_split_bf16": (C.c_int, [P, I64, I32, I64, P, P]),
-    "fh_xe_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, P, P, P]),
+    "fh_xe_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, I32, P, P, P]),
     "fh_xg_bf16_splits": (C.c_int, [I32, I64]),
-    "fh_xg_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, I32, P, P, P, P]),
+    "fh_xg_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, I32, I32, P, P, P, P]),
     "fh_procrustes_f32": (C.c_int, [P, P, I64, I32, I32, P, P, I32, P, P, I32, I32, I32, P, P,
                                     P, P, P]),
     "fh_projection_g_f32": (C.c_int, [P, P, I64, I32, I32, P, I32, P, P, I32, I32, I32, P, P,

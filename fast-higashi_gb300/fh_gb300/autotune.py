@@ -2,8 +2,9 @@
 the fastest.
 
 A choice is keyed by (device, knob, problem signature).  It is cached in memory and in a JSON
-file (``FH_TUNE_CACHE``, default ``~/.cache/fh_gb300/tune.json``), so a shape is tuned once per
-machine and later processes reuse the result; ``FH_AUTOTUNE=0`` turns tuning off and every
+file (``FH_TUNE_CACHE``, default ``~/.cache/fh_gb300/tune.json``; set but empty: memory only),
+so a shape is tuned once per machine and later processes reuse the result; ``FH_AUTOTUNE=0``
+turns tuning off and every
 knob keeps its built-in heuristic.  Each candidate runs once untimed, then ``reps`` times
 between CUDA events on the current stream; the smallest time wins and ties keep the earlier
 candidate (callers list the heuristic first).  Tuning launches kernels, so it must not run
@@ -28,8 +29,12 @@ import threading
 
 
 def _default_path():
-    return os.environ.get("FH_TUNE_CACHE") or os.path.join(
-        os.path.expanduser("~"), ".cache", "fh_gb300", "tune.json")
+    """FH_TUNE_CACHE when set (an empty value keeps choices in memory only), else the file
+    under ~/.cache."""
+    v = os.environ.get("FH_TUNE_CACHE")
+    if v is not None:
+        return v
+    return os.path.join(os.path.expanduser("~"), ".cache", "fh_gb300", "tune.json")
 
 
 class Tuner:

@@ -52,6 +52,9 @@ class FitEngine:
         self.bf16 = precision != "fp32"
         self.planes = 2 if precision == "bf16x2" else 1
         self.timing = None   # {kernel family: [(start event, end event)]} when enabled
+        # K chunks of 64 per tensor-memory accumulator run in the bf16 X passes (0: the
+        # library's default); shorter runs, more compensated folds
+        self.fold = 0
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise _lib.FHError("FitEngine", 2, "the fit runs on a CUDA device only")
@@ -350,7 +353,7 @@ class FitEngine:
                                       device=self.device)
             _lib.call("fh_split_bf16", P(E), n_cells, rp, rp, P(E2), self.sp())
             _lib.call("fh_xe_bf16", P(self.X16[0, :, a0:]), self.ldx, self.Ct, self.planes,
-                      n_cells, rows, P(E2), rp, P(W), P(self.status), self.sp())
+                      n_cells, rows, P(E2), rp, self.fold, P(W), P(self.status), self.sp())
         else:
             _lib.call("fh_xe_f32", P(self.X[:, a0:]), self.ldx, n_cells, rows, P(E), rp, P(W),
                       self.sp())
@@ -364,8 +367,8 @@ class FitEngine:
                                       device=self.device)
             _lib.call("fh_split_bf16", P(Gt), rows, rp, rp, P(G2), self.sp())
             _lib.call("fh_xg_bf16", P(self.X16[0, :, a0:]), self.ldx, self.Ct, self.planes,
-                      n_cells, rows, P(G2), rp, splits, P(partial), P(out), P(self.status),
-                      self.sp())
+                      n_cells, rows, P(G2), rp, splits, self.fold, P(partial), P(out),
+                      P(self.status), self.sp())
         else:
             _lib.call("fh_xg_f32", P(self.X[:, a0:]), self.ldx, n_cells, rows, P(Gt), rp, splits,
                       P(partial), P(out), self.sp())

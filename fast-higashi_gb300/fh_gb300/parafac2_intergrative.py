@@ -75,10 +75,6 @@ class Fast_Higashi_core:
                                            self.chrom2num_bin[d.chrom] + d.num_bin)
                 self.chrom2num_bin[d.chrom] += d.num_bin
 
-    @staticmethod
-    def _check_options(do_conv, do_col):
-        """Every combination of do_conv / do_rwr / do_col is supported."""
-
     # ------------------------------------------------------------------ init
     def init_params(self, schic, do_conv, do_rwr, do_col, seed=None):
         """Initial factors (parafac2_intergrative.py:61-301): A = 1 + 0.01 N(0,1) and
@@ -127,7 +123,6 @@ class Fast_Higashi_core:
     def fit(self, schic, size_ratio=0.3, n_iter_max=2000, n_iter_parafac=5, do_conv=True,
             do_rwr=False, do_col=False, tol=1e-8, size_list=None, gpu_id=None, verbose=True,
             run_init=True):
-        self._check_options(do_conv, do_col)
         self.gpu_id = gpu_id
         self._sizes(schic, size_ratio, size_list)
         if verbose:
@@ -148,6 +143,9 @@ class Fast_Higashi_core:
                 if it % 10 == 0 and it > 0 and n_iter_parafac < 10:
                     n_iter_parafac += 1
                 eng.iterate(it == 0, n_iter_parafac, hist[it])
+                # _record reads the loss scalars (a device round trip each iteration), so a
+                # kernel error stops the fit here instead of running on NaN losses
+                eng.check_status("fit")
                 if self._record(eng, hist[it], it, lines, verbose, t_start, tol):
                     done = it + 1
                     break
@@ -199,7 +197,6 @@ class Fast_Higashi_core:
         """One update (parafac2_intergrative.py:304-540) from the current state.  Returns
         (projection_list, projected_tensor_list, rec_error_x_U, rec_error_x_V
         [, rec_error_tensor_norm])."""
-        self._check_options(do_conv, do_col)
         eng = self._engine(schic, do_rwr, do_conv, do_col)
         eng.set_state(self.A_list, self.B_dict, self.D_dict, self.meta_embedding)
         eng.update(first=True)
@@ -215,7 +212,6 @@ class Fast_Higashi_core:
 
     # ------------------------------------------------------------------ transform
     def transform(self, schic, do_conv, do_rwr, do_col):
-        self._check_options(do_conv, do_col)
         eng = self._engine(schic, do_rwr, do_conv, do_col)
         E = eng.transform()
         eng.check_status("transform")

@@ -254,17 +254,21 @@ int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const 
  *                (bf16[n_cells][2 rp]).  rp in {32, 64, 128}.
  * fh_xg_bf16:    out[c][m] = sum_row X16[c][row] Gt[row][m] for c < n_cells;  G2 = split of
  *                Gt (bf16[rows][2 rp]); partial: float[splits][n_cells][rp] with splits from
- *                fh_xg_bf16_splits (fixed-order reduction).
+ *                fh_xg_bf16_splits (fixed-order reduction in fp64).
+ * fold: K chunks of 64 (cells for fh_xe_bf16, band rows for fh_xg_bf16) summed in one tensor
+ *       memory accumulator before the epilogue folds them into Kahan-compensated fp32 running
+ *       sums; 0 selects the library default (8).  Short runs keep the fp32 rounding of long K
+ *       ranges out of the result.
  * status: int32 device word; a device-side wait that runs out sets FH_ERR_TIMEOUT. */
 int fh_split_bf16(const float* src, int64_t n_rows, int32_t rp, int64_t ld_src, uint16_t* dst,
                   void* stream);
 int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t planes,
-               int32_t n_cells, int64_t rows, const uint16_t* E2, int32_t rp, float* W,
-               int* status, void* stream);
+               int32_t n_cells, int64_t rows, const uint16_t* E2, int32_t rp, int32_t fold,
+               float* W, int* status, void* stream);
 int fh_xg_bf16_splits(int32_t n_cells, int64_t rows);
 int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t planes,
                int32_t n_cells, int64_t rows, const uint16_t* G2, int32_t rp, int32_t splits,
-               float* partial, float* out, int* status, void* stream);
+               int32_t fold, float* partial, float* out, int* status, void* stream);
 
 /* Y[g][l][m] = sum_j U_g[j][l] W[xoff + i*width + j][m] for every bin row g (K16 tail,
  * parafac2_intergrative.py:522-529); Y: float[n_rows][ldy_l][rp]; row_tile: int32[n_rows];

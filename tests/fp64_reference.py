@@ -1,32 +1,106 @@
 """FP64 restatement of the fit on a torch device (TEST INFRASTRUCTURE: the precision yardstick).
 
-The algorithm of ``oracle.fh_oracle.ALSOracle`` (which restates the reference step by step and
-cites it: fasthigashi/partial_rwr.py:75-138, project2orthogonal.py:6-34,
-parafac2_intergrative.py:304-737, parafac_integrative.py:12-112), with every array a torch
+The fit loop of the reference (fasthigashi/partial_rwr.py:75-138, project2orthogonal.py:6-34,
+parafac2_intergrative.py:304-737, parafac_integrative.py:12-112) with every array a torch
 float64 tensor, so a full-size fit (10,000 cells at 500 kb) runs on a GPU in minutes instead of
-hours on host cores.  Cells are not split into batches: in exact arithmetic the reference's
-cell batching only changes summation order.  ``tests/test_precision.py`` pins this module
-against the numpy oracle before using it to state the FP64 error of the fp32 and bf16 forms.
+hours on host cores.  It is exact-arithmetic equal to the reference; the rounding it leaves is
+fp64's.  Three choices make it fast, none of which changes the exact result:
+  * cells are not split into batches (the reference's cell batching only orders sums);
+  * each iteration makes two passes over the RWR output X per bin batch instead of three:
+    W = X^T E gives temp_i = W_i M_i (M_i = D diag(A_i) B^T, the reference's lhs contracted
+    with E) and, with the new E, the projected tensor Y_i = U_i^T W_i; S^T = X G^T with
+    G_i = U_i M_i^T gives SVD_term (the reference's lhs2 @ U^T X);
+  * the per-bin polar factors are batched on the device: Householder QR of temp_i, then the
+    polar factor of the r x r triangle by Newton's iteration with Higham's scaling (a matrix
+    that does not converge falls back to a host SVD); the sum of singular values is
+    trace(U^T temp).
+It does not import the oracle (so benchmark code may use it as a checker); tests/
+test_precision.py pins it against the numpy oracle (oracle/fh_oracle.py) first.
 """
 from __future__ import annotations
 
 import math
+from dataclasses import dataclass
 
 import numpy as np
 import torch
 
-from oracle import fh_oracle as O
-
 F64 = torch.float64
 
 
+@dataclass
+class BinBatch:
+    start: int
+    rows: int
+    local: slice      # the batch's rows inside its compact columns
+    col: slice        # compact columns in chromosome bins
+    width: int
+    shift: int        # first compact column
+
+
+def tile_layout(num_bin, bs_bin, flank):
+    """Bin batches of a chromosome in the compact layout (sparse_for_schic.py:401-492): rows
+    [i, i + b), columns from i - flank (clipped at 0) to i + b + flank (clipped at num_bin)."""
+    out = []
+    for i in range(0, num_bin, bs_bin):
+        b = min(bs_bin, num_bin - i)
+        right = flank if num_bin - i - b - flank > 0 else num_bin - i - b
+        if i > flank:
+            out.append(BinBatch(i, b, slice(flank, flank + b), slice(i - flank, i + b + right),
+                                b + flank + right, i - flank))
+        else:
+            out.append(BinBatch(i, b, slice(i, i + b), slice(0, i + b + right), i + b + right, 0))
+    return out
+
+
+@dataclass
+class ChromRecord:
+    """One chromosome's COO (row, col, cell) and its batching."""
+    name: str
+    indices: np.ndarray
+    values: np.ndarray
+    num_bin: int
+    num_cell: int
+    bs_bin: int
+    bs_cell: int
+    flank: int
+
+    def layout(self):
+        return tile_layout(self.num_bin, self.bs_bin, self.flank)
+
+
 def polar(m):
-    """U Vh of the thin SVD and S (project2orthogonal.py:6-34), batched over leading dims.
-    Batches of small matrices go through LAPACK on the host (a loop of per-matrix device
-    SVD calls is far slower for them); single large matrices stay on the device."""
-    if m.dim() == 3:
-        U, S, Vh = np.linalg.svd(m.detach().cpu().numpy(), full_matrices=False)
-        return torch.from_numpy(U @ Vh).to(m.device), torch.from_numpy(S).to(m.device)
+    """The polar factor U (U Vh of the thin SVD, project2orthogonal.py:6-34) of every matrix of
+    a (batch, n, r) float64 stack with n >= r, and the sum of all their singular values."""
+    Q, Rt = torch.linalg.qr(m)
+    r = Rt.shape[-1]
+    X = Rt.clone()
+    eye = torch.eye(r, dtype=F64, device=m.device)
+    for _ in range(40):
+        Xi = torch.linalg.inv(X)
+        nx = torch.linalg.norm(X, dim=(1, 2))
+        ni = torch.linalg.norm(Xi, dim=(1, 2))
+        z = torch.sqrt(ni / nx)[:, None, None]
+        Xn = 0.5 * (z * X + Xi.transpose(1, 2) / z)
+        d = torch.linalg.norm(Xn - X, dim=(1, 2)) / torch.linalg.norm(Xn, dim=(1, 2))
+        X = Xn
+        if bool((d < 1e-14).all()):
+            break
+    ortho = torch.linalg.norm(X.transpose(1, 2) @ X - eye, dim=(1, 2))
+    bad = ~torch.isfinite(ortho) | (ortho > 1e-10)
+    if bool(bad.any()):
+        idx = torch.nonzero(bad).flatten()
+        Uh, _, Vh = np.linalg.svd(m[idx].cpu().numpy(), full_matrices=False)
+        Up = torch.from_numpy(Uh @ Vh).to(m.device)
+    U = Q @ X
+    if bool(bad.any()):
+        U[idx] = Up
+    ssum = float((U * m).sum())
+    return U, ssum
+
+
+def polar_single(m):
+    """Polar factor and singular values of one (C, R) matrix (the meta polar, :483-486)."""
     U, S, Vh = torch.linalg.svd(m, full_matrices=False)
     return U @ Vh, S
 
@@ -139,6 +213,7 @@ class FP64Fit:
         self.norm_tensor = np.sqrt(self.tnorm)
         self.norm_all = float(np.linalg.norm(self.norm_tensor))
         self.core = self._core_norm()
+        self.W = {}           # X^T E per bin batch for the current E (the next iteration's temp)
         self.rec_errors_total = []
 
     def _core_norm(self):
@@ -153,31 +228,33 @@ class FP64Fit:
     def iterate(self, n_iter_parafac):
         E = self.E
         R = self.rank
-        SVD = torch.zeros((E.shape[1], self.C), dtype=F64, device=self.dev)
+        SVD = torch.zeros((self.C, E.shape[1]), dtype=F64, device=self.dev)    # SVD_term^T
         err_u = np.zeros(len(self.datas))
         U_all = {}
         for ci, d in enumerate(self.datas):
             A, B, D = self.A[ci], self.B[d.name], self.D[d.name]
-            Cm = E @ D
             for bi, bb in enumerate(d.layout()):
                 rs = slice(bb.start, bb.start + bb.rows)
-                X = self.X[(ci, bi)]                                    # (C, b, n)
-                lhs = torch.einsum("ir,jr,kr->ikj", A[rs], B, Cm)         # (b, C, r)
-                temp = torch.bmm(X.permute(1, 2, 0), lhs)                # (b, n, r)
-                U, S = polar(temp)
+                X = self.X[(ci, bi)].reshape(self.C, -1)                   # (C, b n)
+                W = self.W.get((ci, bi))
+                if W is None:
+                    W = (X.T @ E).reshape(bb.rows, bb.width, -1)           # (b, n, R)
+                M = torch.einsum("mr,ir,jr->imj", D, A[rs], B)             # (b, R, r)
+                temp = torch.bmm(W, M)                                     # (b, n, r)
+                U, ssum = polar(temp)
                 U_all[(ci, bi)] = U
-                err_u[ci] += float(S.sum())
-                lhs2 = torch.einsum("ir,jr,kr->kij", A[rs], B, D).reshape(D.shape[0], -1)
-                proj = torch.bmm(U.transpose(1, 2), X.permute(1, 2, 0))  # (b, r, C)
-                SVD += lhs2 @ proj.reshape(-1, self.C)
-        E_new, _ = polar(SVD.T)
-        err_v = float((E_new * SVD.T).sum())
+                err_u[ci] += ssum
+                Gt = torch.bmm(U, M.transpose(1, 2)).reshape(-1, E.shape[1])   # (b n, R)
+                SVD += X @ Gt
+        E_new, _ = polar_single(SVD)
+        err_v = float((E_new * SVD).sum())
         for ci, d in enumerate(self.datas):
             Yc = torch.zeros((d.num_bin, self.size[d.name], R), dtype=F64, device=self.dev)
             for bi, bb in enumerate(d.layout()):
-                X = self.X[(ci, bi)]
-                XE = torch.einsum("kij,km->ijm", X, E_new)               # (b, n, R)
-                Yc[bb.start:bb.start + bb.rows] = torch.bmm(U_all[(ci, bi)].transpose(1, 2), XE)
+                X = self.X[(ci, bi)].reshape(self.C, -1)
+                W = (X.T @ E_new).reshape(bb.rows, bb.width, -1)          # (b, n, R)
+                self.W[(ci, bi)] = W
+                Yc[bb.start:bb.start + bb.rows] = torch.bmm(U_all[(ci, bi)].transpose(1, 2), W)
             r = self.size[d.name]
             f = parafac(Yc, r, n_iter_parafac, [self.A[ci], self.B[d.name], self.D[d.name]])
             self.A[ci], self.B[d.name], self.D[d.name] = f
@@ -195,10 +272,10 @@ class FP64Fit:
 
 
 def chrom_datas(coo, names, bs_bins, bs_cells, flank):
-    """ChromData records of the oracle from COO triples (indices, values, shape)."""
+    """ChromRecords from COO triples (indices, values, shape)."""
     out = []
     for (idx, val, shape), name, bsb, bsc in zip(coo, names, bs_bins, bs_cells):
-        out.append(O.ChromData(name, idx, val, int(shape[0]), int(shape[2]), int(bsb), int(bsc),
+        out.append(ChromRecord(name, idx, val, int(shape[0]), int(shape[2]), int(bsb), int(bsc),
                                int(flank)))
     return out
 
@@ -229,4 +306,5 @@ def aligned_error(E, E_ref):
     """Relative Frobenius error of E after the orthogonal Procrustes rotation onto E_ref."""
     E = np.asarray(E, dtype=np.float64)
     E_ref = np.asarray(E_ref, dtype=np.float64)
-    return O.rel_err(O.procrustes_align(E, E_ref), E_ref)
+    U, _, Vh = np.linalg.svd(E.T @ E_ref)
+    return float(np.linalg.norm(E @ (U @ Vh) - E_ref) / max(np.linalg.norm(E_ref), 1e-300))

@@ -210,22 +210,31 @@ def test_ctypes_signatures_match_the_header():
 
 
 def test_bench_reference_arm_prints_the_contract_line():
-    """bench.py --impl reference (the oracle port on host cores) prints one JSON line with the
-    keys the benchmark contract names, on the smallest workload."""
+    """bench.py --impl reference (the reference's own fit on host cores, from its install under
+    baseline/_ref) prints one JSON line with the keys the benchmark contract names, on the
+    smallest workload; without the install it prints its unavailable line."""
     import json
     import subprocess
     import sys
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                        "--config", "c1", "--steps", "1", "--warmup", "1"],
+                        "--config", "c1", "--steps", "1", "--warmup", "1", "--sample-cells", "40"],
                        capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    if not os.path.isdir(os.path.join(ROOT, "baseline", "_ref", "fasthigashi")):
+        assert "unavailable" in line
+        return
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
               "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "impl",
               "cpu_baseline", "e2e"):
         assert k in line, k
-    assert line["impl"] == "reference" and line["value"] > 0
-    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["value"] > 0
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "reference" and cb["cores"] >= 1 and cb["extrapolated"] is True
+    assert cb["sample_cells"] == 40 and len(cb["measured_s"]) == 1
+    # ms_per_step is the measured step, so steps x ms_per_step is the timed region
+    assert abs(line["ms_per_step"] - 1000 * cb["measured_s"][0]) < 1.0
     assert line["e2e"]["value"] == line["value"]
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
 

@@ -73,7 +73,7 @@ def test_xe_bf16(rp, ct, c, rows, planes):
     E2 = split(E)
     W = torch.full((rows, rp), float("nan"), device=CUDA)
     st = torch.zeros(1, dtype=torch.int32, device=CUDA)
-    _lib.call("fh_xe_bf16", P(X16), ldx, ct, planes, c, rows, P(E2), rp, P(W), P(st), sp())
+    _lib.call("fh_xe_bf16", P(X16), ldx, ct, planes, c, rows, P(E2), rp, 0, P(W), P(st), sp())
     torch.cuda.synchronize()
     assert int(st.item()) == 0
     ref = Xv[:c, :rows].T @ E.double()
@@ -92,7 +92,7 @@ def test_xg_bf16(rp, ct, n, rows, planes):
     partial = torch.empty((splits, n, rp), device=CUDA)
     out = torch.full((n, rp), float("nan"), device=CUDA)
     st = torch.zeros(1, dtype=torch.int32, device=CUDA)
-    _lib.call("fh_xg_bf16", P(X16), ldx, ct, planes, n, rows, P(G2), rp, splits, P(partial),
+    _lib.call("fh_xg_bf16", P(X16), ldx, ct, planes, n, rows, P(G2), rp, splits, 0, P(partial),
               P(out), P(st), sp())
     torch.cuda.synchronize()
     assert int(st.item()) == 0
@@ -110,7 +110,7 @@ def test_xpass_bf16_deterministic():
     st = torch.zeros(1, dtype=torch.int32, device=CUDA)
     for _ in range(2):
         out = torch.empty((1000, 64), device=CUDA)
-        _lib.call("fh_xg_bf16", P(X16), ldx, 1000, 2, 1000, 30000, P(G2), 64, splits,
+        _lib.call("fh_xg_bf16", P(X16), ldx, 1000, 2, 1000, 30000, P(G2), 64, splits, 0,
                   P(partial), P(out), P(st), sp())
         outs.append(out)
     torch.cuda.synchronize()

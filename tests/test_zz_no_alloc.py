@@ -4,6 +4,10 @@ fh_exclusive_scan_noalloc serves callers that cannot allocate device memory them
 takes only the input and output buffers and keeps its scratch in a fixed array inside the
 library.  This file is collected last so that a run stopping at its first failure has
 already run every other test; it also passes on its own in a fresh process.
+
+Sizes: the scan works in blocks of 2,048 counts; the block totals are scanned in chunks of
+1,024, so n > 2,097,152 runs the multi-chunk path, and n = 8,191 x 2,048 (the largest size the
+library's scratch array holds) writes its last entry.
 """
 import numpy as np
 import pytest
@@ -34,16 +38,28 @@ def scan_noalloc(counts):
     return out
 
 
+def check(counts):
+    ref = scan_with_workspace(counts)
+    got = scan_noalloc(counts)
+    torch.cuda.synchronize()
+    assert torch.equal(got, ref)           # integer work: bit-exact
+    expect = np.concatenate([[0], np.cumsum(counts.cpu().numpy().astype(np.int64))])
+    assert np.array_equal(got.cpu().numpy(), expect)
+
+
 def test_noalloc_scan_matches_workspace_scan_twice():
     g = torch.Generator(device="cpu").manual_seed(7)
     for n in (2_000_003, 68_000):              # two calls in a row, the larger first
-        counts = torch.randint(0, 5000, (n,), generator=g, dtype=torch.int32).cuda()
-        ref = scan_with_workspace(counts)
-        got = scan_noalloc(counts)
-        torch.cuda.synchronize()
-        assert torch.equal(got, ref)           # integer work: bit-exact
-        expect = np.concatenate([[0], np.cumsum(counts.cpu().numpy().astype(np.int64))])
-        assert np.array_equal(got.cpu().numpy(), expect)
+        check(torch.randint(0, 5000, (n,), generator=g, dtype=torch.int32).cuda())
+
+
+def test_noalloc_scan_multi_chunk_and_largest_size():
+    """Past 1,024 blocks (the block totals' multi-chunk scan) and at the largest size, where
+    the last scratch entry is written; each call follows a larger one, so stale scratch from
+    the call before would show."""
+    g = torch.Generator(device="cpu").manual_seed(11)
+    for n in (MAX_N, 2_097_153, 5_000_000 + 77):
+        check(torch.randint(0, 200, (n,), generator=g, dtype=torch.int32).cuda())
 
 
 def test_noalloc_scan_rejects_sizes_beyond_its_scratch():
