@@ -11,7 +11,7 @@ namespace fh {
 
 constexpr int kJacThreads = 512;
 constexpr int kJacWarps = kJacThreads / 32;
-constexpr int kJacMaxSweeps = 12;
+constexpr int kJacMaxSweeps = 24;
 constexpr float kJacTol = 1e-6f;   // rotate a pair while |<t_p, t_q>| > tol ||t_p|| ||t_q||
 
 __host__ __device__ inline int jac_ldn(int n) { return n | 1; }   // odd column stride

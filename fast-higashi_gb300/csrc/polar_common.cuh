@@ -144,6 +144,131 @@ __device__ inline void householder_qr(float* T, int n, int r, int ldt, PolarScra
   householder_panel(T, n, 0, r, ldt, s);
 }
 
+// ---- Householder QR with warp-owned columns held in registers --------------------------
+// The same factorization and output layout as householder_qr, organised so that each step
+// costs one hardware barrier instead of three CTA-wide ones: warp w owns columns
+// j = w + NW c (c < NC) and keeps them in registers, lane l holding rows l + 32 t (t < NT).
+// Step k: the owner of column k (whose column has had reflectors 0..k-1 applied) forms
+// reflector k from its registers (norm by a warp reduction), writes v_k below the diagonal of
+// T, vh[k], beta[k] and R[k][k] = alpha, and signals with bar.arrive on named barrier
+// 1 + (k & 1); every other warp waits there with bar.sync.  Then each warp applies reflector
+// k to its own columns j > k (warp-reduced dot products, no further synchronisation).  A warp
+// reaches step k + 2's barrier (the same id) only after every warp passed step k + 1's, so two
+// ids suffice.  At the end the warps store R's strict upper triangle.  Every warp executes
+// exactly one barrier operation per step, for every step, whatever the data (a zero column
+// gives beta = 0 and the step still synchronises).
+template <int ID>
+__device__ __forceinline__ void named_bar_sync(int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"n"(ID), "r"(nthreads) : "memory");
+}
+template <int ID>
+__device__ __forceinline__ void named_bar_arrive(int nthreads) {
+  asm volatile("bar.arrive %0, %1;" ::"n"(ID), "r"(nthreads) : "memory");
+}
+
+template <int NC, int NT>
+__device__ inline void householder_qr_cols(float* T, int n, int r, int ldt, PolarScratch& s) {
+  const int tx = pc_lane(), w = pc_warp(), nw = pc_nwarps();
+  const int nthreads = (int)blockDim.x;
+  float a[NC][NT];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const int j = w + nw * c;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int i = tx + 32 * t;
+      a[c][t] = (j < r && i < n) ? T[i * ldt + j] : 0.f;
+    }
+  }
+  __syncthreads();   // every warp has its columns before any column of T is overwritten
+  for (int k = 0; k < r; ++k) {
+    if (k % nw == w) {
+      const int kc = k / nw;        // the local column holding column k
+      float ss = 0.f, x0 = 0.f;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        if (c == kc) {
+#pragma unroll
+          for (int t = 0; t < NT; ++t) {
+            const int i = tx + 32 * t;
+            if (i > k && i < n) {
+              ss = fmaf(a[c][t], a[c][t], ss);
+              T[i * ldt + k] = a[c][t];            // v_k below the diagonal
+            }
+            if (i == k) x0 = a[c][t];
+          }
+        }
+      }
+      ss = warp_sum(ss);
+      x0 = __shfl_sync(0xffffffffu, x0, k & 31);
+      if (tx == 0) {
+        const float s2 = fmaf(x0, x0, ss);
+        if (s2 == 0.f) {
+          s.beta[k] = 0.f;
+          s.vh[k] = 0.f;
+          T[k * ldt + k] = 0.f;
+        } else {
+          const float nrm = sqrtf(s2);
+          const float alpha = x0 >= 0.f ? -nrm : nrm;
+          s.vh[k] = x0 - alpha;
+          s.beta[k] = 1.f / (s2 - x0 * alpha);
+          T[k * ldt + k] = alpha;
+        }
+      }
+      __threadfence_block();
+      if (k & 1) named_bar_arrive<2>(nthreads);
+      else named_bar_arrive<1>(nthreads);
+      __syncwarp();                 // lane 0's vh / beta visible to the owner's other lanes
+    } else {
+      if (k & 1) named_bar_sync<2>(nthreads);
+      else named_bar_sync<1>(nthreads);
+    }
+    const float beta = s.beta[k];
+    if (beta == 0.f) continue;      // uniform: every warp read the same value
+    const float vh = s.vh[k];
+    float v[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int i = tx + 32 * t;
+      v[t] = (i > k && i < n) ? T[i * ldt + k] : (i == k ? vh : 0.f);
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const int j = w + nw * c;
+      if (j > k && j < r) {
+        float d = 0.f;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) d = fmaf(v[t], a[c][t], d);
+        d = -beta * warp_sum(d);
+#pragma unroll
+        for (int t = 0; t < NT; ++t) a[c][t] = fmaf(d, v[t], a[c][t]);
+      }
+    }
+  }
+  // R's strict upper triangle (rows i < j of column j); the diagonal and the reflectors are
+  // in T already
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const int j = w + nw * c;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int i = tx + 32 * t;
+      if (j < r && i < j) T[i * ldt + j] = a[c][t];
+    }
+  }
+  __syncthreads();
+}
+
+// Dispatch on the row count: NT = 4, 6 or 8 rows per lane (n <= 256); wider tiles take the
+// CTA-wide householder_qr.
+template <int NC>
+__device__ inline void householder_qr_fast(float* T, int n, int r, int ldt, PolarScratch& s) {
+  if (n <= 128) householder_qr_cols<NC, 4>(T, n, r, ldt, s);
+  else if (n <= 192) householder_qr_cols<NC, 6>(T, n, r, ldt, s);
+  else if (n <= 256) householder_qr_cols<NC, 8>(T, n, r, ldt, s);
+  else householder_qr(T, n, r, ldt, s);
+}
+
 // ---- U = Q U: apply the stored reflectors in reverse to U (n x r, stride ldu) ----------
 // The dot products v^T U[:, j] go four columns per warp (independent chains, one pass over v);
 // each column's sum runs in the same order as one column at a time.

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kProcThreads, 2) procrustes_qr_kernel(ProcArgs
     __syncthreads();
   }
   // ---- QR, polar factor of R, sum(S)
-  householder_qr(R0, n, r, ldt, s);
+  householder_qr_fast<(RP + 15) / 16>(R0, n, r, ldt, s);
   // polar(R) on 16-byte aligned rows of stride ldv (4 x 4 register-tiled products), then
   // back to stride ldt in region 1 for the Q apply
   const int ldv = ((r + 3) & ~3) + 4;
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kProcThreads, 1) procrustes_qr_big_kernel(Proc
     }
     __syncthreads();
   }
-  householder_qr(RA, n, r, ldt, s);
+  householder_qr_fast<8>(RA, n, r, ldt, s);
   // park R and the reflectors; the iterate X = R (upper) at stride ldv in RB, scratch in RA
   for (int i = ty; i < n; i += nw)
     for (int l = tx; l < r; l += 32) Ug[(int64_t)i * r + l] = RA[i * ldt + l];
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(kProcThreads) polar_qr_kernel(const float* __r
   for (int i = ty; i < n; i += nw)
     for (int l = tx; l < r; l += 32) Tm[i * ldt + l] = Mb[(int64_t)i * r + l];
   __syncthreads();
-  householder_qr(Tm, n, r, ldt, s);
+  householder_qr_fast<8>(Tm, n, r, ldt, s);
   float* X = reg;
   for (int p = ty; p < r; p += nw)
     for (int q = tx; q < r; q += 32) X[p * ldt + q] = q >= p ? Tm[p * ldt + q] : 0.f;
