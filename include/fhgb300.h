@@ -376,6 +376,13 @@ int fh_core_norm(int32_t nchrom, int32_t nchunks, const int32_t* meta, float* A,
                  double* core, void* workspace, size_t workspace_bytes, int* status,
                  void* stream);
 
+/* ---- self-test of the bounded device-side waits (no reference counterpart: the reference
+ * has no device code).  One warp allocates tensor memory, waits on an mbarrier that nothing
+ * arrives on until limit_ns of device time pass, sets *status = FH_ERR_TIMEOUT, frees the
+ * tensor memory and returns: the path every tcgen05 kernel here takes when a wait runs out.
+ * limit_ns in (0, 1e9]; status: int32 device word (cleared by the caller). */
+int fh_selftest_wait(int* status, int64_t limit_ns, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
