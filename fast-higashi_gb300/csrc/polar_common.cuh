@@ -152,11 +152,14 @@ __device__ inline void householder_qr(float* T, int n, int r, int ldt, PolarScra
 // reflector k from its registers (norm by a warp reduction), writes v_k below the diagonal of
 // T, vh[k], beta[k] and R[k][k] = alpha, and signals with bar.arrive on named barrier
 // 1 + (k & 1); every other warp waits there with bar.sync.  Then each warp applies reflector
-// k to its own columns j > k (warp-reduced dot products, no further synchronisation).  A warp
+// k to its own columns j > k (warp-reduced dot products, no further synchronisation); the
+// owner of column k + 1 does that column first and forms reflector k + 1 at once (look-ahead),
+// so the chain from one barrier to the next is one column update and one norm.  A warp
 // reaches step k + 2's barrier (the same id) only after every warp passed step k + 1's, so two
-// ids suffice.  At the end the warps store R's strict upper triangle.  Every warp executes
-// exactly one barrier operation per step, for every step, whatever the data (a zero column
-// gives beta = 0 and the step still synchronises).
+// ids suffice (the owner of k + 1 arrives after its own wait at step k).  At the end the warps
+// store R's strict upper triangle.  Every warp executes exactly one barrier operation per step,
+// for every step, whatever the data (a zero column gives beta = 0 and the step still
+// synchronises).
 template <int ID>
 __device__ __forceinline__ void named_bar_sync(int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"n"(ID), "r"(nthreads) : "memory");
@@ -181,67 +184,87 @@ __device__ inline void householder_qr_cols(float* T, int n, int r, int ldt, Pola
     }
   }
   __syncthreads();   // every warp has its columns before any column of T is overwritten
-  for (int k = 0; k < r; ++k) {
-    if (k % nw == w) {
-      const int kc = k / nw;        // the local column holding column k
-      float ss = 0.f, x0 = 0.f;
+  // The owner of column k forms reflector k from its registers and arrives on k's barrier.
+  auto form = [&](int k) {
+    const int kc = k / nw;
+    float ss = 0.f, x0 = 0.f;
 #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        if (c == kc) {
+    for (int c = 0; c < NC; ++c) {
+      if (c == kc) {
 #pragma unroll
-          for (int t = 0; t < NT; ++t) {
-            const int i = tx + 32 * t;
-            if (i > k && i < n) {
-              ss = fmaf(a[c][t], a[c][t], ss);
-              T[i * ldt + k] = a[c][t];            // v_k below the diagonal
-            }
-            if (i == k) x0 = a[c][t];
+        for (int t = 0; t < NT; ++t) {
+          const int i = tx + 32 * t;
+          if (i > k && i < n) {
+            ss = fmaf(a[c][t], a[c][t], ss);
+            T[i * ldt + k] = a[c][t];              // v_k below the diagonal
           }
+          if (i == k) x0 = a[c][t];
         }
       }
-      ss = warp_sum(ss);
-      x0 = __shfl_sync(0xffffffffu, x0, k & 31);
-      if (tx == 0) {
-        const float s2 = fmaf(x0, x0, ss);
-        if (s2 == 0.f) {
-          s.beta[k] = 0.f;
-          s.vh[k] = 0.f;
-          T[k * ldt + k] = 0.f;
-        } else {
-          const float nrm = sqrtf(s2);
-          const float alpha = x0 >= 0.f ? -nrm : nrm;
-          s.vh[k] = x0 - alpha;
-          s.beta[k] = 1.f / (s2 - x0 * alpha);
-          T[k * ldt + k] = alpha;
-        }
+    }
+    ss = warp_sum(ss);
+    x0 = __shfl_sync(0xffffffffu, x0, k & 31);
+    if (tx == 0) {
+      const float s2 = fmaf(x0, x0, ss);
+      if (s2 == 0.f) {
+        s.beta[k] = 0.f;
+        s.vh[k] = 0.f;
+        T[k * ldt + k] = 0.f;
+      } else {
+        const float nrm = sqrtf(s2);
+        const float alpha = x0 >= 0.f ? -nrm : nrm;
+        s.vh[k] = x0 - alpha;
+        s.beta[k] = 1.f / (s2 - x0 * alpha);
+        T[k * ldt + k] = alpha;
       }
-      __threadfence_block();
-      if (k & 1) named_bar_arrive<2>(nthreads);
-      else named_bar_arrive<1>(nthreads);
-      __syncwarp();                 // lane 0's vh / beta visible to the owner's other lanes
-    } else {
+    }
+    __threadfence_block();
+    if (k & 1) named_bar_arrive<2>(nthreads);
+    else named_bar_arrive<1>(nthreads);
+    __syncwarp();                   // lane 0's vh / beta visible to the owner's other lanes
+  };
+  // Applies reflector k (v, -beta) to local column c.
+  auto update = [&](int c, float nbeta, const float (&v)[NT]) {
+#pragma unroll
+    for (int cc = 0; cc < NC; ++cc) {
+      if (cc == c) {
+        float d = 0.f;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) d = fmaf(v[t], a[cc][t], d);
+        d = nbeta * warp_sum(d);
+#pragma unroll
+        for (int t = 0; t < NT; ++t) a[cc][t] = fmaf(d, v[t], a[cc][t]);
+      }
+    }
+  };
+  if (w == 0 && r > 0) form(0);
+  for (int k = 0; k < r; ++k) {
+    if (k % nw != w) {              // the owner of k arrived when it formed the reflector
       if (k & 1) named_bar_sync<2>(nthreads);
       else named_bar_sync<1>(nthreads);
     }
     const float beta = s.beta[k];
-    if (beta == 0.f) continue;      // uniform: every warp read the same value
-    const float vh = s.vh[k];
     float v[NT];
+    if (beta != 0.f) {
+      const float vh = s.vh[k];
 #pragma unroll
-    for (int t = 0; t < NT; ++t) {
-      const int i = tx + 32 * t;
-      v[t] = (i > k && i < n) ? T[i * ldt + k] : (i == k ? vh : 0.f);
+      for (int t = 0; t < NT; ++t) {
+        const int i = tx + 32 * t;
+        v[t] = (i > k && i < n) ? T[i * ldt + k] : (i == k ? vh : 0.f);
+      }
     }
+    // look-ahead: the owner of column k + 1 updates it first and forms reflector k + 1 before
+    // its other columns, so the next step's barrier waits on one column update, not all
+    const bool ahead = k + 1 < r && (k + 1) % nw == w;
+    if (ahead) {
+      if (beta != 0.f) update((k + 1) / nw, -beta, v);
+      form(k + 1);
+    }
+    if (beta != 0.f) {
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      const int j = w + nw * c;
-      if (j > k && j < r) {
-        float d = 0.f;
-#pragma unroll
-        for (int t = 0; t < NT; ++t) d = fmaf(v[t], a[c][t], d);
-        d = -beta * warp_sum(d);
-#pragma unroll
-        for (int t = 0; t < NT; ++t) a[c][t] = fmaf(d, v[t], a[c][t]);
+      for (int c = 0; c < NC; ++c) {
+        const int j = w + nw * c;
+        if (j > k && j < r && !(ahead && j == k + 1)) update(c, -beta, v);
       }
     }
   }
@@ -300,6 +323,79 @@ __device__ inline void apply_q(const float* T, int ldt, float* U, int ldu, int n
       for (int j = tx; j < r; j += 32) U[i * ldu + j] = fmaf(bv, s.wv[j], U[i * ldu + j]);
     }
     __syncthreads();
+  }
+}
+
+// ---- U = Q U with warp-owned columns in registers (no barriers) ------------------------
+// The product of the reflectors stored by householder_qr / householder_qr_cols (v_k below the
+// diagonal of T, vh[k], beta[k]) applied in reverse to U (n x r, stride ldu; rows < r hold X on
+// entry, the rows below are taken as zero; all n rows of U on return).  Each warp owns columns
+// j = w + NW c and applies every reflector to them in registers, lane l holding rows l + 32 t:
+// a column's dot product with v_k is a warp reduction, so the warps never wait on one another.
+// The caller synchronises before (X and the reflectors complete) and this routine once after.
+template <int NC, int NT>
+__device__ inline void apply_q_cols(const float* T, int ldt, float* U, int ldu, int n, int r,
+                                    PolarScratch& s) {
+  const int tx = pc_lane(), w = pc_warp(), nw = pc_nwarps();
+  float u[NC][NT];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const int j = w + nw * c;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int i = tx + 32 * t;
+      u[c][t] = (j < r && i < r) ? U[i * ldu + j] : 0.f;
+    }
+  }
+  for (int k = r - 1; k >= 0; --k) {
+    const float beta = s.beta[k];
+    if (beta == 0.f) continue;      // uniform across the warp
+    const float vh = s.vh[k];
+    float v[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int i = tx + 32 * t;
+      v[t] = (i > k && i < n) ? T[i * ldt + k] : (i == k ? vh : 0.f);
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      float d = 0.f;
+#pragma unroll
+      for (int t = 0; t < NT; ++t) d = fmaf(v[t], u[c][t], d);
+      d = -beta * warp_sum(d);
+#pragma unroll
+      for (int t = 0; t < NT; ++t) u[c][t] = fmaf(d, v[t], u[c][t]);
+    }
+  }
+  __syncthreads();   // every warp has read its columns of X before any row of U is written
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const int j = w + nw * c;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int i = tx + 32 * t;
+      if (j < r && i < n) U[i * ldu + j] = u[c][t];
+    }
+  }
+  __syncthreads();
+}
+
+// Dispatch on the row count: NT = 4, 6 or 8 rows per lane (n <= 256); wider tiles zero U's
+// rows past r and take the CTA-wide apply_q.
+template <int NC>
+__device__ inline void apply_q_fast(const float* T, int ldt, float* U, int ldu, int n, int r,
+                                    PolarScratch& s) {
+  if (n <= 128) {
+    apply_q_cols<NC, 4>(T, ldt, U, ldu, n, r, s);
+  } else if (n <= 192) {
+    apply_q_cols<NC, 6>(T, ldt, U, ldu, n, r, s);
+  } else if (n <= 256) {
+    apply_q_cols<NC, 8>(T, ldt, U, ldu, n, r, s);
+  } else {
+    for (int j = r + pc_warp(); j < n; j += pc_nwarps())
+      for (int l = pc_lane(); l < r; l += 32) U[j * ldu + l] = 0.f;
+    __syncthreads();
+    apply_q(T, ldt, U, ldu, n, r, s);
   }
 }
 

@@ -180,14 +180,7 @@ __global__ void __launch_bounds__(kProcThreads, 2) procrustes_qr_kernel(ProcArgs
     if (tid == 0) a.ssum[g] = acc;
   }
   // ---- U = Q [P; 0]: U's first r rows are X (same storage and stride)
-  if (n <= 192) {
-    apply_q_ut(R0, ldt, R1, ldt, R1 + (size_t)r * ldt, n, r, s);
-  } else {
-    for (int j = r + ty; j < n; j += nw)
-      for (int l = tx; l < r; l += 32) R1[j * ldt + l] = 0.f;
-    __syncthreads();
-    apply_q(R0, ldt, R1, ldt, n, r, s);
-  }
+  apply_q_fast<(RP + 15) / 16>(R0, ldt, R1, ldt, n, r, s);
   float* Ug = a.U + T.uoff + (int64_t)i0 * n * r;
   for (int j = ty; j < n; j += nw)
     for (int l = tx; l < r; l += 32) Ug[(int64_t)j * r + l] = R1[j * ldt + l];
@@ -297,10 +290,8 @@ __global__ void __launch_bounds__(kProcThreads, 1) procrustes_qr_big_kernel(Proc
     if (tid == 0) a.ssum[g] = acc;
   }
   // ---- U = Q [P; 0]
-  for (int j = r + ty; j < n; j += nw)
-    for (int l = tx; l < r; l += 32) RB[j * ldt + l] = 0.f;
   __syncthreads();
-  apply_q(RA, ldt, RB, ldt, n, r, s);
+  apply_q_fast<8>(RA, ldt, RB, ldt, n, r, s);
   for (int j = ty; j < n; j += nw)
     for (int l = tx; l < r; l += 32) Ug[(int64_t)j * r + l] = RB[j * ldt + l];
   // ---- Gt = U M^T with the parked M
@@ -347,10 +338,8 @@ __global__ void __launch_bounds__(kProcThreads) polar_qr_kernel(const float* __r
     for (int q = p + tx; q < r; q += 32) acc += (double)X[p * ldt + q] * (double)Tm[p * ldt + q];
   acc = block_sum<double>(acc, dred);
   if (tid == 0 && ssum) ssum[b] = acc;
-  for (int j = r + ty; j < n; j += nw)
-    for (int l = tx; l < r; l += 32) reg[j * ldt + l] = 0.f;
   __syncthreads();
-  apply_q(Tm, ldt, reg, ldt, n, r, s);
+  apply_q_fast<8>(Tm, ldt, reg, ldt, n, r, s);
   float* Ub = U + b * (int64_t)n * r;
   for (int j = ty; j < n; j += nw)
     for (int l = tx; l < r; l += 32) Ub[(int64_t)j * r + l] = reg[j * ldt + l];
