@@ -152,14 +152,14 @@ __device__ inline void householder_qr(float* T, int n, int r, int ldt, PolarScra
 // reflector k from its registers (norm by a warp reduction), writes v_k below the diagonal of
 // T, vh[k], beta[k] and R[k][k] = alpha, and signals with bar.arrive on named barrier
 // 1 + (k & 1); every other warp waits there with bar.sync.  Then each warp applies reflector
-// k to its own columns j > k (warp-reduced dot products, no further synchronisation); the
-// owner of column k + 1 does that column first and forms reflector k + 1 at once (look-ahead),
-// so the chain from one barrier to the next is one column update and one norm.  A warp
+// k to its own columns j > k (warp-reduced dot products, no further synchronisation).  A warp
 // reaches step k + 2's barrier (the same id) only after every warp passed step k + 1's, so two
-// ids suffice (the owner of k + 1 arrives after its own wait at step k).  At the end the warps
-// store R's strict upper triangle.  Every warp executes exactly one barrier operation per step,
-// for every step, whatever the data (a zero column gives beta = 0 and the step still
-// synchronises).
+// ids suffice.  At the end the warps store R's strict upper triangle.  Every warp executes
+// exactly one barrier operation per step, for every step, whatever the data (a zero column
+// gives beta = 0 and the step still synchronises).  (A look-ahead variant, the owner of column
+// k + 1 forming its reflector before updating its other columns, measured 1 % slower: the
+// kernel is issue-bound with two CTAs per SM, and the extra selects cost more than the
+// shortened chain gains.)
 template <int ID>
 __device__ __forceinline__ void named_bar_sync(int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"n"(ID), "r"(nthreads) : "memory");
@@ -237,35 +237,26 @@ __device__ inline void householder_qr_cols(float* T, int n, int r, int ldt, Pola
       }
     }
   };
-  if (w == 0 && r > 0) form(0);
   for (int k = 0; k < r; ++k) {
-    if (k % nw != w) {              // the owner of k arrived when it formed the reflector
+    if (k % nw == w) {
+      form(k);
+    } else {
       if (k & 1) named_bar_sync<2>(nthreads);
       else named_bar_sync<1>(nthreads);
     }
     const float beta = s.beta[k];
+    if (beta == 0.f) continue;      // uniform: every warp read the same value
     float v[NT];
-    if (beta != 0.f) {
-      const float vh = s.vh[k];
+    const float vh = s.vh[k];
 #pragma unroll
-      for (int t = 0; t < NT; ++t) {
-        const int i = tx + 32 * t;
-        v[t] = (i > k && i < n) ? T[i * ldt + k] : (i == k ? vh : 0.f);
-      }
+    for (int t = 0; t < NT; ++t) {
+      const int i = tx + 32 * t;
+      v[t] = (i > k && i < n) ? T[i * ldt + k] : (i == k ? vh : 0.f);
     }
-    // look-ahead: the owner of column k + 1 updates it first and forms reflector k + 1 before
-    // its other columns, so the next step's barrier waits on one column update, not all
-    const bool ahead = k + 1 < r && (k + 1) % nw == w;
-    if (ahead) {
-      if (beta != 0.f) update((k + 1) / nw, -beta, v);
-      form(k + 1);
-    }
-    if (beta != 0.f) {
 #pragma unroll
-      for (int c = 0; c < NC; ++c) {
-        const int j = w + nw * c;
-        if (j > k && j < r && !(ahead && j == k + 1)) update(c, -beta, v);
-      }
+    for (int c = 0; c < NC; ++c) {
+      const int j = w + nw * c;
+      if (j > k && j < r) update(c, -beta, v);
     }
   }
   // R's strict upper triangle (rows i < j of column j); the diagonal and the reflectors are
