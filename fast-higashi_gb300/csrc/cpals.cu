@@ -8,11 +8,12 @@
 //     A <- MTTKRP_A (B^T B * D^T D + 1e-10 I)^{-1}   (and likewise for B, D)
 //     MTTKRP_A[i] = sum_j B[j] * (Y_i D)[j],   MTTKRP_B = sum_i A_i (x) (Y_i D),
 //     MTTKRP_D   = sum_i A_i (x) (Y_i^T B)      ((x): column-wise product).
-// The r x r systems (symmetric positive definite) are inverted in fp32, the reference's own
-// precision (parafac_integrative.py:12-15 solves in fp32), by Gauss-Jordan without pivoting
-// once per chromosome, so every right-hand side is a register-tiled product instead of a
-// serial substitution: this GB300 runs fp64 at ~0.33 TFLOP/s, so fp64 is kept to the scalar
-// sums (loss, core norm).  The reconstruction loss needs no Xhat:
+// The r x r systems (symmetric positive definite) are formed and inverted in fp64 by
+// Gauss-Jordan without pivoting (the sweep operator) once per chromosome, and the B and D
+// right-hand sides are multiplied by the fp64 inverse with fp64 sums, so every solve is a
+// register-tiled product instead of a serial substitution; the A rows (many small solves in
+// cp_rows_kernel) use the fp64 inverse rounded to fp32.  The reference solves in fp32
+// (parafac_integrative.py:12-15).  Scalar sums (loss, core norm) are fp64 too.  The reconstruction loss needs no Xhat:
 // ||Xhat||^2 = sum(A^TA * B^TB * D^TD) and <Xhat, Y> = sum(D * MTTKRP_D) with the final
 // A, B.  balance_norm (unit columns, the product of the column norms folded into D) follows
 // each sweep unless the relative loss change fell below 1e-5, as the reference breaks before
@@ -373,66 +374,6 @@ __global__ void __launch_bounds__(4 * MR) cp_rows_kernel(CpArgs a, int mode) {
   }
 }
 
-// Gi = G^{-1} for an SPD G (r x r, stride lg) by in-place Gauss-Jordan without pivoting (the
-// sweep operator; the pivots of an SPD matrix are positive).  Two barriers per pivot, against
-// three per column for the Cholesky factor plus a serial triangular inverse.  scratch:
-// 2 * MR floats.  Returns false on a pivot that is not positive (in every thread).
-template <int MR>
-__device__ bool cp_spd_inverse(const float* G, int r, int lg, float* scratch, float* Gi) {
-  constexpr int NW = CpShape<MR>::NW;
-  __shared__ int bad;
-  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
-  float* prow = scratch;
-  float* pcol = scratch + MR;
-  if (tid == 0) bad = 0;
-  for (int p = ty; p < r; p += NW)
-    for (int q = tx; q < r; q += 32) Gi[p * lg + q] = G[p * lg + q];
-  __syncthreads();
-  for (int k = 0; k < r; ++k) {
-    if (tid < r) {
-      prow[tid] = Gi[k * lg + tid];
-      pcol[tid] = Gi[tid * lg + k];
-    }
-    __syncthreads();
-    float d = prow[k];
-    if (!(d > 0.f)) {
-      d = 1e-30f;
-      if (tid == 0) bad = 1;
-    }
-    const float inv = 1.f / d;
-    for (int p = ty; p < r; p += NW) {
-      const float cp = pcol[p] * inv;
-      for (int q = tx; q < r; q += 32) {
-        float v;
-        if (p == k) v = (q == k) ? inv : prow[q] * inv;
-        else if (q == k) v = -cp;
-        else v = fmaf(-cp, prow[q], Gi[p * lg + q]);
-        Gi[p * lg + q] = v;
-      }
-    }
-    __syncthreads();
-  }
-  return bad == 0;
-}
-
-// out rows = RHS rows G^{-1} (RHS: nrhs x r, stride ldr, nrhs <= MR; Gi symmetric, stride lg).
-template <int MR>
-__device__ void cp_apply_inverse(const float* RHS, int ldr, int nrhs, const float* Gi, int r,
-                                 int lg, float* out, int ldo) {
-  constexpr int NW = CpShape<MR>::NW, TN = CpShape<MR>::TN;
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  float acc[8][TN];
-  cp_mm<MR>(nrhs, r, r, [&](int row, int p) { return RHS[(size_t)row * ldr + p]; },
-            [&](int p, int q) { return Gi[p * lg + q]; }, acc);
-#pragma unroll
-  for (int u = 0; u < 8; ++u)
-#pragma unroll
-    for (int v = 0; v < TN; ++v) {
-      const int row = w + NW * u, q = l + 32 * v;
-      if (row < nrhs && q < r) out[(size_t)row * ldo + q] = acc[u][v];
-    }
-}
-
 // Gram F^T F of an (nrows x r, stride ld) factor into G (stride ld), fp32.
 template <int MR>
 __device__ void cp_gram(const float* F, int nrows, int r, int ld, float* G) {
@@ -450,10 +391,86 @@ __device__ void cp_gram(const float* F, int nrows, int r, int ld, float* G) {
     }
 }
 
-// Dynamic shared memory of cp_small_kernel: the system and its inverse (ld x (ld + 1) each),
-// the inverse's two scratch rows and an RP x ld work tile.
+// Dynamic shared memory of cp_small_kernel: the fp64 system, inverted in place (ld x (ld + 1)
+// doubles), the inverse's two fp64 scratch rows and an RP x ld fp32 work tile.
 __host__ __device__ inline size_t cp_small_smem(int ld, int rp, int mr) {
-  return (2 * (size_t)ld * (ld + 1) + 2 * (size_t)mr + (size_t)rp * ld) * sizeof(float);
+  return ((size_t)ld * (ld + 1) + 2 * (size_t)mr) * sizeof(double) + (size_t)rp * ld * sizeof(float);
+}
+
+// In place: Gd (r x r, stride lg, SPD) <- Gd^{-1} in fp64 by Gauss-Jordan without pivoting
+// (the sweep operator; an SPD matrix's pivots are positive), two barriers per pivot.
+// scratch: 2 MR doubles.  Returns false on a pivot that is not positive (in every thread).
+template <int MR>
+__device__ bool cp_spd_inverse_d(double* Gd, int r, int lg, double* scratch) {
+  constexpr int NW = CpShape<MR>::NW;
+  __shared__ int bad;
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  double* prow = scratch;
+  double* pcol = scratch + MR;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < r; ++k) {
+    if (tid < r) {
+      prow[tid] = Gd[k * lg + tid];
+      pcol[tid] = Gd[tid * lg + k];
+    }
+    __syncthreads();
+    double d = prow[k];
+    if (!(d > 0.0)) {
+      d = 1e-300;
+      if (tid == 0) bad = 1;
+    }
+    const double inv = 1.0 / d;
+    for (int p = ty; p < r; p += NW) {
+      const double cp = pcol[p] * inv;
+      for (int q = tx; q < r; q += 32) {
+        double v;
+        if (p == k) v = (q == k) ? inv : prow[q] * inv;
+        else if (q == k) v = -cp;
+        else v = fma(-cp, prow[q], Gd[p * lg + q]);
+        Gd[p * lg + q] = v;
+      }
+    }
+    __syncthreads();
+  }
+  return bad == 0;
+}
+
+// out rows = RHS rows Gd^{-1} (RHS fp32 nrhs x r, stride ldr; Gd the fp64 inverse, stride lg),
+// summed in fp64 and rounded once.
+template <int MR>
+__device__ void cp_apply_inverse_d(const float* RHS, int ldr, int nrhs, const double* Gd, int r,
+                                   int lg, float* out, int ldo) {
+  constexpr int NW = CpShape<MR>::NW, TN = CpShape<MR>::TN;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  int ri[8], cj[TN];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) ri[u] = min(w + NW * u, nrhs - 1);
+#pragma unroll
+  for (int v = 0; v < TN; ++v) cj[v] = min(l + 32 * v, r - 1);
+  double acc[8][TN];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < TN; ++v) acc[u][v] = 0.0;
+  for (int p = 0; p < r; ++p) {
+    double av[8], bv[TN];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) av[u] = (double)RHS[(size_t)ri[u] * ldr + p];
+#pragma unroll
+    for (int v = 0; v < TN; ++v) bv[v] = Gd[p * lg + cj[v]];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < TN; ++v) acc[u][v] = fma(av[u], bv[v], acc[u][v]);
+  }
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < TN; ++v) {
+      const int row = w + NW * u, q = l + 32 * v;
+      if (row < nrhs && q < r) out[(size_t)row * ldo + q] = (float)acc[u][v];
+    }
 }
 
 template <int MR>
@@ -464,10 +481,9 @@ __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
   const int r = a.c_rank[ci], R = a.R, ld = a.ld;
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   const int lg = ld + 1;                  // odd stride: column walks hit distinct banks
-  float* G = sf;                          // ld x lg: the system
-  float* Gi = G + ld * lg;                // ld x lg: the system's inverse
-  float* Li = Gi + ld * lg;               // 2 MR: scratch rows of the inverse
-  float* work = Li + 2 * MR;              // RP*ld
+  double* Gd = reinterpret_cast<double*>(sf);   // ld x lg: the system, inverted in place (fp64)
+  double* Li = Gd + ld * lg;              // 2 MR: scratch rows of the inverse
+  float* work = reinterpret_cast<float*>(Li + 2 * MR);   // RP*ld
   __shared__ double dred[32];
   __shared__ float nA[MR], nB[MR], nD[MR];
   __shared__ int stop;
@@ -523,11 +539,11 @@ __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
         const float t = chunk_sum(a.part + k0 * ps + ld * ld + p * ld + q, ps, nk);
         gAA[p * ld + q] = s;
         work[p * ld + q] = t;
-        G[p * lg + q] = s * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
+        Gd[p * lg + q] = (double)s * (double)gDD[p * ld + q] + (p == q ? 1e-10 : 0.0);
       }
     __syncthreads();
-    if (!cp_spd_inverse<MR>(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
-    cp_apply_inverse<MR>(work, ld, r, Gi, r, lg, Bc, ld);
+    if (!cp_spd_inverse_d<MR>(Gd, r, lg, Li) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+    cp_apply_inverse_d<MR>(work, ld, r, Gd, r, lg, Bc, ld);
     __syncthreads();
     cp_gram<MR>(Bc, r, r, ld, gBB);
     return;
@@ -540,10 +556,10 @@ __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
       }
     for (int p = ty; p < r; p += NW)
       for (int q = tx; q < r; q += 32)
-        G[p * lg + q] = gAA[p * ld + q] * gBB[p * ld + q] + (p == q ? 1e-10f : 0.f);
+        Gd[p * lg + q] = (double)gAA[p * ld + q] * (double)gBB[p * ld + q] + (p == q ? 1e-10 : 0.0);
     __syncthreads();
-    if (!cp_spd_inverse<MR>(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
-    cp_apply_inverse<MR>(work, ld, R, Gi, r, lg, Dc, ld);
+    if (!cp_spd_inverse_d<MR>(Gd, r, lg, Li) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+    cp_apply_inverse_d<MR>(work, ld, R, Gd, r, lg, Dc, ld);
     __syncthreads();
     cp_gram<MR>(Dc, R, r, ld, gDD);
     __syncthreads();
@@ -595,11 +611,11 @@ __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
   __syncthreads();
   for (int p = ty; p < r; p += NW)
     for (int q = tx; q < r; q += 32)
-      G[p * lg + q] = gBB[p * ld + q] * gDD[p * ld + q] + (p == q ? 1e-10f : 0.f);
+      Gd[p * lg + q] = (double)gBB[p * ld + q] * (double)gDD[p * ld + q] + (p == q ? 1e-10 : 0.0);
   __syncthreads();
-  if (!cp_spd_inverse<MR>(G, r, lg, Li, Gi) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+  if (!cp_spd_inverse_d<MR>(Gd, r, lg, Li) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
   for (int p = ty; p < r; p += NW)
-    for (int q = tx; q < r; q += 32) Lc[p * ld + q] = Gi[p * lg + q];
+    for (int q = tx; q < r; q += 32) Lc[p * ld + q] = (float)Gd[p * lg + q];
 }
 
 }  // namespace fh

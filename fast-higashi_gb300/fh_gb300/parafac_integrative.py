@@ -1,8 +1,8 @@
 """CP-ALS on one 3-way tensor (drop-in for fasthigashi.parafac_integrative.parafac).
 
 parafac(X, rank, n_iter_max, init=[A, B, D]) runs n_iter_max sweeps of the library's CP-ALS
-kernels (parafac_integrative.py:28-112: fp64 normal-equation solves, balance_norm, the
-1e-5 relative-change stop) and returns (factors, loss_norm, loss_x) with
+kernels (the steps of parafac_integrative.py:28-112 with the normal-equation systems formed
+and inverted in fp64, balance_norm, the 1e-5 relative-change stop) and returns (factors, loss_norm, loss_x) with
 loss_norm = ||[[A,B,D]]||^2 and loss_x = <[[A,B,D]], X> of the last sweep.
 """
 from __future__ import annotations
