@@ -97,6 +97,9 @@ SIGNATURES = {
                             P]),
     "fh_core_norm": (C.c_int, [I32, I32, P, P, P, P, P, I32, I32, I32, I32, P, P, SZ, P, P]),
     "fh_selftest_wait": (C.c_int, [P, I64, P]),
+    "fh_pack_workspace": (SZ, [I32, I32, I32]),
+    "fh_pack_chromosome": (C.c_int, [P, P, P, P, I32, P, I32, I32, I32, I32, P, P, I64, P, P,
+                                     SZ, P, P]),
 }
 
 # kernels each entry point launches (the count the benchmark reports as gpu_launches)
@@ -111,7 +114,7 @@ _KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_exclusive_scan_n
             "fh_recon_loss_bwd_f32": 4, "fh_factor_grad_f32": 2, "fh_rwr_col_tiles": 1,
             "fh_rwr_col_dense": 1, "fh_col_coverage": 1, "fh_col_coverage_finalize": 1,
             "fh_polar_f32": 1, "fh_polar_svals_f32": 1, "fh_meta_polar": 5, "fh_core_norm": 2,
-            "fh_selftest_wait": 1}
+            "fh_selftest_wait": 1, "fh_pack_chromosome": 12}
 launches = 0
 
 

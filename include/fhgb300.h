@@ -376,6 +376,25 @@ int fh_core_norm(int32_t nchrom, int32_t nchunks, const int32_t* meta, float* A,
                  double* core, void* workspace, size_t workspace_bytes, int* status,
                  void* stream);
 
+/* ---- input packing of one chromosome (FastHigashi.pack_training_data_one_process,
+ * fasthigashi/FastHigashi_Wrapper.py:221-366 with preprocessing.py:114-193, 474-489; no
+ * blacklist, no batch ids).  Raw cell c's contacts are row/col/val[cell_off[c] ..
+ * cell_off[c + 1]) (device; coordinates in [0, nbin), values non-negative), n_raw cells;
+ * output cell k takes raw cell reorder[k] (n_cells entries).  Coordinates are divided by merge,
+ * contacts with |col - row| > off_diag dropped, merged bin rows with no positive kept contact
+ * removed and the rest renumbered, each cell scaled so that its kept contacts sum to
+ * ceil(nbin / merge), then log1p and a clip at mean + 15 std of all values.  Output, in the
+ * reference's order (cell by cell, each cell's entries in input order): out_idx int32[3][cap]
+ * (row, col, cell), out_val float32[cap] (cap >= the input's contacts suffices);
+ * out_counts int64[2] (device) = { entries written, kept bins }.  Workspace size from
+ * fh_pack_workspace.  status: FH_ERR_INDEX for a coordinate or reorder entry out of range. */
+size_t fh_pack_workspace(int32_t n_cells, int32_t nbin, int32_t merge);
+int fh_pack_chromosome(const int32_t* row, const int32_t* col, const float* val,
+                       const int64_t* cell_off, int32_t n_raw, const int32_t* reorder,
+                       int32_t n_cells, int32_t nbin, int32_t merge, int32_t off_diag,
+                       int32_t* out_idx, float* out_val, int64_t cap, int64_t* out_counts,
+                       void* workspace, size_t workspace_bytes, int* status, void* stream);
+
 /* ---- self-test of the bounded device-side waits (no reference counterpart: the reference
  * has no device code).  One warp allocates tensor memory, waits on an mbarrier that nothing
  * arrives on until limit_ns of device time pass, sets *status = FH_ERR_TIMEOUT, frees the
