@@ -16,6 +16,7 @@ Reference files (paths within ma-compbio/Fast-Higashi):
   fasthigashi/project2orthogonal.py    polar factor U Vh (thin SVD)
   fasthigashi/parafac_integrative.py   CP-ALS inner solver
   fasthigashi/parafac2_intergrative.py the PARAFAC2-like ALS driver
+  fasthigashi/FastHigashi_Wrapper.py   input packing, embedding post-processing
 """
 from __future__ import annotations
 
@@ -492,6 +493,190 @@ def col_coverage(datas, dtype=np.float64, do_conv=False, mark_inf=True, bad=Fals
             cov[cov <= dt(1e-4)] = np.inf                                 # :266-267
         out.append(cov)
     return out
+
+
+# ----------------------------------------------------------------------------------------
+# Imputed maps: restates FastHigashi.only_partial_rwr (FastHigashi_Wrapper.py:569-655).
+# ----------------------------------------------------------------------------------------
+def only_partial_rwr(d, do_conv=False, do_rwr=True, dtype=np.float64):
+    """{cell: map} of one chromosome: each (bin batch, cell batch) tile walked with the
+    auto-stop (force_rwr_epochs=-1), good batches then bad ones (:576-650), placed at
+    [rows, compact columns] (:598-600), then M + M^T with the diagonal halved (:601-605)."""
+    out = {}
+    for cs in d.cells() + d.bad_cells():
+        M = np.zeros((cs.stop - cs.start, d.num_bin, d.num_bin), dtype=dtype)
+        for bb in d.layout():
+            x = d.tile(bb, cs, dtype)
+            y, _ = partial_rwr(x, bb.local.start, bb.local.stop, do_rwr=do_rwr,
+                               force_rwr_epochs=-1, final_transpose=False, do_conv=do_conv)
+            M[:, bb.start:bb.start + bb.rows, bb.col] = y
+        M = M + M.transpose(0, 2, 1)
+        for i in range(M.shape[0]):
+            m = M[i]
+            out[cs.start + i] = m - np.diag(np.diag(m) / 2)
+    return out
+
+
+# ----------------------------------------------------------------------------------------
+# Post-processing: restates FastHigashi.fetch_cell_embedding and correct_batch_linear
+# (FastHigashi_Wrapper.py:750-878).  The reference calls scikit-learn's TruncatedSVD
+# (randomized, unseeded), quantile_transform, LinearRegression and normalize; these are
+# restated from their published definitions, with the exact SVD standing for the randomized
+# one (they agree when the sketch covers the range, as in the fixtures).
+# ----------------------------------------------------------------------------------------
+def cell_embedding(E, D_list, dtype=np.float64):
+    """Columns of every chromosome's E @ D / ||D||_col, concatenated (:753-758)."""
+    E = np.asarray(E, dtype=dtype)
+    parts = []
+    for D in D_list:
+        D = np.asarray(D, dtype=dtype)
+        parts.append(E @ (D / np.linalg.norm(D, axis=0, keepdims=True)))
+    return np.concatenate(parts, axis=1)
+
+
+def _interp_last(x, xp, fp):
+    """Linear interpolation on increasing xp (ties allowed): for x inside, the segment
+    starting at the last xp[j] <= x; outside, the end values."""
+    n = len(xp)
+    if x < xp[0]:
+        return fp[0]
+    if x >= xp[n - 1]:
+        return fp[n - 1]
+    j = int(np.searchsorted(xp, x, side="right")) - 1
+    if xp[j] == x:
+        return fp[j]
+    slope = (fp[j + 1] - fp[j]) / (xp[j + 1] - xp[j])
+    return slope * (x - xp[j]) + fp[j]
+
+
+def quantile_refs(nq):
+    """nq evenly spaced probabilities from 0 to 1: t * (1 / (nq - 1)), the last exactly 1."""
+    if nq == 1:
+        return np.zeros(1)
+    step = 1.0 / (nq - 1)
+    refs = np.arange(nq, dtype=np.float64) * step
+    refs[-1] = 1.0
+    return refs
+
+
+def linear_percentiles(s, refs):
+    """Percentiles of sorted s at probabilities refs (given as percentages refs * 100, as
+    the reference's caller passes them): virtual index (n - 1) * (p / 100), interpolated
+    from the order statistics either side, from the nearer end (a + (b - a) g below
+    g = 1/2, b - (b - a)(1 - g) from it)."""
+    n = len(s)
+    pr = (refs * 100.0) / 100.0
+    v = (n - 1) * pr
+    v = np.clip(v, 0, n - 1)
+    lo = np.floor(v).astype(np.int64)
+    hi = np.minimum(lo + 1, n - 1)
+    g = v - lo
+    a, b = s[lo], s[hi]
+    d = b - a
+    return np.where(g >= 0.5, b - d * (1 - g), a + d * g)
+
+
+def quantile_uniform(x, n_quantiles=100):
+    """Quantile transform of one column to [0, 1] (the coverage feature, :763): quantiles of
+    the values at evenly spaced probabilities (linear interpolation between order
+    statistics, made non-decreasing), each value mapped by the mean of the forward
+    interpolation and the reversed one (which splits ties evenly), values within 1e-7 of the
+    lowest / highest quantile set to 0 / 1."""
+    x = np.asarray(x, dtype=np.float64).reshape(-1)
+    n = len(x)
+    nq = min(n_quantiles, n)
+    refs = quantile_refs(nq)
+    q = np.maximum.accumulate(linear_percentiles(np.sort(x), refs))
+    out = np.empty_like(x)
+    for i, v in enumerate(x):
+        f = _interp_last(v, q, refs)
+        b = _interp_last(-v, -q[::-1], -refs[::-1])
+        out[i] = 0.5 * (f - b)
+    out[x + 1e-7 > q[-1]] = 1.0
+    out[x - 1e-7 < q[0]] = 0.0
+    return out
+
+
+def truncated_svd(Y, k):
+    """U_k S_k of Y's top k singular triplets, each component's sign fixed so that its entry
+    of largest magnitude (the first such) is positive."""
+    Y = np.asarray(Y, dtype=np.float64)
+    U, S, Vt = np.linalg.svd(Y, full_matrices=False)
+    U, S, Vt = U[:, :k], S[:k], Vt[:k]
+    sign = np.sign(Vt[np.arange(k), np.argmax(np.abs(Vt), axis=1)])
+    sign[sign == 0] = 1.0
+    return U * (S * sign)[None]
+
+
+def l2_rows(Y):
+    """Rows scaled to unit Euclidean norm (zero rows unchanged)."""
+    Y = np.asarray(Y, dtype=np.float64)
+    n = np.linalg.norm(Y, axis=1, keepdims=True)
+    n[n == 0] = 1.0
+    return Y / n
+
+
+def one_hot(labels):
+    """Non-float labels as indicator columns of the sorted distinct values (:829-835)."""
+    labels = np.asarray(labels)
+    uniq = np.unique(labels)
+    return (labels[:, None] == uniq[None]).astype(np.float64)
+
+
+def linear_residual(V, Y, add_intercept_back=False):
+    """Y minus its least-squares fit on V with an intercept (:862-866): centred columns, the
+    minimum-norm coefficients (pseudo-inverse of the centred V's Gram), the intercept added
+    back on request."""
+    V = np.asarray(V, dtype=np.float64)
+    if V.ndim == 1:
+        V = V.reshape((-1, 1))
+    Y = np.asarray(Y, dtype=np.float64)
+    mv, my = V.mean(0), Y.mean(0)
+    Vc, Yc = V - mv, Y - my
+    G = Vc.T @ Vc
+    w, Q = np.linalg.eigh(G)
+    keep = w > 1e-12 * max(w.max(), 1e-300)
+    Ginv = (Q[:, keep] / w[keep]) @ Q[:, keep].T
+    beta = Ginv @ (Vc.T @ Yc)
+    res = Yc - Vc @ beta
+    if add_intercept_back:
+        res = res + (my - mv @ beta)[None]
+    return res
+
+
+def fetch_cell_embedding(E, D_list, readcount, final_dim, restore_order=False, reorder=None):
+    """The store of fetch_cell_embedding (:750-790) with its coverage regression (:785)."""
+    emb = cell_embedding(E, D_list)
+    cov = quantile_uniform(readcount).reshape((-1, 1))
+    embed = truncated_svd(emb, final_dim)
+    if restore_order:
+        emb = restore_order_rows(emb, reorder)
+        embed = restore_order_rows(embed, reorder)
+    store = {"embed_all": emb, "embed_raw": embed, "embed_l2_norm": l2_rows(embed),
+             "restore_order": restore_order, "coverage_fh": cov}
+    correct_batch_linear(store, cov, "coverage_fh", False, reorder)
+    return store
+
+
+def restore_order_rows(x, reorder):
+    out = np.zeros_like(x)
+    out[np.asarray(reorder)] = x
+    return out
+
+
+def correct_batch_linear(store, var, name, add_intercept_back=False, reorder=None):
+    """Regress var out of the stored embedding, then its truncated SVD and row-normalised
+    form (:815-878).  var: floats (one column or several) or labels (one-hot)."""
+    var = np.asarray(var)
+    if store["restore_order"]:
+        var = restore_order_rows(var, reorder)
+    if var.dtype.kind not in "f":
+        var = one_hot(var)
+    res = linear_residual(var, store["embed_all"], add_intercept_back)
+    red = truncated_svd(res, store["embed_raw"].shape[1])
+    store["embed_correct_%s" % name] = red
+    store["embed_l2_norm_correct_%s" % name] = l2_rows(red)
+    return store
 
 
 def procrustes_align(X, Y):

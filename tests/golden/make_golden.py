@@ -31,13 +31,22 @@ Every output is produced by the reference's own functions on seeded synthetic in
                    on seeded raw per-cell contact matrices of two chromosomes (some bins empty in
                    every cell, contacts past the band, a cell order to apply), with merge
                    factors 1 and 2: the packed (row, col, cell) indices, values and shape.
+  impute.npz       FastHigashi.only_partial_rwr (FastHigashi_Wrapper.py:569-655): every
+                   cell's imputed map of the tiny workload (12-row bin batches, cell batches
+                   of 10, 6 bad-QC cells, a cell order), with and without do_conv.
+  postprocess.npz  FastHigashi.fetch_cell_embedding and correct_batch_linear
+                   (FastHigashi_Wrapper.py:750-878): the concatenated embedding, its truncated
+                   SVD and row-normalised form, the quantile-transformed read counts, the
+                   coverage-regressed and label-regressed embeddings, with and without the
+                   restored cell order, for als_small.npz's fitted factors and seeded ones.
   als_defaults_small.npz  the same workload with the reference's fit defaults (do_conv=True,
                    do_rwr=False: the 3 x 3 mean and no walk).
   als_bad_small.npz / als_badcol_small.npz  the same workload with its last 16 cells bad-QC
                    (good_qc_num=80): init, fit and transform (which embeds the bad cells too),
                    with do_col=False / True (the latter with bin_cov and bad_bin_cov).
 
-    python tests/golden/make_golden.py rwr_conv als_conv rwr_col als_col als_bad als_defaults pack
+    FH_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py \
+        rwr_conv als_conv rwr_col als_col als_bad als_defaults pack postprocess impute
 """
 import copy
 import os
@@ -221,6 +230,109 @@ def make_pack():
     print("pack", {k: v.shape for k, v in out.items() if k.startswith("out") and k.endswith("_idx")})
 
 
+def make_postprocess():
+    """FastHigashi.fetch_cell_embedding and correct_batch_linear (FastHigashi_Wrapper.py:
+    750-878) on (0) the fitted factors of als_small.npz and (1) seeded factors of 300 cells,
+    R = 16, four chromosomes of rank 12; coverage regression inside fetch_cell_embedding, then
+    a three-level categorical label with the intercept added back.  TruncatedSVD draws from
+    NumPy's global generator, seeded before each call."""
+    import types as T
+    wr = import_wrapper()
+    z = np.load(os.path.join(HERE, "als_small.npz"))
+    rng = np.random.default_rng(31)
+    cases = [(z["fit_E"].astype(np.float32), [z["fit_D%d" % i].astype(np.float32)
+                                               for i in range(3)], 8, None)]
+    C, R = 300, 16
+    E = rng.standard_normal((C, R)).astype(np.float32) * np.linspace(3, 0.5, R)[None]
+    Ds = [(rng.standard_normal((R, 12)) * rng.uniform(0.5, 2, 12)[None]).astype(np.float32)
+          for _ in range(4)]
+    cases.append((E, Ds, R, 12))
+    out = dict(n_case=len(cases))
+    for k, (E, Ds, rank, final_dim) in enumerate(cases):
+        C = E.shape[0]
+        readcount = np.round(np.exp(rng.normal(10, 0.8, C))).astype(np.int64)
+        readcount[:3] = readcount[3]                 # ties among the quantiles' inputs
+        batch = np.array(["b%d" % v for v in rng.integers(0, 3, C)])
+        reorder = rng.permutation(C)
+        for restore in (False, True):
+            me = T.SimpleNamespace(rank=rank, D_list=Ds, meta_embedding=E,
+                                   coverage_feats=readcount.reshape((-1, 1)),
+                                   label_info={"batch": batch}, reorder=reorder,
+                                   embedding_storage=None)
+            me.restore_order_fun = lambda x, me=me: wr.FastHigashi.restore_order_fun(me, x)
+            me.correct_batch_linear = (lambda name, back, me=me:
+                                       wr.FastHigashi.correct_batch_linear(me, name, back))
+            np.random.seed(100 + k)
+            store = wr.FastHigashi.fetch_cell_embedding(me, final_dim=final_dim,
+                                                        restore_order=restore)
+            np.random.seed(200 + k)
+            wr.FastHigashi.correct_batch_linear(me, "batch", True)
+            key = "c%d_r%d_" % (k, int(restore))
+            for name, v in store.items():
+                if isinstance(v, np.ndarray):
+                    out[key + name] = v
+            out[key + "coverage_fh"] = np.asarray(me.label_info["coverage_fh"])
+        out["c%d_E" % k] = E
+        out["c%d_nD" % k] = len(Ds)
+        for i, D in enumerate(Ds):
+            out["c%d_D%d" % (k, i)] = D
+        out["c%d_readcount" % k] = readcount
+        out["c%d_batch" % k] = batch
+        out["c%d_reorder" % k] = reorder
+        out["c%d_final_dim" % k] = rank if final_dim is None else final_dim
+    np.savez_compressed(os.path.join(HERE, "postprocess.npz"), **out)
+    print("postprocess", sorted(k for k in out if k.startswith("c1_r0")))
+
+
+def make_impute():
+    """FastHigashi.only_partial_rwr (FastHigashi_Wrapper.py:569-655) on the tiny workload with
+    12-row bin batches, cell batches of 10 and its last 6 cells bad-QC, without and with
+    do_conv; h5py is replaced by an in-memory recorder of the datasets it is asked to write."""
+    import types as T
+    wr = import_wrapper()
+    w = synth.workload("tiny")
+    coo, _ = synth.generate(w, seed=4)
+    good = w.n_cells - 6
+    reorder = np.random.default_rng(9).permutation(w.n_cells)
+    out = coo_arrays("in", coo)
+    out.update(n_chrom=len(coo), bs_bin=12, bs_cell=10, flank=w.band, good_qc_num=good,
+               resolution=w.resolution, reorder=reorder)
+
+    class Group(dict):
+        def create_dataset(self, name, data):
+            self[name] = np.asarray(data)
+
+    class File(dict):
+        def __init__(self, path, mode):
+            super().__init__()
+
+        def create_group(self, name):
+            g = self[name] = Group()
+            return g
+
+        def close(self):
+            pass
+
+    files = []
+    fake = T.ModuleType("h5py")
+    fake.File = lambda path, mode: files.append(File(path, mode)) or files[-1]
+    wr.h5py = fake
+    for conv in (False, True):
+        ds = build_chrom_datasets(ref, coo, w.chrom_names, [12] * len(coo), [10] * len(coo),
+                                  w.band, w.resolution, good_qc_num=good)
+        me = T.SimpleNamespace(all_matrix=ds, chrom_list=w.chrom_names, path2result_dir=HERE,
+                               do_conv=conv, do_rwr=True, device=CPU, reorder=reorder)
+        wr.FastHigashi.only_partial_rwr(me)
+        f = files[-1]
+        for k, name in enumerate(w.chrom_names):
+            g = f[name]
+            out["conv%d_shape%d" % (int(conv), k)] = g["shape"]
+            out["conv%d_maps%d" % (int(conv), k)] = np.stack([g[str(int(reorder[c]))]
+                                                              for c in range(w.n_cells)])
+    np.savez_compressed(os.path.join(HERE, "impute.npz"), **out)
+    print("impute", {k: v.shape for k, v in out.items() if "maps" in k})
+
+
 def make_parafac():
     rng = np.random.default_rng(5)
     X = rng.standard_normal((40, 6, 9)).astype(np.float32)
@@ -359,6 +471,10 @@ if __name__ == "__main__":
             make_als("als_col_small.npz", "small", 25, 40, 4, seed=3, do_col=True)
         if "pack" in only:
             make_pack()
+        if "postprocess" in only:
+            make_postprocess()
+        if "impute" in only:
+            make_impute()
         if "als_defaults" in only:
             make_als("als_defaults_small.npz", "small", 25, 40, 4, seed=3, do_conv=True,
                      do_rwr=False)
@@ -379,3 +495,5 @@ if __name__ == "__main__":
     make_als("als_badcol_small.npz", "small", 25, 40, 4, seed=3, do_col=True, good_qc_num=80)
     make_als("als_defaults_small.npz", "small", 25, 40, 4, seed=3, do_conv=True, do_rwr=False)
     make_pack()
+    make_postprocess()
+    make_impute()

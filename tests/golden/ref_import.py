@@ -16,12 +16,22 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get("FH_REFERENCE_ROOT", "/root/reference")
+# the checkout of the reference project (the folder that holds fasthigashi/), named by the
+# caller: fixture generation has no default location
+REF_ROOT = os.environ.get("FH_REFERENCE_ROOT", "")
+
+
+def _root():
+    if not REF_ROOT or not os.path.isdir(os.path.join(REF_ROOT, "fasthigashi")):
+        raise RuntimeError("set FH_REFERENCE_ROOT to a checkout of the reference project "
+                           "(the folder holding fasthigashi/)")
+    return REF_ROOT
 
 
 def import_reference():
-    if REF_ROOT not in sys.path:
-        sys.path.insert(0, REF_ROOT)
+    root = _root()
+    if root not in sys.path:
+        sys.path.insert(0, root)
     had_pd = "pandas" in sys.modules
     if not had_pd:
         sys.modules["pandas"] = types.ModuleType("pandas")
@@ -40,8 +50,9 @@ def import_reference():
 
 def import_wrapper():
     """fasthigashi.FastHigashi_Wrapper with pandas and h5py stubbed during its import."""
-    if REF_ROOT not in sys.path:
-        sys.path.insert(0, REF_ROOT)
+    root = _root()
+    if root not in sys.path:
+        sys.path.insert(0, root)
     stubs = [m for m in ("pandas", "h5py") if m not in sys.modules]
     for m in stubs:
         sys.modules[m] = types.ModuleType(m)

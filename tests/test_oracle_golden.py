@@ -186,3 +186,58 @@ def test_pack_matches_reference(k, case):
     assert tuple(shape) == tuple(z[ref + "_shape"])
     np.testing.assert_array_equal(idx, z[ref + "_idx"])
     np.testing.assert_array_equal(val, z[ref + "_val"])      # bit-exact: same fp32 operations
+
+
+POST_KEYS = ["embed_all", "embed_raw", "embed_l2_norm", "embed_correct_coverage_fh",
+             "embed_l2_norm_correct_coverage_fh", "embed_correct_batch",
+             "embed_l2_norm_correct_batch"]
+
+
+def postprocess_case(z, k):
+    E = z["c%d_E" % k]
+    Ds = [z["c%d_D%d" % (k, i)] for i in range(int(z["c%d_nD" % k]))]
+    return E, Ds, z["c%d_readcount" % k], int(z["c%d_final_dim" % k]), z["c%d_reorder" % k]
+
+
+@pytest.mark.parametrize("k", [0, 1])
+@pytest.mark.parametrize("restore", [False, True])
+def test_postprocess_matches_reference(k, restore):
+    """fetch_cell_embedding + correct_batch_linear (FastHigashi_Wrapper.py:750-878): the
+    embedding, the quantile transform (bit for bit, ties included), the truncated SVDs with
+    the reference's component signs, the regressions.  The reference's randomized fp32 SVD
+    sits within 2e-5 of the exact one."""
+    z = G.load("postprocess.npz")
+    E, Ds, rc, fd, reorder = postprocess_case(z, k)
+    st = O.fetch_cell_embedding(E, Ds, rc, fd, restore, reorder)
+    O.correct_batch_linear(st, z["c%d_batch" % k], "batch", True, reorder)
+    key = "c%d_r%d_" % (k, int(restore))
+    np.testing.assert_array_equal(st["coverage_fh"], z[key + "coverage_fh"])
+    for name in POST_KEYS:
+        assert O.rel_err(st[name], z[key + name]) < 5e-5, name
+
+
+def test_quantile_uniform_matches_published_transform_on_ties():
+    """The restated quantile transform against scikit-learn's own, where it is installed,
+    on heavy ties and sizes below and above the quantile count."""
+    sk = pytest.importorskip("sklearn.preprocessing")
+    rng = np.random.default_rng(5)
+    for n in (1, 2, 7, 99, 100, 101, 2500):
+        x = np.round(np.exp(rng.normal(8, 1.5, n)) / 50) * 50
+        for nq in (100, 10):
+            ref = sk.quantile_transform(x.reshape(-1, 1), n_quantiles=nq, copy=True)[:, 0]
+            np.testing.assert_array_equal(O.quantile_uniform(x, nq), ref)
+
+
+@pytest.mark.parametrize("conv", [False, True])
+@pytest.mark.parametrize("dtype,tol", [(np.float32, 2e-6), (np.float64, 2e-6)])
+def test_only_partial_rwr_matches_reference(conv, dtype, tol):
+    """only_partial_rwr (FastHigashi_Wrapper.py:569-655): auto-stopped walks per (bin batch,
+    cell batch), good then bad-QC batches, placed and symmetrised; maps keyed by raw cell id."""
+    z = G.load("impute.npz")
+    datas = G.chrom_datas(z, O)
+    for k, d in enumerate(datas):
+        maps = O.only_partial_rwr(d, do_conv=conv, dtype=dtype)
+        ref = z["conv%d_maps%d" % (int(conv), k)]
+        assert tuple(z["conv%d_shape%d" % (int(conv), k)]) == (d.num_bin, d.num_bin)
+        got = np.stack([maps[c] for c in range(ref.shape[0])])
+        assert O.rel_err(got, ref) < tol
