@@ -12,6 +12,9 @@ initial state (init_params runs once, untimed, as the metric states).
               the speed-up of the headline form over it
   e2e         the public API (Fast_Higashi_core.fit on host Sparse data) with the COO H2D and
               the embedding / loss D2H inside the timed region
+  input_packing / post_processing  the rows either side of the fit, each device-timed on
+              its own: fh_pack_chromosome over every chromosome from raw contacts in HBM, and
+              fetch_cell_embedding + correct_batch_linear for every cell (--no-extras skips)
   --impl reference   the reference's own Fast_Higashi_core (installed under baseline/_ref) on
                      the host CPU, all cores, one ALS iteration per step on a cell sample,
                      extrapolated to the workload's cells and iterations (cpu_baseline says how)
@@ -61,6 +64,11 @@ def parse():
                          "as two bf16 planes; bf16 one plane; fp32 the plain drop-in")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip timing the plain fp32 form beside the headline form")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the input-packing and post-processing measurements")
+    ap.add_argument("--extras-only", action="store_true",
+                    help="only the input-packing and post-processing measurements (after the "
+                         "GPU init_params), one JSON line")
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the FP64 fit that states both forms' embedding error")
     args = ap.parse_args()
@@ -540,6 +548,159 @@ def reference_arm(args, rank, ws):
 
 
 # --------------------------------------------------------------------------------------
+def _raw_cells_device(idx, val, n_cells, dev):
+    """One chromosome's contacts as raw per-cell arrays on the device (cell-major, each cell's
+    entries in (row, col) order; values expm1 of the packed ones, positive), built with torch
+    outside every timed region."""
+    import torch
+    ii = torch.from_numpy(idx).to(dev)
+    cell, perm = torch.sort(ii[2].long(), stable=True)
+    row = ii[0][perm].contiguous()
+    col = ii[1][perm].contiguous()
+    v = torch.expm1(torch.from_numpy(val).to(dev)[perm]).contiguous()
+    off = torch.zeros(n_cells + 1, dtype=torch.int64, device=dev)
+    off[1:] = torch.cumsum(torch.bincount(cell, minlength=n_cells), 0)
+    return row, col, v, off
+
+
+def pack_measure(w, coo, dev, reps=3, sample_cells=300):
+    """Input packing (fh_pack_chromosome, FastHigashi_Wrapper.py:221-366) of every chromosome
+    of the workload from raw per-cell contacts resident in HBM, device-timed (median of reps
+    per chromosome, summed); algorithmic traffic 28 B per contact (row, col, value read once;
+    row, col, cell, value written once).  Beside it, the oracle's packing (NumPy, one host
+    thread) of the first sample_cells cells of the first chromosome, scaled per contact."""
+    import torch
+    from fh_gb300 import _lib
+    from oracle import fh_oracle as O
+    P = _lib.ptr
+    C = w.n_cells
+    order = torch.arange(C, dtype=torch.int32, device=dev)
+    total_ms, contacts = 0.0, 0
+    for (idx, val, shape), nb in zip(coo, w.chrom_bins):
+        row, col, v, off = _raw_cells_device(idx, val, C, dev)
+        n = int(v.numel())
+        out_idx = torch.empty((3, n), dtype=torch.int32, device=dev)
+        out_val = torch.empty(n, dtype=torch.float32, device=dev)
+        counts = torch.zeros(2, dtype=torch.int64, device=dev)
+        st = torch.zeros(1, dtype=torch.int32, device=dev)
+        ws_ = torch.empty(_lib.value("fh_pack_workspace", C, nb, 1, n), dtype=torch.uint8,
+                          device=dev)
+        a = (P(row), P(col), P(v), P(off), C, P(order), C, nb, 1, w.band, P(out_idx), P(out_val),
+             n, P(counts), P(ws_), ws_.numel(), P(st), _lib.stream_ptr())
+        _lib.call("fh_pack_chromosome", *a)
+        times = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.call("fh_pack_chromosome", *a)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        if int(st.item()) != 0 or int(counts[0].item()) != n:
+            raise RuntimeError("packing check failed")
+        total_ms += float(np.median(times))
+        contacts += n
+        del row, col, v, off, out_idx, out_val, ws_
+    torch.cuda.empty_cache()
+    hbm = peaks()[0]
+    gbs = 28.0 * contacts / (total_ms / 1000.0) / 1e9
+    # the oracle on a sample of the first chromosome's cells (host)
+    idx, val, _ = coo[0]
+    keep = idx[2] < sample_cells
+    r, c, k, vv = idx[0][keep], idx[1][keep], idx[2][keep], np.expm1(val[keep])
+    o = np.argsort(k, kind="stable")
+    bounds = np.searchsorted(k[o], np.arange(sample_cells + 1))
+    cells = [(r[o][bounds[i]:bounds[i + 1]], c[o][bounds[i]:bounds[i + 1]],
+              vv[o][bounds[i]:bounds[i + 1]]) for i in range(sample_cells)]
+    t0 = time.perf_counter()
+    O.pack_chromosome(cells, w.chrom_bins[0], np.arange(sample_cells), w.band)
+    cpu_s = time.perf_counter() - t0
+    cpu_rate = int(keep.sum()) / cpu_s
+    return {"what": "fh_pack_chromosome over all %d chromosomes, %d cells, raw contacts "
+                    "resident in HBM (device time, median of %d per chromosome)"
+                    % (len(coo), C, reps, ),
+            "contacts": contacts, "ms": round(total_ms, 3),
+            "contacts_per_s": contacts / (total_ms / 1000.0),
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": gbs / hbm, "work": "28 B per contact"},
+            "cpu_baseline": {"kind": "port", "cores": 1, "contacts_per_s": cpu_rate,
+                             "sample": "the oracle's pack_chromosome on the first %d cells of "
+                                       "%s (%d contacts), one host thread"
+                                       % (sample_cells, w.chrom_names[0], int(keep.sum())),
+                             "extrapolated_s": contacts / cpu_rate}}
+
+
+def postprocess_measure(w, E, D_list, dev, reps=3, sample_cells=1000):
+    """fetch_cell_embedding + correct_batch_linear (FastHigashi_Wrapper.py:750-878) on the GPU
+    for every cell (the embedding, the quantile transform, both truncated SVDs, the regression,
+    the row normalisations), device-timed; the oracle (NumPy, fp64, exact SVDs) on a sample of
+    cells beside it, scaled per cell."""
+    import torch
+    from fh_gb300.postprocess import (cell_embedding, quantile_transform_uniform,
+                                      linear_residual, truncated_svd_in_span, l2_normalize)
+    from oracle import fh_oracle as O
+    C, R = E.shape
+    rc = np.round(np.exp(np.random.default_rng(7).normal(11, 0.8, C)))
+
+    def chain():
+        Y = cell_embedding(E, D_list, dev)
+        cov = quantile_transform_uniform(rc, 100, dev)
+        emb, _ = truncated_svd_in_span(E, Y, R, dev)
+        l2_normalize(emb, dev)
+        res = linear_residual(cov.reshape(-1, 1), Y, False, dev)
+        F = torch.cat([E, cov.reshape(-1, 1).float(),
+                       torch.ones((C, 1), dtype=torch.float32, device=dev)], dim=1)
+        red, _ = truncated_svd_in_span(F, res, R, dev)
+        return l2_normalize(red, dev)
+
+    chain()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        chain()
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    Eh = E[:sample_cells].cpu().numpy()
+    Dh = [d.cpu().numpy() for d in D_list]
+    t0 = time.perf_counter()
+    st = O.fetch_cell_embedding(Eh, Dh, rc[:sample_cells], R)
+    cpu_s = time.perf_counter() - t0
+    return {"what": "embedding, quantile transform, truncated SVD, coverage regression and its "
+                    "truncated SVD, row normalisation, for %d cells x %d columns (device time, "
+                    "median of %d)" % (C, st["embed_all"].shape[1], reps),
+            "ms": round(ms, 3), "cells_per_s": C / (ms / 1000.0),
+            "cpu_baseline": {"kind": "port", "cores": os.cpu_count(),
+                             "cells_per_s": sample_cells / cpu_s,
+                             "sample": "the oracle's fetch_cell_embedding (with its coverage "
+                                       "regression) on %d cells, NumPy fp64" % sample_cells}}
+
+
+def extras_arm(args, local):
+    """The rows either side of the fit on their own: init_params (for E and D), then the input
+    packing and post-processing measurements."""
+    import torch
+    from fh_gb300 import Fast_Higashi_core
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    w, coo, ds = make_workload(args.config, cells=args.cells)
+    m = Fast_Higashi_core(w.rank, w.band, [w.resolution], precision=args.precision).to(dev)
+    m._sizes(ds, w.dim1, None)
+    m.init_params(ds, False, True, False, seed=0)
+    torch.cuda.synchronize()
+    m.engine = None
+    torch.cuda.empty_cache()
+    line = {"workload": "%s: %d cells, %d bins, R=%d" % (w.name, w.n_cells, sum(w.chrom_bins),
+                                                        w.rank),
+            "input_packing": pack_measure(w, coo, dev),
+            "post_processing": postprocess_measure(w, m.meta_embedding[:, :w.rank].contiguous(),
+                                                   [m.D_dict[d.chrom] for d in ds], dev)}
+    print(json.dumps(line), flush=True)
+
+
 def gb300_arm(args, rank, local, ws):
     import torch
     from fh_gb300 import Fast_Higashi_core, _lib
@@ -672,6 +833,13 @@ def gb300_arm(args, rank, local, ws):
     e2e = {"value": ws * C / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1000.0,
            "ms_steps": [round(t * 1000.0, 1) for t in e2e_times], "statistic": "median"}
+    # ---- the rows either side of the fit: input packing and post-processing (untimed by the
+    # headline; each device-timed on its own)
+    packing = post = None
+    if not args.no_extras and rank == 0:
+        packing = pack_measure(w, coo, dev)
+        post = postprocess_measure(w, m.meta_embedding[:, :w.rank].contiguous(),
+                                   [m.D_dict[d.chrom] for d in ds], dev)
     # ---- both forms' error against an FP64 fit from the same state (untimed)
     precision = None
     if not args.no_fp64:
@@ -701,6 +869,7 @@ def gb300_arm(args, rank, local, ws):
             "plain_fp32": plain,
             "clocks": clk.summary(), "kernel_ms": {k: round(v["mean_ms"], 4) for k, v in kt.items()},
             "autotune": autotune_summary(), "precision_check": precision,
+            "input_packing": packing, "post_processing": post,
             "loss_final": float(m.engine.losses(hist[-1], eng.tensor_norms())[0])}
     print(json.dumps(line), flush=True)
 
@@ -796,6 +965,11 @@ def main():
         grad_arm(args, rank, local, ws)
     elif args.impl == "reference":
         reference_arm(args, rank, ws)
+    elif args.extras_only:
+        from fh_gb300 import build as _b
+        _b.build()
+        if rank == 0:
+            extras_arm(args, local)
     else:
         from fh_gb300 import build as _b
         _b.build()

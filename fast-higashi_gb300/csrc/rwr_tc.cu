@@ -25,6 +25,18 @@
 // The split products carry every operand to 16 significant bits, so the result is fp32-class.
 // Thread (warp w, lane l) serves row p = 32 (w % 4) + l (the TMEM lane quarter its warp may
 // read) and the column quarter w / 4 (16 warps).  Tiles wider than 256 columns use rwr_f32.cu.
+// The contacts of an item are loaded into registers before its Z init, so their latency
+// overlaps the init (per item, measured with clock stamps at c3 shapes: 3.2k -> 1.1k cycles).
+//
+// Form 2 (kPipe, tiles up to 192 columns): P goes to tensor memory (columns 384-511) as the
+// A operand of the epoch products, the epochs are issued per 64-column block of Z with an
+// mbarrier each (block j's epilogue overlaps blocks j+1..'s products; the columns of Z are
+// independent recurrences sharing P), and the output leaves through a dedicated staging
+// buffer by bulk copies that run on into the next item.  Measured at c3 shapes it is the
+// slower form (epochs 39k against 30k cycles per item: each block's epilogue pays a full
+// tensor-memory round trip and two barriers, more than the products it hides behind, while
+// the bulk output saves 2k cycles), so form 1 is the default and the engine's autotuner
+// times both.
 #include "tc_common.cuh"
 
 namespace fh {
@@ -33,6 +45,7 @@ constexpr int kRtThreads = 512;   // 16 warps: four per TMEM lane quarter
 constexpr float kRtFloor = 1e-8f;  // densify floor, sparse_for_schic.py:320
 constexpr float kRtEps = 1e-15f;   // column-sum guard, partial_rwr.py:90,91,111
 constexpr int kRtMaxPad = 256;     // npad: columns rounded up to 64, at most one MMA's N
+constexpr int kRtPre = 8;          // contacts per thread loaded ahead of the Z init
 
 struct RtArgs {
   const fh_tile* tiles;
@@ -101,11 +114,54 @@ __device__ __forceinline__ float ld_split(const uint8_t* hi, const uint8_t* lo, 
          __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(lo + off));
 }
 
-__host__ __device__ inline size_t rt_smem_bytes(int npad_max) {
-  return (size_t)npad_max / 64 * 16384 * 2 + 65536 + 11 * 128 * sizeof(float) + 64 * sizeof(double) +
-         64 + 1024;
+// Output staging of the pipelined form: both planes of a 128 x 192 tile with their 16-byte
+// phase offsets.
+constexpr uint32_t kRpStageBytes = 2u * 128u * 192u * 2u + 256u;
+constexpr int kRpMaxPad = 192;
+// tensor memory columns of the pipelined form: D [0, 192), A [192, 384), P hi / lo [384, 512)
+constexpr uint32_t kRpColA = 192, kRpColPh = 384, kRpColPl = 448;
+
+// Shared memory of the kernel: Z planes, then P planes (plain form) or the output staging
+// (pipelined form), then the per-column sums, factors, reductions and barriers.
+__host__ __device__ inline size_t rt_smem_bytes(int npad_max, bool pipe) {
+  return (size_t)npad_max / 64 * 16384 * 2 + (pipe ? kRpStageBytes : 65536u) +
+         11 * 128 * sizeof(float) + 64 * sizeof(double) + 64 + 1024;
 }
 
+// D[tmem] (+)= A[tmem] * B[smem] (A: 128 lanes, K along the columns as bf16 pairs).
+__device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc,
+                                            uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st8(uint32_t ta, const uint32_t (&v)[8]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(ta),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+      : "memory");
+}
+// Shared -> global bulk copy (both addresses 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_store(void* gdst, uint32_t ssrc, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
+               "r"(ssrc), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// Waits until the committed bulk copies have read their shared memory / have completed.
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+template <bool kPipe>
 __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
@@ -114,23 +170,24 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
   const uint32_t zbytes = (uint32_t)(a.npad_max / 64) * 16384u;
   uint8_t* Zhi = g;
   uint8_t* Zlo = g + zbytes;
-  uint8_t* Phi = g + 2 * zbytes;
+  uint8_t* Phi = g + 2 * zbytes;        // plain form: P planes; pipelined form: the staging
   uint8_t* Plo = Phi + 32768;
-  float* cs1p = reinterpret_cast<float*>(Plo + 32768);  // [4][128] partial column sums of S1
+  uint8_t* Stg = g + 2 * zbytes;
+  float* cs1p = reinterpret_cast<float*>(g + 2 * zbytes + (kPipe ? kRpStageBytes : 65536u));
   float* cs2p = cs1p + 512;                              // [4][128] partial row sums of S2
   float* fac = cs2p + 512;                               // [3][128] per-column P factors
   double* dred = reinterpret_cast<double*>(fac + 384);   // [64]
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(dred + 64);
-  uint32_t* misc = reinterpret_cast<uint32_t*>(mbar + 1);  // [0] TMEM base
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(dred + 64);  // [0] A A^T, [1 + j] block j
+  uint32_t* misc = reinterpret_cast<uint32_t*>(mbar + 4);  // [0] TMEM base
   const uint32_t sZhi = base, sZlo = base + zbytes, sPhi = base + 2 * zbytes,
-                 sPlo = sPhi + 32768;
+                 sPlo = sPhi + 32768, sStg = base + 2 * zbytes;
 
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
   const int q4 = w & 3, h = w >> 2;
   const int p = 32 * q4 + lane;
   const uint32_t bar = smem_u32(mbar);
   if (tid == 0) {
-    mbar_init(bar, 1);
+    for (int i = 0; i < (kPipe ? 4 : 1); ++i) mbar_init(bar + 8u * i, 1);
     mbar_fence_init();
   }
   if (w == 0) {
@@ -142,10 +199,11 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
   tc_fence_after();
   const uint32_t tmem = misc[0];
   const uint32_t lane_off = (uint32_t)(32 * q4) << 16;
-  const uint32_t tD = tmem + lane_off, tA = tmem + 256 + lane_off;
+  const uint32_t tD = tmem + lane_off, tA = tmem + (kPipe ? kRpColA : 256u) + lane_off;
   const __nv_bfloat16 fl_hi = __float2bfloat16_rn(kRtFloor);
   const __nv_bfloat16 fl_lo = __float2bfloat16_rn(kRtFloor - __bfloat162float(fl_hi));
   uint32_t phase = 0;
+  uint32_t bphase = 0;   // pipelined form, bit j: parity of block j's next mbarrier phase
   bool ok = true;
 
   // Issues the MMAs of one product group (thread 0) and waits for them (all threads).
@@ -164,12 +222,22 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     const fh_tile T = a.tiles[t];
     const int b = T.rows, n = T.width, s0 = T.s0, epochs = T.n_rwr;
     if (b <= 0 || b > a.max_rows || b > 128 || n < b || n > a.max_width || n > a.npad_max ||
-        s0 < 0 || s0 + b > n || epochs < 0) {
+        s0 < 0 || s0 + b > n || epochs < 0 || (kPipe && n > kRpMaxPad)) {
       if (tid == 0) set_status(a.status, FH_ERR_ARG);
       continue;
     }
     const int npad = (n + 63) & ~63;
     const int hw = npad / 4;  // columns per quarter (a multiple of 16)
+    // the first kRtPre entries of every thread go to registers now: their loads overlap the
+    // Z init below
+    const int64_t e0 = a.offsets[(int64_t)t * a.n_cells + c];
+    const int64_t e1 = a.offsets[(int64_t)t * a.n_cells + c + 1];
+    uint2 pre[kRtPre];
+#pragma unroll
+    for (int u = 0; u < kRtPre; ++u) {
+      const int64_t e = e0 + tid + (int64_t)u * kRtThreads;
+      pre[u] = e < e1 ? a.entries[e] : make_uint2(0u, 0u);
+    }
     // ---- 1. Z = floor on the tile, zero on the padding (both planes)
     {
       const int cpr = npad / 8;  // 16-byte chunks per row
@@ -191,14 +259,11 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     __syncthreads();
     // ---- 2. the cell's contacts (floored at 1e-8)
     {
-      const int64_t e0 = a.offsets[(int64_t)t * a.n_cells + c];
-      const int64_t e1 = a.offsets[(int64_t)t * a.n_cells + c + 1];
-      for (int64_t e = e0 + tid; e < e1; e += kRtThreads) {
-        const uint2 en = a.entries[e];
+      auto put = [&](const uint2 en) {
         const int r = (int)(en.x & 0xffffu), j = (int)(en.x >> 16);
         if (r >= b || j >= n) {
           set_status(a.status, FH_ERR_INDEX);
-          continue;
+          return;
         }
         const float v = fmaxf(__uint_as_float(en.y), kRtFloor);
         uint32_t hv, lv;
@@ -206,7 +271,12 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
         const uint32_t off = sw_off(r, j);
         *reinterpret_cast<uint16_t*>(Zhi + off) = (uint16_t)(hv & 0xffffu);
         *reinterpret_cast<uint16_t*>(Zlo + off) = (uint16_t)(lv & 0xffffu);
-      }
+      };
+#pragma unroll
+      for (int u = 0; u < kRtPre; ++u)
+        if (e0 + tid + (int64_t)u * kRtThreads < e1) put(pre[u]);
+      for (int64_t e = e0 + tid + (int64_t)kRtPre * kRtThreads; e < e1; e += kRtThreads)
+        put(a.entries[e]);
     }
     __syncthreads();
     // ---- 3. row p of A into TMEM (this thread's column quarter); column sums of S1
@@ -232,6 +302,7 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
       float s = 0.f;
       if (q < b) {
         const int pe = min(b, 32 * part + 32);
+#pragma unroll 8
         for (int pp = 32 * part; pp < pe; ++pp) s += ld_split(Zhi, Zlo, sw_off(pp, s0 + q));
       }
       cs1p[part * 128 + q] = s;
@@ -281,8 +352,8 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     __syncthreads();
     for (int q0 = 32 * h; q0 < 32 * h + 32; q0 += 16) {
       // S2 from D; S1 = A[p][s0 + q] from A's fp32 copy in TMEM when the 16-column window
-      // lies inside A's 256 columns (else from the smem planes, same values)
-      const bool in_tm = s0 + q0 + 16 <= kRtMaxPad;
+      // lies inside A's columns (else from the smem planes, same values)
+      const bool in_tm = s0 + q0 + 16 <= (kPipe ? npad : kRtMaxPad);
       float d[16], a1v[16], pv[16];
       tmem_ld16x2(tD + q0, in_tm ? tA + s0 + q0 : tA, d, a1v);
 #pragma unroll
@@ -301,14 +372,25 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
         }
         pv[e] = v;
       }
-      store_split8(Phi, Plo, sw_off(p, q0), pv);
-      store_split8(Phi, Plo, sw_off(p, q0 + 8), pv + 8);
+      if constexpr (kPipe) {
+        // row p of P as bf16 pairs (K along the columns) for the A operand of the epochs
+        uint32_t hv[8], lv[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) split2(pv[2 * e], pv[2 * e + 1], hv[e], lv[e]);
+        tmem_st8(tmem + lane_off + kRpColPh + (uint32_t)(q0 >> 1), hv);
+        tmem_st8(tmem + lane_off + kRpColPl + (uint32_t)(q0 >> 1), lv);
+      } else {
+        store_split8(Phi, Plo, sw_off(p, q0), pv);
+        store_split8(Phi, Plo, sw_off(p, q0 + 8), pv + 8);
+      }
     }
-    fence_proxy_async();
+    if constexpr (kPipe) tmem_wait_st();
+    else fence_proxy_async();
     tc_fence_before();
     __syncthreads();
     // ---- 6. Z_{t+1} = 0.5 P Z_t + 0.5 A; the last epoch writes the output staging
-    uint8_t* stage = Zhi;                    // free once the last MMA has completed
+    // plain form: the staging overlaps Zhi, free once the last MMA has completed
+    uint8_t* stage = kPipe ? Stg : Zhi;
     const int64_t g0 = (int64_t)c * a.cell_stride + T.xoff;
     const int mis = (int)(g0 & 7);           // staging shares the global 16-byte phase
     float ss = 0.f;
@@ -340,24 +422,30 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
         }
       }
     };
-    for (int ep = 0; ep < epochs; ++ep) {
-      if (tid == 0) {
+    if constexpr (kPipe) {
+      const int nblk = npad / 64;
+      // block j's products of one epoch: D[:, 64 j ..] = P Z[:, 64 j ..] split three ways,
+      // P (the A operand) from tensor memory, Z from shared memory
+      auto issue_block = [&](int jb) {
         tc_fence_after();
-        const uint32_t idesc = idesc_bf16(128, npad, false, true);
+        const uint32_t idesc = idesc_bf16(128, 64, false, true);
+        const uint32_t d = tmem + 64u * (uint32_t)jb;
         for (int ks = 0; ks < 8; ++ks) {
-          const uint32_t pk = (uint32_t)(ks >> 2) * 16384u + (uint32_t)(ks & 3) * 32u;
-          const uint32_t zk = (uint32_t)ks * 2048u;
-          const uint64_t ph = sdesc_sw128(sPhi + pk, 16, 1024), pl = sdesc_sw128(sPlo + pk, 16, 1024);
+          const uint32_t zk = (uint32_t)jb * 16384u + (uint32_t)ks * 2048u;
           const uint64_t zh = sdesc_sw128(sZhi + zk, 16384, 1024),
                          zl = sdesc_sw128(sZlo + zk, 16384, 1024);
-          mma_bf16(tmem, ph, zh, idesc, ks > 0 ? 1u : 0u);
-          mma_bf16(tmem, ph, zl, idesc, 1u);
-          mma_bf16(tmem, pl, zh, idesc, 1u);
+          const uint32_t ph = tmem + kRpColPh + 8u * (uint32_t)ks;
+          const uint32_t pl = tmem + kRpColPl + 8u * (uint32_t)ks;
+          mma_bf16_ta(d, ph, zh, idesc, ks > 0 ? 1u : 0u);
+          mma_bf16_ta(d, ph, zl, idesc, 1u);
+          mma_bf16_ta(d, pl, zh, idesc, 1u);
         }
-      }
-      if (ep == 0) {
-        // the next item's contact segment into L2 while this item's first
-        // epoch runs on the tensor cores (issued above)
+        mma_commit(bar + 8u * (uint32_t)(1 + jb));
+      };
+      if (epochs > 0) {
+        if (tid == 0)
+          for (int jb = 0; jb < nblk; ++jb) issue_block(jb);
+        // the next item's contact segment into L2 while this item's epochs run
         const int64_t nitem = item + gridDim.x;
         if (nitem < items) {
           const int tn = (int)(nitem / a.n_cells), cn = (int)(nitem - (int64_t)tn * a.n_cells);
@@ -368,27 +456,102 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
             asm volatile("prefetch.global.L2 [%0];" ::"l"(seg + off));
         }
       }
-      if (!mma_wait()) { ok = false; break; }
-      const bool last = ep == epochs - 1;
-      if (last) __syncthreads();   // nobody reads Z any more: the staging may overwrite it
-      for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
-        float d[16], av[16], z[16];
-        tmem_ld16x2(tD + j0, tA + j0, d, av);
+      for (int ep = 0; ep < epochs && ok; ++ep) {
+        if (ep == epochs - 1) {
+          // every block's products; the previous item's bulk copy has read the staging
+          bool got = true;
+          for (int jb = 0; jb < nblk; ++jb) {
+            got = mbar_wait(bar + 8u * (uint32_t)(1 + jb), (bphase >> jb) & 1u, nullptr) && got;
+            bphase ^= 1u << jb;
+          }
+          if (tid == 0) bulk_wait_read();
+          if (__syncthreads_or(!got)) { ok = false; break; }
+          tc_fence_after();
+          for (int jb = 0; jb < nblk; ++jb) {
+            const int j0 = 64 * jb + 16 * h;
+            float d[16], av[16], z[16];
+            tmem_ld16x2(tD + j0, tA + j0, d, av);
 #pragma unroll
-        for (int e = 0; e < 16; ++e) z[e] = fmaf(0.5f, d[e], 0.5f * av[e]);
-        if (last) {
-          emit(j0, z);
-        } else {
-          store_split8(Zhi, Zlo, sw_off(p, j0), z);
-          store_split8(Zhi, Zlo, sw_off(p, j0 + 8), z + 8);
+            for (int e = 0; e < 16; ++e) z[e] = fmaf(0.5f, d[e], 0.5f * av[e]);
+            emit(j0, z);
+          }
+          tc_fence_before();
+          break;
+        }
+        for (int jb = 0; jb < nblk; ++jb) {
+          const bool got = mbar_wait(bar + 8u * (uint32_t)(1 + jb), (bphase >> jb) & 1u, nullptr);
+          bphase ^= 1u << jb;
+          tc_fence_after();
+          if (got) {
+            const int j0 = 64 * jb + 16 * h;
+            float d[16], av[16], z[16];
+            tmem_ld16x2(tD + j0, tA + j0, d, av);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) z[e] = fmaf(0.5f, d[e], 0.5f * av[e]);
+            store_split8(Zhi, Zlo, sw_off(p, j0), z);
+            store_split8(Zhi, Zlo, sw_off(p, j0 + 8), z + 8);
+          }
+          fence_proxy_async();
+          tc_fence_before();
+          if (__syncthreads_or(!got)) { ok = false; break; }
+          if (tid == 0) issue_block(jb);
         }
       }
-      if (!last) fence_proxy_async();
-      tc_fence_before();
-      __syncthreads();
+    } else {
+      for (int ep = 0; ep < epochs; ++ep) {
+        if (tid == 0) {
+          tc_fence_after();
+          const uint32_t idesc = idesc_bf16(128, npad, false, true);
+          for (int ks = 0; ks < 8; ++ks) {
+            const uint32_t pk = (uint32_t)(ks >> 2) * 16384u + (uint32_t)(ks & 3) * 32u;
+            const uint32_t zk = (uint32_t)ks * 2048u;
+            const uint64_t ph = sdesc_sw128(sPhi + pk, 16, 1024), pl = sdesc_sw128(sPlo + pk, 16, 1024);
+            const uint64_t zh = sdesc_sw128(sZhi + zk, 16384, 1024),
+                           zl = sdesc_sw128(sZlo + zk, 16384, 1024);
+            mma_bf16(tmem, ph, zh, idesc, ks > 0 ? 1u : 0u);
+            mma_bf16(tmem, ph, zl, idesc, 1u);
+            mma_bf16(tmem, pl, zh, idesc, 1u);
+          }
+        }
+        if (ep == 0) {
+          // the next item's contact segment into L2 while this item's first
+          // epoch runs on the tensor cores (issued above)
+          const int64_t nitem = item + gridDim.x;
+          if (nitem < items) {
+            const int tn = (int)(nitem / a.n_cells), cn = (int)(nitem - (int64_t)tn * a.n_cells);
+            const int64_t f0 = a.offsets[(int64_t)tn * a.n_cells + cn];
+            const int64_t f1 = a.offsets[(int64_t)tn * a.n_cells + cn + 1];
+            const char* seg = reinterpret_cast<const char*>(a.entries + f0);
+            for (int64_t off = (int64_t)tid * 128; off < (f1 - f0) * 8; off += kRtThreads * 128)
+              asm volatile("prefetch.global.L2 [%0];" ::"l"(seg + off));
+          }
+        }
+        if (!mma_wait()) { ok = false; break; }
+        const bool last = ep == epochs - 1;
+        if (last) __syncthreads();   // nobody reads Z any more: the staging may overwrite it
+        for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
+          float d[16], av[16], z[16];
+          tmem_ld16x2(tD + j0, tA + j0, d, av);
+  #pragma unroll
+          for (int e = 0; e < 16; ++e) z[e] = fmaf(0.5f, d[e], 0.5f * av[e]);
+          if (last) {
+            emit(j0, z);
+          } else {
+            store_split8(Zhi, Zlo, sw_off(p, j0), z);
+            store_split8(Zhi, Zlo, sw_off(p, j0 + 8), z + 8);
+          }
+        }
+        if (!last) fence_proxy_async();
+        tc_fence_before();
+        __syncthreads();
+      }
     }
     if (!ok) break;
     if (epochs == 0) {
+      if constexpr (kPipe) {
+        if (tid == 0) bulk_wait_read();
+        __syncthreads();
+      }
       for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
         float av[16], unused[16];
         tmem_ld16x2(tA + j0, tA + j0, av, unused);
@@ -398,6 +561,10 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
       __syncthreads();
     }
     // ---- 7. staging -> X16 (contiguous b x n run of the cell's row), squared norm
+    if constexpr (kPipe) {
+      fence_proxy_async();
+      __syncthreads();
+    }
     {
       // the staging holds element k at index k + mis, and X16's planes start 16-byte aligned
       // with every plane a multiple of 8 elements long, so element k and its staging copy
@@ -409,10 +576,21 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
         const int64_t nvec = tot > head ? (tot - head) >> 3 : 0;
         const int64_t tail0 = head + (nvec << 3);
         for (int64_t k = tid; k < head && k < tot; k += kRtThreads) o[k] = st[k + mis];
-        const uint4* sv = reinterpret_cast<const uint4*>(st + head + mis);
-        uint4* ov = reinterpret_cast<uint4*>(o + head);
-        for (int64_t k = tid; k < nvec; k += kRtThreads) ov[k] = sv[k];
+        if constexpr (kPipe) {
+          // the middle as one bulk copy that runs on while the next item starts (its
+          // last epoch waits for the copy to have read the staging)
+          if (tid == 0 && nvec > 0)
+            bulk_store(o + head, sStg + (uint32_t)(pl * lo_base + head + mis) * 2u,
+                       (uint32_t)(nvec * 16));
+        } else {
+          const uint4* sv = reinterpret_cast<const uint4*>(st + head + mis);
+          uint4* ov = reinterpret_cast<uint4*>(o + head);
+          for (int64_t k = tid; k < nvec; k += kRtThreads) ov[k] = sv[k];
+        }
         for (int64_t k = tail0 + tid; k < tot; k += kRtThreads) o[k] = st[k + mis];
+      }
+      if constexpr (kPipe) {
+        if (tid == 0) bulk_commit();
       }
       const double sst = block_sum<double>((double)ss, dred);
       if (tid == 0 && a.sumsq) a.sumsq[(int64_t)t * a.n_cells + c] = sst;
@@ -420,6 +598,9 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
     }
   }
 
+  if constexpr (kPipe) {
+    if (tid == 0) bulk_wait_all();
+  }
   tc_fence_before();
   __syncthreads();
   if (!ok) {
@@ -443,9 +624,10 @@ using namespace fh;
 extern "C" int fh_rwr_tiles_tc(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
                                int32_t mr, int32_t mw, const fh_entry* entries,
                                const int64_t* offsets, uint16_t* out16, int64_t cell_stride,
-                               int64_t plane_stride, double* sumsq, int* status, void* stream) {
+                               int64_t plane_stride, double* sumsq, int32_t form, int* status,
+                               void* stream) {
   if (!tiles || n_tiles <= 0 || n_cells <= 0 || !offsets || !out16 || mr <= 0 || mw < mr ||
-      plane_stride < 0)
+      plane_stride < 0 || form < 0 || form > 2)
     return FH_ERR_ARG;
   if (mr > 128 || mw > kRtMaxPad) return FH_ERR_UNSUPPORTED;
   RtArgs a{};
@@ -462,16 +644,23 @@ extern "C" int fh_rwr_tiles_tc(const fh_tile* tiles, int32_t n_tiles, int32_t n_
   a.plane_stride = plane_stride;
   a.sumsq = sumsq;
   a.status = status;
+  // form 2: P in tensor memory, epochs pipelined by 64-column blocks, bulk output copies
+  const bool pipe = form == 2;
+  if (pipe && a.npad_max > kRpMaxPad) return FH_ERR_UNSUPPORTED;
+  const void* kern = pipe ? (const void*)rwr_tc_kernel<true> : (const void*)rwr_tc_kernel<false>;
   // at least 120 KB so that one CTA (and one 512-column TMEM allocation) sits on an SM
-  size_t smem = rt_smem_bytes(a.npad_max);
+  size_t smem = rt_smem_bytes(a.npad_max, pipe);
   if (smem < 120 * 1024) smem = 120 * 1024;
   if (smem > 227 * 1024) return FH_ERR_UNSUPPORTED;
-  if (ensure_smem((const void*)rwr_tc_kernel, smem)) return FH_ERR_LAUNCH;
+  if (ensure_smem(kern, smem)) return FH_ERR_LAUNCH;
   const int sms = sm_count();
   if (sms <= 0) return FH_ERR_LAUNCH;
   const int64_t items = (int64_t)n_tiles * n_cells;
   const int64_t grid = items < sms ? items : sms;
-  rwr_tc_kernel<<<(unsigned)grid, kRtThreads, smem, (cudaStream_t)stream>>>(a);
+  if (pipe)
+    rwr_tc_kernel<true><<<(unsigned)grid, kRtThreads, smem, (cudaStream_t)stream>>>(a);
+  else
+    rwr_tc_kernel<false><<<(unsigned)grid, kRtThreads, smem, (cudaStream_t)stream>>>(a);
   FH_CHECK_LAUNCH();
   return FH_OK;
 }

@@ -78,7 +78,7 @@ SIGNATURES = {
     "fh_xg_f32": (C.c_int, [P, I64, I32, I64, P, I32, I32, P, P, P]),
     "fh_project_y_f32": (C.c_int, [P, P, I64, P, P, I32, P, I32, P]),
     "fh_rwr_tiles_bf16": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, I64, P, P, P]),
-    "fh_rwr_tiles_tc": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, I64, P, P, P]),
+    "fh_rwr_tiles_tc": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, I64, P, I32, P, P]),
     "fh_split_bf16": (C.c_int, [P, I64, I32, I64, P, P]),
     "fh_xe_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, I32, P, P, P]),
     "fh_xg_bf16_splits": (C.c_int, [I32, I64]),
@@ -97,7 +97,18 @@ SIGNATURES = {
                             P]),
     "fh_core_norm": (C.c_int, [I32, I32, P, P, P, P, P, I32, I32, I32, I32, P, P, SZ, P, P]),
     "fh_selftest_wait": (C.c_int, [P, I64, P]),
-    "fh_pack_workspace": (SZ, [I32, I32, I32]),
+    "fh_pack_workspace": (SZ, [I32, I32, I32, I64]),
+    "fh_embed_assemble": (C.c_int, [P, I32, I32, I64, P, I32, I64, P, P, I64, P]),
+    "fh_gemm_scale_f32": (C.c_int, [P, I64, P, I64, P, I32, I32, I32, P, I64, P]),
+    "fh_quantile_workspace": (SZ, [I32, I32]),
+    "fh_quantile_uniform": (C.c_int, [P, I32, I32, P, P, SZ, P]),
+    "fh_lstsq_workspace": (SZ, [I32, I32]),
+    "fh_lstsq_residual": (C.c_int, [P, I32, I32, P, I64, I32, I32, P, I64, P, SZ, P, P]),
+    "fh_range_svd_workspace": (SZ, [I32, I32, I32]),
+    "fh_range_svd": (C.c_int, [P, I64, I32, I32, P, I64, I32, I32, P, I64, P, P, SZ, P, P]),
+    "fh_l2_rows": (C.c_int, [P, I64, I32, I32, P, I64, P]),
+    "fh_impute_maps": (C.c_int, [P, P, I64, I32, P, I64, I32, I32, P, P, P]),
+    "fh_cross_f32": (C.c_int, [P, I64, I32, P, I64, I32, I32, P, I64, P]),
     "fh_pack_chromosome": (C.c_int, [P, P, P, P, I32, P, I32, I32, I32, I32, P, P, I64, P, P,
                                      SZ, P, P]),
 }
@@ -114,7 +125,10 @@ _KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_exclusive_scan_n
             "fh_recon_loss_bwd_f32": 4, "fh_factor_grad_f32": 2, "fh_rwr_col_tiles": 1,
             "fh_rwr_col_dense": 1, "fh_col_coverage": 1, "fh_col_coverage_finalize": 1,
             "fh_polar_f32": 1, "fh_polar_svals_f32": 1, "fh_meta_polar": 5, "fh_core_norm": 2,
-            "fh_selftest_wait": 1, "fh_pack_chromosome": 12}
+            "fh_selftest_wait": 1, "fh_pack_chromosome": 19,
+            "fh_embed_assemble": 2, "fh_gemm_scale_f32": 1, "fh_quantile_uniform": 3,
+            "fh_lstsq_residual": 7, "fh_range_svd": 13, "fh_l2_rows": 1,
+            "fh_impute_maps": 1, "fh_cross_f32": 1}
 launches = 0
 
 
@@ -122,6 +136,8 @@ def _kernel_count(name, args):
     if name == "fh_cp_als":
         n_iter = args[11]
         return 2 if n_iter == 0 else 3 + 4 * n_iter
+    if name == "fh_range_svd":
+        return 14 if args[10] else 13
     return _KERNELS.get(name, 0)
 
 

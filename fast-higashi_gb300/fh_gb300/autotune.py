@@ -15,6 +15,10 @@ Knobs in use (fh_gb300.engine):
               more splits fill more SMs, fewer splits cut the partial-sum traffic and the
               reduction; candidates: the heuristic (fh_xg_splits / fh_xg_bf16_splits), half,
               twice and four times it.
+  rwr_form    the form of the tensor-core walk (fh_rwr_tiles_tc): P in shared memory with
+              one product group per epoch (1, the default), or P in tensor memory with the
+              epochs pipelined by 64-column blocks and bulk output copies (2, tiles up to 192
+              columns); timed as one full walk of the engine's tiles.
   cp_chunk_rows  bin rows per CTA of the CP-ALS row kernels (fh_cp_als chunk table): more
               rows per chunk mean fewer partial sums for the per-chromosome kernel and fewer
               CTAs; candidates 8 (the default), 4 and 16, timed as one sweep on the live

@@ -52,6 +52,7 @@ class FitEngine:
         self.bf16 = precision != "fp32"
         self.planes = 2 if precision == "bf16x2" else 1
         self.timing = None   # {kernel family: [(start event, end event)]} when enabled
+        self._rwr_form = None  # form of the tensor-core walk, tuned at its first run
         # K chunks of 64 per tensor-memory accumulator run in the bf16 X passes (0: the
         # library's default); shorter runs, more compensated folds
         self.fold = 0
@@ -321,11 +322,7 @@ class FitEngine:
                           P(self.sumsq), P(self.status), self.sp())
             return
         if self.bf16 and self.max_rows <= 128 and self.max_width <= 256:
-            _lib.call("fh_rwr_tiles_tc", P(self.tiles_dev), self.n_tiles, self.Ct,
-                      self.max_rows, self.max_width, P(self.store.entries),
-                      P(self.store.offsets), P(self.X16), self.ldx,
-                      self.Ct * self.ldx if self.planes == 2 else 0, P(self.sumsq),
-                      P(self.status), self.sp())
+            self._rwr_tc(self.tuned_rwr_form())
         elif self.bf16:
             _lib.call("fh_rwr_tiles_bf16", P(self.tiles_dev), self.n_tiles, self.Ct,
                       self.max_rows, self.max_width, P(self.store.entries),
@@ -337,6 +334,28 @@ class FitEngine:
                       self.max_rows, self.max_width, P(self.store.entries),
                       P(self.store.offsets), P(self.X), self.ldx, P(self.sumsq),
                       P(self.status), self.sp())
+
+    def _rwr_tc(self, form):
+        P = _lib.ptr
+        _lib.call("fh_rwr_tiles_tc", P(self.tiles_dev), self.n_tiles, self.Ct, self.max_rows,
+                  self.max_width, P(self.store.entries), P(self.store.offsets), P(self.X16),
+                  self.ldx, self.Ct * self.ldx if self.planes == 2 else 0, P(self.sumsq),
+                  int(form), P(self.status), self.sp())
+
+    def tuned_rwr_form(self):
+        """Form of the tensor-core walk (fh_rwr_tiles_tc): the autotuner's pick between P in
+        shared memory (1, the default) and the block-pipelined form with P in tensor memory
+        (2, tiles up to 192 columns), timed on this engine's own tiles at the first call."""
+        if self._rwr_form is None:
+            if self.max_width > 192 or self.torch.cuda.is_current_stream_capturing():
+                return 1
+            from . import autotune
+            sig = (self.precision, self.Ct, self.n_tiles, self.max_width,
+                   int(np.asarray(self.tiles["n_rwr"]).max()))
+            dev = self.torch.cuda.get_device_name(self.device)
+            self._rwr_form = autotune.default_tuner().choose(dev, "rwr_form", sig, [1, 2],
+                                                             self._rwr_tc, reps=1)
+        return self._rwr_form
 
     # ------------------------------------------------------------------ X passes
     def xg_splits(self, n_cells, rows):

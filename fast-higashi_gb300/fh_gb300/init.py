@@ -9,10 +9,13 @@
    (:265).  The features use the stopped output Q_{e+1} A as the reference does.
 3. Per chromosome, a randomized truncated SVD of the cells x band features (the
    reference's sklearn TruncatedSVD(n_components=r, n_iter=2), :257-258) whose tall
-   products F Omega, F^T Q run as the library's X passes; the (r+10)-column QR and SVD
-   factorizations of that sketch run on the host in float64.  The concatenated features'
-   top-R singular triplets give meta_embedding = U[:, :R] and D = (S Vh)[:R] (:283-290),
-   taken from the eigen-decomposition of their Gram matrix.
+   products F Omega, F^T Q run as the library's X passes; the sketch's orthonormal basis and
+   the SVD of F in it come from fh_range_svd (fp64 Gram and Jacobi eigenbasis of the
+   (r+10)-column sketch, on the device).  The concatenated features' top-R singular triplets
+   give meta_embedding = U[:, :R] and D = (S Vh)[:R] (:283-290): exactly by fh_range_svd when
+   they are at most 256 columns wide, else from a randomized range of R + 10 columns (three
+   power iterations, each re-orthonormalised) that fh_range_svd resolves; D = E^T [features]
+   by the fp64 fh_cross_f32.  Nothing of the factorization runs on the host.
 At resolutions finer than 1 Mb the reference pools the features to 1 Mb first; this
 restatement sketches the unpooled band features.
 With do_col (and do_rwr) the coverage rows bin_cov come first (:96-200): 1e-4 plus the
@@ -28,6 +31,12 @@ import numpy as np
 
 from . import _lib
 from .engine import FitEngine
+from .postprocess import truncated_svd_in_span
+
+
+def _torch():
+    import torch
+    return torch
 
 
 def _stop_epochs(deltas, cap, tol=0.01):
@@ -100,8 +109,10 @@ def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
     n = n_comp + n_oversamples
     dev, f32 = eng.device, torch.float32
     lo, hi = x0 - a0, x1 - a0
-    blocks = [(c0, min(c0 + 128, n)) for c0 in range(0, n, 128)]
     bufs = {}
+
+    def blocks_of(w):
+        return [(c0, min(c0 + 128, w)) for c0 in range(0, w, 128)]
 
     def buffers(w):
         rp = 128 if w > 64 else (64 if w > 32 else (32 if w > 16 or eng.bf16 else 16))
@@ -114,7 +125,7 @@ def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
 
     def ft_times(Ecells):                     # F^T E: (band rows of k) x n
         out = []
-        for c0, c1 in blocks:
+        for c0, c1 in blocks_of(Ecells.shape[1]):
             rp, (W, _, _, _) = buffers(c1 - c0)
             E = torch.zeros((C, rp), dtype=f32, device=dev)
             E[:, :c1 - c0] = Ecells[:, c0:c1]
@@ -124,7 +135,7 @@ def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
 
     def f_times(Qrows):                       # F Q: cells x n
         out = []
-        for c0, c1 in blocks:
+        for c0, c1 in blocks_of(Qrows.shape[1]):
             rp, (_, S, splits, part) = buffers(c1 - c0)
             G = torch.zeros((rows, rp), dtype=f32, device=dev)
             G[lo:hi, :c1 - c0] = Qrows[:, c0:c1]
@@ -133,14 +144,79 @@ def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
         return torch.cat(out, dim=1)
 
     omega = torch.from_numpy(rng.standard_normal((C, n)).astype(np.float32)).to(dev)
-    Q = ft_times(omega)                       # range of F^T (band rows x n)
+    # range of F^T (band rows x n), re-orthonormalised after every product (F and F^T alike)
+    # so that the power iterations keep the sketch's conditioning at that of F
+    Qh = orthonormal_columns(ft_times(omega))
     for _ in range(n_iter):
-        Q = ft_times(f_times(Q))
-    Qh, _ = np.linalg.qr(Q.double().cpu().numpy())
-    Bt = f_times(torch.from_numpy(Qh.astype(np.float32)).to(dev)).double().cpu().numpy()  # (Q^T F^T)^T
-    # F^T = Qh Bt^T  =>  F = Bt Qh^T ; SVD of Bt (cells x n) gives F's left factors
-    Uc, s, _ = np.linalg.svd(Bt, full_matrices=False)
-    return Uc[:, :n_comp] * s[:n_comp]
+        Qh = orthonormal_columns(ft_times(orthonormal_columns(f_times(Qh))))
+    Bt = f_times(Qh)                          # (Q^T F^T)^T, cells x n
+    # F^T = Qh Bt^T  =>  F = Bt Qh^T ; the SVD of Bt (cells x n) gives F's left factors
+    k = min(n_comp, Bt.shape[1])
+    emb, _ = truncated_svd_in_span(Bt, Bt, k, dev)
+    if k < n_comp:
+        emb = torch.cat([emb, torch.zeros((C, n_comp - k), dtype=f32, device=dev)], dim=1)
+    return emb
+
+
+def orthonormal_columns(Q, rel=1e-7):
+    """An orthonormal basis of Q's columns (rows x n, n <= 256) on the device: Q's exact SVD in
+    its own span (fh_range_svd) as U S, then U; directions below rel of the largest singular
+    value (fp32 noise) are dropped."""
+    n = Q.shape[1]
+    us, sig = truncated_svd_in_span(Q, Q, n, Q.device)
+    keep = sig > rel * sig[0]
+    m = int(keep.sum().item())
+    return (us[:, :m] / sig[:m].float()[None]).contiguous()
+
+
+def _gemm(A, B):
+    """A (n x K) B (K x m) in fp32 on the device (fh_gemm_scale_f32)."""
+    torch = _torch()
+    A, B = A.contiguous(), B.contiguous()
+    out = torch.empty((A.shape[0], B.shape[1]), dtype=torch.float32, device=A.device)
+    P = _lib.ptr
+    _lib.call("fh_gemm_scale_f32", P(A), A.shape[1], P(B), B.shape[1], None, A.shape[0],
+              B.shape[1], A.shape[1], P(out), B.shape[1], _lib.stream_ptr())
+    return out
+
+
+def _cross(A, B):
+    """A^T B (A: rows x na, B: rows x nb) summed in fp64 on the device (fh_cross_f32)."""
+    torch = _torch()
+    A, B = A.contiguous(), B.contiguous()
+    out = torch.empty((A.shape[1], B.shape[1]), dtype=torch.float64, device=A.device)
+    P = _lib.ptr
+    _lib.call("fh_cross_f32", P(A), A.shape[1], A.shape[1], P(B), B.shape[1], B.shape[1],
+              A.shape[0], P(out), B.shape[1], _lib.stream_ptr())
+    return out
+
+
+def top_singular(Y, R, rng, n_iter=3, oversample=10):
+    """(U_R, S_R) of Y (cells x m) on the device: exact (fh_range_svd in Y's own span) when
+    m <= 256, else within a randomized range of R + oversample columns refined by n_iter power
+    iterations (each re-orthonormalised)."""
+    torch = _torch()
+    m = Y.shape[1]
+    if m <= 256:
+        us, sig = truncated_svd_in_span(Y, Y, R, Y.device)
+    else:
+        q = min(R + oversample, m, 256)
+        omega = torch.from_numpy(rng.standard_normal((m, q)).astype(np.float32)).to(Y.device)
+        Z = _gemm(Y, omega)
+        for _ in range(n_iter):
+            W = orthonormal_columns(_cross(Y, orthonormal_columns(Z)).float())
+            Z = _gemm(Y, W)
+        F = orthonormal_columns(Z)
+        us, sig = truncated_svd_in_span(F, Y, min(R, F.shape[1]), Y.device)
+        if us.shape[1] < R:
+            pad = R - us.shape[1]
+            us = torch.cat([us, torch.zeros((us.shape[0], pad), dtype=us.dtype,
+                                            device=us.device)], dim=1)
+            sig = torch.cat([sig, torch.zeros(pad, dtype=sig.dtype, device=sig.device)])
+    live = sig > 0
+    U = torch.where(live[None], us / torch.where(live, sig, torch.ones_like(sig)).float()[None],
+                    torch.zeros_like(us))
+    return U.contiguous(), sig
 
 
 def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
@@ -177,19 +253,15 @@ def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
         feats.append(f)
         cols.append((d.chrom, start, start + f.shape[1]))
         start += f.shape[1]
-    Call = np.concatenate(feats, axis=1)                   # cells x sum(r)
-    G = Call.T @ Call
-    lam, V = np.linalg.eigh(G)
-    lam, V = lam[::-1], V[:, ::-1]
+    Call = torch.cat(feats, dim=1).contiguous()            # cells x sum(r), on the device
     R = min(rank, Call.shape[1])
-    sv = np.sqrt(np.maximum(lam[:R], 1e-300))
-    E = np.zeros((Call.shape[0], rank))
-    E[:, :R] = (Call @ V[:, :R]) / sv
-    SVh = np.zeros((rank, Call.shape[1]))
-    SVh[:R] = sv[:, None] * V[:, :R].T
-    model.meta_embedding = torch.from_numpy(E.astype(np.float32)).to(device)
-    model.D_dict = {c: torch.from_numpy(np.ascontiguousarray(SVh[:, a:b]).astype(np.float32)).to(device)
-                    for c, a, b in cols}
+    U, _ = top_singular(Call, R, rng)
+    E = torch.zeros((Call.shape[0], rank), dtype=torch.float32, device=Call.device)
+    E[:, :R] = U
+    SVh = torch.zeros((rank, Call.shape[1]), dtype=torch.float32, device=Call.device)
+    SVh[:R] = _cross(U, Call).float()                       # U^T Call = S Vh
+    model.meta_embedding = E.to(device)
+    model.D_dict = {c: SVh[:, a:b].contiguous().to(device) for c, a, b in cols}
     model.A_list = A_list
     model.B_dict = B_dict
     model.n_i = np.asarray(n_i)

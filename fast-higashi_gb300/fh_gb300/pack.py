@@ -45,7 +45,7 @@ def pack_chromosome(cells, nbin, reorder, off_diag, merge=1, device="cuda"):
     out_val = torch.empty(cap, dtype=torch.float32, device=dev)
     counts = torch.zeros(2, dtype=torch.int64, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
-    ws = torch.empty(_lib.value("fh_pack_workspace", n_cells, int(nbin), int(merge)),
+    ws = torch.empty(_lib.value("fh_pack_workspace", n_cells, int(nbin), int(merge), cap),
                      dtype=torch.uint8, device=dev)
     P = _lib.ptr
     _lib.call("fh_pack_chromosome", P(row), P(col), P(val), P(off_d), n_raw, P(order), n_cells,

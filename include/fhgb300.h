@@ -124,11 +124,17 @@ int fh_rwr_tiles_bf16(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
  * runs torch.bmm in fp32, partial_rwr.py:85-138): S2 = A A^T and every P Z_t product with
  * bf16 operands split hi|lo (three products, fp32 accumulators in TMEM), the recurrence
  * Z_{t+1} = 0.5 P Z_t + 0.5 A of fh_rwr_tiles_f32, and the same output planes as
- * fh_rwr_tiles_bf16.  max_rows <= 128 and max_width <= 256 (FH_ERR_UNSUPPORTED otherwise). */
+ * fh_rwr_tiles_bf16.  max_rows <= 128 and max_width <= 256 (FH_ERR_UNSUPPORTED otherwise).
+ * form: 0 the library default (1); 1 P in shared memory, one product group per epoch over the
+ * tile's width; 2 P in tensor memory as the MMAs' A operand, epochs pipelined by 64-column
+ * blocks of Z (each block's epilogue behind the other blocks' products) and the output moved
+ * by bulk copies that run on into the next item (max_width <= 192, FH_ERR_UNSUPPORTED
+ * otherwise).  Both forms give the same values; which is faster depends on the shape (the
+ * engine's autotuner times both). */
 int fh_rwr_tiles_tc(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells, int32_t max_rows,
                     int32_t max_width, const fh_entry* entries, const int64_t* offsets,
                     uint16_t* out16, int64_t cell_stride, int64_t plane_stride, double* sumsq,
-                    int* status, void* stream);
+                    int32_t form, int* status, void* stream);
 
 /* fh_rwr_tiles_f32 with the walk weight free: Q_{t+1} = rp Q_t P + (1 - rp) I, the form of
  * partial_rwr.py:109,116-118 where rp is fixed at 0.5 (0 <= rp < 1).  The forward of the
@@ -385,15 +391,69 @@ int fh_core_norm(int32_t nchrom, int32_t nchunks, const int32_t* meta, float* A,
  * removed and the rest renumbered, each cell scaled so that its kept contacts sum to
  * ceil(nbin / merge), then log1p and a clip at mean + 15 std of all values.  Output, in the
  * reference's order (cell by cell, each cell's entries in input order): out_idx int32[3][cap]
- * (row, col, cell), out_val float32[cap] (cap >= the input's contacts suffices);
- * out_counts int64[2] (device) = { entries written, kept bins }.  Workspace size from
- * fh_pack_workspace.  status: FH_ERR_INDEX for a coordinate or reorder entry out of range. */
-size_t fh_pack_workspace(int32_t n_cells, int32_t nbin, int32_t merge);
+ * (row, col, cell), out_val float32[cap], cap >= the input's contacts (the work is cut into
+ * segments of at most 4,096 contacts sized by cap); out_counts int64[2] (device) = { entries
+ * written, kept bins }.  Workspace size from fh_pack_workspace (the same cap).  status:
+ * FH_ERR_INDEX for a coordinate or reorder entry out of range, or more contacts than cap. */
+size_t fh_pack_workspace(int32_t n_cells, int32_t nbin, int32_t merge, int64_t cap);
 int fh_pack_chromosome(const int32_t* row, const int32_t* col, const float* val,
                        const int64_t* cell_off, int32_t n_raw, const int32_t* reorder,
                        int32_t n_cells, int32_t nbin, int32_t merge, int32_t off_diag,
                        int32_t* out_idx, float* out_val, int64_t cap, int64_t* out_counts,
                        void* workspace, size_t workspace_bytes, int* status, void* stream);
+
+/* ---- embedding post-processing (FastHigashi.fetch_cell_embedding / correct_batch_linear,
+ * fasthigashi/FastHigashi_Wrapper.py:750-878).  All buffers are device memory.
+ * fh_embed_assemble:  Y[c][j] = sum_l E[c][l] D[l][j] / ||D[:, j]|| (:753-758): D is every
+ *                     chromosome's D (R x r_i) side by side (R x m, row stride ldd);
+ *                     inv_norm: float[m] scratch (receives 1 / ||D[:, j]||).
+ * fh_gemm_scale_f32:  out[i][j] = scale[j] * sum_l A[i][l] B[l][j] (scale optional).
+ * fh_quantile_uniform: the quantile transform of one column (:763, n_quantiles = 100 there)
+ *                     to [0, 1], fp64 in and out.
+ * fh_lstsq_residual:  out = Y minus its least-squares fit on V (double[n_cells][p]) with an
+ *                     intercept, the minimum-norm coefficients (:861-866); the intercept is
+ *                     added back when add_intercept_back != 0.  p <= 256.
+ * fh_range_svd:       out[c][j] = U[c][j] s_j for the top k singular triplets of Y (n_cells x
+ *                     m) whose columns lie in the column space of F (n_cells x r, r <= 256):
+ *                     the truncated SVD of :767-768 and :870-871 (TruncatedSVD.fit_transform,
+ *                     component signs by its rule: each component's largest-magnitude entry
+ *                     positive); sigma (optional): double[k].
+ * fh_l2_rows:         rows scaled to unit Euclidean norm, zero rows unchanged (:778, :873).
+ * fh_cross_f32:       out[i][j] = sum_c A[c][i] B[c][j] in fp64 (A: n_rows x na, B: n_rows x
+ *                     nb), fixed order; init_params' sketch products use it too.
+ * status (fh_lstsq_residual, fh_range_svd): FH_ERR_ILLCOND if an fp64 Jacobi eigen-solve did
+ * not converge. */
+int fh_embed_assemble(const float* E, int32_t n_cells, int32_t R, int64_t lde, const float* D,
+                      int32_t m, int64_t ldd, float* inv_norm, float* Y, int64_t ldy,
+                      void* stream);
+int fh_gemm_scale_f32(const float* A, int64_t lda, const float* B, int64_t ldb,
+                      const float* scale, int32_t n, int32_t m, int32_t K, float* out,
+                      int64_t ldo, void* stream);
+size_t fh_quantile_workspace(int32_t n, int32_t n_quantiles);
+int fh_quantile_uniform(const double* x, int32_t n, int32_t n_quantiles, double* out,
+                        void* workspace, size_t workspace_bytes, void* stream);
+size_t fh_lstsq_workspace(int32_t p, int32_t m);
+int fh_lstsq_residual(const double* V, int32_t n_cells, int32_t p, const float* Y, int64_t ldy,
+                      int32_t m, int32_t add_intercept_back, float* out, int64_t ldo,
+                      void* workspace, size_t workspace_bytes, int* status, void* stream);
+size_t fh_range_svd_workspace(int32_t r, int32_t m, int32_t k);
+int fh_range_svd(const float* F, int64_t ldf, int32_t n_cells, int32_t r, const float* Y,
+                 int64_t ldy, int32_t m, int32_t k, float* out, int64_t ldo, double* sigma,
+                 void* workspace, size_t workspace_bytes, int* status, void* stream);
+int fh_l2_rows(const float* X, int64_t ldx, int32_t n, int32_t m, float* out, int64_t ldo,
+               void* stream);
+int fh_cross_f32(const float* A, int64_t lda, int32_t na, const float* B, int64_t ldb,
+                 int32_t nb, int32_t n_rows, double* out, int64_t ldo, void* stream);
+
+/* ---- imputed contact maps (FastHigashi.only_partial_rwr, FastHigashi_Wrapper.py:569-655):
+ * out[c][i][j] (float[ncell][nbin][nbin]) = M[i][j] + M[j][i] for i != j and M[i][i] on the
+ * diagonal, M[i][j] = the walk output X[cell0 + c] of the tile holding row i at compact
+ * column j - shift (0 outside its columns).  row_tile[row_base + i]: the tile of the
+ * chromosome's row i (tiles as the fit's table); X: float[cells][ldx] in the compact band
+ * layout.  status: FH_ERR_INDEX when row_tile names a tile without row i. */
+int fh_impute_maps(const fh_tile* tiles, const int32_t* row_tile, int64_t row_base,
+                   int32_t nbin, const float* X, int64_t ldx, int32_t cell0, int32_t ncell,
+                   float* out, int* status, void* stream);
 
 /* ---- self-test of the bounded device-side waits (no reference counterpart: the reference
  * has no device code).  One warp allocates tensor memory, waits on an mbarrier that nothing

@@ -134,8 +134,8 @@ def test_rwr_tiles_bf16_planes_are_split_fp32():
     np.testing.assert_allclose(ss.cpu().numpy(), eng.sumsq.cpu().numpy(), rtol=1e-4)
 
 
-@pytest.mark.parametrize("planes", [1, 2])
-def test_rwr_tiles_tc_matches_fp32(planes):
+@pytest.mark.parametrize("planes,form", [(1, 1), (2, 1), (1, 2), (2, 2)])
+def test_rwr_tiles_tc_matches_fp32(planes, form):
     """tcgen05 RWR (split bf16 products) against the fp32 CUDA-core RWR on the golden tiles."""
     from fh_gb300.engine import FitEngine
     z = G.load("rwr_tiles.npz")
@@ -145,7 +145,7 @@ def test_rwr_tiles_tc_matches_fp32(planes):
     ss = torch.zeros_like(eng.sumsq)
     _lib.call("fh_rwr_tiles_tc", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
               eng.max_width, P(eng.store.entries), P(eng.store.offsets), P(X16), eng.ldx,
-              eng.Ct * eng.ldx if planes == 2 else 0, P(ss), P(eng.status), sp())
+              eng.Ct * eng.ldx if planes == 2 else 0, P(ss), form, P(eng.status), sp())
     torch.cuda.synchronize()
     assert int(eng.status.item()) == 0
     got = X16.double().sum(0)
@@ -154,14 +154,18 @@ def test_rwr_tiles_tc_matches_fp32(planes):
     np.testing.assert_allclose(ss.cpu().numpy(), eng.sumsq.cpu().numpy(), rtol=10 * tol)
 
 
-@pytest.mark.parametrize("epochs", [0, 1, 6])
-def test_rwr_tiles_tc_full_tiles(epochs):
-    """125-row bin batches of a 1 Mb genome-like chromosome (widths 145-165), 300 cells."""
+@pytest.mark.parametrize("epochs,band,form", [(0, 20, 1), (1, 20, 1), (6, 20, 1), (0, 20, 2),
+                                              (1, 20, 2), (6, 20, 2), (0, 60, 1), (6, 60, 1)])
+def test_rwr_tiles_tc_full_tiles(epochs, band, form):
+    """Up-to-128-row bin batches of a 1 Mb genome-like chromosome, 300 cells: band 20 (widths
+    up to 168) in both forms, band 60 (widths up to 248) in the form with P in shared memory;
+    the pipelined form refuses it."""
     from fh_gb300 import synth
     from fh_gb300.engine import FitEngine
     from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
     w = synth.workload("c2")
     w.n_cells = 300
+    w.band = band
     w.chrom_bins = w.chrom_bins[:2]
     w.chrom_names = w.chrom_names[:2]
     coo, _ = synth.generate(w, seed=3)
@@ -171,10 +175,13 @@ def test_rwr_tiles_tc_full_tiles(epochs):
     eng = FitEngine(ds, 64, {d.chrom: 64 for d in ds}, [epochs] * len(ds), CUDA)
     X16 = torch.zeros((2, eng.Ct, eng.ldx), dtype=torch.bfloat16, device=CUDA)
     ss = torch.zeros_like(eng.sumsq)
-    _lib.call("fh_rwr_tiles_tc", P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows,
-              eng.max_width, P(eng.store.entries), P(eng.store.offsets), P(X16), eng.ldx,
-              eng.Ct * eng.ldx, P(ss), P(eng.status), sp())
+    args = (P(eng.tiles_dev), eng.n_tiles, eng.Ct, eng.max_rows, eng.max_width,
+            P(eng.store.entries), P(eng.store.offsets), P(X16), eng.ldx, eng.Ct * eng.ldx,
+            P(ss))
+    _lib.call("fh_rwr_tiles_tc", *args, form, P(eng.status), sp())
     torch.cuda.synchronize()
     assert int(eng.status.item()) == 0
     assert rel64(X16.double().sum(0), eng.X.double()) < 1e-4
     assert float(X16[:, :, eng.rows:].abs().max()) == 0.0
+    if band == 60:
+        assert _lib.value("fh_rwr_tiles_tc", *args, 2, P(eng.status), sp()) == 2  # unsupported
