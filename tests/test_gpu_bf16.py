@@ -155,11 +155,11 @@ def test_rwr_tiles_tc_matches_fp32(planes, form):
 
 
 @pytest.mark.parametrize("epochs,band,form", [(0, 20, 1), (1, 20, 1), (6, 20, 1), (0, 20, 2),
-                                              (1, 20, 2), (6, 20, 2), (0, 60, 1), (6, 60, 1)])
+                                              (1, 20, 2), (6, 20, 2), (0, 70, 1), (6, 70, 1)])
 def test_rwr_tiles_tc_full_tiles(epochs, band, form):
-    """Up-to-128-row bin batches of a 1 Mb genome-like chromosome, 300 cells: band 20 (widths
-    up to 168) in both forms, band 60 (widths up to 248) in the form with P in shared memory;
-    the pipelined form refuses it."""
+    """125-row bin batches of a 1 Mb genome-like chromosome, 300 cells: band 20 (widths up to
+    145, padded to 192) in both forms, band 70 (widths up to 195, padded to 256) in the form
+    with P in shared memory; the pipelined form refuses it."""
     from fh_gb300 import synth
     from fh_gb300.engine import FitEngine
     from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
@@ -183,5 +183,6 @@ def test_rwr_tiles_tc_full_tiles(epochs, band, form):
     assert int(eng.status.item()) == 0
     assert rel64(X16.double().sum(0), eng.X.double()) < 1e-4
     assert float(X16[:, :, eng.rows:].abs().max()) == 0.0
-    if band == 60:
+    if band == 70:
+        assert eng.max_width > 192
         assert _lib.value("fh_rwr_tiles_tc", *args, 2, P(eng.status), sp()) == 2  # unsupported
