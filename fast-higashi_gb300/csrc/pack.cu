@@ -23,11 +23,11 @@
 //   pack_mark    band filter, positive-row marks for the bin filter, fp64 coverage partials
 //   pack_cov     per-cell coverage: the cell's partials summed in segment order
 //   (scan)       kept bins -> new ids, then pack_ids: int32 new id or -1
-//   pack_count   entries of each segment that survive the band and the bin filter
+//   pack_count   entries of each segment that survive the band and the bin filter, and the
+//                fp64 moment partials of their values log1p(value * scale)
 //   (scan)       -> each segment's output offset
-//   pack_write   the output entries and values log1p(value * scale), fp64 moment partials
 //   pack_stats   the mean + 15 std threshold (fp64 sums in segment order)
-//   pack_clip    values above the threshold set to it
+//   pack_write   the output entries and values min(log1p(value * scale), threshold)
 // The coverage sum and the moments are accumulated in fp64 where the reference sums fp32 in
 // numpy's order, so values agree with the reference's to an ulp or two, indices exactly.
 // Contact values are taken as non-negative (counts): a bin row is kept when one of its kept
@@ -113,20 +113,27 @@ __device__ __forceinline__ bool pack_band(const PackArgs& a, int r0, int c0, int
     set_status(a.status, FH_ERR_INDEX);
     return false;
   }
-  r = r0 / a.merge;
-  c = c0 / a.merge;
+  if (a.merge == 1) {            // the common case: no division
+    r = r0;
+    c = c0;
+  } else {
+    r = r0 / a.merge;
+    c = c0 / a.merge;
+  }
   const int d = c - r;
   return (d < 0 ? -d : d) <= a.off_diag;
 }
 
 // Output offsets of one chunk of kPackChunk entries in input order: entry base + 256 u + t is
 // kept when keep[u]; its offset within the chunk is the kept entries of rows u' < u plus
-// those of row u before it.  cnt: >= 4 * 8 ints of shared memory.  Returns this thread's
-// offsets for its rows in off[u] and the chunk's kept total.
+// those of row u before it.  The 32 counts (row u, warp w) sit at cnt[8 u + w] in input order;
+// every warp scans them with shuffles (lane i holds count i), so a thread needs one shared
+// load and no loop.  cnt: >= 32 ints of shared memory.  Returns the chunk's kept total.
 __device__ __forceinline__ int pack_chunk_offsets(const bool (&keep)[kPackPer], int* cnt,
                                                   int (&off)[kPackPer]) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   constexpr int kW = kPackThreads / 32;
+  static_assert(kPackPer * kW == 32, "one count per lane");
   unsigned m[kPackPer];
 #pragma unroll
   for (int u = 0; u < kPackPer; ++u) m[u] = __ballot_sync(0xffffffffu, keep[u]);
@@ -138,21 +145,18 @@ __device__ __forceinline__ int pack_chunk_offsets(const bool (&keep)[kPackPer], 
     cnt[lane * kW + w] = __popc(mm);
   }
   __syncthreads();
-  int run = 0, total = 0;
+  const int c = cnt[lane];
+  int x = c;                                 // inclusive scan of the 32 counts
 #pragma unroll
-  for (int u = 0; u < kPackPer; ++u) {
-    int before = 0, row = 0;
-#pragma unroll
-    for (int i = 0; i < kW; ++i) {
-      const int c = cnt[u * kW + i];
-      before += i < w ? c : 0;
-      row += c;
-    }
-    off[u] = run + before + __popc(m[u] & ((1u << lane) - 1u));
-    run += row;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  total = run;
-  return total;
+  const int ex = x - c;                      // exclusive
+#pragma unroll
+  for (int u = 0; u < kPackPer; ++u)
+    off[u] = __shfl_sync(0xffffffffu, ex, u * kW + w) + __popc(m[u] & ((1u << lane) - 1u));
+  return __shfl_sync(0xffffffffu, x, 31);
 }
 
 __global__ void __launch_bounds__(kPackThreads) pack_mark_kernel(PackArgs a) {
@@ -206,43 +210,59 @@ __global__ void pack_ids_kernel(PackArgs a) {
 
 __global__ void __launch_bounds__(kPackThreads) pack_count_kernel(PackArgs a) {
   __shared__ int red[32];
+  __shared__ double dred[32];
   int k;
   int64_t e0, e1;
   if (!pack_segment(a, k, e0, e1)) {
     if (threadIdx.x == 0) a.seg_cnt[blockIdx.x] = 0;
     return;
   }
+  // normalize_by_coverage: scale = bins / total, in fp32 as the reference's float32 arrays
+  const float scale = (float)a.nb / ((float)a.cov[k] + 1e-15f);
   int n = 0;
+  double s1 = 0.0, s2 = 0.0;     // moments of the kept values (the clip threshold's)
   for (int64_t base = e0 + threadIdx.x; base < e1; base += kPackChunk) {
     int r0[kPackPer], c0[kPackPer];
+    float v[kPackPer];
 #pragma unroll
     for (int u = 0; u < kPackPer; ++u) {
       const int64_t e = base + (int64_t)u * kPackThreads;
-      r0[u] = e < e1 ? a.row[e] : 0;
-      c0[u] = e < e1 ? a.col[e] : 0;
+      const bool in = e < e1;
+      r0[u] = in ? a.row[e] : 0;
+      c0[u] = in ? a.col[e] : 0;
+      v[u] = in ? a.val[e] : 0.f;
     }
 #pragma unroll
     for (int u = 0; u < kPackPer; ++u) {
       int r, c;
       if (base + (int64_t)u * kPackThreads < e1 && pack_band(a, r0[u], c0[u], r, c) &&
-          a.new_id[r] >= 0 && a.new_id[c] >= 0)
+          a.new_id[r] >= 0 && a.new_id[c] >= 0) {
         ++n;
+        const float x = log1pf(v[u] * scale);
+        s1 += (double)x;
+        s2 += (double)x * (double)x;
+      }
     }
   }
   n = block_sum<int>(n, red);
-  if (threadIdx.x == 0) a.seg_cnt[blockIdx.x] = n;
+  s1 = block_sum<double>(s1, dred);
+  s2 = block_sum<double>(s2, dred);
+  if (threadIdx.x == 0) {
+    a.seg_cnt[blockIdx.x] = n;
+    a.seg_mom[2 * blockIdx.x] = s1;
+    a.seg_mom[2 * blockIdx.x + 1] = s2;
+  }
 }
 
 __global__ void __launch_bounds__(kPackThreads) pack_write_kernel(PackArgs a) {
   __shared__ int cnt[kPackPer * (kPackThreads / 32)];
-  __shared__ double red[32];
   int k;
   int64_t e0, e1;
   if (!pack_segment(a, k, e0, e1)) return;
   // normalize_by_coverage: scale = bins / total, in fp32 as the reference's float32 arrays
   const float scale = (float)a.nb / ((float)a.cov[k] + 1e-15f);
+  const float thr = *a.thr;      // the mean + 15 std clip, from pack_count's moments
   int64_t pos = a.seg_out[blockIdx.x];
-  double s1 = 0.0, s2 = 0.0;
   // every thread runs the same number of chunks (the offsets' barriers)
   for (int64_t chunk = e0; chunk < e1; chunk += kPackChunk) {
     int nr[kPackPer], nc[kPackPer];
@@ -268,7 +288,7 @@ __global__ void __launch_bounds__(kPackThreads) pack_write_kernel(PackArgs a) {
     for (int u = 0; u < kPackPer; ++u) {
       if (!keep[u]) continue;
       const int64_t o = pos + off[u];
-      const float x = log1pf(v[u] * scale);
+      const float x = fminf(log1pf(v[u] * scale), thr);
       if (o < a.cap) {
         a.out_idx[o] = nr[u];
         a.out_idx[a.cap + o] = nc[u];
@@ -277,16 +297,8 @@ __global__ void __launch_bounds__(kPackThreads) pack_write_kernel(PackArgs a) {
       } else {
         set_status(a.status, FH_ERR_INDEX);
       }
-      s1 += (double)x;
-      s2 += (double)x * (double)x;
     }
     pos += total;
-  }
-  s1 = block_sum<double>(s1, red);
-  s2 = block_sum<double>(s2, red);
-  if (threadIdx.x == 0) {
-    a.seg_mom[2 * blockIdx.x] = s1;
-    a.seg_mom[2 * blockIdx.x + 1] = s2;
   }
 }
 
@@ -314,14 +326,6 @@ __global__ void __launch_bounds__(256) pack_stats_kernel(PackArgs a) {
     }
     *a.thr = t;
   }
-}
-
-__global__ void pack_clip_kernel(PackArgs a) {
-  const int64_t n = a.seg_out[a.max_seg] < a.cap ? a.seg_out[a.max_seg] : a.cap;
-  const float t = *a.thr;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    a.out_val[i] = fminf(a.out_val[i], t);
 }
 
 __global__ void pack_counts_kernel(PackArgs a, int64_t* out_counts) {
@@ -412,11 +416,8 @@ extern "C" int fh_pack_chromosome(const int32_t* row, const int32_t* col, const 
   FH_CHECK_LAUNCH();
   rc = fh_exclusive_scan(a.seg_cnt, ms, a.seg_out, scan_ws, scan_bytes, stream);
   if (rc) return rc;
-  pack_write_kernel<<<(unsigned)ms, kPackThreads, 0, s>>>(a);
   pack_stats_kernel<<<1, 256, 0, s>>>(a);
-  int64_t blocks = ceil_div(cap, 256);
-  if (blocks > 4096) blocks = 4096;
-  pack_clip_kernel<<<(unsigned)blocks, 256, 0, s>>>(a);
+  pack_write_kernel<<<(unsigned)ms, kPackThreads, 0, s>>>(a);
   pack_counts_kernel<<<1, 1, 0, s>>>(a, out_counts);
   FH_CHECK_LAUNCH();
   return FH_OK;

@@ -26,7 +26,10 @@
 // Thread (warp w, lane l) serves row p = 32 (w % 4) + l (the TMEM lane quarter its warp may
 // read) and the column quarter w / 4 (16 warps).  Tiles wider than 256 columns use rwr_f32.cu.
 // The contacts of an item are loaded into registers before its Z init, so their latency
-// overlaps the init (per item, measured with clock stamps at c3 shapes: 3.2k -> 1.1k cycles).
+// overlaps the init (per item, measured with clock stamps at c3 shapes: 3.2k -> 1.1k cycles),
+// and the Z init writes whole 16-byte chunks of the thread's row and column quarter without a
+// division (3.2k -> 2.0k cycles).  Loading two 16-column chunks per tensor-memory wait in the
+// epochs and in the P build measured slower (127 registers; 107 against 105 ms per c3 fit).
 //
 // Form 2 (kPipe, tiles up to 192 columns): P goes to tensor memory (columns 384-511) as the
 // A operand of the epoch products, the epochs are issued per 64-column block of Z with an
@@ -238,22 +241,30 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
       const int64_t e = e0 + tid + (int64_t)u * kRtThreads;
       pre[u] = e < e1 ? a.entries[e] : make_uint2(0u, 0u);
     }
-    // ---- 1. Z = floor on the tile, zero on the padding (both planes)
+    // ---- 1. Z = floor on the tile, zero on the padding (both planes): row p, the thread's
+    // column quarter, 16-byte chunks; only the chunk holding column n is mixed
     {
-      const int cpr = npad / 8;  // 16-byte chunks per row
-      for (int idx = tid; idx < 128 * cpr; idx += kRtThreads) {
-        const int row = idx / cpr, j0 = (idx - row * cpr) * 8;
-        uint32_t hv[4], lv[4];
+      const uint32_t fh2 = pack2(fl_hi, fl_hi), fl2 = pack2(fl_lo, fl_lo);
+      const __nv_bfloat16 zb = __float2bfloat16_rn(0.f);
+      for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 8) {
+        uint4 hv = make_uint4(0u, 0u, 0u, 0u), lv = hv;
+        if (p < b && j0 + 8 <= n) {
+          hv = make_uint4(fh2, fh2, fh2, fh2);
+          lv = make_uint4(fl2, fl2, fl2, fl2);
+        } else if (p < b && j0 < n) {
+          uint32_t h4[4], l4[4];
 #pragma unroll
-        for (int e = 0; e < 8; e += 2) {
-          const bool in0 = row < b && j0 + e < n, in1 = row < b && j0 + e + 1 < n;
-          const __nv_bfloat16 z = __float2bfloat16_rn(0.f);
-          hv[e / 2] = pack2(in0 ? fl_hi : z, in1 ? fl_hi : z);
-          lv[e / 2] = pack2(in0 ? fl_lo : z, in1 ? fl_lo : z);
+          for (int e = 0; e < 8; e += 2) {
+            const bool in0 = j0 + e < n, in1 = j0 + e + 1 < n;
+            h4[e / 2] = pack2(in0 ? fl_hi : zb, in1 ? fl_hi : zb);
+            l4[e / 2] = pack2(in0 ? fl_lo : zb, in1 ? fl_lo : zb);
+          }
+          hv = make_uint4(h4[0], h4[1], h4[2], h4[3]);
+          lv = make_uint4(l4[0], l4[1], l4[2], l4[3]);
         }
-        const uint32_t off = sw_off(row, j0);
-        *reinterpret_cast<uint4*>(Zhi + off) = make_uint4(hv[0], hv[1], hv[2], hv[3]);
-        *reinterpret_cast<uint4*>(Zlo + off) = make_uint4(lv[0], lv[1], lv[2], lv[3]);
+        const uint32_t off = sw_off(p, j0);
+        *reinterpret_cast<uint4*>(Zhi + off) = hv;
+        *reinterpret_cast<uint4*>(Zlo + off) = lv;
       }
     }
     __syncthreads();
@@ -532,7 +543,7 @@ __global__ void __launch_bounds__(kRtThreads, 1) rwr_tc_kernel(RtArgs a) {
         for (int j0 = h * hw; j0 < (h + 1) * hw; j0 += 16) {
           float d[16], av[16], z[16];
           tmem_ld16x2(tD + j0, tA + j0, d, av);
-  #pragma unroll
+#pragma unroll
           for (int e = 0; e < 16; ++e) z[e] = fmaf(0.5f, d[e], 0.5f * av[e]);
           if (last) {
             emit(j0, z);

@@ -125,7 +125,7 @@ _KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_exclusive_scan_n
             "fh_recon_loss_bwd_f32": 4, "fh_factor_grad_f32": 2, "fh_rwr_col_tiles": 1,
             "fh_rwr_col_dense": 1, "fh_col_coverage": 1, "fh_col_coverage_finalize": 1,
             "fh_polar_f32": 1, "fh_polar_svals_f32": 1, "fh_meta_polar": 5, "fh_core_norm": 2,
-            "fh_selftest_wait": 1, "fh_pack_chromosome": 19,
+            "fh_selftest_wait": 1, "fh_pack_chromosome": 18,
             "fh_embed_assemble": 2, "fh_gemm_scale_f32": 1, "fh_quantile_uniform": 3,
             "fh_lstsq_residual": 7, "fh_range_svd": 13, "fh_l2_rows": 1,
             "fh_impute_maps": 1, "fh_cross_f32": 1}
