@@ -109,6 +109,8 @@ SIGNATURES = {
     "fh_l2_rows": (C.c_int, [P, I64, I32, I32, P, I64, P]),
     "fh_impute_maps": (C.c_int, [P, P, I64, I32, P, I64, I32, I32, P, P, P]),
     "fh_cross_f32": (C.c_int, [P, I64, I32, P, I64, I32, I32, P, I64, P]),
+    "fh_pool_rows": (C.c_int, [P, I32, P, P, I64, P, I64, I32, P, I64, P]),
+    "fh_unpool_rows": (C.c_int, [P, I32, P, P, I64, I64, P, I64, I32, P, I64, P]),
     "fh_pack_chromosome": (C.c_int, [P, P, P, P, I32, P, I32, I32, I32, I32, P, P, I64, P, P,
                                      SZ, P, P]),
 }
@@ -128,7 +130,8 @@ _KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_exclusive_scan_n
             "fh_selftest_wait": 1, "fh_pack_chromosome": 18,
             "fh_embed_assemble": 2, "fh_gemm_scale_f32": 1, "fh_quantile_uniform": 3,
             "fh_lstsq_residual": 7, "fh_range_svd": 13, "fh_l2_rows": 1,
-            "fh_impute_maps": 1, "fh_cross_f32": 1}
+            "fh_impute_maps": 1, "fh_cross_f32": 1, "fh_pool_rows": 1,
+            "fh_unpool_rows": 1}
 launches = 0
 
 

@@ -75,9 +75,10 @@ class FitEngine:
         for d in schic:
             if d.chrom not in self.names:
                 self.names.append(d.chrom)
-        if len(self.names) != len(schic):
-            raise _lib.FHError("FitEngine", 2, "one dataset per chromosome (single resolution)")
         self.chrom_index = [self.names.index(d.chrom) for d in schic]
+        # several resolutions: the datasets of a chromosome share its B and D, its CP-ALS runs
+        # on their bin rows together, and the per-dataset losses need per-dataset core norms
+        self.multi = len(self.names) != len(schic)
         self.ranks = [int(chrom2size[d.chrom]) for d in schic]
         if max(self.ranks) > 128 or self.R > 128:
             raise _lib.FHError("FitEngine", 2, "ranks above 128 are not supported")
@@ -443,8 +444,9 @@ class FitEngine:
         return out
 
     def projected_views(self):
-        return {self.schic[k].chrom: self.Y[self.ds_rows[k], :self.ranks[k], :self.R]
-                for k in range(len(self.schic))}
+        """projected_tensor_list: Y per chromosome over all its datasets' bin rows."""
+        return {n: self.Y[self.chrom_rows(ci), :self.ranks[self.chrom_index.index(ci)], :self.R]
+                for ci, n in enumerate(self.names)}
 
     # ------------------------------------------------------------------ kernels
     def xe(self):
@@ -494,6 +496,50 @@ class FitEngine:
             "fh_project_y_f32", P(self.tiles_dev), P(self.row_tile), self.nb, P(self.U),
             P(self.W), self.rp, P(self.Y), self.ld, self.sp()))
 
+    def chrom_rows(self, ci):
+        """Bin rows of chromosome ci: its datasets' rows, adjacent in the row order."""
+        ks = [k for k in range(len(self.schic)) if self.chrom_index[k] == ci]
+        start = min(self.ds_rows[k].start for k in ks)
+        stop = max(self.ds_rows[k].stop for k in ks)
+        if stop - start != sum(self.ds_rows[k].stop - self.ds_rows[k].start for k in ks):
+            raise _lib.FHError("FitEngine", 2, "a chromosome's datasets are not adjacent")
+        return slice(start, stop)
+
+    def dataset_cores(self):
+        """core[k] = ||[[A_k, B, D]]||^2 per dataset (parafac2_intergrative.py:697-706) when a
+        chromosome has several datasets: fh_core_norm over a table of the datasets' rows, with
+        each dataset's B and D gathered from its chromosome's."""
+        torch, P = self.torch, _lib.ptr
+        if not hasattr(self, "_ds_core"):
+            n = len(self.schic)
+            c_row0, c_nbin, c_rank, c_chunk0, c_nchunk = [], [], [], [], []
+            k_chrom, k_row0, k_nrow = [], [], []
+            for k in range(n):
+                rs = self.ds_rows[k]
+                c_row0.append(rs.start); c_nbin.append(rs.stop - rs.start)
+                c_rank.append(self.ranks[k]); c_chunk0.append(len(k_chrom))
+                for r0 in range(rs.start, rs.stop, 8):
+                    k_chrom.append(k); k_row0.append(r0); k_nrow.append(min(8, rs.stop - r0))
+                c_nchunk.append(len(k_chrom) - c_chunk0[-1])
+            meta = np.array(c_row0 + c_nbin + c_rank + c_chunk0 + c_nchunk + k_chrom + k_row0 +
+                            k_nrow, dtype=np.int32)
+            idx = torch.as_tensor(self.chrom_index, dtype=torch.long, device=self.device)
+            ws = torch.empty(_lib.value("fh_cp_workspace", n, len(k_chrom), self.ld, self.rp),
+                             dtype=torch.uint8, device=self.device)
+            self._ds_core = dict(meta=torch.from_numpy(meta).to(self.device), nch=len(k_chrom),
+                                 idx=idx, ws=ws,
+                                 B=torch.zeros((n, self.ld, self.ld), dtype=torch.float32,
+                                               device=self.device),
+                                 D=torch.zeros((n, self.rp, self.ld), dtype=torch.float32,
+                                               device=self.device))
+            self.core_ds = torch.zeros(n, dtype=torch.float64, device=self.device)
+        c = self._ds_core
+        torch.index_select(self.B, 0, c["idx"], out=c["B"])
+        torch.index_select(self.D, 0, c["idx"], out=c["D"])
+        _lib.call("fh_core_norm", len(self.schic), c["nch"], P(c["meta"]), P(self.A), P(c["B"]),
+                  P(c["D"]), P(self.Y), self.ld, self.rp, self.R, self.ld, P(self.core_ds),
+                  P(c["ws"]), c["ws"].numel(), P(self.status), self.sp())
+
     def cp_table(self, rows):
         """CP-ALS chunk table: chunks of <= rows bin rows inside one chromosome, as the int32
         meta block of fh_cp_als (cached per size).  Returns (device tensor, number of chunks)."""
@@ -502,7 +548,7 @@ class FitEngine:
             k_chrom, k_row0, k_nrow = [], [], []
             for ci, name in enumerate(self.names):
                 k = self.chrom_index.index(ci)
-                rs = self.ds_rows[k]
+                rs = self.chrom_rows(ci)
                 c_row0.append(rs.start); c_nbin.append(rs.stop - rs.start)
                 c_rank.append(self.ranks[k]); c_chunk0.append(len(k_chrom))
                 for r0 in range(rs.start, rs.stop, rows):
@@ -566,8 +612,10 @@ class FitEngine:
         self.update(first)
         hist["ssum"].copy_(self.ssum)
         hist["meta"].copy_(self.meta_ssum)
-        hist["core"].copy_(self.core)
+        hist["core"].copy_(self.core_ds if self.multi else self.core)
         self.cp_als(n_iter_parafac)
+        if self.multi:
+            self.dataset_cores()
 
     @staticmethod
     def parafac_schedule(n_iter, n_iter_parafac):
@@ -621,12 +669,15 @@ class FitEngine:
         _lib.call("fh_core_norm", len(self.names), self.nchunks, P(self.cp_meta), P(self.A),
                   P(self.B), P(self.D), P(self.Y), self.ld, self.rp, self.R, self.ld,
                   P(self.core), P(self.cp_ws), self.cp_ws.numel(), P(self.status), self.sp())
+        if self.multi:
+            self.dataset_cores()
 
     def new_history(self, n):
         torch = self.torch
         return [dict(ssum=torch.zeros(self.nb, dtype=torch.float64, device=self.device),
                      meta=torch.zeros(1, dtype=torch.float64, device=self.device),
-                     core=torch.zeros(len(self.names), dtype=torch.float64, device=self.device))
+                     core=torch.zeros(len(self.schic) if self.multi else len(self.names),
+                                      dtype=torch.float64, device=self.device))
                 for _ in range(n)]
 
     def losses(self, hist, tnorm):
@@ -634,7 +685,8 @@ class FitEngine:
         ssum = hist["ssum"].cpu().numpy()
         core = hist["core"].cpu().numpy()
         xU = np.array([ssum[self.ds_rows[k]].sum() for k in range(len(self.schic))])
-        core_ds = np.array([core[self.chrom_index[k]] for k in range(len(self.schic))])
+        core_ds = core if self.multi else np.array([core[self.chrom_index[k]]
+                                                    for k in range(len(self.schic))])
         by_block = tnorm + core_ds - 2 * xU
         rec_V = tnorm.sum() + core_ds.sum() - 2 * float(hist["meta"].item())
         norm_tensor = np.sqrt(tnorm)

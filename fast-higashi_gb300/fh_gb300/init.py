@@ -16,8 +16,9 @@
    they are at most 256 columns wide, else from a randomized range of R + 10 columns (three
    power iterations, each re-orthonormalised) that fh_range_svd resolves; D = E^T [features]
    by the fp64 fh_cross_f32.  Nothing of the factorization runs on the host.
-At resolutions finer than 1 Mb the reference pools the features to 1 Mb first; this
-restatement sketches the unpooled band features.
+At resolutions finer than 1 Mb the features are pooled to 1 Mb first as the reference pools
+them (ll x ll block means of every tile, :102-151), through fh_pool_rows / fh_unpool_rows on the
+sketch's products.
 With do_col (and do_rwr) the coverage rows bin_cov come first (:96-200): 1e-4 plus the
 column sums of the auto-stopped plain walk, every cell batch (good and bad) stopping on its
 own; the features are then the do_col walk's output with the same per-batch epochs
@@ -86,23 +87,25 @@ def auto_epochs(eng, schic, per_cell=False):
     return (n_i, feat_epochs, cell_ep) if per_cell else (n_i, feat_epochs)
 
 
-def _chrom_band_rows(eng, k):
-    t0 = eng.tile_base[k]
-    d = eng.schic[k]
+def _chrom_band_rows(eng, ks):
+    """Band rows of X holding the datasets ks (one chromosome's resolutions, adjacent)."""
     t = eng.tiles
-    x0 = int(t["xoff"][t0])
-    last = t0 + d.num_bin_batch - 1
-    x1 = int(t["xoff"][last] + t["rows"][last] * t["width"][last])
+    x0 = min(int(t["xoff"][eng.tile_base[k]]) for k in ks)
+    x1 = 0
+    for k in ks:
+        last = eng.tile_base[k] + eng.schic[k].num_bin_batch - 1
+        x1 = max(x1, int(t["xoff"][last] + t["rows"][last] * t["width"][last]))
     return x0, x1
 
 
-def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
-    """U_k S_k (cells x n_comp) of chromosome k's band features F (cells x band rows).
-    The sketch's n_comp + n_oversamples columns go through the X passes in blocks of at most
-    128 (the passes' widest operand)."""
+def randomized_features(eng, ks, n_comp, rng, n_oversamples=10, n_iter=2):
+    """U_k S_k (cells x n_comp) of one chromosome's band features F (cells x band rows of its
+    datasets ks, every resolution side by side, as the reference concatenates a chromosome's
+    features across resolutions).  The sketch's n_comp + n_oversamples columns go through the
+    X passes in blocks of at most 128 (the passes' widest operand)."""
     torch = eng.torch
     C = eng.C
-    x0, x1 = _chrom_band_rows(eng, k)
+    x0, x1 = _chrom_band_rows(eng, ks)
     a0 = (x0 // 128) * 128
     a1 = min(eng.ldx, int(math.ceil(x1 / 128) * 128))
     rows = a1 - a0
@@ -143,6 +146,13 @@ def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
             out.append(S[:, :c1 - c0].clone())
         return torch.cat(out, dim=1)
 
+    # the 1 Mb pooling (:102-151): features of a dataset finer than 1 Mb are its tiles' ll x ll
+    # block means; the sketch works in pooled rows through Pm^T (after F^T E) and Pm (before F Q)
+    pool = _pooling(eng, ks)
+    if pool is not None:
+        ft_plain, f_plain = ft_times, f_times
+        ft_times = lambda Ecells: pool.pool(ft_plain(Ecells))
+        f_times = lambda Qp: f_plain(pool.unpool(Qp))
     omega = torch.from_numpy(rng.standard_normal((C, n)).astype(np.float32)).to(dev)
     # range of F^T (band rows x n), re-orthonormalised after every product (F and F^T alike)
     # so that the power iterations keep the sketch's conditioning at that of F
@@ -156,6 +166,61 @@ def randomized_features(eng, k, n_comp, rng, n_oversamples=10, n_iter=2):
     if k < n_comp:
         emb = torch.cat([emb, torch.zeros((C, n_comp - k), dtype=f32, device=dev)], dim=1)
     return emb
+
+
+class _Pool:
+    """The pooling maps of one chromosome's tiles (fh_pool_rows / fh_unpool_rows)."""
+
+    def __init__(self, eng, t0, t1, lls, x0, x1):
+        torch = eng.torch
+        t = eng.tiles
+        pr = [0]
+        for k in range(t0, t1):
+            ll = lls[k - t0]
+            pr.append(pr[-1] + (int(t["rows"][k]) // ll) * (int(t["width"][k]) // ll))
+        self.n = t1 - t0
+        self.prows = pr[-1]
+        self.x0, self.rows = x0, x1 - x0
+        self.prow0 = torch.as_tensor(np.asarray(pr, dtype=np.int64)).to(eng.device)
+        self.ll = torch.as_tensor(np.asarray(lls, dtype=np.int32)).to(eng.device)
+        self.tiles = _lib.ptr(eng.tiles_dev) + t0 * _lib.TILE_DTYPE.itemsize
+        self.dev = eng.device
+        self.torch = torch
+
+    def pool(self, W):
+        W = W.contiguous()
+        out = self.torch.empty((self.prows, W.shape[1]), dtype=self.torch.float32,
+                               device=self.dev)
+        P = _lib.ptr
+        _lib.call("fh_pool_rows", self.tiles, self.n, P(self.prow0), P(self.ll), self.x0, P(W),
+                  W.shape[1], W.shape[1], P(out), W.shape[1], _lib.stream_ptr())
+        return out
+
+    def unpool(self, Qp):
+        Qp = Qp.contiguous()
+        out = self.torch.empty((self.rows, Qp.shape[1]), dtype=self.torch.float32,
+                               device=self.dev)
+        P = _lib.ptr
+        _lib.call("fh_unpool_rows", self.tiles, self.n, P(self.prow0), P(self.ll), self.x0,
+                  self.rows, P(Qp), Qp.shape[1], Qp.shape[1], P(out), Qp.shape[1],
+                  _lib.stream_ptr())
+        return out
+
+
+def _pooling(eng, ks):
+    """The pooling of datasets ks (one chromosome) when one of them is finer than 1 Mb, else
+    None.  ll = ceil(1 Mb / resolution) per dataset (:110)."""
+    lls_ds = [int(math.ceil(1000000 / eng.schic[k].resolution)) for k in ks]
+    if max(lls_ds) <= 1:
+        return None
+    t0 = min(eng.tile_base[k] for k in ks)
+    t1 = max(eng.tile_base[k] + eng.schic[k].num_bin_batch for k in ks)
+    lls = []
+    for tt in range(t0, t1):
+        k = next(k for k in ks if eng.tile_base[k] <= tt < eng.tile_base[k] + eng.schic[k].num_bin_batch)
+        lls.append(max(1, int(math.ceil(1000000 / eng.schic[k].resolution))))
+    x0, x1 = _chrom_band_rows(eng, ks)
+    return _Pool(eng, t0, t1, lls, x0, x1)
 
 
 def orthonormal_columns(Q, rel=1e-7):
@@ -248,10 +313,11 @@ def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
     rng = np.random.default_rng(seed)
     feats, cols = [], []
     start = 0
-    for k, d in enumerate(schic):
-        f = randomized_features(eng, k, sizes[d.chrom], rng)
+    for ci, name in enumerate(eng.names):
+        ks = [k for k in range(len(schic)) if eng.chrom_index[k] == ci]
+        f = randomized_features(eng, ks, sizes[name], rng)
         feats.append(f)
-        cols.append((d.chrom, start, start + f.shape[1]))
+        cols.append((name, start, start + f.shape[1]))
         start += f.shape[1]
     Call = torch.cat(feats, dim=1).contiguous()            # cells x sum(r), on the device
     R = min(rank, Call.shape[1])

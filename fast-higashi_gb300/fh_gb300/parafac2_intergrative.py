@@ -10,8 +10,10 @@ Supported options: do_rwr True/False, do_conv True/False (the 3 x 3 mean of
 partial_rwr.py:79-83 runs on the fp32 CUDA-core walk in every precision form), do_col
 True/False (the column-normalised walk of partial_rwr.py:131-138 on fp32 CUDA cores, with the
 coverage rows bin_cov_list / bad_bin_cov_list that init_params computes or the caller
-assigns), one resolution, ranks r <= R <= 128 with at least r compact columns in every bin
-batch.  Anything else raises NotImplementedError or FHError.
+assigns), one or several resolutions (res_list: the datasets of a chromosome share its B and
+D, and its CP-ALS runs on their bin rows together, parafac2_intergrative.py:558-590, 674-706),
+ranks r <= R <= 128 with at least r compact columns in every bin batch.  Anything else raises
+NotImplementedError or FHError.
 """
 from __future__ import annotations
 

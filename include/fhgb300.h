@@ -455,6 +455,19 @@ int fh_impute_maps(const fh_tile* tiles, const int32_t* row_tile, int64_t row_ba
                    int32_t nbin, const float* X, int64_t ldx, int32_t cell0, int32_t ncell,
                    float* out, int* status, void* stream);
 
+/* ---- the 1 Mb pooling of init_params' features (parafac2_intergrative.py:102-151): for the
+ * n_tiles consecutive tiles at tiles (one chromosome's datasets), block (py, px) of tile t is
+ * pooled row prow0[t] + py * (width_t / ll_t) + px (prow0: int64[n_tiles + 1]), the mean of
+ * band rows xoff_t + (py ll + dy) width_t + px ll + dx (dy, dx < ll_t); rows are counted from
+ * band row x0.  fh_pool_rows: out (pooled rows x m) = Pm^T in (band rows x m);
+ * fh_unpool_rows: out (rows x m) = Pm in (pooled rows x m), zero on the cropped remainders. */
+int fh_pool_rows(const fh_tile* tiles, int32_t n_tiles, const int64_t* prow0,
+                 const int32_t* ll, int64_t x0, const float* in, int64_t ldi, int32_t m,
+                 float* out, int64_t ldo, void* stream);
+int fh_unpool_rows(const fh_tile* tiles, int32_t n_tiles, const int64_t* prow0,
+                   const int32_t* ll, int64_t x0, int64_t rows, const float* in, int64_t ldi,
+                   int32_t m, float* out, int64_t ldo, void* stream);
+
 /* ---- self-test of the bounded device-side waits (no reference counterpart: the reference
  * has no device code).  One warp allocates tensor memory, waits on an mbarrier that nothing
  * arrives on until limit_ns of device time pass, sets *status = FH_ERR_TIMEOUT, frees the

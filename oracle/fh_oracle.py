@@ -410,8 +410,9 @@ class ALSOracle:
         return U_all, Y, err_x_U, err_x_V, tnorm
 
     def iterate(self, iteration, n_iter_parafac=1):
-        """One iteration of the fit loop (parafac2_intergrative.py:635-737).  Datasets are one
-        per chromosome (single resolution), so the per-chromosome Y is the dataset's Y."""
+        """One iteration of the fit loop (parafac2_intergrative.py:635-737).  The datasets of a
+        chromosome (one per resolution) share its B and D: its CP-ALS runs on their Y stacked
+        along the bins, in dataset order, and the A rows go back to each dataset (:674-695)."""
         first = self.norm_tensor is None
         U_all, Y, err_x_U, err_x_V, tnorm = self.update(first_iter=first)
         self.U_last = U_all                      # the projections transform reuses (:750)
@@ -421,11 +422,21 @@ class ALSOracle:
             self.norm_tensor_all = float(np.linalg.norm(self.norm_tensor))
         by_block = self.tensor_norm + self.core_norm - 2 * err_x_U
         rec_V = self.tensor_norm.sum() + self.core_norm.sum() - 2 * err_x_V
+        groups = {}
         for ci, d in enumerate(self.datas):                              # :674-695
-            r = self.size[d.name]
-            f, _, _ = parafac(Y[ci], rank=r, n_iter_max=n_iter_parafac,
-                              init=[self.A_list[ci], self.B[d.name], self.D[d.name]], dtype=self.dt)
-            self.A_list[ci], self.B[d.name], self.D[d.name] = f
+            groups.setdefault(d.name, []).append(ci)
+        for name, ids in groups.items():
+            r = self.size[name]
+            Yc = np.concatenate([Y[ci] for ci in ids], axis=0)
+            Ac = np.concatenate([self.A_list[ci] for ci in ids], axis=0)
+            f, _, _ = parafac(Yc, rank=r, n_iter_max=n_iter_parafac,
+                              init=[Ac, self.B[name], self.D[name]], dtype=self.dt)
+            off = 0
+            for ci in ids:
+                nb = self.datas[ci].num_bin
+                self.A_list[ci] = f[0][off:off + nb]
+                off += nb
+            self.B[name], self.D[name] = f[1], f[2]
         self.core_norm = self._core_norm()                                # :697-706
         rec = math.sqrt(rec_V) / self.norm_tensor_all                     # :710
         self.rec_errors_total.append(rec)

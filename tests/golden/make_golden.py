@@ -31,6 +31,9 @@ Every output is produced by the reference's own functions on seeded synthetic in
                    on seeded raw per-cell contact matrices of two chromosomes (some bins empty in
                    every cell, contacts past the band, a cell order to apply), with merge
                    factors 1 and 2: the packed (row, col, cell) indices, values and shape.
+  als_multires_small.npz  the small workload's chromosomes at 1 Mb and at 500 kb under the same
+                   names, fitted with res_list=[1 Mb, 500 kb] (B and D shared per chromosome):
+                   init, trajectory, final state, transform.
   impute.npz       FastHigashi.only_partial_rwr (FastHigashi_Wrapper.py:569-655): every
                    cell's imputed map of the tiny workload (12-row bin batches, cell batches
                    of 10, 6 bad-QC cells, a cell order), with and without do_conv.
@@ -46,7 +49,7 @@ Every output is produced by the reference's own functions on seeded synthetic in
                    with do_col=False / True (the latter with bin_cov and bad_bin_cov).
 
     FH_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py \
-        rwr_conv als_conv rwr_col als_col als_bad als_defaults pack postprocess impute
+        rwr_conv als_conv rwr_col als_col als_bad als_defaults pack postprocess impute multires
 """
 import copy
 import os
@@ -333,6 +336,50 @@ def make_impute():
     print("impute", {k: v.shape for k, v in out.items() if "maps" in k})
 
 
+def make_multires():
+    """als_multires_small.npz: the small workload's three chromosomes at 1 Mb and, under the
+    same names, an independent draw at 500 kb (twice the bins), fitted together with
+    res_list=[1 Mb, 500 kb]: six datasets, B and D shared by the two resolutions of a
+    chromosome.  The reference's init, its 4-iteration trajectory and final state, and
+    transform's embedding."""
+    import dataclasses
+    w1 = synth.workload("small")
+    w2 = dataclasses.replace(w1, name="small500", chrom_bins=[2 * b for b in w1.chrom_bins],
+                             resolution=500_000, chrom_names=list(w1.chrom_names))
+    coo1, _ = synth.generate(w1, seed=3)
+    coo2, _ = synth.generate(w2, seed=4)
+    n = len(coo1)
+    ds = (build_chrom_datasets(ref, coo1, w1.chrom_names, [25] * n, [40] * n, w1.band,
+                               w1.resolution) +
+          build_chrom_datasets(ref, coo2, w2.chrom_names, [25] * n, [40] * n, w2.band,
+                               w2.resolution))
+    res_list = [w1.resolution, w2.resolution]
+    np.random.seed(5)
+    torch.manual_seed(5)
+    m = core.Fast_Higashi_core(rank=w1.rank, off_diag=w1.band, res_list=res_list).to(CPU)
+    m.fit(ds, size_ratio=w1.dim1, n_iter_max=0, n_iter_parafac=1, do_conv=False, do_rwr=True,
+          do_col=False, tol=0, run_init=True)
+    st0 = snapshot(m)
+    out = coo_arrays("in", coo1 + coo2)
+    out.update(state_arrays("init", st0, w1.chrom_names))
+    out.update(n_chrom=2 * n, names=np.asarray(w1.chrom_names + w2.chrom_names),
+               res=np.asarray([w1.resolution] * n + [w2.resolution] * n, dtype=np.int64),
+               bs_bin=25, bs_cell=40, flank=w1.band, rank=w1.rank, dim1=w1.dim1, n_iter=4,
+               sizes=np.asarray([m.chrom2size[c] for c in w1.chrom_names]))
+    m2 = core.Fast_Higashi_core(rank=w1.rank, off_diag=w1.band, res_list=res_list).to(CPU)
+    inject(m2, st0)
+    with FitLocals() as fl:
+        m2.fit(ds, size_ratio=w1.dim1, n_iter_max=4, n_iter_parafac=1, do_conv=False,
+               do_rwr=True, do_col=False, tol=0, run_init=False)
+    res = m2.transform(ds, False, True, False)
+    out["fit_rec_total"] = np.asarray(fl.locals["rec_errors_total"], dtype=np.float64)
+    out["fit_rec_block"] = np.stack([np.asarray(x).ravel() for x in fl.locals["rec_errors"]])
+    out.update(state_arrays("fit", snapshot(m2), w1.chrom_names))
+    out["fit_E_transform"] = res[1][3].numpy()
+    np.savez_compressed(os.path.join(HERE, "als_multires_small.npz"), **out)
+    print("multires rec trajectory", out["fit_rec_total"], "blocks", out["fit_rec_block"].shape)
+
+
 def make_parafac():
     rng = np.random.default_rng(5)
     X = rng.standard_normal((40, 6, 9)).astype(np.float32)
@@ -475,6 +522,8 @@ if __name__ == "__main__":
             make_postprocess()
         if "impute" in only:
             make_impute()
+        if "multires" in only:
+            make_multires()
         if "als_defaults" in only:
             make_als("als_defaults_small.npz", "small", 25, 40, 4, seed=3, do_conv=True,
                      do_rwr=False)
@@ -497,3 +546,4 @@ if __name__ == "__main__":
     make_pack()
     make_postprocess()
     make_impute()
+    make_multires()

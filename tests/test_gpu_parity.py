@@ -403,3 +403,44 @@ def test_fit_trajectory(fixture, n_iter, ref_tol, conv, col):
     print(fixture, "transform embedding error against FP64 (ours, reference):", e_ours, e_ref)
     assert e_ours < 1e-3 and e_ours < max(1e-5, 2 * e_ref)
     assert O.rel_err(O.procrustes_align(Et, Et_ref), Et_ref) < e_ours + e_ref + 1e-6
+
+
+def test_multiresolution_fit_matches_reference_and_oracle():
+    """res_list = [1 Mb, 500 kb] (parafac2_intergrative.py:558-590, 674-706): six datasets,
+    each chromosome's two resolutions sharing B and D, from the reference's init.  The loss
+    trajectory and per-dataset block errors against the FP64 oracle (1e-5) and the reference
+    (its fp32 error), the fitted embedding and transform's, aligned, against both."""
+    from fh_gb300 import Fast_Higashi_core
+    from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
+    z = G.load("als_multires_small.npz")
+    names = [str(s) for s in z["names"]]
+    ds = [Chrom_Dataset(Sparse(idx, val, shape), int(z["bs_bin"]), int(z["bs_cell"]),
+                        compact=True, flank=int(z["flank"]), chrom=names[k],
+                        resolution=int(z["res"][k]))
+          for k, (idx, val, shape) in enumerate(G.coo_list(z))]
+    A, B, D, E, n_i = G.multires_state(z, "init")
+    m = Fast_Higashi_core(int(z["rank"]), int(z["flank"]), sorted(set(int(r) for r in z["res"]),
+                                                                 reverse=True)).to(CUDA)
+    m._sizes(ds, float(z["dim1"]), None)
+    m.A_list = [torch.from_numpy(a) for a in A]
+    m.B_dict = {k: torch.from_numpy(v) for k, v in B.items()}
+    m.D_dict = {k: torch.from_numpy(v) for k, v in D.items()}
+    m.meta_embedding = torch.from_numpy(E)
+    m.n_i = np.asarray(n_i)
+    m.bin_cov_list = [None] * len(ds)
+    n_iter = int(z["n_iter"])
+    m.fit(ds, size_ratio=float(z["dim1"]), n_iter_max=n_iter, n_iter_parafac=1, do_conv=False,
+          do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
+    orc = O.ALSOracle(G.multires_datas(z, O), int(z["rank"]), A, B, D, E, n_i).fit(n_iter)
+    np.testing.assert_allclose(m.rec_errors_total, orc.rec_errors_total, rtol=1e-5)
+    np.testing.assert_allclose(np.stack(m.rec_errors), np.stack(orc.rec_errors), rtol=1e-5)
+    np.testing.assert_allclose(m.rec_errors_total, z["fit_rec_total"], rtol=1e-4)
+    Eg = m.meta_embedding.cpu().numpy()
+    assert O.rel_err(O.procrustes_align(Eg, orc.E), orc.E) < 1e-4
+    assert set(m.projected_tensor_list) == set(names)
+    for c in set(names):
+        nb = sum(d.num_bin for d in ds if d.chrom == c)
+        assert m.projected_tensor_list[c].shape[0] == nb
+    Et = m.transform(ds, False, True, False)[1][3].cpu().numpy()
+    Et_o = orc.transform(orc.U_last)
+    assert O.rel_err(O.procrustes_align(Et, Et_o), Et_o) < 1e-3

@@ -241,3 +241,17 @@ def test_only_partial_rwr_matches_reference(conv, dtype, tol):
         assert tuple(z["conv%d_shape%d" % (int(conv), k)]) == (d.num_bin, d.num_bin)
         got = np.stack([maps[c] for c in range(ref.shape[0])])
         assert O.rel_err(got, ref) < tol
+
+
+def test_multiresolution_fit_matches_reference():
+    """res_list = [1 Mb, 500 kb] (parafac2_intergrative.py:558-590, 674-695): each chromosome's
+    two datasets share B and D; its CP-ALS runs on their projected tensors stacked along the
+    bins.  The trajectory, the per-dataset block errors and the fitted embedding."""
+    z = G.load("als_multires_small.npz")
+    datas = G.multires_datas(z, O)
+    A, B, D, E, n_i = G.multires_state(z, "init")
+    orc = O.ALSOracle(datas, int(z["rank"]), A, B, D, E, n_i).fit(int(z["n_iter"]))
+    np.testing.assert_allclose(orc.rec_errors_total, z["fit_rec_total"], rtol=1e-4)
+    np.testing.assert_allclose(np.stack(orc.rec_errors), z["fit_rec_block"], rtol=1e-4)
+    _, _, _, Ef, _ = G.multires_state(z, "fit")
+    assert O.rel_err(O.procrustes_align(orc.E, Ef), Ef) < 1e-3
