@@ -158,9 +158,28 @@ __global__ void densify_tile_kernel(const fh_tile* __restrict__ tiles, int t, in
   }
 }
 
+// x[i] += *base for i < n: chains a scan of one dataset's counts onto the previous dataset's
+// total, read on the device (no host round trip).
+__global__ void scan_add_base_kernel(int64_t* __restrict__ x, int64_t n,
+                                     const int64_t* __restrict__ base) {
+  const int64_t b = *base;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += b;
+}
+
 }  // namespace fh
 
 using namespace fh;
+
+extern "C" int fh_scan_add_base(int64_t* x, int64_t n, const int64_t* base, void* stream) {
+  if (!x || !base || n <= 0) return FH_ERR_ARG;
+  int64_t grid = ceil_div(n, 256);
+  if (grid > 152 * 8) grid = 152 * 8;
+  scan_add_base_kernel<<<(unsigned)grid, 256, 0, (cudaStream_t)stream>>>(x, n, base);
+  FH_CHECK_LAUNCH();
+  return FH_OK;
+}
 
 extern "C" int fh_densify_tile(const fh_tile* tiles, int32_t t, int32_t n_cells, int32_t c0,
                                int32_t ncell, const int64_t* offsets, const fh_entry* entries,

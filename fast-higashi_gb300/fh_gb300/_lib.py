@@ -46,6 +46,7 @@ SIGNATURES = {
     "fh_version": (C.c_int, []),
     "fh_contacts_count": (C.c_int, [P, P, P, I64, I32, P, I32, I32, I32, P, P, P]),
     "fh_scan_workspace": (SZ, [I64]),
+    "fh_scan_add_base": (C.c_int, [P, I64, P, P]),
     "fh_exclusive_scan": (C.c_int, [P, I64, P, P, SZ, P]),
     "fh_exclusive_scan_noalloc": (C.c_int, [P, I64, P, P]),
     "fh_contacts_scatter": (C.c_int, [P, P, P, P, I64, I32, P, I32, I32, I32, P, P, P, P]),
@@ -116,7 +117,7 @@ SIGNATURES = {
 }
 
 # kernels each entry point launches (the count the benchmark reports as gpu_launches)
-_KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_exclusive_scan_noalloc": 3, "fh_contacts_scatter": 1,
+_KERNELS = {"fh_contacts_count": 1, "fh_exclusive_scan": 3, "fh_scan_add_base": 1, "fh_exclusive_scan_noalloc": 3, "fh_contacts_scatter": 1,
             "fh_densify_tile": 1, "fh_rwr_tiles_f32": 1, "fh_rwr_dense_f32": 1,
             "fh_rwr_dense_deltas": 1, "fh_rwr_tiles_deltas": 1, "fh_xe_f32": 1, "fh_xg_f32": 2,
             "fh_project_y_f32": 1, "fh_procrustes_f32": 1, "fh_projection_g_f32": 1,

@@ -89,6 +89,15 @@ class Tuner:
         return "%s|%s|%s" % (device, knob, ",".join(str(s) for s in signature))
 
     # ------------------------------------------------------------------ choose
+    def lookup(self, device, knob, signature):
+        """The cached choice for this key, or None (no tuning)."""
+        if not self.enabled:
+            return None
+        k = self.key(device, knob, signature)
+        with self._lock:
+            self._load()
+            return self._mem.get(k)
+
     def choose(self, device, knob, signature, candidates, run, reps=3):
         """The fastest of candidates for run(candidate); candidates[0] when tuning is off."""
         cands = []

@@ -117,7 +117,8 @@ class FitEngine:
         self.row_tile = torch.from_numpy(row_tile).to(dev)
         self.status = torch.zeros(1, dtype=i32, device=dev)
         # ---- contacts and RWR (once)
-        self.store = ContactStore(schic, dev, self.tiles, self.tile_base, stream)
+        self.store = ContactStore(schic, dev, self.tiles, self.tile_base, stream, order=order,
+                                  defer=True)
         self.tiles_dev = self.store.tiles_dev
         if self.bf16:
             self.X = None
@@ -127,10 +128,20 @@ class FitEngine:
             self.X = torch.zeros((self.Ct, self.ldx), dtype=f32, device=dev)
             self.X16 = None
         self.sumsq = torch.zeros(self.n_tiles * self.Ct, dtype=f64, device=dev)
-        if self.do_col and bin_cov is not None:
-            self.set_coverage(*bin_cov)
-        if n_i is not None:
-            self.run_rwr()
+        if n_i is not None and not (self.do_col or self.do_conv):
+            # each dataset's walk starts as soon as its contacts are built, while the next
+            # dataset's host-to-device copy is still in flight
+            for k in order:
+                self.store.build(k)
+                self._rwr_dataset(k)
+            self.store.finish()
+        else:
+            self.store.build_all()
+            self.store.finish()
+            if self.do_col and bin_cov is not None:
+                self.set_coverage(*bin_cov)
+            if n_i is not None:
+                self.run_rwr()
         # ---- factor state and work buffers
         nchrom = len(self.names)
         self.A = torch.zeros((self.nb, self.ld), dtype=f32, device=dev)
@@ -336,6 +347,40 @@ class FitEngine:
                       P(self.store.offsets), P(self.X), self.ldx, P(self.sumsq),
                       P(self.status), self.sp())
 
+    def _rwr_dataset(self, k):
+        """The plain walk of dataset k's tiles alone (its slice of the tile table, offsets and
+        sums; X rows are absolute), in the form the full walk would use."""
+        P = _lib.ptr
+        tb, nbb = self.tile_base[k], self.schic[k].num_bin_batch
+        tiles = P(self.tiles_dev) + tb * _lib.TILE_DTYPE.itemsize
+        offs = P(self.store.offsets) + tb * self.Ct * 8
+        ss = P(self.sumsq) + tb * self.Ct * 8
+        if self.bf16 and self.max_rows <= 128 and self.max_width <= 256:
+            form = self._rwr_form or self.cached_rwr_form() or 1
+            _lib.call("fh_rwr_tiles_tc", tiles, nbb, self.Ct, self.max_rows, self.max_width,
+                      P(self.store.entries), offs, P(self.X16), self.ldx,
+                      self.Ct * self.ldx if self.planes == 2 else 0, ss, int(form),
+                      P(self.status), self.sp())
+        elif self.bf16:
+            _lib.call("fh_rwr_tiles_bf16", tiles, nbb, self.Ct, self.max_rows, self.max_width,
+                      P(self.store.entries), offs, P(self.X16), self.ldx,
+                      self.Ct * self.ldx if self.planes == 2 else 0, ss, P(self.status),
+                      self.sp())
+        else:
+            _lib.call("fh_rwr_tiles_f32", tiles, nbb, self.Ct, self.max_rows, self.max_width,
+                      P(self.store.entries), offs, P(self.X), self.ldx, ss, P(self.status),
+                      self.sp())
+
+    def _rwr_signature(self):
+        return (self.precision, self.Ct, self.n_tiles, self.max_width,
+                int(np.asarray(self.tiles["n_rwr"]).max()))
+
+    def cached_rwr_form(self):
+        """The tuner's earlier choice of the walk's form for this shape, without tuning."""
+        from . import autotune
+        dev = self.torch.cuda.get_device_name(self.device)
+        return autotune.default_tuner().lookup(dev, "rwr_form", self._rwr_signature())
+
     def _rwr_tc(self, form):
         P = _lib.ptr
         _lib.call("fh_rwr_tiles_tc", P(self.tiles_dev), self.n_tiles, self.Ct, self.max_rows,
@@ -351,10 +396,9 @@ class FitEngine:
             if self.max_width > 192 or self.torch.cuda.is_current_stream_capturing():
                 return 1
             from . import autotune
-            sig = (self.precision, self.Ct, self.n_tiles, self.max_width,
-                   int(np.asarray(self.tiles["n_rwr"]).max()))
             dev = self.torch.cuda.get_device_name(self.device)
-            self._rwr_form = autotune.default_tuner().choose(dev, "rwr_form", sig, [1, 2],
+            self._rwr_form = autotune.default_tuner().choose(dev, "rwr_form",
+                                                             self._rwr_signature(), [1, 2],
                                                              self._rwr_tc, reps=1)
         return self._rwr_form
 

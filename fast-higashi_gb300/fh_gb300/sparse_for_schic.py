@@ -302,72 +302,117 @@ class ContactStore:
     """Packed per-(tile, cell) contact segments of one or more datasets on a CUDA device.
 
     Built by the library's counting sort: fh_contacts_count -> fh_exclusive_scan ->
-    fh_contacts_scatter, one chromosome at a time, from the host COO (H2D once)."""
+    fh_contacts_scatter, dataset by dataset in tile order, from the host COO.  The H2D copies
+    run on their own stream from page-locked host memory, one event per dataset, so a caller
+    that builds dataset k (build(k)) and starts work on it while dataset k + 1 is still in
+    flight overlaps the copies with its own kernels; each dataset's offsets are scanned on their
+    own and chained onto the previous dataset's total on the device (fh_scan_add_base), and the
+    segment buffer is sized by its bound (one slot per contact), so nothing waits on the host
+    until finish()."""
 
-    def __init__(self, datasets, device, tiles=None, tile_base=None, stream=None):
+    def __init__(self, datasets, device, tiles=None, tile_base=None, stream=None, order=None,
+                 defer=False):
         import torch
+        self.torch = torch
         self.device = device
         self.n_cells = datasets[0].total_cell_num
         if tiles is None:
-            tiles, tile_base = tile_table(datasets)
+            tiles, tile_base = tile_table(datasets, order=order)
         self.tiles_np = tiles
         self.tiles_dev = torch.from_numpy(tiles.view(np.uint8).copy()).to(device)
         self.n_tiles = len(tiles)
         self.stream = stream
         self.meta = [(d.bs_bin, base, d.num_bin_batch) for d, base in zip(datasets, tile_base)]
-        # H2D of the host COO (Sparse.indices int32 x 3, values fp32), once, from page-locked
-        # host memory (the arrays are registered in place, no host copy)
-        self.coo = []
-        host = []                       # keeps every source alive until the copies land
-        for d in datasets:
-            t = d.tensor
-            hi = _pin(np.ascontiguousarray(np.asarray(t.indices, dtype=np.int32)))
-            hv = _pin(np.ascontiguousarray(np.asarray(t.values, dtype=np.float32)))
-            host += [hi, hv]
-            idx = torch.from_numpy(hi).to(device, non_blocking=True)
-            val = torch.from_numpy(hv).to(device, non_blocking=True)
-            self.coo.append((idx, val, int(val.numel())))
-        torch.cuda.current_stream(device).synchronize()
-        del host
+        self.order = list(range(len(datasets))) if order is None else list(order)
+        # H2D of the host COO (Sparse.indices int32 x 3, values fp32) on a copy stream, from
+        # page-locked host memory (the arrays are registered in place, no host copy)
+        main = self._main()
+        self.copy_stream = torch.cuda.Stream(device=device)
+        self.copy_stream.wait_stream(main)
+        self.coo = [None] * len(datasets)
+        self.ready = [None] * len(datasets)
+        self._host = []                 # keeps every source alive until the copies land
+        with torch.cuda.stream(self.copy_stream):
+            for k in self.order:
+                t = datasets[k].tensor
+                hi = _pin(np.ascontiguousarray(np.asarray(t.indices, dtype=np.int32)))
+                hv = _pin(np.ascontiguousarray(np.asarray(t.values, dtype=np.float32)))
+                self._host += [hi, hv]
+                idx = torch.from_numpy(hi).to(device, non_blocking=True)
+                val = torch.from_numpy(hv).to(device, non_blocking=True)
+                self.coo[k] = (idx, val, int(val.numel()))
+                ev = torch.cuda.Event()
+                ev.record(self.copy_stream)
+                self.ready[k] = ev
         self.h2d_bytes = sum(i.numel() * 4 + v.numel() * 4 for i, v, _ in self.coo)
-        self.counts = torch.zeros(self.n_tiles * self.n_cells, dtype=torch.int32, device=device)
+        C = self.n_cells
+        self.counts = torch.zeros(self.n_tiles * C, dtype=torch.int32, device=device)
         self.cursor = torch.zeros_like(self.counts)
         self.status = torch.zeros(1, dtype=torch.int32, device=device)
-        self.offsets = torch.empty(self.n_tiles * self.n_cells + 1, dtype=torch.int64, device=device)
-        ws_bytes = _lib.value("fh_scan_workspace", self.counts.numel())
-        self.scan_ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
-        self.count_and_scan()
-        total = int(self.offsets[-1].item())
-        self.entries = torch.empty(max(total, 1) * 2, dtype=torch.int32, device=device)
-        self.scatter()
+        self.offsets = torch.zeros(self.n_tiles * C + 1, dtype=torch.int64, device=device)
+        self.bases = torch.zeros(len(datasets) + 1, dtype=torch.int64, device=device)
+        n_max = max(nbb for _, _, nbb in self.meta) * C
+        self.scan_ws = torch.empty(_lib.value("fh_scan_workspace", n_max), dtype=torch.uint8,
+                                   device=device)
+        bound = sum(nnz for _, _, nnz in self.coo)
+        self.entries = torch.empty(max(bound, 1) * 2, dtype=torch.int32, device=device)
+        self.nnz_packed = None
+        if not defer:
+            self.build_all()
+            self.finish()
+
+    def _main(self):
+        torch = self.torch
+        return self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+
+    def build(self, k):
+        """Counts, offsets and segments of dataset k on the caller's stream, after its copy."""
+        main = self._main()
+        with self.torch.cuda.stream(main):
+            self._build(k, main)
+
+    def _build(self, k, main):
+        main.wait_event(self.ready[k])
+        sp = main.cuda_stream
+        P = _lib.ptr
+        bs_bin, base, nbb = self.meta[k]
+        idx, val, nnz = self.coo[k]
+        C = self.n_cells
+        start, n = base * C, nbb * C
+        self.counts[start:start + n].zero_()
+        self.cursor[start:start + n].zero_()
+        _lib.call("fh_contacts_count", P(idx[0]), P(idx[1]), P(idx[2]), nnz, bs_bin,
+                  P(self.tiles_dev), base, nbb, C, P(self.counts), P(self.status), sp)
+        # the datasets before this one (in tile order) end at offsets[start]: keep that total,
+        # scan this dataset's counts from zero, then add it back
+        self.bases[k:k + 1].copy_(self.offsets[start:start + 1])
+        _lib.call("fh_exclusive_scan", P(self.counts[start:]), n, P(self.offsets[start:]),
+                  P(self.scan_ws), self.scan_ws.numel(), sp)
+        _lib.call("fh_scan_add_base", P(self.offsets[start:]), n + 1, P(self.bases[k:]), sp)
+        _lib.call("fh_contacts_scatter", P(idx[0]), P(idx[1]), P(idx[2]), P(val), nnz, bs_bin,
+                  P(self.tiles_dev), base, nbb, C, P(self.offsets), P(self.cursor),
+                  P(self.entries), sp)
+
+    def build_all(self):
+        main = self._main()
+        with self.torch.cuda.stream(main):
+            self.offsets[:1].zero_()
+        for k in self.order:
+            self.build(k)
+
+    def finish(self):
+        """Waits for the build, checks its status and releases the host sources."""
+        self._main().synchronize()
+        self.copy_stream.synchronize()
+        self._host = []
         st = int(self.status.item())
         if st:
             raise _lib.FHError("contact build", st)
-        self.nnz_packed = total
-
-    def count_and_scan(self):
-        sp = _lib.stream_ptr(self.stream)
-        self.counts.zero_()
-        for (bs_bin, base, nbb), (idx, val, nnz) in zip(self.meta, self.coo):
-            _lib.call("fh_contacts_count", _lib.ptr(idx[0]), _lib.ptr(idx[1]), _lib.ptr(idx[2]),
-                      nnz, bs_bin, _lib.ptr(self.tiles_dev), base, nbb, self.n_cells,
-                      _lib.ptr(self.counts), _lib.ptr(self.status), sp)
-        _lib.call("fh_exclusive_scan", _lib.ptr(self.counts), self.counts.numel(),
-                  _lib.ptr(self.offsets), _lib.ptr(self.scan_ws), self.scan_ws.numel(), sp)
-
-    def scatter(self):
-        sp = _lib.stream_ptr(self.stream)
-        self.cursor.zero_()
-        for (bs_bin, base, nbb), (idx, val, nnz) in zip(self.meta, self.coo):
-            _lib.call("fh_contacts_scatter", _lib.ptr(idx[0]), _lib.ptr(idx[1]), _lib.ptr(idx[2]),
-                      _lib.ptr(val), nnz, bs_bin, _lib.ptr(self.tiles_dev), base, nbb,
-                      self.n_cells, _lib.ptr(self.offsets), _lib.ptr(self.cursor),
-                      _lib.ptr(self.entries), sp)
+        self.nnz_packed = int(self.offsets[-1].item())
 
     def rebuild(self):
         """Re-runs the contact build from the device-resident COO (no host sync)."""
-        self.count_and_scan()
-        self.scatter()
+        self.build_all()
 
 
 def tile_table(datasets, chrom_index=None, ranks=None, n_rwr=None, order=None):

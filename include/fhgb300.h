@@ -71,6 +71,11 @@ size_t fh_scan_workspace(int64_t n);
 int fh_exclusive_scan(const int32_t* counts, int64_t n, int64_t* offsets, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* x[i] += *base for i < n (base: one device int64).  Chains the scan of one dataset's counts
+ * onto the total of the datasets before it, so a contact build can proceed dataset by dataset
+ * without a host round trip. */
+int fh_scan_add_base(int64_t* x, int64_t n, const int64_t* base, void* stream);
+
 /* fh_exclusive_scan without a workspace argument, for callers that cannot allocate device
  * memory (a foreign-language binding that holds only its own buffers, or code that must not
  * call cudaMalloc because it synchronizes the device).  No counterpart in the reference.
