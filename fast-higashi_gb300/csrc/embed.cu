@@ -264,18 +264,29 @@ __device__ __forceinline__ void eig_pair(int k, int rnd, int m, int& p, int& q) 
   q = max(a, b);
 }
 
-__global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* __restrict__ G, int n,
+// G and Q move to shared memory when 2 n^2 doubles fit (n <= kEigSmemMax): the rotations are
+// then latency-bound on shared memory instead of L2.
+constexpr int kEigSmemMax = 100;
+
+__global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* __restrict__ Gg, int n,
                                                                double* __restrict__ w,
-                                                               double* __restrict__ Q,
+                                                               double* __restrict__ Qg,
                                                                double* __restrict__ Qs,
                                                                int* status) {
+  extern __shared__ double eig_sm[];
   __shared__ double cs_c[kEigMax / 2], cs_s[kEigMax / 2];
   __shared__ int pr_p[kEigMax / 2], pr_q[kEigMax / 2];
   __shared__ int any;
   __shared__ double gmax;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int m = n + (n & 1);            // even count: the extra index is a dummy
+  const bool on_chip = n <= kEigSmemMax;
+  double* G = on_chip ? eig_sm : Gg;
+  double* Q = on_chip ? eig_sm + n * n : Qg;
+  if (on_chip)
+    for (int e = threadIdx.x; e < n * n; e += kEigThreads) G[e] = Gg[e];
   for (int e = threadIdx.x; e < n * n; e += kEigThreads) Q[e] = (e / n == e % n) ? 1.0 : 0.0;
+  __syncthreads();
   if (threadIdx.x == 0) {
     double g = 0.0;
     for (int i = 0; i < n; ++i) g = fmax(g, fabs(G[i * n + i]));
@@ -477,6 +488,15 @@ __global__ void __launch_bounds__(kEmThreads) l2_rows_kernel(const float* __rest
 
 __host__ __device__ inline size_t em_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
+inline size_t eig_smem(int n) {
+  return n <= kEigSmemMax ? 2 * (size_t)n * n * sizeof(double) : 0;
+}
+
+// The on-chip eigen-solve's shared memory (up to 160 KB) needs the opt-in once.
+inline int eig_prepare() {
+  return ensure_smem((const void*)sym_eig_kernel, eig_smem(kEigSmemMax)) ? FH_ERR_LAUNCH : FH_OK;
+}
+
 inline unsigned em_grid(int64_t n, int t = kEmThreads) { return (unsigned)ceil_div(n, t); }
 
 }  // namespace fh
@@ -547,6 +567,7 @@ extern "C" int fh_lstsq_residual(const double* V, int32_t n_cells, int32_t p, co
     return FH_ERR_ARG;
   if (p > kEigMax) return FH_ERR_UNSUPPORTED;
   if (workspace_bytes < fh_lstsq_workspace(p, m)) return FH_ERR_ARG;
+  if (eig_prepare()) return FH_ERR_LAUNCH;
   cudaStream_t s = (cudaStream_t)stream;
   uint8_t* w = (uint8_t*)workspace;
   double* mv = (double*)w;    w += em_align(sizeof(double) * p);
@@ -563,7 +584,7 @@ extern "C" int fh_lstsq_residual(const double* V, int32_t n_cells, int32_t p, co
                                  kEmThreads, 0, s>>>(V, p, p, mv, V, p, p, mv, n_cells, G, p);
   cross_kernel<double, float><<<dim3((unsigned)ceil_div(m, kCrT), (unsigned)ceil_div(p, kCrT)),
                                 kEmThreads, 0, s>>>(V, p, p, mv, Y, ldy, m, my, n_cells, H, m);
-  sym_eig_kernel<<<1, kEigThreads, 0, s>>>(G, p, ev, Q, Qs, status);
+  sym_eig_kernel<<<1, kEigThreads, eig_smem(p), s>>>(G, p, ev, Q, Qs, status);
   lstsq_coef_kernel<<<em_grid((int64_t)p * m), kEmThreads, 0, s>>>(ev, Qs, H, p, m, coef);
   lstsq_apply_kernel<<<em_grid((int64_t)n_cells * m), kEmThreads, 0, s>>>(
       V, p, Y, ldy, n_cells, m, mv, my, coef, add_intercept_back, out, ldo);
@@ -589,6 +610,7 @@ extern "C" int fh_range_svd(const float* F, int64_t ldf, int32_t n_cells, int32_
     return FH_ERR_ARG;
   if (r > kEigMax) return FH_ERR_UNSUPPORTED;
   if (workspace_bytes < fh_range_svd_workspace(r, m, k)) return FH_ERR_ARG;
+  if (eig_prepare()) return FH_ERR_LAUNCH;
   cudaStream_t s = (cudaStream_t)stream;
   uint8_t* w = (uint8_t*)workspace;
   const size_t rr = sizeof(double) * (size_t)r * r;
@@ -614,7 +636,7 @@ extern "C" int fh_range_svd(const float* F, int64_t ldf, int32_t n_cells, int32_
                                kEmThreads, 0, s>>>(F, ldf, r, nullptr, Y, ldy, m, nullptr,
                                                    n_cells, FY, m);
   // U_F = F T with T = Q L^-1/2 (kept directions)
-  sym_eig_kernel<<<1, kEigThreads, 0, s>>>(G, r, ev, Q, Qs, status);
+  sym_eig_kernel<<<1, kEigThreads, eig_smem(r), s>>>(G, r, ev, Q, Qs, status);
   range_basis_kernel<<<em_grid((int64_t)r * r), kEmThreads, 0, s>>>(ev, Qs, r, T);
   // B = T^T (F^T Y)  (r x m)
   dsmall_kernel<<<em_grid((int64_t)r * m), kEmThreads, 0, s>>>(T, 1, r, FY, m, 1, nullptr, r, m,
@@ -622,7 +644,7 @@ extern "C" int fh_range_svd(const float* F, int64_t ldf, int32_t n_cells, int32_
   // B B^T = U_B S^2 U_B^T
   dsmall_kernel<<<em_grid((int64_t)r * r), kEmThreads, 0, s>>>(Bm, m, 1, Bm, 1, m, nullptr, r, r,
                                                                 m, G, r);
-  sym_eig_kernel<<<1, kEigThreads, 0, s>>>(G, r, ev2, Q, Ub, status);
+  sym_eig_kernel<<<1, kEigThreads, eig_smem(r), s>>>(G, r, ev2, Q, Ub, status);
   // components V_B = B^T U_B / S (m x k) and their signs
   inv_sigma_kernel<<<em_grid(k), kEmThreads, 0, s>>>(ev2, k, isg);
   dsmall_kernel<<<em_grid((int64_t)m * k), kEmThreads, 0, s>>>(Bm, 1, m, Ub, r, 1, isg, m, k, r,

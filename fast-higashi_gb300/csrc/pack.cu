@@ -28,8 +28,9 @@
 //   (scan)       -> each segment's output offset
 //   pack_stats   the mean + 15 std threshold (fp64 sums in segment order)
 //   pack_write   the output entries and values min(log1p(value * scale), threshold)
-// The coverage sum and the moments are accumulated in fp64 where the reference sums fp32 in
-// numpy's order, so values agree with the reference's to an ulp or two, indices exactly.
+// The coverage sum and the moments are summed per thread in fp32 (at most 16 contacts of a
+// segment) and across threads and segments in fp64, where the reference sums fp32 in numpy's
+// order, so values agree with the reference's to an ulp or two, indices exactly.
 // Contact values are taken as non-negative (counts): a bin row is kept when one of its kept
 // contacts is positive, as its row sum is then positive.
 #include "fh_common.cuh"
@@ -166,7 +167,9 @@ __global__ void __launch_bounds__(kPackThreads) pack_mark_kernel(PackArgs a) {
   int k;
   int64_t e0, e1;
   if (!pack_segment(a, k, e0, e1)) return;
-  double s = 0.0;
+  // a thread sums its (at most 16) contacts of the segment in fp32 (integer counts: exact),
+  // then the block adds the partials in fp64: fp64 adds per contact are slow on this GPU
+  float sf = 0.f;
   for (int64_t base = e0 + threadIdx.x; base < e1; base += kPackChunk) {
     int r0[kPackPer], c0[kPackPer];
     float v[kPackPer];
@@ -182,14 +185,14 @@ __global__ void __launch_bounds__(kPackThreads) pack_mark_kernel(PackArgs a) {
     for (int u = 0; u < kPackPer; ++u) {
       int r, c;
       if (base + (int64_t)u * kPackThreads < e1 && pack_band(a, r0[u], c0[u], r, c)) {
-        s += (double)v[u];
+        sf += v[u];
         // read before writing: after the first few segments every row is marked, and the
         // stores of all CTAs to the same few words would serialise in L2
         if (v[u] > 0.f && a.mark[r] == 0) a.mark[r] = 1;
       }
     }
   }
-  s = block_sum<double>(s, red);
+  const double s = block_sum<double>((double)sf, red);
   if (threadIdx.x == 0) a.seg_cov[blockIdx.x] = s;
 }
 
@@ -220,7 +223,9 @@ __global__ void __launch_bounds__(kPackThreads) pack_count_kernel(PackArgs a) {
   // normalize_by_coverage: scale = bins / total, in fp32 as the reference's float32 arrays
   const float scale = (float)a.nb / ((float)a.cov[k] + 1e-15f);
   int n = 0;
-  double s1 = 0.0, s2 = 0.0;     // moments of the kept values (the clip threshold's)
+  // moments of the kept values (the clip threshold's): fp32 over a thread's (at most 16)
+  // contacts of the segment, then fp64 across the block
+  float s1f = 0.f, s2f = 0.f;
   for (int64_t base = e0 + threadIdx.x; base < e1; base += kPackChunk) {
     int r0[kPackPer], c0[kPackPer];
     float v[kPackPer];
@@ -239,14 +244,14 @@ __global__ void __launch_bounds__(kPackThreads) pack_count_kernel(PackArgs a) {
           a.new_id[r] >= 0 && a.new_id[c] >= 0) {
         ++n;
         const float x = log1pf(v[u] * scale);
-        s1 += (double)x;
-        s2 += (double)x * (double)x;
+        s1f += x;
+        s2f = fmaf(x, x, s2f);
       }
     }
   }
   n = block_sum<int>(n, red);
-  s1 = block_sum<double>(s1, dred);
-  s2 = block_sum<double>(s2, dred);
+  const double s1 = block_sum<double>((double)s1f, dred);
+  const double s2 = block_sum<double>((double)s2f, dred);
   if (threadIdx.x == 0) {
     a.seg_cnt[blockIdx.x] = n;
     a.seg_mom[2 * blockIdx.x] = s1;
