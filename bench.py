@@ -71,6 +71,11 @@ def parse():
                          "GPU init_params), one JSON line")
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the FP64 fit that states both forms' embedding error")
+    ap.add_argument("--hbm-budget-gb", type=float, default=None,
+                    help="hold each fit within this many GB of device memory: X's last "
+                         "chromosomes stream from host memory when X does not fit, the contact "
+                         "segments are built one dataset at a time (the 50,000-cell c5 case: "
+                         "--config c5 --hbm-budget-gb 180); prints its own JSON line")
     args = ap.parse_args()
     args.config = args.config or ("c4" if args.grad else "c3")
     return args
@@ -701,6 +706,141 @@ def extras_arm(args, local):
     print(json.dumps(line), flush=True)
 
 
+def budget_arm(args, rank, local, ws):
+    """A workload whose X is larger than the HBM budget (c5: 50,000 cells at 500 kb, R = 128,
+    band 40; X is 179 GB in two bf16 planes or in fp32): both forms run with hbm_budget, so
+    X's last chromosomes stream through two staging slots from page-locked host memory and the
+    contact segments are built one dataset at a time from the host COO read in place.  A step
+    is a whole fit: the contact build and walk (the COO crosses the host link inside the step)
+    and the 30 ALS iterations (one CUDA graph, the window copies as memcpy nodes).  The COO is
+    generated on the GPU (synth.generate_on_device) and kept in host memory, as a caller's
+    input would be.  No end-to-end line beyond the step itself (its input already comes from
+    host memory), no FP64 fit at this size (run --config c5 --cells 2000 for the precision
+    report on the same shapes)."""
+    import dataclasses
+    import gc
+    import torch
+    from fh_gb300 import Fast_Higashi_core, _lib, synth
+    from fh_gb300.engine import FitEngine
+    from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    budget = int(args.hbm_budget_gb * 1e9)
+    w = synth.workload(args.config)
+    if args.cells:
+        w = dataclasses.replace(w, n_cells=int(args.cells),
+                                name="%s at %d cells" % (args.config, args.cells))
+    iters = args.iters or w.n_iter
+    C = w.n_cells
+    t0 = time.time()
+    coo, _ = synth.generate_on_device(w, seed=0, device=dev)
+    gen_s = time.time() - t0
+    ds = []
+    for (idx, val, shape), cname, nb in zip(coo, w.chrom_names, w.chrom_bins):
+        bsb, bsc = synth.recommend_batches(w, nb, w.n_cells)
+        ds.append(Chrom_Dataset(Sparse(idx, val, shape, copy=False), bsb, bsc, compact=True,
+                                flank=w.band, chrom=cname, resolution=w.resolution))
+    nnz = int(sum(v.size for _, v, _ in coo))
+    torch.cuda.empty_cache()
+    torch.cuda.reset_peak_memory_stats(dev)
+    torch.manual_seed(0)
+    m = Fast_Higashi_core(w.rank, w.band, [w.resolution], precision=args.precision,
+                          hbm_budget=budget).to(dev)
+    m._sizes(ds, w.dim1, None)
+    t0 = time.time()
+    m.init_params(ds, False, True, False, seed=0)
+    torch.cuda.synchronize()
+    init_s = time.time() - t0
+    state = ([a.clone() for a in m.A_list], {k: v.clone() for k, v in m.B_dict.items()},
+             {k: v.clone() for k, v in m.D_dict.items()}, m.meta_embedding.clone())
+    n_i = np.asarray(m.n_i).copy()
+    chrom2size = dict(m.chrom2size)
+
+    def device_step(e, h, graph=True):
+        e.run_rwr()
+        e.set_state(*state)
+        e.core_norm()
+        e.run_iterations(iters, 1, h, graph=graph)
+
+    def timed(e, h, warmup, steps, clocks):
+        for _ in range(warmup):
+            device_step(e, h)
+        torch.cuda.synchronize()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0, l0 = _lib.launches, e.xs.link_bytes
+        with Clocks(local) if clocks else _Null() as clk:
+            torch.cuda.synchronize()
+            s0.record()
+            for _ in range(steps):
+                device_step(e, h)
+            s1.record()
+            torch.cuda.synchronize()
+        e.check_status("bench")
+        return (s0.elapsed_time(s1) / steps, (_lib.launches - n0) // steps,
+                (e.xs.link_bytes - l0) / steps, clk)
+
+    def plan_of(e):
+        p = e.xs.plan
+        return {"resident_gb": round(p.res_bytes / 1e9, 2),
+                "streamed_gb": round(p.streamed_bytes / 1e9, 2),
+                "windows": [{"chromosomes": [w.chrom_names[c] for c in win.chroms],
+                             "gb": round(win.nbytes / 1e9, 2)} for win in p.windows],
+                "staging_gb": round(p.staging_bytes / 1e9, 2)}
+
+    eng = m.engine
+    hist = eng.new_history(iters)
+    ms, launches, win_bytes, clk = timed(eng, hist, args.warmup, args.steps, True)
+    eng.timing = {}
+    device_step(eng, hist, graph=False)
+    torch.cuda.synchronize()
+    kt = {k: round(v["mean_ms"], 3) for k, v in eng.timing_summary().items()}
+    eng.timing = None
+    E_main = eng.E[:, :w.rank].clone()
+    loss = float(eng.losses(hist[-1], eng.tensor_norms())[0])
+    peak = torch.cuda.max_memory_reserved(dev)
+    free, total = torch.cuda.mem_get_info(dev)
+    mem = {"budget_gb": budget / 1e9, "peak_reserved_gb": round(peak / 1e9, 2),
+           "device_used_gb_after": round((total - free) / 1e9, 2)}
+    main_plan = plan_of(eng)
+    link = {"coo_read_in_place_gb": round(eng.store.link_bytes / 1e9, 2),
+            "window_copies_gb": round(win_bytes / 1e9, 2)}
+    del m, eng, hist
+    gc.collect()
+    torch.cuda.empty_cache()
+    plain = None
+    if args.precision != "fp32" and not args.no_plain:
+        torch.cuda.reset_peak_memory_stats(dev)
+        peng = FitEngine(ds, w.rank, chrom2size, n_i, dev, precision="fp32", hbm_budget=budget)
+        phist = peng.new_history(iters)
+        pms, plaunch, pwin, _ = timed(peng, phist, args.warmup, args.steps, False)
+        plain = {"value": C / (pms / 1000.0), "unit": "cells/s", "ms_per_step": pms,
+                 "gpu_launches": int(plaunch), "speedup_of_headline": pms / ms,
+                 "embedding_aligned_rel_diff": aligned_diff(E_main, peng.E[:, :w.rank]),
+                 "peak_reserved_gb": round(torch.cuda.max_memory_reserved(dev) / 1e9, 2),
+                 "x_plan": plan_of(peng), "window_copies_gb": round(pwin / 1e9, 2)}
+        del peng, phist
+        gc.collect()
+        torch.cuda.empty_cache()
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": C / (ms / 1000.0), "unit": "cells/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16" if args.precision != "fp32" else "fp32",
+            "data": "synthetic (seeded generator on the GPU, %s)" % args.config,
+            "config": {"workload": "%s: %d cells, %d bins, R=%d, band %d, %d ALS iterations" %
+                                   (w.name, C, sum(w.chrom_bins), w.rank, w.band, iters),
+                       "contacts": nnz, "hbm_budget_gb": budget / 1e9,
+                       "l2": "inputs larger than L2 (X %.0f GB)" % (C * band_rows(w) * 4 / 1e9),
+                       "parallelism": "single GPU"},
+            "precision": args.precision, "rwr_epochs": [int(v) for v in n_i],
+            "memory": mem, "x_plan": main_plan, "host_link_per_step": link,
+            "kernel_ms": kt, "gpu_launches": int(launches), "clocks": clk.summary(),
+            "plain_fp32": plain, "loss_final": loss,
+            "setup_s": {"generate": round(gen_s, 1), "init_params": round(init_s, 1)}}))
+        sys.stdout.flush()
+
+
 def gb300_arm(args, rank, local, ws):
     import torch
     from fh_gb300 import Fast_Higashi_core, _lib
@@ -753,6 +893,43 @@ def gb300_arm(args, rank, local, ws):
 
     ms, launches, clk = timed(eng, hist, True)
     value = ws * C / (ms / 1000.0)
+    # ---- end to end through the public API, host data in and out (before the plain form, so
+    # that each measurement starts from the same device state: this engine and nothing else)
+    A0, B0, D0, E0 = [x.cpu() for x in state[0]], {k: v.cpu() for k, v in state[1].items()}, \
+        {k: v.cpu() for k, v in state[2].items()}, state[3].cpu()
+    n_i = m.n_i.copy()
+
+    store_h2d = [0]
+
+    def e2e_step():
+        mm = Fast_Higashi_core(w.rank, w.band, [w.resolution], precision=args.precision).to(dev)
+        mm._sizes(ds, w.dim1, None)
+        mm.A_list, mm.B_dict, mm.D_dict, mm.meta_embedding = A0, B0, D0, E0
+        mm.n_i, mm.bin_cov_list = n_i, [None] * len(ds)
+        mm.fit(ds, size_ratio=w.dim1, n_iter_max=iters, n_iter_parafac=1, do_conv=False,
+               do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
+        emb = mm.meta_embedding.cpu()
+        store_h2d[0] = mm.engine.store.h2d_bytes
+        del mm                       # the next step's engine reuses the freed device memory
+        return emb
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(max(2, args.steps)):
+        barrier()
+        t0 = time.perf_counter()
+        emb = e2e_step()
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = float(np.median(e2e_times))     # each step is a whole fit through the public API
+    e2e_s = float(max_over_ranks(torch.tensor([e2e_s], device=dev), ws).item())
+    h2d = store_h2d[0] + sum(a.numel() * 4 for a in A0) + E0.numel() * 4 + \
+        sum(v.numel() * 4 for v in B0.values()) + sum(v.numel() * 4 for v in D0.values())
+    d2h = emb.numel() * 4 + iters * (eng.nb + 1 + len(eng.names)) * 8
+    e2e = {"value": ws * C / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1000.0,
+           "ms_steps": [round(t * 1000.0, 1) for t in e2e_times], "statistic": "median"}
     # ---- the plain fp32 form on the same state, for the BF16-batched vs plain FP32 ratio
     plain = None
     if args.precision != "fp32" and not args.no_plain:
@@ -797,42 +974,6 @@ def gb300_arm(args, rank, local, ws):
     roof["note"] = ("the family with the largest share of the step; every family in families, "
                     "shares of the step: %s" % share)
     roof["families"] = fams
-    # ---- end to end through the public API, host data in and out
-    A0, B0, D0, E0 = [x.cpu() for x in state[0]], {k: v.cpu() for k, v in state[1].items()}, \
-        {k: v.cpu() for k, v in state[2].items()}, state[3].cpu()
-    n_i = m.n_i.copy()
-
-    store_h2d = [0]
-
-    def e2e_step():
-        mm = Fast_Higashi_core(w.rank, w.band, [w.resolution], precision=args.precision).to(dev)
-        mm._sizes(ds, w.dim1, None)
-        mm.A_list, mm.B_dict, mm.D_dict, mm.meta_embedding = A0, B0, D0, E0
-        mm.n_i, mm.bin_cov_list = n_i, [None] * len(ds)
-        mm.fit(ds, size_ratio=w.dim1, n_iter_max=iters, n_iter_parafac=1, do_conv=False,
-               do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
-        emb = mm.meta_embedding.cpu()
-        store_h2d[0] = mm.engine.store.h2d_bytes
-        del mm                       # the next step's engine reuses the freed device memory
-        return emb
-
-    e2e_step()
-    torch.cuda.synchronize()
-    e2e_times = []
-    for _ in range(max(2, args.steps)):
-        barrier()
-        t0 = time.perf_counter()
-        emb = e2e_step()
-        torch.cuda.synchronize()
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_s = float(np.median(e2e_times))     # each step is a whole fit through the public API
-    e2e_s = float(max_over_ranks(torch.tensor([e2e_s], device=dev), ws).item())
-    h2d = store_h2d[0] + sum(a.numel() * 4 for a in A0) + E0.numel() * 4 + \
-        sum(v.numel() * 4 for v in B0.values()) + sum(v.numel() * 4 for v in D0.values())
-    d2h = emb.numel() * 4 + iters * (eng.nb + 1 + len(eng.names)) * 8
-    e2e = {"value": ws * C / e2e_s, "unit": "cells/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1000.0,
-           "ms_steps": [round(t * 1000.0, 1) for t in e2e_times], "statistic": "median"}
     # ---- the rows either side of the fit: input packing and post-processing (untimed by the
     # headline; each device-timed on its own)
     packing = post = None
@@ -970,6 +1111,10 @@ def main():
         _b.build()
         if rank == 0:
             extras_arm(args, local)
+    elif args.hbm_budget_gb is not None:
+        from fh_gb300 import build as _b
+        _b.build()
+        budget_arm(args, rank, local, ws)
     else:
         from fh_gb300 import build as _b
         _b.build()

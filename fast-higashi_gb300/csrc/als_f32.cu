@@ -310,7 +310,7 @@ extern "C" int fh_xg_splits(int32_t n_cells, int64_t rows) {
 
 extern "C" int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows,
                          const float* Gt, int32_t rp, int32_t splits, float* partial,
-                         float* out, void* stream) {
+                         float* out, int32_t accumulate, void* stream) {
   if (!X || !Gt || !partial || !out || n_cells <= 0 || rows <= 0 || ldx < rows || ldx % 128 ||
       !rp_ok(rp) || splits <= 0)
     return FH_ERR_ARG;
@@ -324,7 +324,8 @@ extern "C" int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t r
     default: xg_f32_kernel<128><<<grid, 256, 0, s>>>(X, ldx, n_cells, Gt, rows, per, partial); break;
   }
   const int64_t n = (int64_t)n_cells * rp;
-  reduce_splits_kernel<float><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(partial, splits, n, out);
+  reduce_splits_kernel<float><<<(unsigned)ceil_div(n, 256), 256, 0, s>>>(partial, splits, n, out,
+                                                                      accumulate != 0);
   FH_CHECK_LAUNCH();
   return FH_OK;
 }

@@ -47,13 +47,14 @@ __device__ inline T block_sum(T v, T* scratch /* >= 32 */) {
 }
 
 // out[i] = sum over k of partial[k][i] in a fixed order (deterministic split-K reduction),
-// added in fp64 and rounded once.
+// added in fp64 and rounded once; with accumulate the sum starts from out[i] (a pass over X
+// held in several row ranges adds each range's sum into one result).
 template <typename T>
 __global__ void reduce_splits_kernel(const T* __restrict__ partial, int splits, int64_t n,
-                                     T* __restrict__ out) {
+                                     T* __restrict__ out, bool accumulate) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    double s = 0.0;
+    double s = accumulate ? (double)out[i] : 0.0;
     for (int k = 0; k < splits; ++k) s += (double)partial[(int64_t)k * n + i];
     out[i] = (T)s;
   }

@@ -434,7 +434,7 @@ extern "C" int fh_xg_bf16_splits(int32_t n_cells, int64_t rows) {
 extern "C" int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total,
                           int32_t planes, int32_t n_cells, int64_t rows, const uint16_t* G2,
                           int32_t rp, int32_t splits, int32_t fold, float* partial, float* out,
-                          int* status, void* stream) {
+                          int32_t accumulate, int* status, void* stream) {
   if (!X16 || !G2 || !partial || !out || n_cells <= 0 || n_cells > n_cells_total || rows <= 0 ||
       ldx < rows || ldx % 128 || splits <= 0 || (planes != 1 && planes != 2) || fold < 0)
     return FH_ERR_ARG;
@@ -465,7 +465,8 @@ extern "C" int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_tota
   const int64_t n = (int64_t)n_cells * rp;
   int64_t blocks = ceil_div(n, 256);
   if (blocks > 4096) blocks = 4096;
-  reduce_splits_kernel<float><<<(unsigned)blocks, 256, 0, s>>>(partial, used, n, out);
+  reduce_splits_kernel<float><<<(unsigned)blocks, 256, 0, s>>>(partial, used, n, out,
+                                                                accumulate != 0);
   FH_CHECK_LAUNCH();
   return FH_OK;
 }

@@ -76,14 +76,14 @@ SIGNATURES = {
     "fh_rwr_tiles_deltas": (C.c_int, [P, I32, I32, I32, I32, P, P, I32, P, P, P]),
     "fh_xe_f32": (C.c_int, [P, I64, I32, I64, P, I32, P, P]),
     "fh_xg_splits": (C.c_int, [I32, I64]),
-    "fh_xg_f32": (C.c_int, [P, I64, I32, I64, P, I32, I32, P, P, P]),
+    "fh_xg_f32": (C.c_int, [P, I64, I32, I64, P, I32, I32, P, P, I32, P]),
     "fh_project_y_f32": (C.c_int, [P, P, I64, P, P, I32, P, I32, P]),
     "fh_rwr_tiles_bf16": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, I64, P, P, P]),
     "fh_rwr_tiles_tc": (C.c_int, [P, I32, I32, I32, I32, P, P, P, I64, I64, P, I32, P, P]),
     "fh_split_bf16": (C.c_int, [P, I64, I32, I64, P, P]),
     "fh_xe_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, I32, P, P, P]),
     "fh_xg_bf16_splits": (C.c_int, [I32, I64]),
-    "fh_xg_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, I32, I32, P, P, P, P]),
+    "fh_xg_bf16": (C.c_int, [P, I64, I32, I32, I32, I64, P, I32, I32, I32, P, P, I32, P, P]),
     "fh_procrustes_f32": (C.c_int, [P, P, I64, I32, I32, P, P, I32, P, P, I32, I32, I32, P, P,
                                     P, P, P]),
     "fh_projection_g_f32": (C.c_int, [P, P, I64, I32, I32, P, I32, P, P, I32, I32, I32, P, P,
@@ -114,6 +114,10 @@ SIGNATURES = {
     "fh_unpool_rows": (C.c_int, [P, I32, P, P, I64, I64, P, I64, I32, P, I64, P]),
     "fh_pack_chromosome": (C.c_int, [P, P, P, P, I32, P, I32, I32, I32, I32, P, P, I64, P, P,
                                      SZ, P, P]),
+    "fh_host_alloc": (C.c_int, [I64, P]),
+    "fh_host_free": (C.c_int, [P]),
+    "fh_host_device_pointer": (C.c_int, [P, P]),
+    "fh_memcpy_async": (C.c_int, [P, P, I64, P]),
 }
 
 # kernels each entry point launches (the count the benchmark reports as gpu_launches)

@@ -44,6 +44,9 @@ class ReconstructionLoss:
         if eng.do_conv or eng.do_col:
             raise _lib.FHError("ReconstructionLoss", 2,
                                "the differentiable walk covers do_conv=False, do_col=False")
+        if getattr(eng, "xs", None) is not None:
+            raise _lib.FHError("ReconstructionLoss", 2,
+                               "the differentiable walk needs X resident (no hbm_budget)")
         self.eng = eng
         self.torch = torch
         self._ws = {}

@@ -40,10 +40,17 @@ def _pad_rank(R):
 
 
 class FitEngine:
+    # bytes of a budget kept back for transient buffers (init's sketches, the auto-stop deltas)
+    BUDGET_RESERVE = 2 << 30
+
     def __init__(self, schic, rank, chrom2size, n_i, device, do_rwr=True, stream=None,
-                 precision="fp32", do_conv=False, do_col=False, bin_cov=None):
+                 precision="fp32", do_conv=False, do_col=False, bin_cov=None, hbm_budget=None):
         """bin_cov: (bin_cov_list, bad_bin_cov_list) of the model, required with do_col when
-        n_i is given (the walk runs at construction); init_params computes it otherwise."""
+        n_i is given (the walk runs at construction); init_params computes it otherwise.
+        hbm_budget: bytes of device memory this engine may hold, or None (X and every
+        dataset's contact segments resident).  With a budget, the contact segments are built
+        one dataset at a time from the host COO read in place, and X's last chromosomes stream
+        from host memory when X does not fit (xstream.py)."""
         import torch
         self.torch = torch
         if precision not in ("fp32", "bf16", "bf16x2"):
@@ -99,6 +106,7 @@ class FitEngine:
         self.n_tiles = len(t)
         self.rows = int((t["rows"] * t["width"]).sum())
         self.ldx = int(math.ceil(self.rows / 128) * 128)
+        self.ldw = self.ldx                  # rows of W and Gt (all band rows)
         self.nb = int(t["rows"].sum())
         self.max_rows = int(t["rows"].max())
         self.max_width = int(t["width"].max())
@@ -116,9 +124,22 @@ class FitEngine:
         f32, f64, i32 = torch.float32, torch.float64, torch.int32
         self.row_tile = torch.from_numpy(row_tile).to(dev)
         self.status = torch.zeros(1, dtype=i32, device=dev)
+        self.xs = None
+        self.order = order
+        if hbm_budget is not None:
+            self._budgeted(hbm_budget, n_i)
+        else:
+            self._resident(n_i, bin_cov)
+        self._buffers()
+
+    def _resident(self, n_i, bin_cov):
+        """X and every dataset's contact segments in HBM; the walk at construction when n_i
+        is given (each dataset's walk right behind its contact build)."""
+        torch, dev, order = self.torch, self.device, self.order
+        f32, f64 = torch.float32, torch.float64
         # ---- contacts and RWR (once)
-        self.store = ContactStore(schic, dev, self.tiles, self.tile_base, stream, order=order,
-                                  defer=True)
+        self.store = ContactStore(self.schic, dev, self.tiles, self.tile_base, self.stream,
+                                  order=order, defer=True)
         self.tiles_dev = self.store.tiles_dev
         if self.bf16:
             self.X = None
@@ -142,19 +163,87 @@ class FitEngine:
                 self.set_coverage(*bin_cov)
             if n_i is not None:
                 self.run_rwr()
+
+    def _budgeted(self, budget, n_i):
+        """The engine within hbm_budget bytes: the factor buffers' share first, then the plan
+        of X (xstream.plan_x) over what remains, less a reserve for the transient buffers of
+        init and the walk's auto-stop deltas."""
+        from .sparse_for_schic import StreamedContacts
+        from .xstream import XStream, plan_x
+        torch, dev = self.torch, self.device
+        if self.do_conv or self.do_col:
+            raise _lib.FHError("FitEngine", 2, "do_conv and do_col need X resident "
+                                               "(no hbm_budget)")
+        self.store = StreamedContacts(self.schic, dev, self.tiles, self.tile_base, self.status,
+                                      order=self.order)
+        self.tiles_dev = self.store.tiles_dev
+        groups = []                          # chromosome groups in tile order: (datasets, t0, t1)
+        for ci in range(len(self.names)):
+            ks = [k for k in self.order if self.chrom_index[k] == ci]
+            t0 = min(self.tile_base[k] for k in ks)
+            t1 = max(self.tile_base[k] + self.schic[k].num_bin_batch for k in ks)
+            groups.append((ks, t0, t1))
+        groups.sort(key=lambda g: g[1])
+        t = self.tiles
+        chrom_rows = [(int(t["xoff"][t0]), int(t["xoff"][t1 - 1] + t["rows"][t1 - 1] * t["width"][t1 - 1]))
+                      for _, t0, t1 in groups]
+        entries = [max(self.store.entries_bytes(k) for k in ks) for ks, _, _ in groups]
+        elem = 2 * self.planes if self.bf16 else 4
+        x_budget = int(budget) - self._buffer_bytes(True) - self.store_bytes() - \
+            self.BUDGET_RESERVE
+        plan = plan_x(chrom_rows, elem, self.Ct, entries, x_budget)
+        self.groups = groups
+        self.xs = XStream(plan, self.planes, self.Ct,
+                          torch.bfloat16 if self.bf16 else torch.float32, dev, self.tiles,
+                          [(t0, t1) for _, t0, t1 in groups])
+        self.ldx = plan.ld_res
+        if self.bf16:
+            self.X, self.X16 = None, self.xs.res
+        else:
+            self.X, self.X16 = self.xs.res, None
+        self.sumsq = torch.zeros(self.n_tiles * self.Ct, dtype=torch.float64, device=dev)
+        if n_i is not None:
+            self.run_rwr()
+
+    def store_bytes(self):
+        s = self.store
+        return s.counts.numel() * 8 + s.offsets.numel() * 8 + s.scan_ws.numel()
+
+    def _partial_splits(self, budgeted=None):
+        if budgeted if budgeted is not None else self.xs is not None:
+            # the streamed passes take the heuristic split count of each row range
+            return max(self.xg_splits(self.C, self.rows), self.xg_splits(self.Ct, self.rows))
+        # room for the autotuner's largest split candidate (four times the heuristic)
+        return 4 * max(self.xg_splits(self.C, self.rows), self.xg_splits(self.Ct, self.rows))
+
+    def _buffer_bytes(self, budgeted=None):
+        """Bytes of the factor state and work buffers that _buffers allocates."""
+        nchrom, ld, rp, C, Ct = len(self.names), self.ld, self.rp, self.C, self.Ct
+        b = 4 * (self.nb * ld + nchrom * ld * ld + nchrom * rp * ld + C * rp)
+        b += 4 * 2 * self.ldw * rp + 4 * max(self.u_size, 1) + 4 * self.nb * ld * rp
+        b += 4 * Ct * rp + 4 * self._partial_splits(budgeted) * Ct * rp + 8 * (self.nb + 1 + nchrom)
+        if self.bf16:
+            b += 2 * Ct * 2 * rp + 2 * self.rows * 2 * rp
+        b += _lib.value("fh_meta_polar_workspace", Ct, self.R)
+        b += 8 * self.n_tiles * Ct                  # sumsq
+        return b
+
+    def _buffers(self):
+        """Factor state and work buffers."""
+        torch, dev = self.torch, self.device
+        f32, f64 = torch.float32, torch.float64
         # ---- factor state and work buffers
         nchrom = len(self.names)
         self.A = torch.zeros((self.nb, self.ld), dtype=f32, device=dev)
         self.B = torch.zeros((nchrom, self.ld, self.ld), dtype=f32, device=dev)
         self.D = torch.zeros((nchrom, self.rp, self.ld), dtype=f32, device=dev)
         self.E = torch.zeros((self.C, self.rp), dtype=f32, device=dev)
-        self.W = torch.zeros((self.ldx, self.rp), dtype=f32, device=dev)
-        self.Gt = torch.zeros((self.ldx, self.rp), dtype=f32, device=dev)
+        self.W = torch.zeros((self.ldw, self.rp), dtype=f32, device=dev)
+        self.Gt = torch.zeros((self.ldw, self.rp), dtype=f32, device=dev)
         self.U = torch.zeros(max(self.u_size, 1), dtype=f32, device=dev)
         self.Y = torch.zeros((self.nb, self.ld, self.rp), dtype=f32, device=dev)
         self.S = torch.zeros((self.Ct, self.rp), dtype=f32, device=dev)
-        # room for the autotuner's largest split candidate (four times the heuristic)
-        self.splits = 4 * max(self.xg_splits(self.C, self.rows), self.xg_splits(self.Ct, self.rows))
+        self.splits = self._partial_splits()
         self._tuned = {}
         if self.bf16:
             self.E2 = torch.zeros((self.Ct, 2 * self.rp), dtype=torch.bfloat16, device=dev)
@@ -209,6 +298,8 @@ class FitEngine:
         """Sets the RWR epoch count of every tile (force_rwr_epochs) and re-uploads the table."""
         self.tiles["n_rwr"] = np.asarray(per_tile, dtype=np.int32)
         self.tiles_dev.copy_(self.torch.from_numpy(self.tiles.view(np.uint8).copy()))
+        if self.xs is not None:
+            self.xs.set_tiles(self.tiles)
 
     def set_n_i(self, n_i):
         self.n_rwr = [int(v) if self.do_rwr else 0 for v in n_i]
@@ -223,7 +314,19 @@ class FitEngine:
         P = _lib.ptr
         out = self.torch.zeros((self.n_tiles, self.Ct, cap), dtype=self.torch.float32,
                                device=self.device)
-        if self.do_conv:
+        if self.xs is not None:
+            # one dataset's segments at a time, at the start of the staging area
+            ent = self.xs.entries_ptr(False)
+            main = self.stream if self.stream is not None else \
+                self.torch.cuda.current_stream(self.device)
+            for k in self.order:
+                tb, nbb = self.tile_base[k], self.schic[k].num_bin_batch
+                self.store.build(k, ent, main)
+                _lib.call("fh_rwr_tiles_deltas", P(self.tiles_dev) + tb * _lib.TILE_DTYPE.itemsize,
+                          nbb, self.Ct, self.max_rows, self.max_width, ent,
+                          P(self.store.offsets), cap, P(out) + tb * self.Ct * cap * 4,
+                          P(self.status), self.sp())
+        elif self.do_conv:
             src = self.conv_source()
             _lib.call("fh_rwr_tiles_dense_deltas", P(self.tiles_dev), self.n_tiles, self.Ct,
                       self.max_rows, self.max_width, P(src), self.ldx, cap, P(out),
@@ -315,6 +418,9 @@ class FitEngine:
 
     def _run_rwr(self):
         P = _lib.ptr
+        if self.xs is not None:
+            self._walk_streamed()
+            return
         if self.do_col:
             if self.cov is None:
                 raise _lib.FHError("FitEngine", 1, "do_col needs the coverage rows (bin_cov_list)")
@@ -371,6 +477,67 @@ class FitEngine:
                       P(self.store.entries), offs, P(self.X), self.ldx, ss, P(self.status),
                       self.sp())
 
+    def _walk_dataset(self, k, X, ldx, tiles_ptr, entries_ptr):
+        """The plain walk of dataset k (budgeted engine): its segments at entries_ptr with
+        the store's dataset-local offsets, its tiles at tiles_ptr (band rows relative to X's
+        column 0), X [planes][cells][ldx] or [cells][ldx]."""
+        P = _lib.ptr
+        tb, nbb = self.tile_base[k], self.schic[k].num_bin_batch
+        ss = P(self.sumsq) + tb * self.Ct * 8
+        offs = P(self.store.offsets)
+        pst = self.Ct * ldx if self.planes == 2 else 0
+        if self.bf16 and self.max_rows <= 128 and self.max_width <= 256:
+            form = self._rwr_form or self.cached_rwr_form() or 1
+            if form == 2 and self.max_width > 192:
+                form = 1
+            _lib.call("fh_rwr_tiles_tc", tiles_ptr, nbb, self.Ct, self.max_rows, self.max_width,
+                      entries_ptr, offs, P(X), ldx, pst, ss, int(form), P(self.status), self.sp())
+        elif self.bf16:
+            _lib.call("fh_rwr_tiles_bf16", tiles_ptr, nbb, self.Ct, self.max_rows,
+                      self.max_width, entries_ptr, offs, P(X), ldx, pst, ss, P(self.status),
+                      self.sp())
+        else:
+            _lib.call("fh_rwr_tiles_f32", tiles_ptr, nbb, self.Ct, self.max_rows, self.max_width,
+                      entries_ptr, offs, P(X), ldx, ss, P(self.status), self.sp())
+
+    def _walk_streamed(self):
+        """The walk of a budgeted engine.  The streamed windows first: each window's datasets
+        are walked into slot 0 (zeroed, so its padding columns are zero) with their segments
+        beside it, and the slot is copied out to the window's host buffer on the copy stream;
+        then the resident chromosomes, their segments at the start of the staging area (after
+        the last copy-out has read slot 0)."""
+        torch, P = self.torch, _lib.ptr
+        xs = self.xs
+        main = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        xs.reset()
+        last = None
+        for wi, w in enumerate(xs.plan.windows):
+            if last is not None:
+                main.wait_event(last)
+            view = xs.view(0, wi)
+            with torch.cuda.stream(main):
+                view.zero_()
+            for c in w.chroms:
+                for k in self.groups[c][0]:
+                    tiles = P(xs.win_tiles[wi]) + (self.tile_base[k] - xs.win_t0[wi]) * \
+                        _lib.TILE_DTYPE.itemsize
+                    ent = xs.entries_ptr(True)
+                    self.store.build(k, ent, main)
+                    self._walk_dataset(k, view, w.ld, tiles, ent)
+            last = xs.store_window(wi, 0, main)
+        if last is not None:
+            main.wait_event(last)
+        n_res = xs.plan.first_streamed_chrom
+        n_res = len(self.groups) if n_res is None else n_res
+        for c in range(n_res):
+            for k in self.groups[c][0]:
+                ent = xs.entries_ptr(False)
+                self.store.build(k, ent, main)
+                self._walk_dataset(k, xs.res, xs.plan.ld_res,
+                                   P(self.tiles_dev) + self.tile_base[k] * _lib.TILE_DTYPE.itemsize,
+                                   ent)
+        xs.reset()
+
     def _rwr_signature(self):
         return (self.precision, self.Ct, self.n_tiles, self.max_width,
                 int(np.asarray(self.tiles["n_rwr"]).max()))
@@ -407,35 +574,96 @@ class FitEngine:
         name = "fh_xg_bf16_splits" if self.bf16 else "fh_xg_splits"
         return _lib.value(name, n_cells, rows)
 
-    def x_times_e(self, a0, rows, n_cells, E, rp, W, E2=None):
+    def x_rows(self, x0, x1):
+        """A view of X holding band rows [x0, x1): (tensor, row stride, band row of its column
+        0).  X itself when it is resident; with a budget, the resident part or the slot that
+        holds the window of those rows (copied in if needed; [x0, x1) within one chromosome
+        group's rows)."""
+        if self.xs is None:
+            return (self.X16 if self.bf16 else self.X), self.ldx, 0
+        plan = self.xs.plan
+        if x1 <= plan.split:
+            return self.xs.res, plan.ld_res, 0
+        for wi, w in enumerate(plan.windows):
+            if w.x0 <= x0 and x1 <= w.x1:
+                return self.xs.hold(wi, self.stream), w.ld, w.x0
+        raise _lib.FHError("x_rows", 1, "rows [%d, %d) span a streamed window's edge" % (x0, x1))
+
+    def x_times_e(self, a0, rows, n_cells, E, rp, W, E2=None, view=None):
         """W[row][m] = sum_{c < n_cells} X[c][a0 + row] E[c][m]  (E: [n_cells][rp] fp32,
-        W: [rows][rp]); a0 is a multiple of 128."""
+        W: [rows][rp]); a0 is a multiple of 128.  view: (X tensor, row stride) from x_rows
+        (default: X itself)."""
         P = _lib.ptr
+        X, ld = view if view is not None else ((self.X16 if self.bf16 else self.X), self.ldx)
         if self.bf16:
             if E2 is None:
                 E2 = self.torch.empty((n_cells, 2 * rp), dtype=self.torch.bfloat16,
                                       device=self.device)
             _lib.call("fh_split_bf16", P(E), n_cells, rp, rp, P(E2), self.sp())
-            _lib.call("fh_xe_bf16", P(self.X16[0, :, a0:]), self.ldx, self.Ct, self.planes,
-                      n_cells, rows, P(E2), rp, self.fold, P(W), P(self.status), self.sp())
+            _lib.call("fh_xe_bf16", P(X[0, :, a0:]), ld, self.Ct, self.planes, n_cells, rows,
+                      P(E2), rp, self.fold, P(W), P(self.status), self.sp())
         else:
-            _lib.call("fh_xe_f32", P(self.X[:, a0:]), self.ldx, n_cells, rows, P(E), rp, P(W),
-                      self.sp())
+            _lib.call("fh_xe_f32", P(X[:, a0:]), ld, n_cells, rows, P(E), rp, P(W), self.sp())
 
-    def x_times_g(self, a0, rows, n_cells, Gt, rp, splits, partial, out, G2=None):
-        """out[c][m] = sum_row X[c][a0 + row] Gt[row][m] for c < n_cells (Gt: [rows][rp])."""
+    def x_times_g(self, a0, rows, n_cells, Gt, rp, splits, partial, out, G2=None, view=None):
+        """out[c][m] = sum_row X[c][a0 + row] Gt[row][m] for c < n_cells (Gt: [rows][rp]).
+        view: as for x_times_e."""
         P = _lib.ptr
+        X, ld = view if view is not None else ((self.X16 if self.bf16 else self.X), self.ldx)
         if self.bf16:
             if G2 is None:
                 G2 = self.torch.empty((rows, 2 * rp), dtype=self.torch.bfloat16,
                                       device=self.device)
             _lib.call("fh_split_bf16", P(Gt), rows, rp, rp, P(G2), self.sp())
-            _lib.call("fh_xg_bf16", P(self.X16[0, :, a0:]), self.ldx, self.Ct, self.planes,
-                      n_cells, rows, P(G2), rp, splits, self.fold, P(partial), P(out),
-                      P(self.status), self.sp())
+            _lib.call("fh_xg_bf16", P(X[0, :, a0:]), ld, self.Ct, self.planes, n_cells, rows,
+                      P(G2), rp, splits, self.fold, P(partial), P(out), 0, P(self.status),
+                      self.sp())
         else:
-            _lib.call("fh_xg_f32", P(self.X[:, a0:]), self.ldx, n_cells, rows, P(Gt), rp, splits,
-                      P(partial), P(out), self.sp())
+            _lib.call("fh_xg_f32", P(X[:, a0:]), ld, n_cells, rows, P(Gt), rp, splits,
+                      P(partial), P(out), 0, self.sp())
+
+    def _stream_xe(self, n_cells, E, rp, W, E2):
+        """W = X^T E over every band row of a budgeted engine: E split once, then one pass per
+        row range (resident rows, then each window at its rows of W)."""
+        P = _lib.ptr
+        sp = self.sp()
+        if self.bf16:
+            _lib.call("fh_split_bf16", P(E), n_cells, rp, rp, P(E2), sp)
+
+        def seg(X, ld, x0, rows):
+            w = P(W) + x0 * rp * 4
+            if self.bf16:
+                _lib.call("fh_xe_bf16", P(X), ld, self.Ct, self.planes, n_cells, rows, P(E2), rp,
+                          self.fold, w, P(self.status), sp)
+            else:
+                _lib.call("fh_xe_f32", P(X), ld, n_cells, rows, P(E), rp, w, sp)
+
+        self.xs.run_pass(lambda X, rows: seg(X, self.xs.plan.ld_res, 0, rows),
+                         lambda X, w: seg(X, w.ld, w.x0, w.x1 - w.x0), self.stream)
+
+    def _stream_xg(self, n_cells, Gt, rp, out, G2):
+        """out = X Gt over every band row of a budgeted engine: Gt split once; the first row
+        range writes out, the others add into it."""
+        P = _lib.ptr
+        sp = self.sp()
+        if self.bf16:
+            _lib.call("fh_split_bf16", P(Gt), self.rows, rp, rp, P(G2), sp)
+        first = [True]
+
+        def seg(X, ld, x0, rows):
+            acc = 0 if first[0] else 1
+            first[0] = False
+            splits = min(self.xg_splits(n_cells, rows), self.partial.shape[0])
+            if self.bf16:
+                _lib.call("fh_xg_bf16", P(X), ld, self.Ct, self.planes, n_cells, rows,
+                          P(G2) + x0 * 2 * rp * 2, rp, splits, self.fold, P(self.partial),
+                          P(out), acc, P(self.status), sp)
+            else:
+                _lib.call("fh_xg_f32", P(X), ld, n_cells, rows, P(Gt) + x0 * rp * 4, rp, splits,
+                          P(self.partial), P(out), acc, sp)
+
+        self.xs.run_pass(lambda X, rows: seg(X, self.xs.plan.ld_res, 0, rows),
+                         lambda X, w: seg(X, w.ld, w.x0, w.x1 - w.x0), self.stream)
 
     def tensor_norms(self):
         """||X||^2 per dataset over the good-QC cells (parafac2_intergrative.py:369)."""
@@ -494,6 +722,10 @@ class FitEngine:
 
     # ------------------------------------------------------------------ kernels
     def xe(self):
+        if self.xs is not None:
+            self._timed("xe", lambda: self._stream_xe(self.C, self.E, self.rp, self.W,
+                                                      self.E2[:self.C] if self.bf16 else None))
+            return
         self._timed("xe", lambda: self.x_times_e(0, self.rows, self.C, self.E, self.rp, self.W,
                                                  self.E2[:self.C] if self.bf16 else None))
 
@@ -523,6 +755,10 @@ class FitEngine:
         return self._tuned[n_cells]
 
     def xg(self, n_cells):
+        if self.xs is not None:
+            self._timed("xg", lambda: self._stream_xg(n_cells, self.Gt, self.rp, self.S,
+                                                      self.G2 if self.bf16 else None))
+            return
         splits = self.tuned_splits(n_cells)
         self._timed("xg", lambda: self.x_times_g(0, self.rows, n_cells, self.Gt, self.rp,
                                                  splits, self.partial, self.S,
@@ -677,9 +913,14 @@ class FitEngine:
         sequence is captured once into a CUDA graph (per schedule and history buffers) and
         replayed: every launch, buffer and tensor map in it is fixed, so replays are exact
         repeats of the eager launches.  The capture runs after one eager pass has set every
-        kernel's shared-memory attribute."""
+        kernel's shared-memory attribute.  A budgeted engine starts every sequence with empty
+        staging slots (its first pass copies its windows in), so a replay depends on nothing
+        an earlier launch left in them; after a replay the slots hold what the captured
+        sequence left."""
         torch = self.torch
         sched = self.parafac_schedule(n_iter, n_iter_parafac)
+        if self.xs is not None:
+            self.xs.reset()
         if not graph:
             for it in range(n_iter):
                 self.iterate(it == 0, sched[it], hist[it])
@@ -703,9 +944,12 @@ class FitEngine:
             _lib.launches = n0
             if not hasattr(self, "_graphs"):
                 self._graphs = {}
-            self._graphs[key] = (g, n_kernels)
-        g, n_kernels = self._graphs[key]
+            slots = list(self.xs.slot_win) if self.xs is not None else None
+            self._graphs[key] = (g, n_kernels, slots)
+        g, n_kernels, slots = self._graphs[key]
         g.replay()
+        if self.xs is not None:
+            self.xs.slot_win = list(slots)
         _lib.launches += n_kernels                  # the kernels each replay runs
 
     def core_norm(self):

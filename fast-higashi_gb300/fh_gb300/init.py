@@ -106,12 +106,14 @@ def randomized_features(eng, ks, n_comp, rng, n_oversamples=10, n_iter=2):
     torch = eng.torch
     C = eng.C
     x0, x1 = _chrom_band_rows(eng, ks)
-    a0 = (x0 // 128) * 128
-    a1 = min(eng.ldx, int(math.ceil(x1 / 128) * 128))
+    view = eng.x_rows(x0, x1)                 # (X or the part holding these rows, stride, base)
+    X, ld, base = view
+    a0 = ((x0 - base) // 128) * 128
+    a1 = min(ld, int(math.ceil((x1 - base) / 128) * 128))
     rows = a1 - a0
     n = n_comp + n_oversamples
     dev, f32 = eng.device, torch.float32
-    lo, hi = x0 - a0, x1 - a0
+    lo, hi = x0 - base - a0, x1 - base - a0
     bufs = {}
 
     def blocks_of(w):
@@ -132,7 +134,7 @@ def randomized_features(eng, ks, n_comp, rng, n_oversamples=10, n_iter=2):
             rp, (W, _, _, _) = buffers(c1 - c0)
             E = torch.zeros((C, rp), dtype=f32, device=dev)
             E[:, :c1 - c0] = Ecells[:, c0:c1]
-            eng.x_times_e(a0, rows, C, E, rp, W)
+            eng.x_times_e(a0, rows, C, E, rp, W, view=(X, ld))
             out.append(W[lo:hi, :c1 - c0].clone())
         return torch.cat(out, dim=1)
 
@@ -142,7 +144,7 @@ def randomized_features(eng, ks, n_comp, rng, n_oversamples=10, n_iter=2):
             rp, (_, S, splits, part) = buffers(c1 - c0)
             G = torch.zeros((rows, rp), dtype=f32, device=dev)
             G[lo:hi, :c1 - c0] = Qrows[:, c0:c1]
-            eng.x_times_g(a0, rows, C, G, rp, splits, part, S)
+            eng.x_times_g(a0, rows, C, G, rp, splits, part, S, view=(X, ld))
             out.append(S[:, :c1 - c0].clone())
         return torch.cat(out, dim=1)
 
@@ -295,7 +297,7 @@ def init_params(model, schic, do_conv, do_rwr, do_col, seed=None):
               for c, s in sizes.items()}
     eng = FitEngine(schic, rank, sizes, None, device, do_rwr=do_rwr,
                     precision=getattr(model, "precision", "fp32"), do_conv=do_conv,
-                    do_col=do_col)
+                    do_col=do_col, hbm_budget=getattr(model, "hbm_budget", None))
     model.engine = eng
     if eng.do_col:
         # coverage from the plain walk, then the features from the do_col walk (:96-240)

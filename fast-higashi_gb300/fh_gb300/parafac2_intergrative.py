@@ -28,12 +28,16 @@ from .engine import FitEngine
 
 
 class Fast_Higashi_core:
-    def __init__(self, rank, off_diag, res_list, precision="fp32"):
+    def __init__(self, rank, off_diag, res_list, precision="fp32", hbm_budget=None):
         """precision: "fp32" is the plain drop-in (the reference's arithmetic on CUDA cores);
         "bf16x2" keeps the RWR output as two bf16 planes (16 significant bits) and runs the
-        passes over it on the tensor cores; "bf16" keeps one plane (X rounded to bf16)."""
+        passes over it on the tensor cores; "bf16" keeps one plane (X rounded to bf16).
+        hbm_budget: bytes of device memory the fit may hold (None: everything resident); when
+        X does not fit, its last chromosomes stream from host memory (fh_gb300/xstream.py) and
+        the contact segments are built one dataset at a time."""
         self.rank = rank
         self.precision = precision
+        self.hbm_budget = hbm_budget
         self.use_graph = True
         self.sparse_conv = False
         self.off_diag = off_diag
@@ -106,7 +110,8 @@ class Fast_Higashi_core:
                 raise _lib.FHError("fit", 1, "do_col needs bin_cov_list (init_params sets it)")
             self.engine = FitEngine(schic, self.rank, self.chrom2size, self.n_i, self.device,
                                     do_rwr=do_rwr, precision=self.precision, do_conv=do_conv,
-                                    do_col=col, bin_cov=cov)
+                                    do_col=col, bin_cov=cov,
+                                    hbm_budget=getattr(self, "hbm_budget", None))
             if col:
                 self.engine.cov_src = self._coverage_src()
         elif col:

@@ -415,6 +415,87 @@ class ContactStore:
         self.build_all()
 
 
+class StreamedContacts:
+    """The contact build for a fit whose device memory is budgeted: one dataset at a time.
+
+    The host COO stays where the caller holds it, page-locked in place and mapped into the
+    device's address space, and fh_contacts_count / fh_contacts_scatter read it through that
+    mapping (12 + 16 bytes per contact over the host link, no device copy).  Each build(k)
+    writes dataset k's (tile, cell) segments to the buffer the caller names, with offsets
+    local to the dataset (its tiles counted from its first), so the walk of dataset k runs
+    right after it and the next build reuses the same memory."""
+
+    def __init__(self, datasets, device, tiles, tile_base, status, order=None):
+        import ctypes
+        import torch
+        self.torch = torch
+        self.device = device
+        self.n_cells = datasets[0].total_cell_num
+        self.tiles_np = tiles
+        self.tiles_dev = torch.from_numpy(tiles.view(np.uint8).copy()).to(device)
+        self.n_tiles = len(tiles)
+        self.meta = [(d.bs_bin, base, d.num_bin_batch) for d, base in zip(datasets, tile_base)]
+        self.order = list(range(len(datasets))) if order is None else list(order)
+        self.status = status
+        self._host = []
+        self.src = [None] * len(datasets)
+        for k in self.order:
+            t = datasets[k].tensor
+            hi = _pin(np.ascontiguousarray(np.asarray(t.indices, dtype=np.int32)))
+            hv = _pin(np.ascontiguousarray(np.asarray(t.values, dtype=np.float32)))
+            self._host += [hi, hv]
+            nnz = int(hv.size)
+            ptrs = [None] * 4
+            if nnz:
+                # device addresses of the two page-locked arrays (each registered from its
+                # first byte); the index rows are offsets into the first
+                bases = []
+                for a in (hi, hv):
+                    d = ctypes.c_void_p()
+                    _lib.call("fh_host_device_pointer", a.ctypes.data, ctypes.byref(d))
+                    bases.append(int(d.value))
+                ptrs = [bases[0] + r * nnz * 4 for r in range(3)] + [bases[1]]
+            self.src[k] = (ptrs, nnz)
+        self.nnz = [s[1] for s in self.src]
+        self.link_bytes = 28 * sum(self.nnz)      # read in place per build of every dataset
+        C = self.n_cells
+        n_max = max(nbb for _, _, nbb in self.meta) * C
+        self.counts = torch.zeros(n_max, dtype=torch.int32, device=device)
+        self.cursor = torch.zeros_like(self.counts)
+        self.offsets = torch.zeros(n_max + 1, dtype=torch.int64, device=device)
+        self.scan_ws = torch.empty(_lib.value("fh_scan_workspace", n_max), dtype=torch.uint8,
+                                   device=device)
+
+    def entries_bytes(self, k):
+        return 8 * self.nnz[k]
+
+    def build(self, k, entries_ptr, stream):
+        """Segments of dataset k into entries_ptr (entries_bytes(k) bytes), offsets into
+        self.offsets[:num_bin_batch * cells + 1], on the given torch stream."""
+        P = _lib.ptr
+        bs_bin, base, nbb = self.meta[k]
+        (row, col, cell, val), nnz = self.src[k]
+        C = self.n_cells
+        n = nbb * C
+        sp = stream.cuda_stream
+        tiles = P(self.tiles_dev) + base * _lib.TILE_DTYPE.itemsize
+        with self.torch.cuda.stream(stream):
+            self.counts[:n].zero_()
+            self.cursor[:n].zero_()
+        _lib.call("fh_contacts_count", row, col, cell, nnz, bs_bin, tiles, 0, nbb, C,
+                  P(self.counts), P(self.status), sp)
+        _lib.call("fh_exclusive_scan", P(self.counts), n, P(self.offsets), P(self.scan_ws),
+                  self.scan_ws.numel(), sp)
+        _lib.call("fh_contacts_scatter", row, col, cell, val, nnz, bs_bin, tiles, 0, nbb, C,
+                  P(self.offsets), P(self.cursor), entries_ptr, sp)
+
+    def rebuild(self):
+        """Nothing to do: every walk builds its dataset's segments first."""
+
+    def finish(self):
+        pass
+
+
 def tile_table(datasets, chrom_index=None, ranks=None, n_rwr=None, order=None):
     """fh_tile records for the bin batches of the datasets (in the given order), with band
     rows, bin rows and projection offsets laid out consecutively.  Returns (tiles,

@@ -245,12 +245,14 @@ int fh_rwr_tiles_deltas(const fh_tile* tiles, int32_t n_tiles, int32_t n_cells,
  *             temp_i = W_i D diag(A_i) B^T (:336,374-383) and Y_i = U_i^T W_i (:522-529).
  * fh_xg_f32:  out[c][m] = sum_row X[c][row] Gt[row][m]  (SVD_term^T, :422-477) with
  *             Gt_i = U_i lhs2_i^T; partial: float[splits][n_cells][rp] workspace, splits from
- *             fh_xg_splits (the reduction over splits runs in a fixed order). */
+ *             fh_xg_splits (the reduction over splits runs in a fixed order).  accumulate != 0
+ *             adds the sum into out instead (X held in several row ranges, one call each). */
 int fh_xe_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const float* E,
               int32_t rp, float* W, void* stream);
 int fh_xg_splits(int32_t n_cells, int64_t rows);
 int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const float* Gt,
-              int32_t rp, int32_t splits, float* partial, float* out, void* stream);
+              int32_t rp, int32_t splits, float* partial, float* out, int32_t accumulate,
+              void* stream);
 
 /* ---- the same two passes over X held in bf16, on the tcgen05 tensor cores (no reference
  * counterpart: the reference's passes are fp32 torch.bmm / opt_einsum calls at
@@ -265,7 +267,8 @@ int fh_xg_f32(const float* X, int64_t ldx, int32_t n_cells, int64_t rows, const 
  *                (bf16[n_cells][2 rp]).  rp in {32, 64, 128}.
  * fh_xg_bf16:    out[c][m] = sum_row X16[c][row] Gt[row][m] for c < n_cells;  G2 = split of
  *                Gt (bf16[rows][2 rp]); partial: float[splits][n_cells][rp] with splits from
- *                fh_xg_bf16_splits (fixed-order reduction in fp64).
+ *                fh_xg_bf16_splits (fixed-order reduction in fp64); accumulate != 0 adds
+ *                the sum into out.
  * fold: K chunks of 64 (cells for fh_xe_bf16, band rows for fh_xg_bf16) summed in one tensor
  *       memory accumulator before the epilogue folds them into Kahan-compensated fp32 running
  *       sums; 0 selects the library default (8).  Short runs keep the fp32 rounding of long K
@@ -279,7 +282,8 @@ int fh_xe_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t 
 int fh_xg_bf16_splits(int32_t n_cells, int64_t rows);
 int fh_xg_bf16(const uint16_t* X16, int64_t ldx, int32_t n_cells_total, int32_t planes,
                int32_t n_cells, int64_t rows, const uint16_t* G2, int32_t rp, int32_t splits,
-               int32_t fold, float* partial, float* out, int* status, void* stream);
+               int32_t fold, float* partial, float* out, int32_t accumulate, int* status,
+               void* stream);
 
 /* Y[g][l][m] = sum_j U_g[j][l] W[xoff + i*width + j][m] for every bin row g (K16 tail,
  * parafac2_intergrative.py:522-529); Y: float[n_rows][ldy_l][rp]; row_tile: int32[n_rows];
@@ -472,6 +476,22 @@ int fh_pool_rows(const fh_tile* tiles, int32_t n_tiles, const int64_t* prow0,
 int fh_unpool_rows(const fh_tile* tiles, int32_t n_tiles, const int64_t* prow0,
                    const int32_t* ll, int64_t x0, int64_t rows, const float* in, int64_t ldi,
                    int32_t m, float* out, int64_t ldo, void* stream);
+
+/* ---- host memory for X held partly outside HBM and for contacts read in place (no
+ * reference counterpart: the reference tiles its work by free GPU memory instead,
+ * FastHigashi_Wrapper.py:497-517, and copies each tile's COO slice to the device,
+ * sparse_for_schic.py:588-613).
+ * fh_host_alloc: page-locked host memory, mapped into the device address space (cudaHostAlloc,
+ *   portable | mapped); fh_host_free releases it.
+ * fh_host_device_pointer: the device address of page-locked, mapped host memory (host memory
+ *   registered in place, or from fh_host_alloc); FH_ERR_ARG if it is neither.  Kernels read a
+ *   chromosome's COO through it (fh_contacts_count / fh_contacts_scatter) with no device copy.
+ * fh_memcpy_async: one asynchronous copy of bytes between any two of host and device memory on
+ *   stream (a memcpy node when the stream is being captured into a CUDA graph). */
+int fh_host_alloc(int64_t bytes, void** out);
+int fh_host_free(void* p);
+int fh_host_device_pointer(const void* host, void** dev);
+int fh_memcpy_async(void* dst, const void* src, int64_t bytes, void* stream);
 
 /* ---- self-test of the bounded device-side waits (no reference counterpart: the reference
  * has no device code).  One warp allocates tensor memory, waits on an mbarrier that nothing

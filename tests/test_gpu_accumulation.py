@@ -117,7 +117,7 @@ def test_xg_long_sum_35000_rows_per_split():
     partial = torch.empty((splits, n, rp), device=CUDA)
     out = torch.empty((n, rp), device=CUDA)
     errs = {}
-    _lib.call("fh_xg_f32", P(X), ldx, n, rows, P(Gt), rp, splits, P(partial), P(out), sp())
+    _lib.call("fh_xg_f32", P(X), ldx, n, rows, P(Gt), rp, splits, P(partial), P(out), 0, sp())
     errs["fp32"] = rel(out, X[:, :rows].double() @ Gt.double())
     X16, Xv = planes_of(X)
     G2 = split(Gt)
@@ -125,7 +125,7 @@ def test_xg_long_sum_35000_rows_per_split():
     errs["bf16x2_split_floor"] = rel(Xv[:, :rows] @ unsplit(G2, rp), ref)
     for fold in (1, 8, 1 << 20):
         _lib.call("fh_xg_bf16", P(X16), ldx, n, 2, n, rows, P(G2), rp, splits, fold,
-                  P(partial), P(out), P(st), sp())
+                  P(partial), P(out), 0, P(st), sp())
         torch.cuda.synchronize()
         assert int(st.item()) == 0
         errs["bf16x2_fold%d" % fold] = rel(out, ref)
@@ -153,7 +153,7 @@ def test_fold_every_rank(rp):
     partial = torch.empty((splits, C, rp), device=CUDA)
     out = torch.full((C, rp), float("nan"), device=CUDA)
     _lib.call("fh_xg_bf16", P(X16), ldx, C, 2, C, rows, P(G2), rp, splits, 3, P(partial),
-              P(out), P(st), sp())
+              P(out), 0, P(st), sp())
     torch.cuda.synchronize()
     assert int(st.item()) == 0
     e_w = rel(W, Xv[:, :rows].T @ unsplit(E2, rp))

@@ -93,7 +93,7 @@ def test_xg_bf16(rp, ct, n, rows, planes):
     out = torch.full((n, rp), float("nan"), device=CUDA)
     st = torch.zeros(1, dtype=torch.int32, device=CUDA)
     _lib.call("fh_xg_bf16", P(X16), ldx, ct, planes, n, rows, P(G2), rp, splits, 0, P(partial),
-              P(out), P(st), sp())
+              P(out), 0, P(st), sp())
     torch.cuda.synchronize()
     assert int(st.item()) == 0
     ref = Xv[:n, :rows] @ Gt.double()
@@ -111,7 +111,7 @@ def test_xpass_bf16_deterministic():
     for _ in range(2):
         out = torch.empty((1000, 64), device=CUDA)
         _lib.call("fh_xg_bf16", P(X16), ldx, 1000, 2, 1000, 30000, P(G2), 64, splits, 0,
-                  P(partial), P(out), P(st), sp())
+                  P(partial), P(out), 0, P(st), sp())
         outs.append(out)
     torch.cuda.synchronize()
     assert torch.equal(outs[0], outs[1])

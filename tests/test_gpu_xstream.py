@@ -1,0 +1,138 @@
+"""X held partly in host memory (an engine with hbm_budget, fh_gb300/xstream.py) against the
+same fit with X resident, on a 6-chromosome workload whose budget streams at least three
+windows through the two staging slots.
+
+* the walk: the resident part and every host window hold exactly the resident engine's X
+  (the streamed chromosomes walked into a slot with their band rows re-based);
+* init_params through the streamed X passes: the same auto-stop epochs and features;
+* the fit (captured into a CUDA graph, with the window copies as memcpy nodes) and transform
+  from the same state: X^T E is computed row range by row range with the same sums, X G^T
+  adds the ranges' sums, so the embeddings agree to fp32 rounding (1e-5)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+CUDA = "cuda"
+
+
+def _datasets(w, seed=0):
+    from fh_gb300 import synth
+    from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
+    coo, _ = synth.generate(w, seed=seed)
+    ds = []
+    for (idx, val, shape), name, nb in zip(coo, w.chrom_names, w.chrom_bins):
+        bsb, bsc = synth.recommend_batches(w, nb, w.n_cells)
+        ds.append(Chrom_Dataset(Sparse(idx, val, shape), bsb, bsc, compact=True, flank=w.band,
+                                chrom=name, resolution=w.resolution))
+    return ds
+
+
+def _workload():
+    from fh_gb300 import synth
+    return synth.Workload("stream6", 800, [60, 50, 45, 40, 35, 30], 1_000_000, 10, (0.9, 1.3),
+                          8_000, 0.6, 3, 16, 5)
+
+
+def _model(w, precision, budget=None):
+    from fh_gb300 import Fast_Higashi_core
+    m = Fast_Higashi_core(w.rank, w.band, [w.resolution], precision=precision,
+                          hbm_budget=budget).to(CUDA)
+    return m
+
+
+def _budget_for_windows(w, ds, precision, min_windows=3):
+    """The smallest budget (reserve 0) whose plan streams at least min_windows windows, found
+    by lowering the budget until the plan has them."""
+    from fh_gb300.engine import FitEngine
+    m = _model(w, precision)
+    m._sizes(ds, w.dim1, None)
+    elem = 4
+    e0 = FitEngine(ds, w.rank, m.chrom2size, None, CUDA, precision=precision)
+    total = e0.rows * e0.Ct * elem + e0._buffer_bytes() + (64 << 20)
+    del e0
+    for frac in np.linspace(1.0, 0.3, 71):
+        b = int(total * frac)
+        try:
+            e = FitEngine(ds, w.rank, m.chrom2size, None, CUDA, precision=precision, hbm_budget=b)
+        except Exception:
+            continue
+        n = len(e.xs.plan.windows)
+        del e
+        if n >= min_windows:
+            return b
+    raise AssertionError("no budget streams %d windows" % min_windows)
+
+
+def _host_array(buf, dtype, shape):
+    n = int(np.prod(shape))
+    raw = (ctypes.c_uint8 * (n * np.dtype(dtype).itemsize)).from_address(buf.ptr)
+    return np.frombuffer(raw, dtype=dtype).reshape(shape).copy()
+
+
+@pytest.mark.parametrize("precision", ["bf16x2", "fp32"])
+def test_streamed_x_matches_resident_x(precision, monkeypatch):
+    from fh_gb300.engine import FitEngine
+    monkeypatch.setattr(FitEngine, "BUDGET_RESERVE", 0)
+    w = _workload()
+    ds = _datasets(w)
+    budget = _budget_for_windows(w, ds, precision)
+
+    torch.manual_seed(0)
+    mA = _model(w, precision)
+    mA._sizes(ds, w.dim1, None)
+    mA.init_params(ds, False, True, False, seed=0)
+    torch.manual_seed(0)
+    mB = _model(w, precision, budget)
+    mB._sizes(ds, w.dim1, None)
+    mB.init_params(ds, False, True, False, seed=0)
+    eA, eB = mA.engine, mB.engine
+    assert eB.xs is not None and len(eB.xs.plan.windows) >= 3
+    np.testing.assert_array_equal(np.asarray(mA.n_i), np.asarray(mB.n_i))
+    torch.cuda.synchronize()
+
+    # the walk's X, resident part and host windows, bit for bit
+    plan = eB.xs.plan
+    if precision == "fp32":
+        XA = eA.X.cpu().numpy().view(np.uint32)
+        np.testing.assert_array_equal(eB.xs.res[:, :plan.split].cpu().numpy().view(np.uint32),
+                                      XA[:, :plan.split])
+        for wi, win in enumerate(plan.windows):
+            h = _host_array(eB.xs.host[wi], np.uint32, (eB.Ct, win.ld))
+            np.testing.assert_array_equal(h[:, :win.x1 - win.x0], XA[:, win.x0:win.x1])
+            assert not h[:, win.x1 - win.x0:].any()
+    else:
+        XA = eA.X16.view(torch.int16).cpu().numpy()
+        np.testing.assert_array_equal(eB.xs.res.view(torch.int16)[:, :, :plan.split].cpu().numpy(),
+                                      XA[:, :, :plan.split])
+        for wi, win in enumerate(plan.windows):
+            h = _host_array(eB.xs.host[wi], np.int16, (eB.planes, eB.Ct, win.ld))
+            np.testing.assert_array_equal(h[:, :, :win.x1 - win.x0], XA[:, :, win.x0:win.x1])
+            assert not h[:, :, win.x1 - win.x0:].any()
+    np.testing.assert_array_equal(eA.sumsq.cpu().numpy(), eB.sumsq.cpu().numpy())
+
+    # init_params' features through the streamed passes
+    EA, EB = mA.meta_embedding.cpu().double(), mB.meta_embedding.cpu().double()
+    assert float((EA - EB).norm() / EA.norm()) < 1e-4
+
+    # the fit and transform from one state
+    state = ([a.clone() for a in mA.A_list], {k: v.clone() for k, v in mA.B_dict.items()},
+             {k: v.clone() for k, v in mA.D_dict.items()}, mA.meta_embedding.clone())
+    for m in (mA, mB):
+        m.A_list, m.B_dict, m.D_dict, m.meta_embedding = (
+            [a.clone() for a in state[0]], {k: v.clone() for k, v in state[1].items()},
+            {k: v.clone() for k, v in state[2].items()}, state[3].clone())
+        for _ in range(2):                       # the second fit replays the captured graph
+            m.fit(ds, size_ratio=w.dim1, n_iter_max=w.n_iter, n_iter_parafac=1, do_conv=False,
+                  do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
+    fA, fB = mA.meta_embedding.cpu().double(), mB.meta_embedding.cpu().double()
+    assert float((fA - fB).norm() / fA.norm()) < 1e-5
+    np.testing.assert_allclose(mB.rec_errors_total, mA.rec_errors_total, rtol=1e-6)
+    tA = mA.transform(ds, False, True, False)[1][3].cpu().double()
+    tB = mB.transform(ds, False, True, False)[1][3].cpu().double()
+    assert float((tA - tB).norm() / tA.norm()) < 1e-5
+    assert eB.xs.link_bytes > 0

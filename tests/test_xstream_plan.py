@@ -1,0 +1,185 @@
+"""The plan and the copy schedule of X held partly in host memory (fh_gb300/xstream.py), on
+the CPU: which chromosomes stream, how they group into windows, the staging size, and the order
+in which a pass reads the resident rows and the windows and copies windows into the two slots."""
+import itertools
+
+import numpy as np
+import pytest
+
+from fh_gb300 import _lib, synth, xstream
+
+
+def chrom_rows_of(w):
+    rows, x = [], 0
+    for nb in w.chrom_bins:
+        bsb, _ = synth.recommend_batches(w, nb, w.n_cells)
+        t = 0
+        for r0 in range(0, nb, bsb):
+            r = min(bsb, nb - r0)
+            t += r * (min(nb, r0 + r + w.band) - max(0, r0 - w.band))
+        rows.append((x, x + t))
+        x += t
+    return rows
+
+
+def nbytes(r, C, e):
+    return -(-r // 128) * 128 * C * e
+
+
+def test_everything_resident_when_it_fits():
+    rows = [(0, 1000), (1000, 1700), (1700, 2000)]
+    p = xstream.plan_x(rows, 4, 100, [800, 500, 300], 10 ** 9)
+    assert p.windows == [] and p.split == 2000 and p.ld_res == 2048
+    assert p.res_bytes == 2048 * 100 * 4
+    assert p.staging_bytes >= 800
+
+
+def test_c5_shapes_stream_the_last_chromosomes_within_the_budget():
+    """The 50,000-cell, R = 128 workload in two bf16 planes (179 GB) under a 173 GB X budget."""
+    w = synth.workload("c5")
+    rows = chrom_rows_of(w)
+    ent = [int(8 * 7.0e9 * nb / sum(w.chrom_bins)) for nb in w.chrom_bins]
+    budget = 173.4e9
+    p = xstream.plan_x(rows, 4, w.n_cells, ent, budget)
+    assert 0 < len(p.windows) <= 4
+    assert p.res_bytes + p.staging_bytes <= budget
+    assert p.split == p.windows[0].x0 and p.windows[-1].x1 == rows[-1][1]
+    for a, b in zip(p.windows, p.windows[1:]):
+        assert a.x1 == b.x0 and a.chroms[-1] + 1 == b.chroms[0]
+    assert all(wd.nbytes <= p.slot_bytes for wd in p.windows)
+    assert p.staging_bytes >= 2 * p.slot_bytes and p.staging_bytes >= max(ent)
+    # streaming one chromosome fewer does not fit
+    j = p.windows[0].chroms[0]
+    assert nbytes(rows[j][1], w.n_cells, 4) > budget - 2 * p.slot_bytes or j == len(rows) - 1
+
+
+def test_no_split_fits_raises():
+    rows = [(0, 1000), (1000, 2000)]
+    with pytest.raises(_lib.FHError):
+        xstream.plan_x(rows, 4, 100, [0, 0], 1000)
+
+
+def _brute_min_slot(rows, j, C, e, max_windows):
+    """Smallest largest-window size over every split of chromosomes j.. into at most
+    max_windows contiguous groups."""
+    n = len(rows)
+    m = n - j
+    best = None
+    for k in range(1, min(max_windows, m) + 1):
+        for cuts in itertools.combinations(range(1, m), k - 1):
+            bounds = [0, *cuts, m]
+            big = max(nbytes(rows[j + bounds[i + 1] - 1][1] - rows[j + bounds[i]][0], C, e)
+                      for i in range(k))
+            best = big if best is None else min(best, big)
+    return best
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_plan_streams_the_fewest_chromosomes_with_the_smallest_slots(seed):
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(3, 9))
+    sizes = rng.integers(200, 3000, n)
+    rows, x = [], 0
+    for s in sizes:
+        rows.append((x, x + int(s)))
+        x += int(s)
+    C, e = 50, 4
+    ent = [int(v) for v in rng.integers(0, 200_000, n)]
+    total = nbytes(x, C, e)
+    budget = int(total * rng.uniform(0.55, 0.9))
+    try:
+        p = xstream.plan_x(rows, e, C, ent, budget, max_windows=3)
+    except _lib.FHError:
+        p = None
+
+    def staging(j, slot):
+        ent_res = max([ent[c] for c in range(j)], default=0)
+        ent_str = max([ent[c] for c in range(j, n)], default=0)
+        slot = -(-slot // xstream.SLOT_ALIGN) * xstream.SLOT_ALIGN
+        v = max(2 * slot, ent_res, (slot + ent_str) if j < n else 0, 1)
+        return -(-v // xstream.SLOT_ALIGN) * xstream.SLOT_ALIGN
+
+    feasible = []
+    for j in range(n, -1, -1):
+        res = nbytes(rows[j][0], C, e) if j < n and rows[j][0] > 0 else (0 if j < n else total)
+        slot = _brute_min_slot(rows, j, C, e, 3) if j < n else 0
+        if res + staging(j, slot) <= budget:
+            feasible.append((j, slot))
+    if not feasible:
+        assert p is None
+        return
+    j, slot = feasible[0]                       # the fewest chromosomes streamed
+    assert p is not None
+    assert (p.windows[0].chroms[0] if p.windows else n) == j
+    assert max((wd.nbytes for wd in p.windows), default=0) == slot
+
+
+class _FakeStream:
+    def __init__(self, log):
+        self.log = log
+
+    def wait_event(self, ev):
+        self.log.append(("wait", ev))
+
+
+def _fake_xstream(n_windows, split=1):
+    """An XStream with its copies and views replaced by records of what they would do."""
+    xs = xstream.XStream.__new__(xstream.XStream)
+    wins = [xstream.Window((i,), 10 * i + 10, 10 * i + 20, 128, 1000) for i in range(n_windows)]
+    xs.plan = xstream.XPlan(10 * n_windows + 10, split, 128, 1, wins, 1024, 2048)
+    xs.slot_win = [None, None]
+    xs.res = "resident rows"
+    content = [None, None]
+    log = []
+
+    def load(s, wi, main):
+        content[s] = wi
+        xs.slot_win[s] = wi
+        log.append(("load", s, wi))
+        return ("loaded", s, wi)
+
+    xs._load = load
+    xs.view = lambda s, wi: (s, wi)
+    xs._main = lambda stream: stream
+    return xs, content, log
+
+
+@pytest.mark.parametrize("n_windows", [1, 2, 3, 4, 5])
+def test_pass_order_reads_each_window_once_from_the_slot_that_holds_it(n_windows):
+    xs, content, log = _fake_xstream(n_windows)
+    main = _FakeStream(log)
+    loads_per_pass = []
+    for p in range(6):
+        seen, res = [], []
+        n0 = sum(1 for r in log if r[0] == "load")
+
+        def win_fn(view, w):
+            s, wi = view
+            assert content[s] == wi                # the slot holds this window when it is read
+            seen.append(wi)
+
+        xs.run_pass(lambda X, rows: res.append(rows), win_fn, main)
+        assert sorted(seen) == list(range(n_windows)) and res == [1]
+        loads_per_pass.append(sum(1 for r in log if r[0] == "load") - n0)
+    # after the first pass, only the windows beyond the two slots are copied in again
+    assert all(v == max(0, n_windows - 2) for v in loads_per_pass[1:])
+    assert loads_per_pass[0] == n_windows
+
+
+def test_copies_of_later_windows_are_issued_before_the_resident_rows():
+    """With four windows, the two copies a pass needs are issued before the resident rows are
+    read (each as soon as the window read before it frees its slot), so they run behind that
+    read on the copy stream."""
+    xs, content, log = _fake_xstream(4)
+    main = _FakeStream(log)
+    xs.run_pass(lambda X, rows: None, lambda v, w: None, main)     # from empty slots
+    for _ in range(3):
+        log.clear()
+        xs.run_pass(lambda X, rows: log.append(("res",)), lambda v, w: log.append(("win", v[1])),
+                    main)
+        kinds = [r[0] for r in log]
+        loads = [i for i, k in enumerate(kinds) if k == "load"]
+        assert len(loads) == 2 and kinds.index("res") > max(loads)
+        # the windows read first are the two the previous pass ended with
+        wins = [r[1] for r in log if r[0] == "win"]
+        assert wins[:2] != wins[2:]
