@@ -793,7 +793,10 @@ def budget_arm(args, rank, local, ws):
     eng.timing = {}
     device_step(eng, hist, graph=False)
     torch.cuda.synchronize()
-    kt = {k: round(v["mean_ms"], 3) for k, v in eng.timing_summary().items()}
+    summ = eng.timing_summary()
+    kt = {k: round(v["mean_ms"], 3) for k, v in summ.items()}
+    if "contacts" in summ:            # per dataset; the step's total beside it
+        kt["contacts_per_step"] = round(summ["contacts"]["total_ms"], 3)
     eng.timing = None
     E_main = eng.E[:, :w.rank].clone()
     loss = float(eng.losses(hist[-1], eng.tensor_norms())[0])

@@ -522,7 +522,7 @@ class FitEngine:
                     tiles = P(xs.win_tiles[wi]) + (self.tile_base[k] - xs.win_t0[wi]) * \
                         _lib.TILE_DTYPE.itemsize
                     ent = xs.entries_ptr(True)
-                    self.store.build(k, ent, main)
+                    self._timed("contacts", lambda: self.store.build(k, ent, main))
                     self._walk_dataset(k, view, w.ld, tiles, ent)
             last = xs.store_window(wi, 0, main)
         if last is not None:
@@ -532,7 +532,7 @@ class FitEngine:
         for c in range(n_res):
             for k in self.groups[c][0]:
                 ent = xs.entries_ptr(False)
-                self.store.build(k, ent, main)
+                self._timed("contacts", lambda: self.store.build(k, ent, main))
                 self._walk_dataset(k, xs.res, xs.plan.ld_res,
                                    P(self.tiles_dev) + self.tile_base[k] * _lib.TILE_DTYPE.itemsize,
                                    ent)
@@ -936,20 +936,27 @@ class FitEngine:
             cap = torch.cuda.Stream(device=self.device)
             cap.wait_stream(torch.cuda.current_stream(self.device))
             n0 = _lib.launches
+            l0 = self.xs.link_bytes if self.xs is not None else 0
             with torch.cuda.graph(g, stream=cap):
                 for it in range(n_iter):
                     self.iterate(it == 0, sched[it], hist[it])
             torch.cuda.current_stream(self.device).wait_stream(cap)
             n_kernels = _lib.launches - n0          # captured, not yet launched
             _lib.launches = n0
+            copied = 0
+            slots = None
+            if self.xs is not None:                 # window copies: captured, not yet run
+                copied = self.xs.link_bytes - l0
+                self.xs.link_bytes = l0
+                slots = list(self.xs.slot_win)
             if not hasattr(self, "_graphs"):
                 self._graphs = {}
-            slots = list(self.xs.slot_win) if self.xs is not None else None
-            self._graphs[key] = (g, n_kernels, slots)
-        g, n_kernels, slots = self._graphs[key]
+            self._graphs[key] = (g, n_kernels, slots, copied)
+        g, n_kernels, slots, copied = self._graphs[key]
         g.replay()
         if self.xs is not None:
             self.xs.slot_win = list(slots)
+            self.xs.link_bytes += copied
         _lib.launches += n_kernels                  # the kernels each replay runs
 
     def core_norm(self):
