@@ -1,12 +1,11 @@
-// Host memory for X held partly outside HBM, and for contacts read in place.
+// Host memory for X held partly outside HBM.
 //
 // When X does not fit the HBM budget (50,000 cells at R = 128, band 40: 179 GB in two bf16
 // planes), the last chromosomes' band rows live in page-locked host memory and pass through
 // two staging slots in HBM once per pass over X.  The copies are plain cudaMemcpyAsync calls
 // on a copy stream (one per window, contiguous on both sides), so a CUDA graph captures them as
-// memcpy nodes between the kernels that use the slots.  The host COO of a chromosome is read in
-// place by the contact build (page-locked, mapped into the device's address space), so no
-// device copy of it is held.
+// memcpy nodes between the kernels that use the slots.  The contact build copies a
+// chromosome's host COO in chunks the same way.
 #include "fh_common.cuh"
 
 extern "C" int fh_host_alloc(int64_t bytes, void** out) {
@@ -28,18 +27,6 @@ extern "C" int fh_host_free(void* p) {
     cudaGetLastError();
     return FH_ERR_LAUNCH;
   }
-  return FH_OK;
-}
-
-extern "C" int fh_host_device_pointer(const void* host, void** dev) {
-  if (!host || !dev) return FH_ERR_ARG;
-  *dev = nullptr;
-  void* d = nullptr;
-  if (cudaHostGetDevicePointer(&d, const_cast<void*>(host), 0) != cudaSuccess || !d) {
-    cudaGetLastError();
-    return FH_ERR_ARG;               // not page-locked and mapped
-  }
-  *dev = d;
   return FH_OK;
 }
 

@@ -116,7 +116,6 @@ SIGNATURES = {
                                      SZ, P, P]),
     "fh_host_alloc": (C.c_int, [I64, P]),
     "fh_host_free": (C.c_int, [P]),
-    "fh_host_device_pointer": (C.c_int, [P, P]),
     "fh_memcpy_async": (C.c_int, [P, P, I64, P]),
 }
 

@@ -49,8 +49,8 @@ class FitEngine:
         n_i is given (the walk runs at construction); init_params computes it otherwise.
         hbm_budget: bytes of device memory this engine may hold, or None (X and every
         dataset's contact segments resident).  With a budget, the contact segments are built
-        one dataset at a time from the host COO read in place, and X's last chromosomes stream
-        from host memory when X does not fit (xstream.py)."""
+        one dataset at a time from the host COO (copied in chunks through the staging area),
+        and X's last chromosomes stream from host memory when X does not fit (xstream.py)."""
         import torch
         self.torch = torch
         if precision not in ("fp32", "bf16", "bf16x2"):
@@ -316,12 +316,12 @@ class FitEngine:
                                device=self.device)
         if self.xs is not None:
             # one dataset's segments at a time, at the start of the staging area
-            ent = self.xs.entries_ptr(False)
             main = self.stream if self.stream is not None else \
                 self.torch.cuda.current_stream(self.device)
             for k in self.order:
                 tb, nbb = self.tile_base[k], self.schic[k].num_bin_batch
-                self.store.build(k, ent, main)
+                ent, buf, nbuf = self.xs.build_space(False, self.store.entries_bytes(k))
+                self.store.build(k, ent, main, buf, nbuf)
                 _lib.call("fh_rwr_tiles_deltas", P(self.tiles_dev) + tb * _lib.TILE_DTYPE.itemsize,
                           nbb, self.Ct, self.max_rows, self.max_width, ent,
                           P(self.store.offsets), cap, P(out) + tb * self.Ct * cap * 4,
@@ -521,8 +521,8 @@ class FitEngine:
                 for k in self.groups[c][0]:
                     tiles = P(xs.win_tiles[wi]) + (self.tile_base[k] - xs.win_t0[wi]) * \
                         _lib.TILE_DTYPE.itemsize
-                    ent = xs.entries_ptr(True)
-                    self._timed("contacts", lambda: self.store.build(k, ent, main))
+                    ent, buf, nbuf = xs.build_space(True, self.store.entries_bytes(k))
+                    self._timed("contacts", lambda: self.store.build(k, ent, main, buf, nbuf))
                     self._walk_dataset(k, view, w.ld, tiles, ent)
             last = xs.store_window(wi, 0, main)
         if last is not None:
@@ -531,8 +531,8 @@ class FitEngine:
         n_res = len(self.groups) if n_res is None else n_res
         for c in range(n_res):
             for k in self.groups[c][0]:
-                ent = xs.entries_ptr(False)
-                self._timed("contacts", lambda: self.store.build(k, ent, main))
+                ent, buf, nbuf = xs.build_space(False, self.store.entries_bytes(k))
+                self._timed("contacts", lambda: self.store.build(k, ent, main, buf, nbuf))
                 self._walk_dataset(k, xs.res, xs.plan.ld_res,
                                    P(self.tiles_dev) + self.tile_base[k] * _lib.TILE_DTYPE.itemsize,
                                    ent)

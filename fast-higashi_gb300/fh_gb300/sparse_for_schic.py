@@ -418,15 +418,18 @@ class ContactStore:
 class StreamedContacts:
     """The contact build for a fit whose device memory is budgeted: one dataset at a time.
 
-    The host COO stays where the caller holds it, page-locked in place and mapped into the
-    device's address space, and fh_contacts_count / fh_contacts_scatter read it through that
-    mapping (12 + 16 bytes per contact over the host link, no device copy).  Each build(k)
-    writes dataset k's (tile, cell) segments to the buffer the caller names, with offsets
-    local to the dataset (its tiles counted from its first), so the walk of dataset k runs
-    right after it and the next build reuses the same memory."""
+    The host COO stays where the caller holds it (page-locked in place).  build(k) passes over
+    dataset k's contacts twice in chunks, each chunk copied by the copy engine into one of two
+    buffers the caller lends (double-buffered on a copy stream, so the copy of chunk j + 1 runs
+    under the kernel on chunk j): fh_contacts_count on the (row, column, cell) chunks, the scan
+    of the counts, then fh_contacts_scatter on the full chunks (12 + 16 bytes per contact over
+    the host link).  The (tile, cell) segments go to the buffer the caller names, with offsets
+    local to the dataset (its tiles counted from its first), so the walk of dataset k runs right
+    after it and the next build reuses the same memory."""
+
+    CHUNK_ALIGN = 256
 
     def __init__(self, datasets, device, tiles, tile_base, status, order=None):
-        import ctypes
         import torch
         self.torch = torch
         self.device = device
@@ -437,27 +440,14 @@ class StreamedContacts:
         self.meta = [(d.bs_bin, base, d.num_bin_batch) for d, base in zip(datasets, tile_base)]
         self.order = list(range(len(datasets))) if order is None else list(order)
         self.status = status
-        self._host = []
         self.src = [None] * len(datasets)
         for k in self.order:
             t = datasets[k].tensor
             hi = _pin(np.ascontiguousarray(np.asarray(t.indices, dtype=np.int32)))
             hv = _pin(np.ascontiguousarray(np.asarray(t.values, dtype=np.float32)))
-            self._host += [hi, hv]
-            nnz = int(hv.size)
-            ptrs = [None] * 4
-            if nnz:
-                # device addresses of the two page-locked arrays (each registered from its
-                # first byte); the index rows are offsets into the first
-                bases = []
-                for a in (hi, hv):
-                    d = ctypes.c_void_p()
-                    _lib.call("fh_host_device_pointer", a.ctypes.data, ctypes.byref(d))
-                    bases.append(int(d.value))
-                ptrs = [bases[0] + r * nnz * 4 for r in range(3)] + [bases[1]]
-            self.src[k] = (ptrs, nnz)
-        self.nnz = [s[1] for s in self.src]
-        self.link_bytes = 28 * sum(self.nnz)      # read in place per build of every dataset
+            self.src[k] = (hi, hv, int(hv.size))
+        self.nnz = [s[2] for s in self.src]
+        self.link_bytes = 0                 # host -> device bytes copied so far
         C = self.n_cells
         n_max = max(nbb for _, _, nbb in self.meta) * C
         self.counts = torch.zeros(n_max, dtype=torch.int32, device=device)
@@ -465,16 +455,54 @@ class StreamedContacts:
         self.offsets = torch.zeros(n_max + 1, dtype=torch.int64, device=device)
         self.scan_ws = torch.empty(_lib.value("fh_scan_workspace", n_max), dtype=torch.uint8,
                                    device=device)
+        self.copy = torch.cuda.Stream(device=device)
 
     def entries_bytes(self, k):
         return 8 * self.nnz[k]
 
-    def build(self, k, entries_ptr, stream):
+    def _chunked(self, k, buf_ptr, buf_bytes, arrays, kernel, stream):
+        """kernel(device pointers of the chunk's arrays, m) over dataset k's contacts in chunks,
+        each chunk's arrays (row, col, cell[, val]: 4 bytes per contact each) copied into one
+        half of [buf_ptr, buf_ptr + buf_bytes)."""
+        torch = self.torch
+        hi, hv, nnz = self.src[k]
+        half = (buf_bytes // 2) // self.CHUNK_ALIGN * self.CHUNK_ALIGN
+        m_max = (half // (4 * len(arrays))) // 64 * 64
+        if m_max <= 0:
+            raise _lib.FHError("contact build", 1, "no room for a chunk of the COO")
+        srcs = [hi[0], hi[1], hi[2], hv][:len(arrays)]
+        free = [None, None]
+        for j, e0 in enumerate(range(0, nnz, m_max)):
+            m = min(m_max, nnz - e0)
+            b = j & 1
+            base = buf_ptr + b * half
+            if free[b] is not None:
+                self.copy.wait_event(free[b])
+            else:
+                ev = torch.cuda.Event()
+                ev.record(stream)           # after what the stream issued before this build
+                self.copy.wait_event(ev)
+            dst = []
+            for a, src in enumerate(srcs):
+                d = base + a * m_max * 4
+                _lib.call("fh_memcpy_async", d, src.ctypes.data + e0 * 4, m * 4,
+                          self.copy.cuda_stream)
+                dst.append(d)
+            self.link_bytes += m * 4 * len(srcs)
+            ready = torch.cuda.Event()
+            ready.record(self.copy)
+            stream.wait_event(ready)
+            kernel(dst, m)
+            done = torch.cuda.Event()
+            done.record(stream)
+            free[b] = done
+
+    def build(self, k, entries_ptr, stream, buf_ptr, buf_bytes):
         """Segments of dataset k into entries_ptr (entries_bytes(k) bytes), offsets into
-        self.offsets[:num_bin_batch * cells + 1], on the given torch stream."""
+        self.offsets[:num_bin_batch * cells + 1], on the given torch stream; the COO chunks
+        pass through [buf_ptr, buf_ptr + buf_bytes) (device memory not used meanwhile)."""
         P = _lib.ptr
         bs_bin, base, nbb = self.meta[k]
-        (row, col, cell, val), nnz = self.src[k]
         C = self.n_cells
         n = nbb * C
         sp = stream.cuda_stream
@@ -482,12 +510,16 @@ class StreamedContacts:
         with self.torch.cuda.stream(stream):
             self.counts[:n].zero_()
             self.cursor[:n].zero_()
-        _lib.call("fh_contacts_count", row, col, cell, nnz, bs_bin, tiles, 0, nbb, C,
-                  P(self.counts), P(self.status), sp)
+        if self.nnz[k]:
+            self._chunked(k, buf_ptr, buf_bytes, "rcl", lambda d, m: _lib.call(
+                "fh_contacts_count", d[0], d[1], d[2], m, bs_bin, tiles, 0, nbb, C,
+                P(self.counts), P(self.status), sp), stream)
         _lib.call("fh_exclusive_scan", P(self.counts), n, P(self.offsets), P(self.scan_ws),
                   self.scan_ws.numel(), sp)
-        _lib.call("fh_contacts_scatter", row, col, cell, val, nnz, bs_bin, tiles, 0, nbb, C,
-                  P(self.offsets), P(self.cursor), entries_ptr, sp)
+        if self.nnz[k]:
+            self._chunked(k, buf_ptr, buf_bytes, "rclv", lambda d, m: _lib.call(
+                "fh_contacts_scatter", d[0], d[1], d[2], d[3], m, bs_bin, tiles, 0, nbb, C,
+                P(self.offsets), P(self.cursor), entries_ptr, sp), stream)
 
     def rebuild(self):
         """Nothing to do: every walk builds its dataset's segments first."""

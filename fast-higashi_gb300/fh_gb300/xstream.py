@@ -25,8 +25,9 @@ into its output range by range (fh_xg_* with accumulate); X^T E writes each rang
 
 The walk writes the streamed chromosomes' X into a slot (with their tile table's band rows
 re-based to the window) and copies each window out to its host buffer, then walks the resident
-chromosomes.  The contact segments of one dataset at a time live in the staging area too, so
-the budget holds X's resident part, the staging and the factors, nothing else.
+chromosomes.  The contact segments of one dataset at a time live in the staging area too, with
+the chunks of its COO on their way in, so the budget holds X's resident part, the staging and
+the factors, nothing else.
 """
 from __future__ import annotations
 
@@ -72,7 +73,8 @@ class XPlan:
         return self.windows[0].chroms[0] if self.windows else None
 
 
-def plan_x(chrom_rows, elem_bytes, n_cells, entries_bytes, budget, max_windows=4):
+def plan_x(chrom_rows, elem_bytes, n_cells, entries_bytes, budget, max_windows=4,
+           chunk_bytes=256 << 20):
     """The split of X between HBM and host memory that streams the fewest bytes.
 
     chrom_rows: band rows [x0, x1) of each chromosome group in tile order (contiguous, from 0);
@@ -81,7 +83,8 @@ def plan_x(chrom_rows, elem_bytes, n_cells, entries_bytes, budget, max_windows=4
     (8 bytes per contact); budget: bytes for X's resident part and the staging area together.
     Windows are whole chromosome groups; the staging holds two slots of the largest window,
     the largest resident dataset's segments, or a slot plus the largest streamed dataset's
-    segments (a streamed chromosome is walked into one slot with its segments beside it).
+    segments (a streamed chromosome is walked into one slot with its segments beside it), in
+    the last two cases with at least chunk_bytes more for the COO chunks of the contact build.
     Raises FHError when no split fits."""
     n = len(chrom_rows)
     if n == 0:
@@ -120,7 +123,9 @@ def plan_x(chrom_rows, elem_bytes, n_cells, entries_bytes, budget, max_windows=4
         slot = _up(max((w.nbytes for w in windows), default=0), SLOT_ALIGN)
         ent_res = max((entries_bytes[c] for c in range(j)), default=0)
         ent_str = max((entries_bytes[c] for c in range(j, n)), default=0)
-        staging = _up(max(2 * slot, ent_res, (slot + ent_str) if windows else 0, 1), SLOT_ALIGN)
+        need_res = _up(ent_res, SLOT_ALIGN) + chunk_bytes
+        need_str = (slot + _up(ent_str, SLOT_ALIGN) + chunk_bytes) if windows else 0
+        staging = _up(max(2 * slot, need_res, need_str), SLOT_ALIGN)
         if res + staging <= budget:
             return XPlan(rows, split, _up(split, 128) if split > 0 else 0, res, windows, slot,
                          staging)
@@ -205,10 +210,14 @@ class XStream:
             return flat.view(self.planes, self.C, w.ld)
         return flat.view(self.C, w.ld)
 
-    def entries_ptr(self, streamed):
-        """Where one dataset's contact segments go: the start of the staging area for a
-        resident chromosome, beside slot 0 for a streamed one (its walk writes slot 0)."""
-        return self.staging.data_ptr() + (self.plan.slot_bytes if streamed else 0)
+    def build_space(self, streamed, entries_bytes):
+        """(segments, COO chunk buffer, its bytes) for one dataset's contact build in the
+        staging area: from its start for a resident chromosome, after slot 0 for a streamed
+        one (whose walk writes slot 0)."""
+        start = self.plan.slot_bytes if streamed else 0
+        b0 = _up(start + entries_bytes, SLOT_ALIGN)
+        return (self.staging.data_ptr() + start, self.staging.data_ptr() + b0,
+                self.plan.staging_bytes - b0)
 
     def window_of_chrom(self, c):
         for i, w in enumerate(self.plan.windows):

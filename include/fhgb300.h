@@ -477,20 +477,16 @@ int fh_unpool_rows(const fh_tile* tiles, int32_t n_tiles, const int64_t* prow0,
                    const int32_t* ll, int64_t x0, int64_t rows, const float* in, int64_t ldi,
                    int32_t m, float* out, int64_t ldo, void* stream);
 
-/* ---- host memory for X held partly outside HBM and for contacts read in place (no
- * reference counterpart: the reference tiles its work by free GPU memory instead,
- * FastHigashi_Wrapper.py:497-517, and copies each tile's COO slice to the device,
- * sparse_for_schic.py:588-613).
+/* ---- host memory for X held partly outside HBM (no reference counterpart: the reference
+ * tiles its work by free GPU memory instead, FastHigashi_Wrapper.py:497-517, and copies each
+ * tile's COO slice to the device, sparse_for_schic.py:588-613).
  * fh_host_alloc: page-locked host memory, mapped into the device address space (cudaHostAlloc,
  *   portable | mapped); fh_host_free releases it.
- * fh_host_device_pointer: the device address of page-locked, mapped host memory (host memory
- *   registered in place, or from fh_host_alloc); FH_ERR_ARG if it is neither.  Kernels read a
- *   chromosome's COO through it (fh_contacts_count / fh_contacts_scatter) with no device copy.
  * fh_memcpy_async: one asynchronous copy of bytes between any two of host and device memory on
- *   stream (a memcpy node when the stream is being captured into a CUDA graph). */
+ *   stream (a memcpy node when the stream is being captured into a CUDA graph); the streamed
+ *   windows of X and the chunks of a chromosome's COO for the contact build move by it. */
 int fh_host_alloc(int64_t bytes, void** out);
 int fh_host_free(void* p);
-int fh_host_device_pointer(const void* host, void** dev);
 int fh_memcpy_async(void* dst, const void* src, int64_t bytes, void* stream);
 
 /* ---- self-test of the bounded device-side waits (no reference counterpart: the reference

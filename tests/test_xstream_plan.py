@@ -31,7 +31,7 @@ def test_everything_resident_when_it_fits():
     p = xstream.plan_x(rows, 4, 100, [800, 500, 300], 10 ** 9)
     assert p.windows == [] and p.split == 2000 and p.ld_res == 2048
     assert p.res_bytes == 2048 * 100 * 4
-    assert p.staging_bytes >= 800
+    assert p.staging_bytes >= 800 + (256 << 20)
 
 
 def test_c5_shapes_stream_the_last_chromosomes_within_the_budget():
@@ -47,7 +47,7 @@ def test_c5_shapes_stream_the_last_chromosomes_within_the_budget():
     for a, b in zip(p.windows, p.windows[1:]):
         assert a.x1 == b.x0 and a.chroms[-1] + 1 == b.chroms[0]
     assert all(wd.nbytes <= p.slot_bytes for wd in p.windows)
-    assert p.staging_bytes >= 2 * p.slot_bytes and p.staging_bytes >= max(ent)
+    assert p.staging_bytes >= 2 * p.slot_bytes and p.staging_bytes >= max(ent) + (256 << 20)
     # streaming one chromosome fewer does not fit
     j = p.windows[0].chroms[0]
     assert nbytes(rows[j][1], w.n_cells, 4) > budget - 2 * p.slot_bytes or j == len(rows) - 1
@@ -86,18 +86,22 @@ def test_plan_streams_the_fewest_chromosomes_with_the_smallest_slots(seed):
     C, e = 50, 4
     ent = [int(v) for v in rng.integers(0, 200_000, n)]
     total = nbytes(x, C, e)
-    budget = int(total * rng.uniform(0.55, 0.9))
+    budget = int(total * rng.uniform(0.55, 0.9)) + (300 << 20)
     try:
         p = xstream.plan_x(rows, e, C, ent, budget, max_windows=3)
     except _lib.FHError:
         p = None
 
+    def up(v):
+        return -(-v // xstream.SLOT_ALIGN) * xstream.SLOT_ALIGN
+
     def staging(j, slot):
         ent_res = max([ent[c] for c in range(j)], default=0)
         ent_str = max([ent[c] for c in range(j, n)], default=0)
-        slot = -(-slot // xstream.SLOT_ALIGN) * xstream.SLOT_ALIGN
-        v = max(2 * slot, ent_res, (slot + ent_str) if j < n else 0, 1)
-        return -(-v // xstream.SLOT_ALIGN) * xstream.SLOT_ALIGN
+        slot = up(slot)
+        chunk = 256 << 20
+        v = max(2 * slot, up(ent_res) + chunk, (slot + up(ent_str) + chunk) if j < n else 0)
+        return up(v)
 
     feasible = []
     for j in range(n, -1, -1):
