@@ -115,14 +115,15 @@ def make_workload(name, seed=0, cells=None):
     if cells:
         w = dataclasses.replace(w, n_cells=int(cells), name="%s at %d cells" % (name, cells))
     coo, _ = synth.generate(w, seed=seed)
-    # The generator fills each chromosome's arrays in its own worker thread; copy them once in
-    # this thread, as arrays read from a file by the caller would be allocated.  Untimed.
-    coo = [(np.array(idx, copy=True), np.array(val, copy=True), shape) for idx, val, shape in coo]
     ds = []
     for (idx, val, shape), cname, nb in zip(coo, w.chrom_names, w.chrom_bins):
         bsb, bsc = synth.recommend_batches(w, nb, w.n_cells)
         ds.append(Chrom_Dataset(Sparse(idx, val, shape, copy=False), bsb, bsc, compact=True,
                                 flank=w.band, chrom=cname, resolution=w.resolution))
+    # the contacts in page-locked host memory, as the reference's datasets pin theirs
+    # (Chrom_Dataset.pin_memory): every step's host-to-device copy reads pinned memory
+    for d in ds:
+        d.pin_memory()
     return w, coo, ds
 
 
@@ -710,9 +711,9 @@ def budget_arm(args, rank, local, ws):
     """A workload whose X is larger than the HBM budget (c5: 50,000 cells at 500 kb, R = 128,
     band 40; X is 179 GB in two bf16 planes or in fp32): both forms run with hbm_budget, so
     X's last chromosomes stream through two staging slots from page-locked host memory and the
-    contact segments are built one dataset at a time from the host COO, copied in chunks
-    through the staging area.  A step is a whole fit: the contact build and walk (the COO
-    crosses the host link inside the step)
+    contact segments are built one dataset at a time from the host COO (in page-locked
+    memory), copied in chunks through the staging area.  A step is a whole fit: the contact
+    build and walk (the COO crosses the host link inside the step)
     and the 30 ALS iterations (one CUDA graph, the window copies as memcpy nodes).  The COO is
     generated on the GPU (synth.generate_on_device) and kept in host memory, as a caller's
     input would be.  No end-to-end line beyond the step itself (its input already comes from
@@ -734,7 +735,7 @@ def budget_arm(args, rank, local, ws):
     iters = args.iters or w.n_iter
     C = w.n_cells
     t0 = time.time()
-    coo, _ = synth.generate_on_device(w, seed=0, device=dev)
+    coo, _ = synth.generate_on_device(w, seed=0, device=dev, pinned=True)
     gen_s = time.time() - t0
     ds = []
     for (idx, val, shape), cname, nb in zip(coo, w.chrom_names, w.chrom_bins):

@@ -186,6 +186,61 @@ def value(name, *args):
     return getattr(load(), name)(*args)
 
 
+_HOST_BUFFERS = {}     # address -> bytes of the live HostBuffers
+
+
+class HostBuffer:
+    """Page-locked host memory from the library (fh_host_alloc: cudaHostAlloc, exactly the
+    bytes asked for), freed when the last reference to it (or to an array over it) goes."""
+
+    def __init__(self, nbytes, zero=True):
+        p = C.c_void_p()
+        call("fh_host_alloc", int(nbytes), C.byref(p))
+        self.ptr = int(p.value)
+        self.nbytes = int(nbytes)
+        _HOST_BUFFERS[self.ptr] = self.nbytes
+        if zero:
+            C.memset(self.ptr, 0, self.nbytes)
+
+    def array(self, dtype, shape):
+        """A numpy array over the buffer; it keeps the buffer alive."""
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        if n > self.nbytes:
+            raise FHError("HostBuffer", 1, "array larger than the buffer")
+        raw = (C.c_uint8 * max(n, 1)).from_address(self.ptr)
+        raw._owner = self
+        return np.frombuffer(raw, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            _HOST_BUFFERS.pop(self.ptr, None)
+            call("fh_host_free", self.ptr)
+            self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def host_pinned(addr, nbytes):
+    """True if [addr, addr + nbytes) lies in a live HostBuffer (page-locked already)."""
+    for p, n in _HOST_BUFFERS.items():
+        if p <= addr and addr + nbytes <= p + n:
+            return True
+    return False
+
+
+def pinned_copy(a):
+    """A copy of numpy array a in page-locked memory (a HostBuffer)."""
+    a = np.ascontiguousarray(a)
+    out = HostBuffer(max(a.nbytes, 1), zero=False).array(a.dtype, a.shape)
+    np.copyto(out, a)
+    return out
+
+
 def ptr(t):
     """Device (or host) address of a torch tensor / numpy array, or None."""
     if t is None:

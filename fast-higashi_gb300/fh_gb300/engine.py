@@ -42,6 +42,8 @@ def _pad_rank(R):
 class FitEngine:
     # bytes of a budget kept back for transient buffers (init's sketches, the auto-stop deltas)
     BUDGET_RESERVE = 2 << 30
+    # least staging room for the two COO chunk buffers of a budgeted contact build
+    BUDGET_CHUNK = 256 << 20
 
     def __init__(self, schic, rank, chrom2size, n_i, device, do_rwr=True, stream=None,
                  precision="fp32", do_conv=False, do_col=False, bin_cov=None, hbm_budget=None):
@@ -191,7 +193,7 @@ class FitEngine:
         elem = 2 * self.planes if self.bf16 else 4
         x_budget = int(budget) - self._buffer_bytes(True) - self.store_bytes() - \
             self.BUDGET_RESERVE
-        plan = plan_x(chrom_rows, elem, self.Ct, entries, x_budget)
+        plan = plan_x(chrom_rows, elem, self.Ct, entries, x_budget, chunk_bytes=self.BUDGET_CHUNK)
         self.groups = groups
         self.xs = XStream(plan, self.planes, self.Ct,
                           torch.bfloat16 if self.bf16 else torch.float32, dev, self.tiles,

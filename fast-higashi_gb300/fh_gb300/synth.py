@@ -213,7 +213,7 @@ def recommend_batches(w: Workload, nbin: int, n_cells: int, avail_bytes: float =
 
 
 def generate_on_device(w: Workload, seed: int = 0, device="cuda", cell_chunk: int = 8192,
-                       band_chunk: int = 2048):
+                       band_chunk: int = 2048, pinned: bool = False):
     """The same model as generate(), with the Poisson draws and the packing on the GPU.
 
     For the largest workload (50,000 cells at 500 kb, about 7e9 contacts, 112 GB of COO) the
@@ -223,7 +223,8 @@ def generate_on_device(w: Workload, seed: int = 0, device="cuda", cell_chunk: in
     indices, float32 values, sorted by row, column and cell) is copied into host arrays.  The
     per-cell quantities (totals, decay exponents, types) and each chromosome's compartments
     come from the same seeded NumPy generators as generate(); the draws come from torch's
-    seeded CUDA generator, so the contacts are reproducible but differ from generate()'s."""
+    seeded CUDA generator, so the contacts are reproducible but differ from generate()'s.
+    With pinned, the COO lands in page-locked host buffers (exact size), ready for copies."""
     import torch
     dev = torch.device(device)
     ss = np.random.SeedSequence(seed)
@@ -296,8 +297,15 @@ def generate_on_device(w: Workload, seed: int = 0, device="cuda", cell_chunk: in
             m, sd = float(v64.mean()), float(v64.std(unbiased=False))
             del v64
             vals.clamp_(max=m + 15 * sd)
-        h_idx = np.empty((3, idx.shape[1]), dtype=np.int32)
-        h_val = np.empty(vals.numel(), dtype=np.float32)
+        if pinned:
+            from . import _lib
+            h_idx = _lib.HostBuffer(max(12 * idx.shape[1], 1), zero=False).array(
+                np.int32, (3, idx.shape[1]))
+            h_val = _lib.HostBuffer(max(4 * vals.numel(), 1), zero=False).array(
+                np.float32, (vals.numel(),))
+        else:
+            h_idx = np.empty((3, idx.shape[1]), dtype=np.int32)
+            h_val = np.empty(vals.numel(), dtype=np.float32)
         torch.from_numpy(h_idx).copy_(idx)
         torch.from_numpy(h_val).copy_(vals)
         del idx, vals

@@ -31,7 +31,6 @@ the factors, nothing else.
 """
 from __future__ import annotations
 
-import ctypes
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -133,26 +132,7 @@ def plan_x(chrom_rows, elem_bytes, n_cells, entries_bytes, budget, max_windows=4
                        "%.1f GB even with every chromosome streamed" % (rows, n_cells, budget / 1e9))
 
 
-class HostBuffer:
-    """Page-locked, mapped host memory from the library (fh_host_alloc), zero-filled."""
-
-    def __init__(self, nbytes):
-        p = ctypes.c_void_p()
-        _lib.call("fh_host_alloc", int(nbytes), ctypes.byref(p))
-        self.ptr = int(p.value)
-        self.nbytes = int(nbytes)
-        ctypes.memset(self.ptr, 0, self.nbytes)
-
-    def free(self):
-        if self.ptr:
-            _lib.call("fh_host_free", self.ptr)
-            self.ptr = 0
-
-    def __del__(self):
-        try:
-            self.free()
-        except Exception:
-            pass
+HostBuffer = _lib.HostBuffer
 
 
 class XStream:

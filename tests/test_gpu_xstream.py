@@ -3,7 +3,8 @@ same fit with X resident, on a 6-chromosome workload whose budget streams at lea
 windows through the two staging slots.
 
 * the walk: the resident part and every host window hold exactly the resident engine's X
-  (the streamed chromosomes walked into a slot with their band rows re-based);
+  (the streamed chromosomes walked into a slot with their band rows re-based; each dataset's
+  contacts copied in through many double-buffered COO chunks);
 * init_params through the streamed X passes: the same auto-stop epochs, and features equal to
   fp32 rounding amplified by the sketch (1e-3);
 * the fit (captured into a CUDA graph, with the window copies as memcpy nodes) and transform
@@ -79,6 +80,8 @@ def _host_array(buf, dtype, shape):
 def test_streamed_x_matches_resident_x(precision, monkeypatch):
     from fh_gb300.engine import FitEngine
     monkeypatch.setattr(FitEngine, "BUDGET_RESERVE", 0)
+    # 1 MiB of COO chunk buffers: every dataset's build runs through many chunks
+    monkeypatch.setattr(FitEngine, "BUDGET_CHUNK", 1 << 20)
     w = _workload()
     ds = _datasets(w)
     budget = _budget_for_windows(w, ds, precision)
