@@ -144,3 +144,22 @@ def test_streamed_x_matches_resident_x(precision, monkeypatch):
     tB = mB.transform(ds, False, True, False)[1][3].cpu().double()
     assert float((tA - tB).norm() / tA.norm()) < 1e-5
     assert eB.xs.link_bytes > 0
+
+
+def test_pin_memory_moves_the_coo_into_page_locked_buffers():
+    """Chrom_Dataset.pin_memory: the same indices and values, now in library-allocated
+    page-locked buffers (so the contact build copies them at the link's rate)."""
+    from fh_gb300 import _lib
+    w = _workload()
+    ds = _datasets(w)
+    d = ds[0]
+    idx0, val0 = np.array(d.tensor.indices, copy=True), np.array(d.tensor.values, copy=True)
+    assert d.pin_memory() is d
+    t = d.tensor
+    assert _lib.host_pinned(t.indices.ctypes.data, t.indices.nbytes)
+    assert _lib.host_pinned(t.values.ctypes.data, t.values.nbytes)
+    np.testing.assert_array_equal(t.indices, idx0)
+    np.testing.assert_array_equal(t.values, val0)
+    p0 = t.indices.ctypes.data
+    d.pin_memory()                               # a second call keeps the same buffers
+    assert d.tensor.indices.ctypes.data == p0
