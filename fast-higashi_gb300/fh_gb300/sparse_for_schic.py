@@ -422,6 +422,21 @@ class ContactStore:
         self.build_all()
 
 
+def coo_chunks(nnz, buf_bytes, n_arrays, align=256):
+    """The chunks of a budgeted contact build: (buffer half, byte offset of each array's slot
+    in that half, first contact, contacts) for nnz contacts whose n_arrays arrays (4 bytes per
+    contact each) pass through two halves of a buffer of buf_bytes, alternately.  Every slot
+    starts on a 256-byte boundary and a chunk holds a multiple of 64 contacts (the last one
+    the rest)."""
+    half = (buf_bytes // 2) // align * align
+    m_max = (half // (4 * n_arrays)) // 64 * 64
+    if nnz > 0 and m_max <= 0:
+        raise _lib.FHError("contact build", 1, "no room for a chunk of the COO")
+    slots = [a * m_max * 4 for a in range(n_arrays)]
+    return [(j & 1, [j % 2 * half + s for s in slots], e0, min(m_max, nnz - e0))
+            for j, e0 in enumerate(range(0, nnz, m_max))] if nnz > 0 else []
+
+
 class StreamedContacts:
     """The contact build for a fit whose device memory is budgeted: one dataset at a time.
 
@@ -473,16 +488,9 @@ class StreamedContacts:
         half of [buf_ptr, buf_ptr + buf_bytes)."""
         torch = self.torch
         hi, hv, nnz = self.src[k]
-        half = (buf_bytes // 2) // self.CHUNK_ALIGN * self.CHUNK_ALIGN
-        m_max = (half // (4 * len(arrays))) // 64 * 64
-        if m_max <= 0:
-            raise _lib.FHError("contact build", 1, "no room for a chunk of the COO")
         srcs = [hi[0], hi[1], hi[2], hv][:len(arrays)]
         free = [None, None]
-        for j, e0 in enumerate(range(0, nnz, m_max)):
-            m = min(m_max, nnz - e0)
-            b = j & 1
-            base = buf_ptr + b * half
+        for b, offs, e0, m in coo_chunks(nnz, buf_bytes, len(arrays), self.CHUNK_ALIGN):
             if free[b] is not None:
                 self.copy.wait_event(free[b])
             else:
@@ -490,8 +498,8 @@ class StreamedContacts:
                 ev.record(stream)           # after what the stream issued before this build
                 self.copy.wait_event(ev)
             dst = []
-            for a, src in enumerate(srcs):
-                d = base + a * m_max * 4
+            for off, src in zip(offs, srcs):
+                d = buf_ptr + off
                 _lib.call("fh_memcpy_async", d, src.ctypes.data + e0 * 4, m * 4,
                           self.copy.cuda_stream)
                 dst.append(d)

@@ -187,3 +187,31 @@ def test_copies_of_later_windows_are_issued_before_the_resident_rows():
         # the windows read first are the two the previous pass ended with
         wins = [r[1] for r in log if r[0] == "win"]
         assert wins[:2] != wins[2:]
+
+
+@pytest.mark.parametrize("nnz,buf,arrays", [(0, 1 << 20, 3), (1, 1 << 20, 4), (100_000, 1 << 20, 3),
+                                            (12_345_677, 7 << 20, 4), (5_000, 3000, 3)])
+def test_coo_chunks_cover_every_contact_once_inside_their_half(nnz, buf, arrays):
+    """The budgeted contact build's chunking (sparse_for_schic.coo_chunks): chunks cover the
+    contacts in order, each chunk's array slots lie inside its half of the buffer without
+    overlapping, start on 256-byte boundaries, and consecutive chunks alternate halves."""
+    from fh_gb300.sparse_for_schic import coo_chunks
+    if nnz and (buf // 2) // 256 * 256 // (4 * arrays) < 64:
+        with pytest.raises(_lib.FHError):
+            coo_chunks(nnz, buf, arrays)
+        return
+    ch = coo_chunks(nnz, buf, arrays)
+    half = (buf // 2) // 256 * 256
+    nxt = 0
+    for j, (b, offs, e0, m) in enumerate(ch):
+        assert b == j % 2 and e0 == nxt and m > 0
+        nxt += m
+        assert len(offs) == arrays
+        spans = sorted((o, o + 4 * m) for o in offs)
+        for (a0, a1), (c0, _) in zip(spans, spans[1:]):
+            assert a1 <= c0
+        assert all(o % 256 == 0 for o in offs)
+        assert spans[0][0] >= b * half and spans[-1][1] <= (b + 1) * half
+        if j + 1 < len(ch):
+            assert m % 64 == 0
+    assert nxt == nnz
