@@ -163,3 +163,84 @@ def test_pin_memory_moves_the_coo_into_page_locked_buffers():
     p0 = t.indices.ctypes.data
     d.pin_memory()                               # a second call keeps the same buffers
     assert d.tensor.indices.ctypes.data == p0
+
+
+def test_budget_refuses_the_walks_that_need_x_resident():
+    """do_conv and do_col run their walks from dense tiles of X's layout: with a budget the
+    engine refuses them up front."""
+    from fh_gb300 import _lib
+    from fh_gb300.engine import FitEngine
+    w = _workload()
+    ds = _datasets(w)
+    m = _model(w, "bf16x2")
+    m._sizes(ds, w.dim1, None)
+    for kw in (dict(do_conv=True), dict(do_col=True)):
+        with pytest.raises(_lib.FHError):
+            FitEngine(ds, w.rank, m.chrom2size, None, CUDA, precision="bf16x2", hbm_budget=1 << 40,
+                      **kw)
+
+
+def test_streamed_x_with_two_resolutions(monkeypatch):
+    """Three chromosomes at 1 Mb and at 500 kb (res_list: a chromosome's datasets share B and
+    D and stream in the same window): init and fit through the streamed passes agree with the
+    resident engine's."""
+    import dataclasses
+    from fh_gb300 import Fast_Higashi_core, synth
+    from fh_gb300.engine import FitEngine
+    from fh_gb300.sparse_for_schic import Sparse, Chrom_Dataset
+    monkeypatch.setattr(FitEngine, "BUDGET_RESERVE", 0)
+    monkeypatch.setattr(FitEngine, "BUDGET_CHUNK", 1 << 20)
+    w1 = synth.Workload("mr1", 800, [60, 50, 45], 1_000_000, 8, (0.9, 1.3), 6_000, 0.6, 3, 12, 4)
+    w2 = dataclasses.replace(w1, name="mr2", chrom_bins=[120, 100, 90], resolution=500_000)
+    ds = []
+    for w, seed in ((w1, 1), (w2, 2)):
+        coo, _ = synth.generate(w, seed=seed)
+        for (idx, val, shape), name, nb in zip(coo, w.chrom_names, w.chrom_bins):
+            bsb, bsc = synth.recommend_batches(w, nb, w.n_cells)
+            ds.append(Chrom_Dataset(Sparse(idx, val, shape), bsb, bsc, compact=True,
+                                    flank=w.band, chrom=name, resolution=w.resolution))
+    res_list = [1_000_000, 500_000]
+
+    def model(budget=None):
+        m = Fast_Higashi_core(w1.rank, w1.band, res_list, precision="bf16x2",
+                              hbm_budget=budget).to(CUDA)
+        m._sizes(ds, w1.dim1, None)
+        return m
+
+    m0 = model()
+    e0 = FitEngine(ds, w1.rank, m0.chrom2size, None, CUDA, precision="bf16x2")
+    total = e0.rows * e0.Ct * 4 + e0._buffer_bytes() + (64 << 20)
+    del e0
+    budget = None
+    for frac in np.linspace(1.0, 0.3, 71):
+        b = int(total * frac)
+        try:
+            e = FitEngine(ds, w1.rank, m0.chrom2size, None, CUDA, precision="bf16x2",
+                          hbm_budget=b)
+        except Exception:
+            continue
+        n = len(e.xs.plan.windows)
+        del e
+        if n >= 1:
+            budget = b
+            break
+    assert budget is not None
+    torch.manual_seed(0)
+    mA = model()
+    mA.init_params(ds, False, True, False, seed=0)
+    torch.manual_seed(0)
+    mB = model(budget)
+    mB.init_params(ds, False, True, False, seed=0)
+    assert mB.engine.xs is not None and mB.engine.multi
+    np.testing.assert_array_equal(np.asarray(mA.n_i), np.asarray(mB.n_i))
+    state = ([a.clone() for a in mA.A_list], {k: v.clone() for k, v in mA.B_dict.items()},
+             {k: v.clone() for k, v in mA.D_dict.items()}, mA.meta_embedding.clone())
+    for m in (mA, mB):
+        m.A_list, m.B_dict, m.D_dict, m.meta_embedding = (
+            [a.clone() for a in state[0]], {k: v.clone() for k, v in state[1].items()},
+            {k: v.clone() for k, v in state[2].items()}, state[3].clone())
+        m.fit(ds, size_ratio=w1.dim1, n_iter_max=w1.n_iter, n_iter_parafac=1, do_conv=False,
+              do_rwr=True, do_col=False, tol=0, run_init=False, verbose=False)
+    fA, fB = mA.meta_embedding.cpu().double(), mB.meta_embedding.cpu().double()
+    assert float((fA - fB).norm() / fA.norm()) < 1e-5
+    np.testing.assert_allclose(mB.rec_errors_total, mA.rec_errors_total, rtol=1e-5)
