@@ -281,9 +281,3 @@ class XStream:
             if pending:                             # the slot is free once this pass ends
                 nxt = pending.pop(0)
                 queued[nxt] = (s, self._load(s, nxt, main))
-
-    def free(self):
-        self.torch.cuda.synchronize(self.device)
-        for h in self.host:
-            h.free()
-        self.host = []
