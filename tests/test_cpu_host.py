@@ -289,3 +289,28 @@ def test_parafac_sweep_schedule():
     assert s[:10] == [1] * 10 and s[10:20] == [2] * 10 and s[20:30] == [3] * 10 and s[30:] == [4] * 5
     assert FitEngine.parafac_schedule(200, 5)[-1] == 10
     assert FitEngine.parafac_schedule(3, 12) == [12, 12, 12]     # above the cap: left alone
+
+
+def test_device_generator_gives_a_sorted_in_band_coo():
+    """synth.generate_on_device (the 50,000-cell workload's generator), run here with torch on
+    the CPU: every chromosome's COO is sorted by (row, column, cell) without repeats, inside the
+    band and the shape, symmetric in (row, column), with positive values clipped at mean + 15 std;
+    seeded; and close to the host generator's contact count."""
+    import dataclasses
+    from fh_gb300 import synth
+    w = dataclasses.replace(synth.workload("tiny"), n_cells=40)
+    coo, _ = synth.generate_on_device(w, seed=4, device="cpu", cell_chunk=16, band_chunk=7)
+    again, _ = synth.generate_on_device(w, seed=4, device="cpu", cell_chunk=16, band_chunk=7)
+    host, _ = synth.generate(w, seed=4)
+    for (idx, val, shape), (idx2, val2, _), (hidx, _, _), nb in zip(coo, again, host, w.chrom_bins):
+        assert shape == (nb, nb, w.n_cells) and idx.dtype == np.int32 and val.dtype == np.float32
+        np.testing.assert_array_equal(idx, idx2)
+        np.testing.assert_array_equal(val, val2)
+        key = (idx[0].astype(np.int64) * nb + idx[1]) * w.n_cells + idx[2]
+        assert (np.diff(key) > 0).all()
+        assert (idx >= 0).all() and (idx[0] < nb).all() and (idx[1] < nb).all()
+        assert (idx[2] < w.n_cells).all() and (np.abs(idx[0] - idx[1]) <= w.band).all()
+        mirror = np.sort((idx[1].astype(np.int64) * nb + idx[0]) * w.n_cells + idx[2])
+        np.testing.assert_array_equal(np.sort(key), mirror)
+        assert (val > 0).all()
+        assert abs(idx.shape[1] - hidx.shape[1]) < 0.1 * hidx.shape[1]
