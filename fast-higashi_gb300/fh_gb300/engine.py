@@ -143,12 +143,16 @@ class FitEngine:
         self.store = ContactStore(self.schic, dev, self.tiles, self.tile_base, self.stream,
                                   order=order, defer=True)
         self.tiles_dev = self.store.tiles_dev
+        # every walk writes all band rows [0, rows) of X; only the padding columns up to the
+        # 128-row stride need zeros once (the passes read them), not all of X
         if self.bf16:
             self.X = None
-            self.X16 = torch.zeros((self.planes, self.Ct, self.ldx), dtype=torch.bfloat16,
+            self.X16 = torch.empty((self.planes, self.Ct, self.ldx), dtype=torch.bfloat16,
                                    device=dev)
+            self.X16[:, :, self.rows:].zero_()
         else:
-            self.X = torch.zeros((self.Ct, self.ldx), dtype=f32, device=dev)
+            self.X = torch.empty((self.Ct, self.ldx), dtype=f32, device=dev)
+            self.X[:, self.rows:].zero_()
             self.X16 = None
         self.sumsq = torch.zeros(self.n_tiles * self.Ct, dtype=f64, device=dev)
         if n_i is not None and not (self.do_col or self.do_conv):
