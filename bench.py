@@ -18,6 +18,10 @@ initial state (init_params runs once, untimed, as the metric states).
   --impl reference   the reference's own Fast_Higashi_core (installed under baseline/_ref) on
                      the host CPU, all cores, one ALS iteration per step on a cell sample,
                      extrapolated to the workload's cells and iterations (cpu_baseline says how)
+  --hbm-budget-gb G  both forms held within G GB of device memory (X's last chromosomes
+                     streamed from page-locked host memory, contacts built one dataset at a
+                     time): the 50,000-cell, R = 128 case is --config c5 --hbm-budget-gb 180;
+                     its own JSON line with the memory, the X plan and the host-link bytes
 
 Multi-GPU runs (torchrun) are independent replicas: the fit does not shard (scaling weak).
 """
