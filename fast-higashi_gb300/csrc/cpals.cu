@@ -8,13 +8,12 @@
 //     A <- MTTKRP_A (B^T B * D^T D + 1e-10 I)^{-1}   (and likewise for B, D)
 //     MTTKRP_A[i] = sum_j B[j] * (Y_i D)[j],   MTTKRP_B = sum_i A_i (x) (Y_i D),
 //     MTTKRP_D   = sum_i A_i (x) (Y_i^T B)      ((x): column-wise product).
-// The r x r systems (symmetric positive definite) are formed in fp64 and factored by Cholesky
-// once per chromosome (cp_small_kernel, one CTA), and the right-hand sides are solved against
-// the factor in fp64 by forward and back substitution, eight rows per CTA over many CTAs
-// (cp_solve_kernel): fp64 multiply-adds run at 1/200 of the fp32 rate on this GPU, so the
-// solves are spread over the SMs instead of one per chromosome.  The A rows (many small
-// solves in cp_rows_kernel) use the system's fp64 inverse (solved for the identity) rounded
-// to fp32.  The reference solves in fp32 (parafac_integrative.py:12-15).  Scalar sums (loss, core norm) are fp64 too.  The reconstruction loss needs no Xhat:
+// The r x r systems (symmetric positive definite) are formed and inverted in fp64 by
+// Gauss-Jordan without pivoting (the sweep operator) once per chromosome, and the B and D
+// right-hand sides are multiplied by the fp64 inverse with fp64 sums, so every solve is a
+// register-tiled product instead of a serial substitution; the A rows (many small solves in
+// cp_rows_kernel) use the fp64 inverse rounded to fp32.  The reference solves in fp32
+// (parafac_integrative.py:12-15).  Scalar sums (loss, core norm) are fp64 too.  The reconstruction loss needs no Xhat:
 // ||Xhat||^2 = sum(A^TA * B^TB * D^TD) and <Xhat, Y> = sum(D * MTTKRP_D) with the final
 // A, B.  balance_norm (unit columns, the product of the column norms folded into D) follows
 // each sweep unless the relative loss change fell below 1e-5, as the reference breaks before
@@ -57,8 +56,6 @@ struct CpArgs {
   const float* Y;  // [bin rows][ldy][RP]
   int ld, RP, R, ldy;
   float* L;        // [chrom][ld][ld]    inverse of the A-row system (B^T B * D^T D + 1e-10 I)
-  double* chol;    // [chrom][ld][ld + 1] Cholesky factor of the system being solved
-  float* rhs;      // [chrom][RP][ld]     its right-hand sides (MTTKRP_B or MTTKRP_D)
   float* part;     // [chunk][pstride]
   float* gAA;      // [chrom][ld*ld]
   float* gBB;
@@ -73,13 +70,9 @@ struct CpArgs {
 };
 
 enum CpRowMode { kRowsNorm = 0, kRowsAB = 1, kRowsD = 2, kRowsScale = 3, kRowsGram = 4 };
-// Each update is split around cp_solve_kernel: kSmallB / kSmallD form and factor the system
-// and its right-hand sides, the *Post modes continue from the solved factor.  kSmallDLast(Post):
-// the D update of a call's last sweep, whose balanced Grams and A-row inverse nobody reads (the
-// next call starts from kSmallInit).
-enum CpSmallMode { kSmallInit = 0, kSmallB = 1, kSmallD = 2, kSmallCore = 3, kSmallDLast = 4,
-                   kSmallBPost = 5, kSmallDPost = 6, kSmallDLastPost = 7 };
-enum CpSolveTarget { kSolveB = 0, kSolveD = 1, kSolveAinv = 2 };
+// kSmallDLast: the D update of a call's last sweep, whose balanced Grams and A-row inverse
+// nobody reads (the next call starts from kSmallInit).
+enum CpSmallMode { kSmallInit = 0, kSmallB = 1, kSmallD = 2, kSmallCore = 3, kSmallDLast = 4 };
 
 __host__ __device__ inline size_t cp_pstride(int ld) { return (size_t)2 * ld * ld + 2; }
 // Dynamic shared memory of cp_rows_kernel<MR>: two Y tiles and four factor tiles (MR = 64),
@@ -398,55 +391,99 @@ __device__ void cp_gram(const float* F, int nrows, int r, int ld, float* G) {
     }
 }
 
-// Dynamic shared memory of cp_small_kernel: the fp64 system, factored in place (ld x (ld + 1)
-// doubles), and the factor's diagonal.
-__host__ __device__ inline size_t cp_small_smem(int ld, int mr) {
-  return ((size_t)ld * (ld + 1) + (size_t)mr) * sizeof(double);
+// Dynamic shared memory of cp_small_kernel: the fp64 system, inverted in place (ld x (ld + 1)
+// doubles), the inverse's two fp64 scratch rows and an RP x ld fp32 work tile.
+__host__ __device__ inline size_t cp_small_smem(int ld, int rp, int mr) {
+  return ((size_t)ld * (ld + 1) + 2 * (size_t)mr) * sizeof(double) + (size_t)rp * ld * sizeof(float);
 }
 
-// In place: the lower Cholesky factor L of the SPD system Gd (r x r, stride lg; only the lower
-// triangle is read and written), fp64, right-looking with two barriers per column; diag
-// (MR doubles) holds L's diagonal until the end.  Returns false on a pivot that is not
-// positive (in every thread), which the caller reports as FH_ERR_ILLCOND.
+// In place: Gd (r x r, stride lg, SPD) <- Gd^{-1} in fp64 by Gauss-Jordan without pivoting
+// (the sweep operator; an SPD matrix's pivots are positive), two barriers per pivot.
+// scratch: 2 MR doubles.  Returns false on a pivot that is not positive (in every thread).
 template <int MR>
-__device__ bool cp_cholesky_d(double* Gd, int r, int lg, double* diag) {
-  constexpr int NW = CpShape<MR>::NW, NT = CpShape<MR>::NT;
+__device__ bool cp_spd_inverse_d(double* Gd, int r, int lg, double* scratch) {
+  constexpr int NW = CpShape<MR>::NW;
   __shared__ int bad;
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  double* prow = scratch;
+  double* pcol = scratch + MR;
   if (tid == 0) bad = 0;
   __syncthreads();
   for (int k = 0; k < r; ++k) {
-    double d = Gd[k * lg + k];         // final since the previous column's update
+    if (tid < r) {
+      prow[tid] = Gd[k * lg + tid];
+      pcol[tid] = Gd[tid * lg + k];
+    }
+    __syncthreads();
+    double d = prow[k];
     if (!(d > 0.0)) {
       d = 1e-300;
       if (tid == 0) bad = 1;
     }
-    const double lkk = sqrt(d), inv = 1.0 / lkk;
-    if (tid == 0) diag[k] = lkk;
-    for (int i = k + 1 + tid; i < r; i += NT) Gd[i * lg + k] *= inv;
-    __syncthreads();
-    // trailing lower triangle: G[i][j] -= L[i][k] L[j][k] for k < j <= i
-    for (int i = k + 1 + ty; i < r; i += NW) {
-      const double lik = Gd[i * lg + k];
-      for (int j = k + 1 + tx; j <= i; j += 32) Gd[i * lg + j] = fma(-lik, Gd[j * lg + k], Gd[i * lg + j]);
+    const double inv = 1.0 / d;
+    for (int p = ty; p < r; p += NW) {
+      const double cp = pcol[p] * inv;
+      for (int q = tx; q < r; q += 32) {
+        double v;
+        if (p == k) v = (q == k) ? inv : prow[q] * inv;
+        else if (q == k) v = -cp;
+        else v = fma(-cp, prow[q], Gd[p * lg + q]);
+        Gd[p * lg + q] = v;
+      }
     }
     __syncthreads();
   }
-  for (int k = tid; k < r; k += NT) Gd[k * lg + k] = diag[k];
-  __syncthreads();
   return bad == 0;
+}
+
+// out rows = RHS rows Gd^{-1} (RHS fp32 nrhs x r, stride ldr; Gd the fp64 inverse, stride lg),
+// summed in fp64 and rounded once.
+template <int MR>
+__device__ void cp_apply_inverse_d(const float* RHS, int ldr, int nrhs, const double* Gd, int r,
+                                   int lg, float* out, int ldo) {
+  constexpr int NW = CpShape<MR>::NW, TN = CpShape<MR>::TN;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  int ri[8], cj[TN];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) ri[u] = min(w + NW * u, nrhs - 1);
+#pragma unroll
+  for (int v = 0; v < TN; ++v) cj[v] = min(l + 32 * v, r - 1);
+  double acc[8][TN];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < TN; ++v) acc[u][v] = 0.0;
+  for (int p = 0; p < r; ++p) {
+    double av[8], bv[TN];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) av[u] = (double)RHS[(size_t)ri[u] * ldr + p];
+#pragma unroll
+    for (int v = 0; v < TN; ++v) bv[v] = Gd[p * lg + cj[v]];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < TN; ++v) acc[u][v] = fma(av[u], bv[v], acc[u][v]);
+  }
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < TN; ++v) {
+      const int row = w + NW * u, q = l + 32 * v;
+      if (row < nrhs && q < r) out[(size_t)row * ldo + q] = (float)acc[u][v];
+    }
 }
 
 template <int MR>
 __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
-  constexpr int NW = CpShape<MR>::NW, NT = CpShape<MR>::NT;
+  constexpr int NW = CpShape<MR>::NW;
   extern __shared__ __align__(16) float sf[];
   const int ci = blockIdx.x;
   const int r = a.c_rank[ci], R = a.R, ld = a.ld;
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   const int lg = ld + 1;                  // odd stride: column walks hit distinct banks
-  double* Gd = reinterpret_cast<double*>(sf);   // ld x lg: a system, factored in place (fp64)
-  double* diag = Gd + ld * lg;            // MR: the factor's diagonal
+  double* Gd = reinterpret_cast<double*>(sf);   // ld x lg: the system, inverted in place (fp64)
+  double* Li = Gd + ld * lg;              // 2 MR: scratch rows of the inverse
+  float* work = reinterpret_cast<float*>(Li + 2 * MR);   // RP*ld
   __shared__ double dred[32];
   __shared__ float nA[MR], nB[MR], nD[MR];
   __shared__ int stop;
@@ -455,15 +492,9 @@ __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
   float* gDD = a.gDD + (size_t)ci * ld * ld;
   float* Bc = a.B + (size_t)ci * ld * ld;
   float* Dc = a.D + (size_t)ci * a.RP * ld;
-  float* rhs = a.rhs + (size_t)ci * a.RP * ld;
-  double* chol = a.chol + (size_t)ci * ld * lg;
+  float* Lc = a.L + (size_t)ci * ld * ld;
   const int k0 = a.c_chunk0[ci], nk = a.c_nchunk[ci];
   const size_t ps = cp_pstride(ld);
-  // factors the system in Gd and publishes the factor for cp_solve_kernel
-  auto factor = [&]() {
-    if (!cp_cholesky_d<MR>(Gd, r, lg, diag) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
-    for (int i = tid; i < r * lg; i += NT) chol[i] = Gd[i];
-  };
 
   if (mode == kSmallCore) {
     for (int p = ty; p < r; p += NW)
@@ -501,40 +532,35 @@ __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
   }
 
   if (mode == kSmallB) {
-    // A^T A and MTTKRP_B; G_B = A^T A * D^T D + 1e-10 I factored; cp_solve_kernel then sets
-    // B <- MTTKRP_B G_B^{-1}
+    // A^T A, MTTKRP_B; G_B = A^T A * D^T D + 1e-10 I; B <- MTTKRP_B G_B^{-1}
     for (int p = ty; p < r; p += NW)
       for (int q = tx; q < r; q += 32) {
         const float s = chunk_sum(a.part + k0 * ps + p * ld + q, ps, nk);
         const float t = chunk_sum(a.part + k0 * ps + ld * ld + p * ld + q, ps, nk);
         gAA[p * ld + q] = s;
-        rhs[p * ld + q] = t;
+        work[p * ld + q] = t;
         Gd[p * lg + q] = (double)s * (double)gDD[p * ld + q] + (p == q ? 1e-10 : 0.0);
       }
     __syncthreads();
-    factor();
-    return;
-  }
-  if (mode == kSmallBPost) {
+    if (!cp_spd_inverse_d<MR>(Gd, r, lg, Li) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+    cp_apply_inverse_d<MR>(work, ld, r, Gd, r, lg, Bc, ld);
+    __syncthreads();
     cp_gram<MR>(Bc, r, r, ld, gBB);
     return;
   }
   if (mode == kSmallD || mode == kSmallDLast) {
-    // MTTKRP_D; G_D = A^T A * B^T B + 1e-10 I factored; cp_solve_kernel then sets
-    // D <- MTTKRP_D G_D^{-1}
+    // MTTKRP_D; G_D = A^T A * B^T B + 1e-10 I; D <- MTTKRP_D G_D^{-1}; loss; balance
     for (int m = ty; m < R; m += NW)
       for (int q = tx; q < r; q += 32) {
-        rhs[m * ld + q] = chunk_sum(a.part + k0 * ps + m * ld + q, ps, nk);
+        work[m * ld + q] = chunk_sum(a.part + k0 * ps + m * ld + q, ps, nk);
       }
     for (int p = ty; p < r; p += NW)
       for (int q = tx; q < r; q += 32)
         Gd[p * lg + q] = (double)gAA[p * ld + q] * (double)gBB[p * ld + q] + (p == q ? 1e-10 : 0.0);
     __syncthreads();
-    factor();
-    return;
-  }
-  if (mode == kSmallDPost || mode == kSmallDLastPost) {
-    // the solved D: its Gram, the loss, the stopping rule, then balance
+    if (!cp_spd_inverse_d<MR>(Gd, r, lg, Li) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+    cp_apply_inverse_d<MR>(work, ld, R, Gd, r, lg, Dc, ld);
+    __syncthreads();
     cp_gram<MR>(Dc, R, r, ld, gDD);
     __syncthreads();
     double xh = 0.0, xy = 0.0;
@@ -542,7 +568,7 @@ __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
       for (int q = tx; q < r; q += 32)
         xh += (double)gAA[p * ld + q] * (double)gBB[p * ld + q] * (double)gDD[p * ld + q];
     for (int m = ty; m < R; m += NW)
-      for (int q = tx; q < r; q += 32) xy += (double)Dc[m * ld + q] * (double)rhs[m * ld + q];
+      for (int q = tx; q < r; q += 32) xy += (double)Dc[m * ld + q] * (double)work[m * ld + q];
     xh = block_sum<double>(xh, dred);
     xy = block_sum<double>(xy, dred);
     if (tid == 0) {
@@ -578,9 +604,8 @@ __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
     for (int q = tx; q < r; q += 32)
       Dc[m * ld + q] = Dc[m * ld + q] / (nD[q] + 1e-15f) * (nA[q] * nB[q] * nD[q] + 1e-15f);
   __syncthreads();
-  if (mode == kSmallDLastPost) return;
-  // Grams of the balanced factors; B^T B * D^T D + 1e-10 I factored for the next A rows
-  // (cp_solve_kernel writes its inverse, the A-row system, to L)
+  if (mode == kSmallDLast) return;
+  // Grams of the balanced factors; the inverse of B^T B * D^T D + 1e-10 I for the next A rows
   cp_gram<MR>(Bc, r, r, ld, gBB);
   cp_gram<MR>(Dc, R, r, ld, gDD);
   __syncthreads();
@@ -588,63 +613,9 @@ __global__ void __launch_bounds__(4 * MR) cp_small_kernel(CpArgs a, int mode) {
     for (int q = tx; q < r; q += 32)
       Gd[p * lg + q] = (double)gBB[p * ld + q] * (double)gDD[p * ld + q] + (p == q ? 1e-10 : 0.0);
   __syncthreads();
-  factor();
-}
-
-// Right-hand sides of chromosome blockIdx.x solved against its published factor G = L L^T,
-// kCpSolveRows rows per CTA (blockIdx.y), one warp per row: forward substitution z L^T = m,
-// then back substitution x L = z, in fp64 with the dot products split over the lanes (fixed
-// order), so x G = m.  target: B rows (MTTKRP_B), D rows (MTTKRP_D) or the rows of G^{-1}
-// itself (the A-row system, into L).  The fp64 work is spread over the SMs instead of one CTA
-// per chromosome: on this GPU fp64 multiply-adds are the bound of these solves.
-constexpr int kCpSolveRows = 8;
-__host__ __device__ inline size_t cp_solve_smem(int ld, int mr) {
-  return ((size_t)ld * (ld + 1) + (size_t)kCpSolveRows * mr) * sizeof(double);
-}
-
-template <int MR>
-__global__ void __launch_bounds__(4 * MR) cp_solve_kernel(CpArgs a, int target) {
-  constexpr int NT = CpShape<MR>::NT;
-  extern __shared__ __align__(16) double sd[];
-  const int ci = blockIdx.x;
-  if (a.state[ci] & 1) return;
-  const int r = a.c_rank[ci], ld = a.ld, lg = ld + 1;
-  const int nrhs = target == kSolveD ? a.R : r;
-  const int row0 = blockIdx.y * kCpSolveRows;
-  if (row0 >= nrhs) return;
-  const int nrow = min(kCpSolveRows, nrhs - row0);
-  double* Ls = sd;                        // r x lg: the factor (lower triangle)
-  double* y = Ls + (size_t)r * lg;        // kCpSolveRows x MR: the rows being solved
-  const double* chol = a.chol + (size_t)ci * ld * lg;
-  for (int i = threadIdx.x; i < r * lg; i += NT) Ls[i] = chol[i];
-  const float* rhs = a.rhs + (size_t)ci * a.RP * ld;
-  for (int e = threadIdx.x; e < nrow * r; e += NT) {
-    const int i = e / r, q = e - (e / r) * r;
-    y[i * MR + q] = target == kSolveAinv ? (row0 + i == q ? 1.0 : 0.0)
-                                         : (double)rhs[(size_t)(row0 + i) * ld + q];
-  }
-  __syncthreads();
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (w >= nrow) return;
-  double* yr = y + w * MR;
-  for (int q = 0; q < r; ++q) {
-    double s = 0.0;
-    for (int p = lane; p < q; p += 32) s = fma(Ls[q * lg + p], yr[p], s);
-    s = warp_sum<double>(s);
-    if (lane == 0) yr[q] = (yr[q] - s) / Ls[q * lg + q];
-    __syncwarp();
-  }
-  for (int q = r - 1; q >= 0; --q) {
-    double s = 0.0;
-    for (int p = q + 1 + lane; p < r; p += 32) s = fma(Ls[p * lg + q], yr[p], s);
-    s = warp_sum<double>(s);
-    if (lane == 0) yr[q] = (yr[q] - s) / Ls[q * lg + q];
-    __syncwarp();
-  }
-  float* out = target == kSolveB ? a.B + (size_t)ci * ld * ld
-             : target == kSolveD ? a.D + (size_t)ci * a.RP * ld
-                                 : a.L + (size_t)ci * ld * ld;
-  for (int q = lane; q < r; q += 32) out[(size_t)(row0 + w) * ld + q] = (float)yr[q];
+  if (!cp_spd_inverse_d<MR>(Gd, r, lg, Li) && tid == 0) set_status(a.status, FH_ERR_ILLCOND);
+  for (int p = ty; p < r; p += NW)
+    for (int q = tx; q < r; q += 32) Lc[p * ld + q] = (float)Gd[p * lg + q];
 }
 
 }  // namespace fh
@@ -653,10 +624,9 @@ using namespace fh;
 
 extern "C" size_t fh_cp_workspace(int32_t nchrom, int32_t nchunks, int32_t ld, int32_t rp) {
   const size_t l = (size_t)ld * ld;
+  (void)rp;
   return sizeof(double) * (size_t)nchrom * 4 +
-         sizeof(double) * (size_t)nchrom * ld * (ld + 1) +
-         sizeof(float) * ((size_t)nchrom * (4 * l + ld + (size_t)rp * ld) +
-                          (size_t)nchunks * cp_pstride(ld)) +
+         sizeof(float) * ((size_t)nchrom * (4 * l + ld) + (size_t)nchunks * cp_pstride(ld)) +
          sizeof(int) * (size_t)nchrom + 256;
 }
 
@@ -678,9 +648,7 @@ static int cp_launch(int32_t nchrom, int32_t nchunks, const int32_t* meta, float
   a.ynorm = w; w += nchrom;
   a.loss = w; w += 2 * (size_t)nchrom;
   w += nchrom;  // spare
-  a.chol = w; w += (size_t)nchrom * ld * (ld + 1);
   float* f = (float*)w;
-  a.rhs = f; f += (size_t)nchrom * rp * ld;
   a.L = f; f += nchrom * l;
   a.gAA = f; f += nchrom * l;
   a.gBB = f; f += nchrom * l;
@@ -692,15 +660,12 @@ static int cp_launch(int32_t nchrom, int32_t nchunks, const int32_t* meta, float
   a.core = core;
   a.cross = cross;
   a.status = status;
-  const size_t small_smem = cp_small_smem(ld, MR);
+  const size_t small_smem = cp_small_smem(ld, rp, MR);
   const size_t rs = cp_rows_smem<MR>();
-  const size_t solve_smem = cp_solve_smem(ld, MR);
-  if (small_smem > 227 * 1024 || solve_smem > 227 * 1024) return FH_ERR_UNSUPPORTED;
+  if (small_smem > 227 * 1024) return FH_ERR_UNSUPPORTED;
   if (ensure_smem((const void*)cp_small_kernel<MR>, small_smem) ||
-      ensure_smem((const void*)cp_rows_kernel<MR>, rs) ||
-      ensure_smem((const void*)cp_solve_kernel<MR>, solve_smem))
+      ensure_smem((const void*)cp_rows_kernel<MR>, rs))
     return FH_ERR_LAUNCH;
-  const dim3 sgrid((unsigned)nchrom, (unsigned)((ld + kCpSolveRows - 1) / kCpSolveRows));
   if (n_iter == 0) {  // core norm only, factors untouched
     cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsGram);
     cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, kSmallCore);
@@ -712,18 +677,11 @@ static int cp_launch(int32_t nchrom, int32_t nchunks, const int32_t* meta, float
   // and D (in place) and leave A to the next sweep.
   cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsNorm);
   cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, kSmallInit);
-  cp_solve_kernel<MR><<<sgrid, NT, solve_smem, s>>>(a, kSolveAinv);
   for (int it = 0; it < n_iter; ++it) {
-    const bool last = it + 1 == n_iter;
     cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsAB);
     cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, kSmallB);
-    cp_solve_kernel<MR><<<sgrid, NT, solve_smem, s>>>(a, kSolveB);
-    cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, kSmallBPost);
     cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsD);
-    cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, last ? kSmallDLast : kSmallD);
-    cp_solve_kernel<MR><<<sgrid, NT, solve_smem, s>>>(a, kSolveD);
-    cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, last ? kSmallDLastPost : kSmallDPost);
-    if (!last) cp_solve_kernel<MR><<<sgrid, NT, solve_smem, s>>>(a, kSolveAinv);
+    cp_small_kernel<MR><<<nchrom, NT, small_smem, s>>>(a, it + 1 < n_iter ? kSmallD : kSmallDLast);
   }
   cp_rows_kernel<MR><<<nchunks, NT, rs, s>>>(a, kRowsScale);
   FH_CHECK_LAUNCH();

@@ -142,7 +142,7 @@ launches = 0
 def _kernel_count(name, args):
     if name == "fh_cp_als":
         n_iter = args[11]
-        return 2 if n_iter == 0 else 3 + 9 * n_iter
+        return 2 if n_iter == 0 else 3 + 4 * n_iter
     if name == "fh_range_svd":
         return 14 if args[10] else 13
     return _KERNELS.get(name, 0)
