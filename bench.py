@@ -63,6 +63,10 @@ def parse():
     ap.add_argument("--sample-cells", type=int, default=128,
                     help="cells of the reference's CPU sample (at least the rank R)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own torch path on the GPU (context)")
+    ap.add_argument("--gpu-sample-cells", type=int, default=2000,
+                    help="cells of the reference's GPU sample")
     ap.add_argument("--precision", default="bf16x2", choices=["fp32", "bf16x2", "bf16"],
                     help="form timed for the headline: bf16x2 (default) the tensor-core form, X "
                          "as two bf16 planes; bf16 one plane; fp32 the plain drop-in")
@@ -397,14 +401,14 @@ class _Quiet:
         return False
 
 
-def reference_fit_rate(config, n_cells, iters, steps, warmup):
-    """Times the reference's own Fast_Higashi_core.fit on the host CPU (all cores) on a cell
-    sample of the workload: the reference's init_params once (untimed), then warmup + steps
-    fits of one ALS iteration each from that state (every iteration recomputes the RWR of each
-    tile, as the reference does).  One more fit at half the sample separates the cost that
-    does not grow with cells (the per-bin polar factors, CP-ALS); the full fit of the
-    workload's cells is extrapolated as iters x (fixed + per-cell x cells).
-    Returns (cells/s, step seconds, description dict)."""
+def reference_fit_rate(config, n_cells, iters, steps, warmup, device="cpu"):
+    """Times the reference's own Fast_Higashi_core.fit on the host CPU (all cores), or on
+    device="cuda" its torch path on this GPU, on a cell sample of the workload: the
+    reference's init_params once (untimed), then warmup + steps fits of one ALS iteration each
+    from that state (every iteration recomputes the RWR of each tile, as the reference does).
+    One more fit at half the sample separates the cost that does not grow with cells (the
+    per-bin polar factors, CP-ALS); the full fit of the workload's cells is extrapolated as
+    iters x (fixed + per-cell x cells).  Returns (cells/s, step seconds, description dict)."""
     import dataclasses
     import torch
     from fh_gb300 import synth
@@ -413,7 +417,8 @@ def reference_fit_rate(config, n_cells, iters, steps, warmup):
     threads = os.cpu_count()
     torch.set_num_threads(threads)
     w_full = synth.workload(config)
-    cpu = torch.device("cpu")
+    cpu = torch.device(device)
+    on_gpu = cpu.type == "cuda"
 
     def sample(c):
         w = dataclasses.replace(w_full, n_cells=int(c))
@@ -436,10 +441,14 @@ def reference_fit_rate(config, n_cells, iters, steps, warmup):
         m.n_i = state[4].copy()
         m.bin_cov_list = [b.clone() if torch.is_tensor(b) else b for b in state[5]]
         m.bad_bin_cov_list = list(state[6])
+        if on_gpu:
+            torch.cuda.synchronize()
         t0 = time.perf_counter()
         with _Quiet():
             m.fit(ds, size_ratio=w.dim1, n_iter_max=1, n_iter_parafac=1, do_conv=False,
                   do_rwr=True, do_col=False, tol=0, run_init=False)
+        if on_gpu:
+            torch.cuda.synchronize()
         return m, time.perf_counter() - t0
 
     def init_state(w, ds):
@@ -458,12 +467,28 @@ def reference_fit_rate(config, n_cells, iters, steps, warmup):
     t_full = float(np.median(times))
     wh, dsh = sample(max(w.rank, n_cells // 2))
     st_h = init_state(wh, dsh)
-    one_fit(wh, dsh, st_h)
-    _, t_half = one_fit(wh, dsh, st_h)
+    half = []
+    for i in range(warmup + steps):
+        _, t = one_fit(wh, dsh, st_h)
+        if i >= warmup:
+            half.append(t)
+    t_half = float(np.median(half))
     per_cell = max((t_full - t_half) / (w.n_cells - wh.n_cells), 0.0)
     fixed = max(t_full - per_cell * w.n_cells, 0.0)
     fit_s = iters * (fixed + per_cell * w_full.n_cells)
     rate = w_full.n_cells / fit_s
+    if on_gpu:
+        return rate, t_full, {
+            "kind": "reference", "device": torch.cuda.get_device_name(cpu), "extrapolated": True,
+            "sample_cells": w.n_cells, "sample_iters": 1,
+            "measured_s": [round(t, 3) for t in times], "half_sample_cells": wh.n_cells,
+            "half_sample_s": round(t_half, 3), "fixed_s_per_iter": round(fixed, 4),
+            "per_cell_s_per_iter": round(per_cell, 7), "stand_ins": notes,
+            "sample": ("the reference's Fast_Higashi_core.fit with its torch path on this GPU, "
+                       "one ALS iteration (with its RWR recomputations) per step on %d of %d "
+                       "cells, from the reference's own init; one more at %d cells; extrapolated "
+                       "to %d iterations x %d cells" % (w.n_cells, w_full.n_cells, wh.n_cells,
+                                                         iters, w_full.n_cells))}
     desc = {"kind": "reference", "cores": threads, "extrapolated": True,
             "sample_cells": w.n_cells, "sample_iters": 1, "measured_s": [round(t, 3) for t in times],
             "half_sample_cells": wh.n_cells, "half_sample_s": round(t_half, 3),
@@ -1006,6 +1031,17 @@ def gb300_arm(args, rank, local, ws):
             cpu = dict(desc, value=r, unit="cells/s")
         except (ImportError, FileNotFoundError, OSError) as e:
             cpu = {"unavailable": "the reference could not be imported: %s" % e}
+    # context, not a baseline: the reference's own torch path on this GPU (what a current user
+    # of the reference sees), on a larger cell sample
+    ref_gpu = None
+    if ws == 1 and not args.no_cpu_baseline and not args.no_reference_gpu:
+        try:
+            r, _, desc = reference_fit_rate(args.config, args.gpu_sample_cells, iters, 2, 1,
+                                            device="cuda")
+            ref_gpu = dict(desc, value=r, unit="cells/s")
+        except Exception as e:          # reported, never fatal to the line
+            ref_gpu = {"unavailable": "%s: %s" % (type(e).__name__, str(e)[:200])}
+        torch.cuda.empty_cache()
     line = {"metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16" if eng.bf16 else "f32",
@@ -1016,7 +1052,7 @@ def gb300_arm(args, rank, local, ws):
                           .get(eng.precision, "fp32 (plain)")),
             "rwr_epochs": sorted(set(int(v) for v in n_i)), "bin_batches": eng.n_tiles,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-            "plain_fp32": plain,
+            "reference_gpu": ref_gpu, "plain_fp32": plain,
             "clocks": clk.summary(), "kernel_ms": {k: round(v["mean_ms"], 4) for k, v in kt.items()},
             "autotune": autotune_summary(), "precision_check": precision,
             "input_packing": packing, "post_processing": post,
