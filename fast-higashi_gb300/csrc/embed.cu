@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(kEigThreads) sym_eig_kernel(double* __restrict
     if (threadIdx.x == 0) any = 0;
     __syncthreads();
     for (int rnd = 0; rnd < m - 1; ++rnd) {
-      // angles of this round's pairs from the current G
+      // angles of this step's pairs from the current G
       for (int k = threadIdx.x; k < m / 2; k += kEigThreads) {
         int p, q;
         eig_pair(k, rnd, m, p, q);
