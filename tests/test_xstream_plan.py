@@ -215,3 +215,38 @@ def test_coo_chunks_cover_every_contact_once_inside_their_half(nnz, buf, arrays)
         if j + 1 < len(ch):
             assert m % 64 == 0
     assert nxt == nnz
+
+
+def test_staging_layout_keeps_windows_segments_and_chunks_apart():
+    """XStream's views of the staging area (a CPU tensor stands in for the device one): each
+    slot view of each window lies inside its slot; a resident dataset's segments and COO chunks
+    start at the staging start, a streamed dataset's after slot 0 (which its walk writes), and
+    segments and chunk room never overlap or leave the staging area."""
+    import torch
+    w = synth.workload("c5")
+    rows = chrom_rows_of(w)
+    ent = [int(8 * 7.0e9 * nb / sum(w.chrom_bins)) for nb in w.chrom_bins]
+    for elem, planes, dtype in ((4, 2, torch.bfloat16), (4, 1, torch.float32)):
+        p = xstream.plan_x(rows, elem, 500, [e // 100 for e in ent], 1.70e9)
+        assert p.windows
+        xs = xstream.XStream.__new__(xstream.XStream)
+        xs.plan, xs.planes, xs.C, xs.dtype, xs.torch = p, planes, 500, dtype, torch
+        xs.elem = torch.tensor([], dtype=dtype).element_size()
+        xs.staging = torch.zeros(p.staging_bytes, dtype=torch.uint8)
+        base = xs.staging.data_ptr()
+        for wi, win in enumerate(p.windows):
+            for s in (0, 1):
+                v = xs.view(s, wi)
+                assert v.shape == ((planes, 500, win.ld) if dtype == torch.bfloat16 else (500, win.ld))
+                lo = v.data_ptr() - base
+                assert lo == s * p.slot_bytes and lo + v.numel() * xs.elem <= (s + 1) * p.slot_bytes
+        first = p.windows[0].chroms[0]
+        ent_res = max(e // 100 for e in ent[:first])
+        ent_str = max(e // 100 for e in ent[first:])
+        for streamed, emax in ((False, ent_res), (True, ent_str)):
+            for e in (0, 1 << 20, emax):           # what the plan sized the staging for
+                seg, buf, nbuf = xs.build_space(streamed, e)
+                start = p.slot_bytes if streamed else 0
+                assert seg - base == start
+                assert buf - base >= start + e and buf % (2 << 20) == base % (2 << 20)
+                assert buf - base + nbuf == p.staging_bytes and nbuf >= 256 << 20
